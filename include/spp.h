@@ -1,0 +1,198 @@
+/*
+ * spp.h -- C ABI of the GB300 (sm_103a) per-step particle update.
+ *
+ * The reference (hamidallaei/SPP) has no binary interface.  Its hot path is a
+ * set of header-only C++ classes selected at compile time: Box
+ * (parallel/box.h:15-58, serial/box.h:15-61), the Particle models
+ * (shared/particle.h) and Cell (shared/cell.h:8-41), configured through
+ * mutable globals (shared/parameters.h:60-99) and static setters
+ * (shared/particle.h:106-121, 524-557).  This header replaces that surface
+ * with plain functions on an opaque handle.  Each entry point names the
+ * reference member it stands in for.
+ *
+ * Conventions
+ *   - Box is [-L, L) x [-L, L) with L the half-width, as Lx in the reference
+ *     (shared/c2dvector.h:67-73, shared/parameters.h:71-74).
+ *   - Every function returns an int status (SPP_OK == 0).  The reference
+ *     prints and calls exit(0) or MPI_Abort instead (shared/cell.h:45-49,
+ *     parallel/box.h:224-228, parallel/node.h:696).
+ *   - The handle owns all device memory; the caller owns host buffers.  One
+ *     handle is driven from one host thread and one CUDA stream.
+ *   - Host arrays are indexed by particle id (the order of upload), no matter
+ *     how the device reorders particles internally.
+ */
+#ifndef SPP_H
+#define SPP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPP_ABI_VERSION 1
+
+enum SppStatus {
+  SPP_OK = 0,
+  SPP_ERR_INVALID = 1,     /* bad argument or parameter combination */
+  SPP_ERR_ALLOC = 2,       /* device or host allocation failed */
+  SPP_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  SPP_ERR_OVERFLOW = 4,    /* neighbour-list or fixed-point range exceeded */
+  SPP_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
+  SPP_ERR_UNSUPPORTED = 6, /* model/integrator pair not built */
+  SPP_ERR_NUMERIC = 7      /* non-finite value detected */
+};
+
+/* Particle models (shared/particle.h). */
+enum SppModel {
+  SPP_MODEL_VICSEK = 0,            /* theta_i <- arg(sum_{|r_ij|<r} e^{i theta_j}) + eta xi, self included */
+  SPP_MODEL_VICSEK_REF_ANGLE = 1,  /* VicsekParticle, shared/particle.h:145-189 (raw-angle average) */
+  SPP_MODEL_VICSEK_REF_VECTOR = 2, /* VicsekParticle2, shared/particle.h:193-250 */
+  SPP_MODEL_CONTINUOUS = 3,        /* ContinuousParticle, shared/particle.h:254-378 */
+  SPP_MODEL_ABP = 4,               /* RepulsiveParticle, shared/particle.h:499-786 */
+  SPP_MODEL_BEADS = 5              /* ActiveBrownianChain nb=1 + ring membranes, shared/particle.h:792-1056 */
+};
+
+enum SppIntegrator { SPP_INT_EULER = 1, SPP_INT_RK2 = 2, SPP_INT_RK4 = 4 };
+
+enum SppForceLaw {
+  SPP_FORCE_NONE = 0,
+  SPP_FORCE_HARMONIC = 1,  /* k (1 - d / r_rep) along dr/d for d < r_rep (r_rep = 2a) */
+  SPP_FORCE_R12_TRUNC = 2  /* R12_Repulsive_Truncated, shared/force-fields.h:14-39 */
+};
+
+enum SppAlignMode {
+  SPP_ALIGN_REFERENCE = 0, /* g sin(theta_j - theta_i) / (pi R_a^2), shared/particle.h:752 */
+  SPP_ALIGN_MEAN = 1       /* (g / n_i) sum sin(theta_j - theta_i), n_i counts self (shared/particle.h:561) */
+};
+
+enum SppBinRule {
+  SPP_BIN_GEOMETRIC = 0,   /* cell = floor((x + L) D / 2L) */
+  SPP_BIN_REFERENCE = 1    /* cell = (int)((int)(x + L) * D / 2L), serial/box.h:116-117 */
+};
+
+/* Runtime parameters; replaces the compile-time switches and globals of
+ * shared/parameters.h and the static setters of shared/particle.h.
+ * spp_params_init() fills the reference's defaults for a model. */
+typedef struct SppParams {
+  uint32_t struct_size;   /* sizeof(SppParams); checked by spp_create */
+  int32_t model;          /* enum SppModel */
+  int32_t integrator;     /* enum SppIntegrator */
+  int32_t force_law;      /* enum SppForceLaw */
+  int32_t align_mode;     /* enum SppAlignMode */
+  int32_t n;              /* number of bodies */
+  uint64_t seed;          /* Philox key */
+  uint32_t system_id;     /* Philox counter word for a system inside a batch */
+  int32_t n_rings;        /* SPP_MODEL_BEADS: ring membranes (bodies 0 .. n_rings*ring_size-1) */
+  int32_t ring_size;      /* beads per ring */
+  int32_t list_capacity;  /* neighbour-list slots per particle; 0 = automatic */
+  double L;               /* half-width of the periodic box (Lx) */
+  double dt;              /* time step (dt) */
+  double v0;              /* self-propulsion speed (speed / F0) */
+  double Dr;              /* rotational diffusion; noise sigma = sqrt(2 Dr dt) (Set_Dr, particle.h:106-110) */
+  double eta;             /* Vicsek noise amplitude (noise_amplitude of the Vicsek models) */
+  double g;               /* alignment strength */
+  double alpha;           /* ContinuousParticle alpha */
+  double r_align;         /* alignment radius */
+  double r_rep;           /* repulsion cutoff */
+  double k_rep;           /* repulsion amplitude (k, or A_p for R12) */
+  double sigma_rep;       /* R12 sigma */
+  double skin;            /* Verlet skin; list radius = max(r_align, r_rep) + skin */
+  double beta_push;       /* VicsekParticle2::beta (particle.h:249) */
+  double r_push;          /* VicsekParticle2::rc (particle.h:250) */
+  double mu;              /* translational mobility of beads (m_parallel = m_perpendicular, particle.h:861-863) */
+  double k_perp;          /* rotational mobility of beads (k_perpendicular) */
+  double torque0;         /* intrinsic torque (ActiveBrownianChain::torque0) */
+  double k_bond;          /* ring bond stiffness (Spring amplitude, force-fields.h:87-97) */
+  double bond_rest;       /* ring bond rest length */
+  double kappa_bend;      /* bending stiffness on consecutive bond angles */
+} SppParams;
+
+typedef struct SppObservables {
+  int64_t step;           /* steps taken since upload */
+  double t;               /* step * dt */
+  double px, py;          /* mean heading vector (1/N) sum (cos, sin) */
+  double polarization;    /* |(px, py)| (Node::Compute_Polarization, parallel/node.h:1565-1591) */
+  int64_t n_rebuilds;     /* Verlet-list / cell rebuilds so far */
+  int32_t n;
+  int32_t list_capacity;
+  int32_t max_neighbors;  /* largest list length at the last rebuild */
+  int32_t cells_per_side;
+} SppObservables;
+
+typedef struct SppSystem SppSystem;
+
+/* ---- library ---- */
+int spp_abi_version(void);
+const char* spp_status_string(int status);
+/* Last error message of the calling thread ("" if none). */
+const char* spp_last_error(void);
+/* Fill defaults for a model: the static initialisers of shared/particle.h
+ * (e.g. RepulsiveParticle A_p=2, sigma_p=1, R_a=1.1, r_c=1.2, :774-786). */
+int spp_params_init(SppParams* p, int model);
+
+/* ---- one system ---- */
+/* Box constructor + Init (parallel/box.h:69-88, 123-151): validates the
+ * parameters and allocates every device buffer.  No particles yet. */
+int spp_create(const SppParams* p, SppSystem** out);
+/* Releases the device buffers (the reference never frees, box.h:66,87). */
+int spp_destroy(SppSystem* s);
+/* Use the given cudaStream_t for all work on this handle (NULL: the handle's own). */
+int spp_set_stream(SppSystem* s, void* cuda_stream);
+/* Positions and headings, in particle-id order; replaces Positioning_Particles
+ * / Sync / Load (parallel/box.h:106-119, 155-218, 222-243).  img_x/img_y
+ * (may be NULL = zero) are box-crossing counters carried over from a
+ * snapshot.  Bins the particles and builds the neighbour list (Update_Cells
+ * + Update_Neighbor_List).  Sets the step counter (the Philox counter word)
+ * to step0, so reloading a snapshot reproduces the same noise. */
+int spp_upload_state(SppSystem* s, const float* x, const float* y, const float* theta,
+                     const int32_t* img_x, const int32_t* img_y, int n, int64_t step0);
+/* Gathers state back in particle-id order (Save, parallel/box.h:246-267, and
+ * the Root_Gather of operator<<, :476-502).  img_x/img_y (may be NULL) count
+ * box crossings: r_original = r + 2L * img. */
+int spp_download_state(SppSystem* s, float* x, float* y, float* theta, int32_t* img_x,
+                       int32_t* img_y, int n);
+/* Multi_Step(nsteps) (parallel/box.h:394-439): nsteps full integrator steps.
+ * The neighbour list is rebuilt on device when a particle has moved more
+ * than skin/2 since the last build.  Asynchronous on the handle's stream;
+ * errors raised on the device are reported by the next spp_sync. */
+int spp_step(SppSystem* s, int nsteps);
+/* Waits for the handle's stream and reports device-side status. */
+int spp_sync(SppSystem* s);
+/* Polarization and counters (Save_Polarization, parallel/box.h:467-473). */
+int spp_observables(SppSystem* s, SppObservables* out);
+/* Parity hook: the unique pairs (i < j, particle ids) with |r_ij| < r under
+ * the kernels' FP32 predicate, found through the device cell list
+ * (Cell::Neighbor_List, shared/cell.h:74-103).  r must not exceed the list
+ * radius.  *n_pairs receives the full count even when it exceeds cap. */
+int spp_pairs(SppSystem* s, double r, int32_t* pi, int32_t* pj, int cap, int64_t* n_pairs);
+/* Parity hook: cell coordinates of every particle (id order) for a grid of
+ * D x D cells under the given SppBinRule (Box::Update_Cells, serial/box.h:107-134). */
+int spp_cells(SppSystem* s, int D, int rule, int32_t* cell_x, int32_t* cell_y, int n);
+
+/* ---- measurement helpers (no reference counterpart) ---- */
+typedef struct SppProfile {
+  int64_t steps;          /* steps advanced by the profiling run */
+  int64_t stage_launches; /* force/integrator stage kernels timed */
+  double stage_ms;        /* summed CUDA-event time of those launches */
+  int64_t rebuilds;       /* list rebuilds that happened during the run */
+  double rebuild_ms;      /* summed CUDA-event time of the rebuild sequences */
+  double total_ms;        /* event time from the first to the last launch */
+} SppProfile;
+/* Advances nsteps steps with direct (non-graph) launches, bracketing every
+ * stage kernel and every rebuild sequence with CUDA events on the handle's
+ * stream.  The state advances exactly as under spp_step. */
+int spp_profile(SppSystem* s, int nsteps, SppProfile* out);
+/* spp_step(nsteps) bracketed by CUDA events on the handle's stream; waits for
+ * completion and returns the elapsed device time in *ms. */
+int spp_time_steps(SppSystem* s, int nsteps, double* ms);
+/* Number of kernels this handle has launched (graph replays count each
+ * kernel node they run). */
+int64_t spp_kernel_launches(SppSystem* s);
+/* The cudaStream_t the handle launches on. */
+void* spp_stream(SppSystem* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPP_H */

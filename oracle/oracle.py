@@ -1,0 +1,195 @@
+"""ctypes front of the oracle libraries -- test infrastructure only.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module, as the checker.  Nothing in spp_gb300/ imports it.
+"""
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from spp_gb300 import abi
+
+from . import build as _build
+
+_D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
+_I = C.POINTER(C.c_int32)
+_P = C.POINTER(abi.SppParams)
+
+_orc = None
+_ref = None
+
+
+def orc():
+    global _orc
+    if _orc is None:
+        L = C.CDLL(str(_build.build_oracle()))
+        L.orc64_run.argtypes = [_P, C.c_int, C.c_int64, _D, _D, _D, _D, _D]
+        L.orc64_run.restype = C.c_int
+        L.orc64_pairs.argtypes = [C.c_int, _D, _D, C.c_double, C.c_double, _I, _I, C.c_int64]
+        L.orc64_pairs.restype = C.c_int64
+        L.orc_cells.argtypes = [C.c_int, _D, _D, C.c_double, C.c_int, C.c_int, _I, _I]
+        L.orc_polarization.argtypes = [C.c_int, _D, _D, _D]
+        L.orc_polarization.restype = C.c_double
+        L.orc32_run.argtypes = [_P, C.c_int, C.c_int64, _F, _F, _F, _I, _I]
+        L.orc32_run.restype = C.c_int
+        L.orc32_pairs.argtypes = [_P, _F, _F, C.c_double, _I, _I, C.c_int64]
+        L.orc32_pairs.restype = C.c_int64
+        L.orc32_cells.argtypes = [_P, _F, _F, C.c_int, C.c_int, _I, _I]
+        L.orc32_philox.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.orc32_math.argtypes = [C.c_int, C.c_int, _F, _F, _F]
+        _orc = L
+    return _orc
+
+
+def ref():
+    """The reference-harness library, or None where the reference is absent."""
+    global _ref
+    if _ref is None:
+        path = _build.build_ref()
+        if path is None or not Path(path).exists():
+            return None
+        L = C.CDLL(str(path))
+        L.ref_run.argtypes = [_P, C.c_int, C.c_int64, _D, _D, _D, _D, _D]
+        L.ref_run.restype = C.c_int
+        L.ref_r12_truncated.argtypes = [C.c_double] * 5 + [_D, _D]
+        L.ref_spring.argtypes = [C.c_double] * 4 + [_D, _D]
+        _ref = L
+    return _ref
+
+
+def _d(a):
+    return a.ctypes.data_as(_D)
+
+
+def _f(a):
+    return a.ctypes.data_as(_F)
+
+
+def _i(a):
+    return a.ctypes.data_as(_I)
+
+
+class State64:
+    """FP64 state in particle-id order: wrapped r, r_original, theta."""
+
+    def __init__(self, x, y, th, xu=None, yu=None):
+        self.x = np.ascontiguousarray(x, dtype=np.float64)
+        self.y = np.ascontiguousarray(y, dtype=np.float64)
+        self.th = np.ascontiguousarray(th, dtype=np.float64)
+        self.xu = np.ascontiguousarray(self.x if xu is None else xu, dtype=np.float64).copy()
+        self.yu = np.ascontiguousarray(self.y if yu is None else yu, dtype=np.float64).copy()
+
+    def copy(self):
+        return State64(self.x.copy(), self.y.copy(), self.th.copy(), self.xu.copy(), self.yu.copy())
+
+
+def run64(p, state: State64, nsteps, step0=0, fn="orc"):
+    """Advance an FP64 state in place with the restatement (fn='orc') or the
+    reference's own particle.h (fn='ref')."""
+    s = state
+    lib = orc().orc64_run if fn == "orc" else ref().ref_run
+    rc = lib(C.byref(p), int(nsteps), int(step0), _d(s.x), _d(s.y), _d(s.th), _d(s.xu), _d(s.yu))
+    if rc != 0:
+        raise RuntimeError(f"{fn} run failed with status {rc}")
+    return s
+
+
+class State32:
+    def __init__(self, x, y, th, ix=None, iy=None):
+        self.x = np.ascontiguousarray(x, dtype=np.float32).copy()
+        self.y = np.ascontiguousarray(y, dtype=np.float32).copy()
+        self.th = np.ascontiguousarray(th, dtype=np.float32).copy()
+        n = len(self.x)
+        self.ix = np.zeros(n, np.int32) if ix is None else np.ascontiguousarray(ix, np.int32).copy()
+        self.iy = np.zeros(n, np.int32) if iy is None else np.ascontiguousarray(iy, np.int32).copy()
+
+
+def run32(p, state: State32, nsteps, step0=0):
+    s = state
+    rc = orc().orc32_run(C.byref(p), int(nsteps), int(step0), _f(s.x), _f(s.y), _f(s.th),
+                         _i(s.ix), _i(s.iy))
+    if rc != 0:
+        raise RuntimeError(f"mirror run failed with status {rc}")
+    return s
+
+
+def pairs64(x, y, L, r, cap=None):
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    n = len(x)
+    cap = cap or max(16, 8 * n)
+    pi = np.empty(cap, np.int32)
+    pj = np.empty(cap, np.int32)
+    cnt = orc().orc64_pairs(n, _d(x), _d(y), float(L), float(r), _i(pi), _i(pj), cap)
+    if cnt > cap:
+        return pairs64(x, y, L, r, cap=int(cnt))
+    return _sorted_pairs(pi[:cnt], pj[:cnt])
+
+
+def pairs32(p, x, y, r, cap=None):
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    n = len(x)
+    q = p.replace(n=n)
+    cap = cap or max(16, 8 * n)
+    pi = np.empty(cap, np.int32)
+    pj = np.empty(cap, np.int32)
+    cnt = orc().orc32_pairs(C.byref(q), _f(x), _f(y), float(r), _i(pi), _i(pj), cap)
+    if cnt > cap:
+        return pairs32(p, x, y, r, cap=int(cnt))
+    return _sorted_pairs(pi[:cnt], pj[:cnt])
+
+
+def _sorted_pairs(pi, pj):
+    a = np.minimum(pi, pj).astype(np.int64)
+    b = np.maximum(pi, pj).astype(np.int64)
+    key = np.sort(a * (1 << 32) + b)
+    return key
+
+
+def cells64(x, y, L, D, rule):
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    cx = np.empty(len(x), np.int32)
+    cy = np.empty(len(x), np.int32)
+    orc().orc_cells(len(x), _d(x), _d(y), float(L), int(D), int(rule), _i(cx), _i(cy))
+    return cx, cy
+
+
+def cells32(p, x, y, D, rule):
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    q = p.replace(n=len(x))
+    cx = np.empty(len(x), np.int32)
+    cy = np.empty(len(x), np.int32)
+    orc().orc32_cells(C.byref(q), _f(x), _f(y), int(D), int(rule), _i(cx), _i(cy))
+    return cx, cy
+
+
+def polarization(th):
+    th = np.ascontiguousarray(th, np.float64)
+    px = C.c_double()
+    py = C.c_double()
+    P = orc().orc_polarization(len(th), _d(th), C.byref(px), C.byref(py))
+    return P, px.value, py.value
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    orc().orc32_philox(c, k, o)
+    return tuple(o)
+
+
+MATH_FNS = {"sin": 0, "cos": 1, "atan2": 2, "log": 3, "exp": 4, "wrap": 5}
+
+
+def math32(fn, a, b=None):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(a if b is None else b, np.float32)
+    out = np.empty_like(a)
+    orc().orc32_math(MATH_FNS[fn], len(a), _f(a), _f(b), _f(out))
+    return out

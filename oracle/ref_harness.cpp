@@ -1,0 +1,214 @@
+/*
+ * ORACLE -- test infrastructure only.  Built by oracle/Makefile into
+ * oracle/_ref/libspp_ref.so from the reference's own headers, which are
+ * included from the reference checkout (never copied); that library exists
+ * only where the reference is present.
+ *
+ * Drives the reference's particle classes (shared/particle.h) through the
+ * reference's step sequence (serial/box.h:458-506: Interact over every pair
+ * once, then Move*() on every particle, per Runge-Kutta stage), with the
+ * GSL calls answered by the Philox shim in oracle/refshim/gsl.  It stands in
+ * for Box because box.h/node.h need MPI and Boost and do not compile as
+ * shipped (set-up.h assigns the const globals of parameters.h:81,83;
+ * parameters.h:50 fixes Particle to ActiveBrownianChain).  Neither header is
+ * included here, so no reference file needs patching: particle.h,
+ * c2dvector.h, parameters.h and force-fields.h compile unmodified.
+ *
+ * Pair enumeration uses a cell list of width >= the largest cutoff; pairs
+ * are visited in a different order than the reference's cell traversal,
+ * which changes FP64 sums only in the last bits.
+ */
+#include "particle.h"   /* shared/particle.h of the reference */
+#include "../include/spp.h"
+#include <vector>
+#include <cmath>
+
+namespace {
+
+void set_box(double L) {
+  Lx = L; Ly = L; Lx2 = 2 * L; Ly2 = 2 * L;
+}
+void set_dt(double d) {
+  dt = d; half_dt = d / 2; dt_over_6 = d / 6;
+}
+
+template <class P>
+void interact_all(std::vector<P>& ps, double L, double rcut) {
+  int n = (int)ps.size();
+  int D = (int)std::floor(2 * L / rcut);
+  if (D < 3) {
+    for (int i = 0; i < n; ++i)
+      for (int j = i + 1; j < n; ++j) ps[i].Interact(ps[j]);
+    return;
+  }
+  std::vector<int> head((size_t)D * D, -1), next(n, -1);
+  for (int i = n - 1; i >= 0; --i) {
+    int cx = (int)std::floor((ps[i].r.x + L) * D / (2 * L));
+    int cy = (int)std::floor((ps[i].r.y + L) * D / (2 * L));
+    cx = cx < 0 ? 0 : (cx >= D ? D - 1 : cx);
+    cy = cy < 0 ? 0 : (cy >= D ? D - 1 : cy);
+    next[i] = head[cx * D + cy];
+    head[cx * D + cy] = i;
+  }
+  static const int off[4][2] = {{1, 0}, {0, 1}, {1, 1}, {1, -1}};
+  for (int cx = 0; cx < D; ++cx)
+    for (int cy = 0; cy < D; ++cy) {
+      int k = cx * D + cy;
+      for (int i = head[k]; i >= 0; i = next[i])
+        for (int j = next[i]; j >= 0; j = next[j]) ps[i].Interact(ps[j]);
+      for (int o = 0; o < 4; ++o) {
+        int kk = ((cx + off[o][0] + D) % D) * D + (cy + off[o][1] + D) % D;
+        for (int i = head[k]; i >= 0; i = next[i])
+          for (int j = head[kk]; j >= 0; j = next[j]) ps[i].Interact(ps[j]);
+      }
+    }
+}
+
+template <class P>
+void load(std::vector<P>& ps, const double* x, const double* y, const double* th, const double* xu,
+          const double* yu) {
+  for (size_t i = 0; i < ps.size(); ++i) {
+    ps[i].r.x = x[i]; ps[i].r.y = y[i];
+    ps[i].r_original.x = xu[i]; ps[i].r_original.y = yu[i];
+    ps[i].theta = th[i];
+    ps[i].v.x = std::cos(th[i]); ps[i].v.y = std::sin(th[i]);
+    ps[i].Reset();
+  }
+}
+template <class P>
+void store(const std::vector<P>& ps, double* x, double* y, double* th, double* xu, double* yu) {
+  for (size_t i = 0; i < ps.size(); ++i) {
+    x[i] = ps[i].r.x; y[i] = ps[i].r.y; th[i] = ps[i].theta;
+    xu[i] = ps[i].r_original.x; yu[i] = ps[i].r_original.y;
+  }
+}
+
+/* Move functions that draw noise are called with the draw context set to
+ * (particle id, step), so the shim hands each particle the Philox draw the
+ * kernels use for it. */
+template <class P, class F>
+void move_all(std::vector<P>& ps, const SppParams* p, int64_t step, F move) {
+  for (size_t i = 0; i < ps.size(); ++i) {
+    shim_set_context(p->seed, p->system_id, (uint32_t)i, (uint32_t)step);
+    move(ps[i]);
+  }
+}
+
+/* Vicsek-family Move() advances r but not r_original; track it for output. */
+template <class P>
+void vicsek_steps(const SppParams* p, int nsteps, int64_t step0, double* x, double* y, double* th,
+                  double* xu, double* yu) {
+  std::vector<P> ps(p->n);
+  load(ps, x, y, th, xu, yu);
+  BasicDynamicParticle::noise_amplitude = p->eta;
+  BasicDynamicParticle::speed = p->v0;
+  for (int k = 0; k < nsteps; ++k) {
+    for (auto& q : ps) q.Reset();
+    interact_all(ps, p->L, 1.0);
+    move_all(ps, p, step0 + k, [&](P& q) {
+      q.Move();
+      q.r_original.x += q.v.x * (p->dt * p->v0);
+      q.r_original.y += q.v.y * (p->dt * p->v0);
+    });
+  }
+  store(ps, x, y, th, xu, yu);
+}
+
+}  // namespace
+
+extern "C" int ref_run(const SppParams* p, int nsteps, int64_t step0, double* x, double* y,
+                       double* th, double* xu, double* yu) {
+  set_box(p->L);
+  set_dt(p->dt);
+  switch (p->model) {
+    case SPP_MODEL_VICSEK_REF_ANGLE:
+      if (p->r_align != 1.0) return SPP_ERR_UNSUPPORTED;  /* particle.h:179 tests d2 < 1 */
+      vicsek_steps<VicsekParticle>(p, nsteps, step0, x, y, th, xu, yu);
+      return SPP_OK;
+    case SPP_MODEL_VICSEK_REF_VECTOR:
+      if (p->r_align != 1.0) return SPP_ERR_UNSUPPORTED;  /* particle.h:231 */
+      VicsekParticle2::beta = p->beta_push;
+      VicsekParticle2::rc = p->r_push;
+      vicsek_steps<VicsekParticle2>(p, nsteps, step0, x, y, th, xu, yu);
+      return SPP_OK;
+    case SPP_MODEL_CONTINUOUS: {
+      if (p->r_align != 1.0 || p->integrator != SPP_INT_EULER) return SPP_ERR_UNSUPPORTED;
+      std::vector<ContinuousParticle> ps(p->n);
+      ContinuousParticle::Set_g(p->g);
+      ContinuousParticle::Set_alpha(p->alpha);
+      ContinuousParticle::Kamp = 0;
+      BasicDynamicParticle::Set_Dr(p->Dr);
+      BasicDynamicParticle::speed = p->v0;
+      load(ps, x, y, th, xu, yu);
+      for (int k = 0; k < nsteps; ++k) {
+        interact_all(ps, p->L, 1.0);
+        move_all(ps, p, step0 + k, [&](ContinuousParticle& q) {
+          C2DVector before = q.r;
+          q.Move();
+          C2DVector dr = q.r - before;
+          dr.Periodic_Transform();
+          q.r_original += dr;
+        });
+      }
+      store(ps, x, y, th, xu, yu);
+      return SPP_OK;
+    }
+    case SPP_MODEL_ABP: {
+      /* RepulsiveParticle: R12 force, reference alignment normalisation, f = v (unit speed). */
+      if (p->force_law != SPP_FORCE_R12_TRUNC || p->align_mode != SPP_ALIGN_REFERENCE ||
+          p->v0 != 1.0)
+        return SPP_ERR_UNSUPPORTED;
+      std::vector<RepulsiveParticle> ps(p->n);
+      RepulsiveParticle::Set_repulsion_radius(p->r_rep);
+      RepulsiveParticle::Set_alignment_radius(p->r_align);
+      RepulsiveParticle::Set_sigma_p(p->sigma_rep);
+      RepulsiveParticle::Set_A_p(p->k_rep);
+      RepulsiveParticle::Set_g(p->g);
+      BasicDynamicParticle::Set_Dr(p->Dr);
+      load(ps, x, y, th, xu, yu);
+      double rcut = std::max(p->r_rep, p->r_align);
+      for (int k = 0; k < nsteps; ++k) {
+        int64_t step = step0 + k;
+        if (p->integrator == SPP_INT_EULER) {
+          interact_all(ps, p->L, rcut);
+          move_all(ps, p, step, [](RepulsiveParticle& q) { q.Move(); });
+        } else if (p->integrator == SPP_INT_RK2) {
+          interact_all(ps, p->L, rcut);
+          move_all(ps, p, step, [](RepulsiveParticle& q) { q.Move_Runge_Kutta2_1(); });
+          interact_all(ps, p->L, rcut);
+          move_all(ps, p, step, [](RepulsiveParticle& q) { q.Move_Runge_Kutta2_2(); });
+        } else {
+          interact_all(ps, p->L, rcut);
+          move_all(ps, p, step, [](RepulsiveParticle& q) { q.Move_Runge_Kutta4_1(); });
+          interact_all(ps, p->L, rcut);
+          move_all(ps, p, step, [](RepulsiveParticle& q) { q.Move_Runge_Kutta4_2(); });
+          interact_all(ps, p->L, rcut);
+          move_all(ps, p, step, [](RepulsiveParticle& q) { q.Move_Runge_Kutta4_3(); });
+          interact_all(ps, p->L, rcut);
+          move_all(ps, p, step, [](RepulsiveParticle& q) { q.Move_Runge_Kutta4_4(); });
+        }
+      }
+      store(ps, x, y, th, xu, yu);
+      return SPP_OK;
+    }
+    default:
+      return SPP_ERR_UNSUPPORTED;
+  }
+}
+
+/* The reference's force law, for a direct check of the restatement. */
+extern "C" void ref_r12_truncated(double dx, double dy, double cutoff, double sigma, double A,
+                                  double* fx, double* fy) {
+  C2DVector dr;
+  dr.x = dx; dr.y = dy;
+  Real d = std::sqrt(dr.Square());
+  C2DVector f = R12_Repulsive_Truncated(dr, d, cutoff, sigma, A);
+  *fx = f.x; *fy = f.y;
+}
+extern "C" void ref_spring(double dx, double dy, double sigma, double A, double* fx, double* fy) {
+  C2DVector dr;
+  dr.x = dx; dr.y = dy;
+  Real d = std::sqrt(dr.Square());
+  C2DVector f = Spring(dr, d, sigma, A);
+  *fx = f.x; *fy = f.y;
+}

@@ -1,0 +1,270 @@
+/*
+ * ORACLE -- test infrastructure only (tests/, smoke() and bench.py's CPU
+ * baseline call it as the checker; the product never links it).
+ *
+ * CPU execution of the kernels' FP32 arithmetic.  The per-pair and
+ * per-particle formulas come from spp_gb300/csrc/spp_physics.h, the header
+ * the kernels compile; everything around them is restated here in the
+ * simplest serial form: a plain cell list rebuilt every stage, particles in
+ * id order, no Verlet list, no reordering, no graphs.  Because the neighbour
+ * sums are order-independent fixed point, the GPU must reproduce these bits
+ * exactly; any difference is a fault in binning, lists, reordering or the
+ * rebuild trigger.  Its physics is checked independently against the FP64
+ * restatement (spp_oracle64.c), which is itself pinned to the reference
+ * (ref_harness.cpp).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include "../include/spp.h"
+#include "../spp_gb300/csrc/spp_physics.h"
+
+typedef struct {
+  int D;
+  int* head;
+  int* next;
+} mcells;
+
+static void mcells_build(mcells* c, int n, const float* x, const float* y, const SppConsts* k,
+                         double rcut) {
+  int D = (int)floor(2.0 * (double)k->L / (rcut * 1.001));
+  if (D < 3) D = 1;
+  c->D = D;
+  c->head = (int*)malloc(sizeof(int) * (size_t)D * D);
+  c->next = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+  for (int q = 0; q < D * D; ++q) c->head[q] = -1;
+  for (int i = n - 1; i >= 0; --i) {
+    int cx = spp_cell_coord(x[i], k->L, k->L2, D, SPP_BIN_GEOMETRIC);
+    int cy = spp_cell_coord(y[i], k->L, k->L2, D, SPP_BIN_GEOMETRIC);
+    c->next[i] = c->head[cx * D + cy];
+    c->head[cx * D + cy] = i;
+  }
+}
+static void mcells_free(mcells* c) { free(c->head); free(c->next); }
+
+/* Calls visit(j) for every candidate j of particle i (i itself included). */
+#define FOR_CANDIDATES(c, k, xi, yi, n, j, ...)                                      \
+  do {                                                                               \
+    if ((c)->D == 1) {                                                               \
+      for (int j = 0; j < (n); ++j) { __VA_ARGS__ }                                         \
+    } else {                                                                         \
+      int _cx = spp_cell_coord(xi, (k)->L, (k)->L2, (c)->D, SPP_BIN_GEOMETRIC);      \
+      int _cy = spp_cell_coord(yi, (k)->L, (k)->L2, (c)->D, SPP_BIN_GEOMETRIC);      \
+      for (int _ox = -1; _ox <= 1; ++_ox)                                            \
+        for (int _oy = -1; _oy <= 1; ++_oy) {                                        \
+          int _nx = (_cx + _ox + (c)->D) % (c)->D, _ny = (_cy + _oy + (c)->D) % (c)->D; \
+          for (int j = (c)->head[_nx * (c)->D + _ny]; j >= 0; j = (c)->next[j]) { __VA_ARGS__ } \
+        }                                                                            \
+    }                                                                                \
+  } while (0)
+
+static double mirror_rcut(const SppParams* p) {
+  double r = p->r_align;
+  if (p->force_law != SPP_FORCE_NONE && p->r_rep > r) r = p->r_rep;
+  if (p->model == SPP_MODEL_VICSEK_REF_VECTOR && p->r_push > r) r = p->r_push;
+  return r;
+}
+
+/* Sums received by every particle from the state (x, y, c, s). */
+static int abp_accumulate(const SppConsts* k, int n, const float* x, const float* y, const float* c,
+                          const float* s, double rcut, SppAcc* acc) {
+  mcells cl;
+  mcells_build(&cl, n, x, y, k, rcut);
+  int ovf = 0;
+  for (int i = 0; i < n; ++i) {
+    SppAcc a;
+    spp_acc_zero(&a);
+    FOR_CANDIDATES(&cl, k, x[i], y[i], n, j, {
+      if (j != i) spp_pair_abp(k, &a, x[i], y[i], c[i], s[i], x[j], y[j], c[j], s[j]);
+    });
+    ovf |= a.ovf;
+    acc[i] = a;
+  }
+  mcells_free(&cl);
+  return ovf;
+}
+
+static int abp_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t step0, float* x,
+                     float* y, float* th, int32_t* ix, int32_t* iy) {
+  int n = p->n;
+  double rcut = mirror_rcut(p);
+  float* c = (float*)malloc(sizeof(float) * n);
+  float* s = (float*)malloc(sizeof(float) * n);
+  float *hx = (float*)malloc(sizeof(float) * n), *hy = (float*)malloc(sizeof(float) * n);
+  float *hc = (float*)malloc(sizeof(float) * n), *hs = (float*)malloc(sizeof(float) * n);
+  float *kx = (float*)malloc(sizeof(float) * n), *ky = (float*)malloc(sizeof(float) * n);
+  float* kt = (float*)malloc(sizeof(float) * n);
+  SppAcc* acc = (SppAcc*)malloc(sizeof(SppAcc) * (n > 0 ? n : 1));
+  int rc = SPP_OK;
+  for (int i = 0; i < n; ++i) spp_sincosf(th[i], &s[i], &c[i]);
+  for (int st = 0; st < nsteps && rc == SPP_OK; ++st) {
+    uint32_t step = (uint32_t)(step0 + st);
+    if (p->integrator == SPP_INT_EULER) {
+      if (abp_accumulate(k, n, x, y, c, s, rcut, acc)) rc = SPP_ERR_OVERFLOW;
+      for (int i = 0; i < n; ++i) {
+        float fx, fy, tau;
+        spp_abp_forces(k, &acc[i], c[i], s[i], &fx, &fy, &tau);
+        float dth = spp_rot_noise(k, (uint32_t)i, step);
+        int gx = ix[i], gy = iy[i];
+        spp_euler_update(x[i], y[i], th[i], fx, fy, tau, dth, k, &x[i], &y[i], &th[i], &c[i], &s[i],
+                         &gx, &gy);
+        ix[i] = gx; iy[i] = gy;
+      }
+      continue;
+    }
+    int nst = p->integrator == SPP_INT_RK4 ? 4 : 2;
+    for (int stage = 0; stage < nst; ++stage) {
+      const float *cx = stage == 0 ? x : hx, *cy = stage == 0 ? y : hy;
+      const float *cc = stage == 0 ? c : hc, *cs = stage == 0 ? s : hs;
+      if (abp_accumulate(k, n, cx, cy, cc, cs, rcut, acc)) rc = SPP_ERR_OVERFLOW;
+      int last = stage == nst - 1;
+      float* nx = (float*)malloc(sizeof(float) * n);
+      float* ny = (float*)malloc(sizeof(float) * n);
+      float* nc = (float*)malloc(sizeof(float) * n);
+      float* ns = (float*)malloc(sizeof(float) * n);
+      for (int i = 0; i < n; ++i) {
+        float fx, fy, tau;
+        spp_abp_forces(k, &acc[i], cc[i], cs[i], &fx, &fy, &tau);
+        float dth = spp_rot_noise(k, (uint32_t)i, step);
+        float h, frac;
+        if (nst == 2) {
+          h = stage == 0 ? k->half_dt : k->dt;
+          frac = stage == 0 ? 0.5f : 1.0f;
+        } else {
+          if (stage == 0) { kx[i] = fx; ky[i] = fy; kt[i] = tau; }
+          else if (stage < 3) { kx[i] = kx[i] + 2.0f * fx; ky[i] = ky[i] + 2.0f * fy; kt[i] = kt[i] + 2.0f * tau; }
+          else { fx = kx[i] + fx; fy = ky[i] + fy; tau = kt[i] + tau; }
+          h = stage < 2 ? k->half_dt : (stage == 2 ? k->dt : k->dt6);
+          frac = stage < 2 ? 0.5f : 1.0f;
+        }
+        float tnew;
+        int gx = ix[i], gy = iy[i];
+        spp_stage_update(h, frac, x[i], y[i], th[i], fx, fy, tau, dth, k, &nx[i], &ny[i], &tnew,
+                         &nc[i], &ns[i], &gx, &gy);
+        if (last) { th[i] = tnew; ix[i] = gx; iy[i] = gy; }
+      }
+      if (last) {
+        memcpy(x, nx, sizeof(float) * n); memcpy(y, ny, sizeof(float) * n);
+        memcpy(c, nc, sizeof(float) * n); memcpy(s, ns, sizeof(float) * n);
+      } else {
+        memcpy(hx, nx, sizeof(float) * n); memcpy(hy, ny, sizeof(float) * n);
+        memcpy(hc, nc, sizeof(float) * n); memcpy(hs, ns, sizeof(float) * n);
+      }
+      free(nx); free(ny); free(nc); free(ns);
+    }
+  }
+  free(c); free(s); free(hx); free(hy); free(hc); free(hs); free(kx); free(ky); free(kt); free(acc);
+  return rc;
+}
+
+static int vicsek_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t step0, float* x,
+                        float* y, float* th, int32_t* ix, int32_t* iy) {
+  int n = p->n;
+  double rcut = mirror_rcut(p);
+  float* c = (float*)malloc(sizeof(float) * n);
+  float* s = (float*)malloc(sizeof(float) * n);
+  float *nx = (float*)malloc(sizeof(float) * n), *ny = (float*)malloc(sizeof(float) * n);
+  float *nt = (float*)malloc(sizeof(float) * n), *nc = (float*)malloc(sizeof(float) * n);
+  float* ns = (float*)malloc(sizeof(float) * n);
+  int rc = SPP_OK;
+  for (int i = 0; i < n; ++i) spp_sincosf(th[i], &s[i], &c[i]);
+  for (int st = 0; st < nsteps; ++st) {
+    uint32_t step = (uint32_t)(step0 + st);
+    mcells cl;
+    mcells_build(&cl, n, x, y, k, rcut);
+    for (int i = 0; i < n; ++i) {
+      SppAcc a;
+      spp_acc_zero(&a);
+      FOR_CANDIDATES(&cl, k, x[i], y[i], n, j, {
+        spp_pair_vicsek(k, &a, x[i], y[i], x[j], y[j], c[j], s[j], th[j], j == i);
+      });
+      if (a.ovf) rc = SPP_ERR_OVERFLOW;
+      spp_u32x4 d = spp_draw(k->seed, k->system, (uint32_t)i, step, SPP_RNG_VICSEK);
+      int gx = ix[i], gy = iy[i];
+      spp_vicsek_update(k, &a, x[i], y[i], th[i], c[i], s[i], d.v[0], &nx[i], &ny[i], &nt[i], &nc[i],
+                        &ns[i], &gx, &gy);
+      ix[i] = gx; iy[i] = gy;
+    }
+    mcells_free(&cl);
+    memcpy(x, nx, sizeof(float) * n); memcpy(y, ny, sizeof(float) * n);
+    memcpy(th, nt, sizeof(float) * n); memcpy(c, nc, sizeof(float) * n);
+    memcpy(s, ns, sizeof(float) * n);
+  }
+  free(c); free(s); free(nx); free(ny); free(nt); free(nc); free(ns);
+  return rc;
+}
+
+/* Runs nsteps from absolute step step0.  x, y wrapped in [-L, L); ix, iy
+ * box-crossing counts (unwrapped = x + 2L ix). */
+int orc32_run(const SppParams* p, int nsteps, int64_t step0, float* x, float* y, float* th,
+              int32_t* ix, int32_t* iy) {
+  SppConsts k;
+  spp_consts_from_params(&k, p);
+  switch (p->model) {
+    case SPP_MODEL_VICSEK:
+    case SPP_MODEL_VICSEK_REF_ANGLE:
+    case SPP_MODEL_VICSEK_REF_VECTOR:
+      return vicsek_run32(p, &k, nsteps, step0, x, y, th, ix, iy);
+    case SPP_MODEL_ABP:
+    case SPP_MODEL_CONTINUOUS:
+      return abp_run32(p, &k, nsteps, step0, x, y, th, ix, iy);
+    default:
+      return SPP_ERR_UNSUPPORTED;
+  }
+}
+
+/* Unique pairs (i<j) under the kernels' FP32 predicate d2 < (float)(r*r). */
+int64_t orc32_pairs(const SppParams* p, const float* x, const float* y, double r, int32_t* pi,
+                    int32_t* pj, int64_t cap) {
+  SppConsts k;
+  spp_consts_from_params(&k, p);
+  int n = p->n;
+  float r2 = (float)(r * r);
+  mcells cl;
+  mcells_build(&cl, n, x, y, &k, r);
+  int64_t cnt = 0;
+  for (int i = 0; i < n; ++i) {
+    FOR_CANDIDATES(&cl, &k, x[i], y[i], n, j, {
+      if (j > i) {
+        float dx, dy;
+        float d2 = spp_sep(&k, x[i], y[i], x[j], y[j], &dx, &dy);
+        if (d2 < r2) {
+          if (cnt < cap) { pi[cnt] = i; pj[cnt] = j; }
+          cnt++;
+        }
+      }
+    });
+  }
+  mcells_free(&cl);
+  return cnt;
+}
+
+/* Cell coordinates with the kernels' FP32 formula (spp_cell_coord). */
+void orc32_cells(const SppParams* p, const float* x, const float* y, int D, int rule, int32_t* cx,
+                 int32_t* cy) {
+  SppConsts k;
+  spp_consts_from_params(&k, p);
+  for (int i = 0; i < p->n; ++i) {
+    cx[i] = spp_cell_coord(x[i], k.L, k.L2, D, rule);
+    cy[i] = spp_cell_coord(y[i], k.L, k.L2, D, rule);
+  }
+}
+
+/* Exposed primitives of spp_fp32.h, for the CPU tests of the arithmetic. */
+void orc32_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  spp_u32x4 o = spp_philox4x32_10(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1]);
+  memcpy(out, o.v, sizeof(o.v));
+}
+void orc32_math(int fn, int n, const float* a, const float* b, float* out) {
+  for (int i = 0; i < n; ++i) {
+    switch (fn) {
+      case 0: out[i] = spp_sinf(a[i]); break;
+      case 1: out[i] = spp_cosf(a[i]); break;
+      case 2: out[i] = spp_atan2f(a[i], b[i]); break;
+      case 3: out[i] = spp_logf(a[i]); break;
+      case 4: out[i] = spp_expf(a[i]); break;
+      case 5: out[i] = spp_wrap_angle_f(a[i]); break;
+      default: out[i] = 0; break;
+    }
+  }
+}

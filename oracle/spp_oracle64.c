@@ -1,0 +1,532 @@
+/*
+ * ORACLE -- test infrastructure only.  Nothing in the product links this
+ * file; tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg call it
+ * as the checker.
+ *
+ * FP64 CPU restatement of the reference's per-step particle update
+ * (hamidallaei/SPP), with the reference's single global GSL stream replaced
+ * by the Philox counter stream of spp_gb300/csrc/spp_fp32.h (the same draws
+ * the GPU uses, mapped to doubles here).
+ *
+ * What is restated, and from where:
+ *   - min-image / wrap            shared/c2dvector.h:67-73 (Periodic_Transform)
+ *   - half-shell pair traversal   serial/box.h:322-338, shared/cell.h:112-128
+ *                                 (every pair once, Newton's third law)
+ *   - R12_Repulsive_Truncated     shared/force-fields.h:14-39
+ *   - VicsekParticle              shared/particle.h:145-189
+ *   - VicsekParticle2             shared/particle.h:193-250
+ *   - ContinuousParticle (Euler)  shared/particle.h:254-378
+ *   - RepulsiveParticle           Reset :559-564, Noise_Gen :566-569,
+ *                                 Move :571-587, RK2 :589-631, RK4 :633-726,
+ *                                 Interact :728-757
+ *   - polarization                parallel/node.h:1565-1591
+ * Configured extensions that the reference does not have (no reference
+ * oracle; this file is their specification): the arg-of-vector-sum Vicsek
+ * rule, harmonic repulsion k(1 - d/r_rep), the 1/n_i-normalised alignment,
+ * RK2/RK4 for the continuous model.
+ *
+ * Parity pin: oracle/ref_harness.cpp runs the reference's own particle.h
+ * code on the same inputs and Philox draws; tests/test_oracle_pin.py checks
+ * this file against it.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include "../include/spp.h"
+#include "../spp_gb300/csrc/spp_fp32.h"
+
+/* ------------------------------------------------------------------ */
+/* noise (doubles from the same Philox bits the kernels use)           */
+/* ------------------------------------------------------------------ */
+static double orc_normal(const SppParams* p, int pid, int64_t step) {
+  spp_u32x4 d = spp_draw(p->seed, p->system_id, (uint32_t)pid, (uint32_t)step, SPP_RNG_ROT_NOISE);
+  double u1 = spp_u01_open0_d(d.v[0]);
+  double u2 = spp_u01_d(d.v[1]);
+  return sqrt(-2.0 * log(u1)) * cos(2.0 * M_PI * u2);
+}
+static double orc_uniform_pm_pi(const SppParams* p, int pid, int64_t step) {
+  spp_u32x4 d = spp_draw(p->seed, p->system_id, (uint32_t)pid, (uint32_t)step, SPP_RNG_VICSEK);
+  double u = spp_u01_d(d.v[0]);
+  return -M_PI * (1.0 - u) + M_PI * u; /* gsl_ran_flat(r, -pi, pi): a (1-u) + b u */
+}
+
+/* Periodic_Transform, shared/c2dvector.h:67-73 */
+static inline double pt(double x, double L) {
+  double L2 = 2.0 * L;
+  return x - L2 * (double)(int)floor(x / L2 + 0.5);
+}
+/* theta wrap, shared/particle.h:599 */
+static inline double wrap_angle(double th) {
+  return th - floor(th / (2 * M_PI) + 0.5) * 2 * M_PI;
+}
+
+/* ------------------------------------------------------------------ */
+/* cell list (geometric binning, width >= cutoff)                      */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  int D;
+  int* head;
+  int* next;
+} ocells;
+
+static void cells_build(ocells* c, int n, const double* x, const double* y, double L, double rcut) {
+  int D = (int)floor(2.0 * L / rcut);
+  if (D < 3) D = 1; /* brute force */
+  c->D = D;
+  c->head = (int*)malloc(sizeof(int) * (size_t)D * D);
+  c->next = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+  for (int k = 0; k < D * D; ++k) c->head[k] = -1;
+  for (int i = n - 1; i >= 0; --i) {
+    int cx = (int)floor((x[i] + L) * D / (2.0 * L));
+    int cy = (int)floor((y[i] + L) * D / (2.0 * L));
+    if (cx < 0) cx = 0; if (cx >= D) cx = D - 1;
+    if (cy < 0) cy = 0; if (cy >= D) cy = D - 1;
+    int k = cx * D + cy;
+    c->next[i] = c->head[k];
+    c->head[k] = i;
+  }
+}
+static void cells_free(ocells* c) { free(c->head); free(c->next); }
+
+/* Visit every unordered pair once (half shell: self, right, up, up-right,
+ * down-right; serial/box.h:330-338). */
+typedef void (*pair_fn)(void* ctx, int i, int j);
+static void cells_for_pairs(const ocells* c, int n, pair_fn fn, void* ctx) {
+  int D = c->D;
+  if (D == 1) {
+    for (int i = 0; i < n; ++i)
+      for (int j = i + 1; j < n; ++j) fn(ctx, i, j);
+    return;
+  }
+  static const int off[4][2] = {{1, 0}, {0, 1}, {1, 1}, {1, -1}};
+  for (int cx = 0; cx < D; ++cx)
+    for (int cy = 0; cy < D; ++cy) {
+      int k = cx * D + cy;
+      for (int i = c->head[k]; i >= 0; i = c->next[i])
+        for (int j = c->next[i]; j >= 0; j = c->next[j]) fn(ctx, i, j);
+      for (int o = 0; o < 4; ++o) {
+        int nx = (cx + off[o][0] + D) % D, ny = (cy + off[o][1] + D) % D;
+        int kk = nx * D + ny;
+        for (int i = c->head[k]; i >= 0; i = c->next[i])
+          for (int j = c->head[kk]; j >= 0; j = c->next[j]) fn(ctx, i, j);
+      }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* state                                                               */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  const SppParams* p;
+  int n;
+  double *x, *y, *xu, *yu, *th;   /* r (wrapped), r_original, theta */
+  double *vx, *vy;                /* heading */
+  double *fx, *fy, *tq;           /* force, torque accumulators */
+  int* nb;                        /* neighbor_size */
+  double *avx, *avy, *ath;        /* Vicsek averages */
+  double *tho, *xo, *yo, *dth;    /* theta_old, r_old, dtheta */
+  double *k1f_x, *k1f_y, *k1t, *k2f_x, *k2f_y, *k2t, *k3f_x, *k3f_y, *k3t;
+} ostate;
+
+static double* dalloc(int n) { return (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double)); }
+
+static void state_alloc(ostate* s, const SppParams* p) {
+  int n = p->n;
+  memset(s, 0, sizeof(*s));
+  s->p = p; s->n = n;
+  s->x = dalloc(n); s->y = dalloc(n); s->xu = dalloc(n); s->yu = dalloc(n); s->th = dalloc(n);
+  s->vx = dalloc(n); s->vy = dalloc(n); s->fx = dalloc(n); s->fy = dalloc(n); s->tq = dalloc(n);
+  s->nb = (int*)calloc((size_t)(n > 0 ? n : 1), sizeof(int));
+  s->avx = dalloc(n); s->avy = dalloc(n); s->ath = dalloc(n);
+  s->tho = dalloc(n); s->xo = dalloc(n); s->yo = dalloc(n); s->dth = dalloc(n);
+  s->k1f_x = dalloc(n); s->k1f_y = dalloc(n); s->k1t = dalloc(n);
+  s->k2f_x = dalloc(n); s->k2f_y = dalloc(n); s->k2t = dalloc(n);
+  s->k3f_x = dalloc(n); s->k3f_y = dalloc(n); s->k3t = dalloc(n);
+}
+static void state_free(ostate* s) {
+  double* arr[] = {s->x, s->y, s->xu, s->yu, s->th, s->vx, s->vy, s->fx, s->fy, s->tq,
+                   s->avx, s->avy, s->ath, s->tho, s->xo, s->yo, s->dth,
+                   s->k1f_x, s->k1f_y, s->k1t, s->k2f_x, s->k2f_y, s->k2t, s->k3f_x, s->k3f_y, s->k3t};
+  for (size_t k = 0; k < sizeof(arr) / sizeof(arr[0]); ++k) free(arr[k]);
+  free(s->nb);
+}
+
+static double interaction_radius(const SppParams* p) {
+  double r = p->r_align;
+  if (p->force_law != SPP_FORCE_NONE && p->r_rep > r) r = p->r_rep;
+  if (p->model == SPP_MODEL_VICSEK_REF_VECTOR && p->r_push > r) r = p->r_push;
+  return r;
+}
+
+/* ------------------------------------------------------------------ */
+/* pair interactions                                                   */
+/* ------------------------------------------------------------------ */
+/* R12_Repulsive_Truncated, shared/force-fields.h:14-39 */
+static void r12_trunc(double dx, double dy, double d, double rc, double sigma, double A,
+                      double* Fx, double* Fy) {
+  double q = sigma / d, q2 = q * q, q4 = q2 * q2, q8 = q4 * q4, q13 = q8 * q4 * q;
+  double c = sigma / rc, c2 = c * c, c4 = c2 * c2, c8 = c4 * c4, c13 = c8 * c4 * c;
+  double strength = A * (q13 - c13);
+  *Fx = strength * dx / d;
+  *Fy = strength * dy / d;
+}
+
+/* RepulsiveParticle::Interact, shared/particle.h:728-757 (and the harmonic /
+ * 1/n_i variants of the configured model). */
+static void abp_pair(void* ctx, int i, int j) {
+  ostate* s = (ostate*)ctx;
+  const SppParams* p = s->p;
+  double dx = pt(s->x[i] - s->x[j], p->L), dy = pt(s->y[i] - s->y[j], p->L);
+  double d2 = dx * dx + dy * dy;
+  double d = sqrt(d2);
+  if (p->force_law != SPP_FORCE_NONE && d < p->r_rep && d > 0) {
+    double Fx, Fy;
+    if (p->force_law == SPP_FORCE_R12_TRUNC) {
+      r12_trunc(dx, dy, d, p->r_rep, p->sigma_rep, p->k_rep, &Fx, &Fy);
+    } else {
+      double mag = p->k_rep * (1.0 - d / p->r_rep);
+      Fx = mag * dx / d;
+      Fy = mag * dy / d;
+    }
+    s->fx[i] += Fx; s->fy[i] += Fy;
+    s->fx[j] -= Fx; s->fy[j] -= Fy;
+  }
+  if (d < p->r_align) {
+    s->nb[i]++; s->nb[j]++;
+    double t = sin(s->th[j] - s->th[i]);
+    if (p->align_mode == SPP_ALIGN_REFERENCE) t = p->g * t / (M_PI * p->r_align * p->r_align);
+    s->tq[i] += t;
+    s->tq[j] -= t;
+  }
+}
+
+/* ContinuousParticle::Interact, shared/particle.h:296-338 */
+static void cont_pair(void* ctx, int i, int j) {
+  ostate* s = (ostate*)ctx;
+  const SppParams* p = s->p;
+  double dx = pt(s->x[i] - s->x[j], p->L), dy = pt(s->y[i] - s->y[j], p->L);
+  double d2 = dx * dx + dy * dy;
+  if (d2 < p->r_align * p->r_align) {
+    s->nb[i]++; s->nb[j]++;
+    double d = sqrt(d2);
+    double ti = (1 - p->alpha) * sin(s->th[j] - s->th[i]) / M_PI;
+    s->tq[i] += ti;
+    s->tq[j] -= ti;
+    if (p->alpha != 0.0 && d > 0) {
+      s->tq[i] -= p->alpha * (dx * s->vy[i] - dy * s->vx[i]) / (M_PI * d);
+      s->tq[j] += p->alpha * (dx * s->vy[j] - dy * s->vx[j]) / (M_PI * d);
+    }
+  }
+}
+
+/* VicsekParticle::Interact, shared/particle.h:171-188 */
+static void vicsek_angle_pair(void* ctx, int i, int j) {
+  ostate* s = (ostate*)ctx;
+  const SppParams* p = s->p;
+  double dx = pt(s->x[i] - s->x[j], p->L), dy = pt(s->y[i] - s->y[j], p->L);
+  double d2 = dx * dx + dy * dy;
+  if (d2 < p->r_align * p->r_align) {
+    s->nb[i]++; s->nb[j]++;
+    s->ath[i] += s->th[j];
+    s->ath[j] += s->th[i];
+  }
+}
+
+/* VicsekParticle2::Interact, shared/particle.h:221-246 */
+static void vicsek_vector_pair(void* ctx, int i, int j) {
+  ostate* s = (ostate*)ctx;
+  const SppParams* p = s->p;
+  double dx = pt(s->x[i] - s->x[j], p->L), dy = pt(s->y[i] - s->y[j], p->L);
+  double d2 = dx * dx + dy * dy;
+  double d = sqrt(d2);
+  if (d2 < p->r_align * p->r_align) {
+    s->nb[i]++; s->nb[j]++;
+    s->avx[i] += s->vx[j]; s->avy[i] += s->vy[j];
+    s->avx[j] += s->vx[i]; s->avy[j] += s->vy[i];
+    if (d < p->r_push && d > 0) {
+      double fa = p->beta_push / (1 + exp(d / p->r_push - 2));
+      double ex = dx / d, ey = dy / d;
+      s->avx[i] += ex * fa; s->avy[i] += ey * fa;
+      s->avx[j] -= ex * fa; s->avy[j] -= ey * fa;
+    }
+  }
+}
+
+/* arg(sum e^{i theta_j}) over |r_ij| < r, self included (configured rule) */
+static void vicsek_sum_pair(void* ctx, int i, int j) {
+  ostate* s = (ostate*)ctx;
+  const SppParams* p = s->p;
+  double dx = pt(s->x[i] - s->x[j], p->L), dy = pt(s->y[i] - s->y[j], p->L);
+  double d2 = dx * dx + dy * dy;
+  if (d2 < p->r_align * p->r_align) {
+    s->avx[i] += s->vx[j]; s->avy[i] += s->vy[j];
+    s->avx[j] += s->vx[i]; s->avy[j] += s->vy[i];
+  }
+}
+
+static void interact_all(ostate* s, pair_fn fn) {
+  ocells c;
+  cells_build(&c, s->n, s->x, s->y, s->p->L, interaction_radius(s->p));
+  cells_for_pairs(&c, s->n, fn, s);
+  cells_free(&c);
+}
+
+/* ------------------------------------------------------------------ */
+/* RepulsiveParticle moves                                             */
+/* ------------------------------------------------------------------ */
+static void abp_reset(ostate* s) {
+  /* RepulsiveParticle::Reset, particle.h:559-564: f = v (self propulsion). */
+  for (int i = 0; i < s->n; ++i) {
+    s->nb[i] = 1; s->tq[i] = 0;
+    s->fx[i] = s->p->v0 * s->vx[i];
+    s->fy[i] = s->p->v0 * s->vy[i];
+  }
+}
+static double abp_torque(const ostate* s, int i) {
+  const SppParams* p = s->p;
+  if (p->model == SPP_MODEL_CONTINUOUS) return p->g * s->tq[i];
+  if (p->align_mode == SPP_ALIGN_MEAN) return p->g * s->tq[i] / s->nb[i];
+  return s->tq[i];
+}
+static void set_v(ostate* s, int i) { s->vx[i] = cos(s->th[i]); s->vy[i] = sin(s->th[i]); }
+
+static void abp_stage_forces(ostate* s) {
+  abp_reset(s);
+  interact_all(s, s->p->model == SPP_MODEL_CONTINUOUS ? cont_pair : abp_pair);
+}
+
+static void abp_step(ostate* s, int64_t step) {
+  const SppParams* p = s->p;
+  double dt = p->dt, half_dt = 0.5 * dt, dt6 = dt / 6;
+  double sigma = sqrt(2 * p->Dr * dt);
+  int n = s->n;
+  if (p->integrator == SPP_INT_EULER) {
+    /* RepulsiveParticle::Move, particle.h:571-587 */
+    abp_stage_forces(s);
+    for (int i = 0; i < n; ++i) {
+      s->dth[i] = sigma * orc_normal(p, i, step);
+      s->th[i] += dt * abp_torque(s, i);
+      s->th[i] += s->dth[i];
+      set_v(s, i);
+      s->xu[i] += s->fx[i] * dt; s->yu[i] += s->fy[i] * dt;
+      s->x[i] = pt(s->xu[i], p->L); s->y[i] = pt(s->yu[i], p->L);
+    }
+    return;
+  }
+  if (p->integrator == SPP_INT_RK2) {
+    abp_stage_forces(s);
+    for (int i = 0; i < n; ++i) { /* Move_Runge_Kutta2_1, particle.h:589-611 */
+      s->dth[i] = sigma * orc_normal(p, i, step);
+      s->tho[i] = s->th[i]; s->xo[i] = s->xu[i]; s->yo[i] = s->yu[i];
+      s->th[i] += half_dt * abp_torque(s, i);
+      s->th[i] += s->dth[i] / 2;
+      s->th[i] = wrap_angle(s->th[i]);
+      set_v(s, i);
+      s->x[i] += s->fx[i] * half_dt; s->y[i] += s->fy[i] * half_dt;
+      s->x[i] = pt(s->x[i], p->L); s->y[i] = pt(s->y[i], p->L);
+    }
+    abp_stage_forces(s);
+    for (int i = 0; i < n; ++i) { /* Move_Runge_Kutta2_2, particle.h:613-631 */
+      s->th[i] = s->tho[i] + dt * abp_torque(s, i);
+      s->th[i] += s->dth[i];
+      s->th[i] = wrap_angle(s->th[i]);
+      set_v(s, i);
+      s->xu[i] = s->xo[i] + s->fx[i] * dt; s->yu[i] = s->yo[i] + s->fy[i] * dt;
+      s->x[i] = pt(s->xu[i], p->L); s->y[i] = pt(s->yu[i], p->L);
+    }
+    return;
+  }
+  /* RK4, particle.h:633-726 */
+  abp_stage_forces(s);
+  for (int i = 0; i < n; ++i) {
+    s->dth[i] = sigma * orc_normal(p, i, step);
+    s->tho[i] = s->th[i]; s->xo[i] = s->xu[i]; s->yo[i] = s->yu[i];
+    double t = abp_torque(s, i);
+    s->th[i] += half_dt * t;
+    s->th[i] += s->dth[i] / 2;
+    s->th[i] = wrap_angle(s->th[i]);
+    set_v(s, i);
+    s->x[i] += s->fx[i] * half_dt; s->y[i] += s->fy[i] * half_dt;
+    s->x[i] = pt(s->x[i], p->L); s->y[i] = pt(s->y[i], p->L);
+    s->k1f_x[i] = s->fx[i]; s->k1f_y[i] = s->fy[i]; s->k1t[i] = t;
+  }
+  abp_stage_forces(s);
+  for (int i = 0; i < n; ++i) {
+    double t = abp_torque(s, i);
+    s->th[i] = s->tho[i] + half_dt * t;
+    s->th[i] += s->dth[i] / 2;
+    s->th[i] = wrap_angle(s->th[i]);
+    set_v(s, i);
+    s->xu[i] = s->xo[i] + s->fx[i] * half_dt; s->yu[i] = s->yo[i] + s->fy[i] * half_dt;
+    s->x[i] = pt(s->xu[i], p->L); s->y[i] = pt(s->yu[i], p->L);
+    s->k2f_x[i] = s->fx[i]; s->k2f_y[i] = s->fy[i]; s->k2t[i] = t;
+  }
+  abp_stage_forces(s);
+  for (int i = 0; i < n; ++i) {
+    double t = abp_torque(s, i);
+    s->th[i] = s->tho[i] + dt * t;
+    s->th[i] += s->dth[i];
+    s->th[i] = wrap_angle(s->th[i]);
+    set_v(s, i);
+    s->xu[i] = s->xo[i] + s->fx[i] * dt; s->yu[i] = s->yo[i] + s->fy[i] * dt;
+    s->x[i] = pt(s->xu[i], p->L); s->y[i] = pt(s->yu[i], p->L);
+    s->k3f_x[i] = s->fx[i]; s->k3f_y[i] = s->fy[i]; s->k3t[i] = t;
+  }
+  abp_stage_forces(s);
+  for (int i = 0; i < n; ++i) {
+    double t = abp_torque(s, i);
+    s->th[i] = s->tho[i] + (s->k1t[i] + s->k2t[i] * 2 + s->k3t[i] * 2 + t) * dt6;
+    s->th[i] += s->dth[i];
+    s->th[i] = wrap_angle(s->th[i]);
+    set_v(s, i);
+    s->xu[i] = s->xo[i] + (s->k1f_x[i] + s->k2f_x[i] * 2 + s->k3f_x[i] * 2 + s->fx[i]) * dt6;
+    s->yu[i] = s->yo[i] + (s->k1f_y[i] + s->k2f_y[i] * 2 + s->k3f_y[i] * 2 + s->fy[i]) * dt6;
+    s->x[i] = pt(s->xu[i], p->L); s->y[i] = pt(s->yu[i], p->L);
+  }
+}
+
+/* ContinuousParticle::Move (Euler), shared/particle.h:268-293 */
+static void cont_euler_step(ostate* s, int64_t step) {
+  const SppParams* p = s->p;
+  double dt = p->dt, sigma = sqrt(2 * p->Dr * dt);
+  for (int i = 0; i < s->n; ++i) { s->nb[i] = 1; s->tq[i] = 0; }
+  interact_all(s, cont_pair);
+  for (int i = 0; i < s->n; ++i) {
+    double torque = p->g * s->tq[i] + sigma * orc_normal(p, i, step);
+    s->th[i] += torque * dt;
+    set_v(s, i);
+    s->xu[i] += s->vx[i] * (p->v0 * dt); s->yu[i] += s->vy[i] * (p->v0 * dt);
+    s->x[i] = pt(s->xu[i], p->L); s->y[i] = pt(s->yu[i], p->L);
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Vicsek models                                                       */
+/* ------------------------------------------------------------------ */
+static void vicsek_move_common(ostate* s, int i) {
+  const SppParams* p = s->p;
+  set_v(s, i);
+  s->xu[i] += s->vx[i] * (p->dt * p->v0); s->yu[i] += s->vy[i] * (p->dt * p->v0);
+  s->x[i] = pt(s->x[i] + s->vx[i] * (p->dt * p->v0), p->L);
+  s->y[i] = pt(s->y[i] + s->vy[i] * (p->dt * p->v0), p->L);
+}
+
+static void vicsek_step(ostate* s, int64_t step) {
+  const SppParams* p = s->p;
+  int n = s->n;
+  for (int i = 0; i < n; ++i) { s->nb[i] = 0; s->avx[i] = s->avy[i] = s->ath[i] = 0; }
+  if (p->model == SPP_MODEL_VICSEK) {
+    for (int i = 0; i < n; ++i) { s->avx[i] = s->vx[i]; s->avy[i] = s->vy[i]; } /* self term */
+    interact_all(s, vicsek_sum_pair);
+    for (int i = 0; i < n; ++i) {
+      double th = atan2(s->avy[i], s->avx[i]) + p->eta * orc_uniform_pm_pi(p, i, step);
+      s->th[i] = wrap_angle(th);
+      vicsek_move_common(s, i);
+    }
+  } else if (p->model == SPP_MODEL_VICSEK_REF_ANGLE) {
+    interact_all(s, vicsek_angle_pair);
+    for (int i = 0; i < n; ++i) { /* VicsekParticle::Move, particle.h:148-163 */
+      double avg = s->nb[i] > 0 ? s->ath[i] / s->nb[i] : s->th[i];
+      s->th[i] = avg + p->eta * orc_uniform_pm_pi(p, i, step);
+      vicsek_move_common(s, i);
+    }
+  } else {
+    interact_all(s, vicsek_vector_pair);
+    for (int i = 0; i < n; ++i) { /* VicsekParticle2::Move, particle.h:198-213 */
+      if (s->nb[i] == 0) { s->avx[i] = s->vx[i]; s->avy[i] = s->vy[i]; }
+      double ra = orc_uniform_pm_pi(p, i, step);
+      s->avx[i] += s->nb[i] * p->eta * cos(ra);
+      s->avy[i] += s->nb[i] * p->eta * sin(ra);
+      s->th[i] = atan2(s->avy[i], s->avx[i]);
+      vicsek_move_common(s, i);
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* exported                                                            */
+/* ------------------------------------------------------------------ */
+/* Runs nsteps steps starting at absolute step index step0.
+ * x,y: wrapped positions; xu,yu: unwrapped (r_original); th: headings. */
+int orc64_run(const SppParams* p, int nsteps, int64_t step0, double* x, double* y, double* th,
+              double* xu, double* yu) {
+  ostate s;
+  state_alloc(&s, p);
+  int n = p->n;
+  memcpy(s.x, x, sizeof(double) * n); memcpy(s.y, y, sizeof(double) * n);
+  memcpy(s.xu, xu, sizeof(double) * n); memcpy(s.yu, yu, sizeof(double) * n);
+  memcpy(s.th, th, sizeof(double) * n);
+  for (int i = 0; i < n; ++i) set_v(&s, i);
+  int rc = 0;
+  for (int k = 0; k < nsteps; ++k) {
+    int64_t step = step0 + k;
+    switch (p->model) {
+      case SPP_MODEL_VICSEK:
+      case SPP_MODEL_VICSEK_REF_ANGLE:
+      case SPP_MODEL_VICSEK_REF_VECTOR: vicsek_step(&s, step); break;
+      case SPP_MODEL_ABP: abp_step(&s, step); break;
+      case SPP_MODEL_CONTINUOUS:
+        if (p->integrator == SPP_INT_EULER) cont_euler_step(&s, step);
+        else abp_step(&s, step);
+        break;
+      default: rc = SPP_ERR_UNSUPPORTED; k = nsteps; break;
+    }
+  }
+  memcpy(x, s.x, sizeof(double) * n); memcpy(y, s.y, sizeof(double) * n);
+  memcpy(xu, s.xu, sizeof(double) * n); memcpy(yu, s.yu, sizeof(double) * n);
+  memcpy(th, s.th, sizeof(double) * n);
+  state_free(&s);
+  return rc;
+}
+
+/* Unique pairs (i<j) with sqrt(d2) < r, the reference's predicate
+ * (shared/cell.h:84-86). Returns the total count; writes up to cap. */
+typedef struct { const double *x, *y; double L, r; int32_t *pi, *pj; int64_t cap, cnt; } pairctx;
+static void pair_collect(void* ctx, int i, int j) {
+  pairctx* c = (pairctx*)ctx;
+  double dx = pt(c->x[i] - c->x[j], c->L), dy = pt(c->y[i] - c->y[j], c->L);
+  if (sqrt(dx * dx + dy * dy) < c->r) {
+    if (c->cnt < c->cap) {
+      c->pi[c->cnt] = i < j ? i : j;
+      c->pj[c->cnt] = i < j ? j : i;
+    }
+    c->cnt++;
+  }
+}
+int64_t orc64_pairs(int n, const double* x, const double* y, double L, double r, int32_t* pi,
+                    int32_t* pj, int64_t cap) {
+  ocells c;
+  cells_build(&c, n, x, y, L, r);
+  pairctx ctx = {x, y, L, r, pi, pj, cap, 0};
+  cells_for_pairs(&c, n, pair_collect, &ctx);
+  cells_free(&c);
+  return ctx.cnt;
+}
+
+/* Box::Update_Cells binning (serial/box.h:116-117) and the geometric rule. */
+void orc_cells(int n, const double* x, const double* y, double L, int D, int rule, int32_t* cx,
+               int32_t* cy) {
+  for (int i = 0; i < n; ++i) {
+    int a, b;
+    if (rule == SPP_BIN_REFERENCE) {
+      a = (int)((int)(x[i] + L) * D / (2.0 * L));
+      b = (int)((int)(y[i] + L) * D / (2.0 * L));
+    } else {
+      a = (int)floor((x[i] + L) * D / (2.0 * L));
+      b = (int)floor((y[i] + L) * D / (2.0 * L));
+    }
+    if (a >= D) a = D - 1; if (a < 0) a = 0;
+    if (b >= D) b = D - 1; if (b < 0) b = 0;
+    cx[i] = a; cy[i] = b;
+  }
+}
+
+/* Polarization |(1/N) sum v_i| (parallel/node.h:1565-1591). */
+double orc_polarization(int n, const double* th, double* px, double* py) {
+  double sx = 0, sy = 0;
+  for (int i = 0; i < n; ++i) { sx += cos(th[i]); sy += sin(th[i]); }
+  sx /= n; sy /= n;
+  if (px) *px = sx;
+  if (py) *py = sy;
+  return sqrt(sx * sx + sy * sy);
+}

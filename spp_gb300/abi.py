@@ -1,0 +1,146 @@
+"""ctypes mirror of include/spp.h and the loader of the CUDA library.
+
+The product path is ``spp_gb300/lib/libspp_gb300.so`` (hand-written sm_103a
+kernels behind the C ABI).  There is no CPU fallback: if the library is
+missing, :func:`lib` raises.
+"""
+import ctypes as C
+import os
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libspp_gb300.so"
+
+SPP_OK = 0
+STATUS_NAMES = {0: "SPP_OK", 1: "SPP_ERR_INVALID", 2: "SPP_ERR_ALLOC", 3: "SPP_ERR_CUDA",
+                4: "SPP_ERR_OVERFLOW", 5: "SPP_ERR_TIMEOUT", 6: "SPP_ERR_UNSUPPORTED",
+                7: "SPP_ERR_NUMERIC"}
+
+MODEL_VICSEK, MODEL_VICSEK_REF_ANGLE, MODEL_VICSEK_REF_VECTOR = 0, 1, 2
+MODEL_CONTINUOUS, MODEL_ABP, MODEL_BEADS = 3, 4, 5
+INT_EULER, INT_RK2, INT_RK4 = 1, 2, 4
+FORCE_NONE, FORCE_HARMONIC, FORCE_R12_TRUNC = 0, 1, 2
+ALIGN_REFERENCE, ALIGN_MEAN = 0, 1
+BIN_GEOMETRIC, BIN_REFERENCE = 0, 1
+
+
+class SppParams(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_uint32), ("model", C.c_int32), ("integrator", C.c_int32),
+        ("force_law", C.c_int32), ("align_mode", C.c_int32), ("n", C.c_int32),
+        ("seed", C.c_uint64), ("system_id", C.c_uint32), ("n_rings", C.c_int32),
+        ("ring_size", C.c_int32), ("list_capacity", C.c_int32),
+        ("L", C.c_double), ("dt", C.c_double), ("v0", C.c_double), ("Dr", C.c_double),
+        ("eta", C.c_double), ("g", C.c_double), ("alpha", C.c_double), ("r_align", C.c_double),
+        ("r_rep", C.c_double), ("k_rep", C.c_double), ("sigma_rep", C.c_double),
+        ("skin", C.c_double), ("beta_push", C.c_double), ("r_push", C.c_double),
+        ("mu", C.c_double), ("k_perp", C.c_double), ("torque0", C.c_double),
+        ("k_bond", C.c_double), ("bond_rest", C.c_double), ("kappa_bend", C.c_double),
+    ]
+
+    def copy(self):
+        q = SppParams()
+        C.pointer(q)[0] = self
+        return q
+
+    def replace(self, **kw):
+        q = self.copy()
+        for k, v in kw.items():
+            setattr(q, k, v)
+        return q
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class SppObservables(C.Structure):
+    _fields_ = [
+        ("step", C.c_int64), ("t", C.c_double), ("px", C.c_double), ("py", C.c_double),
+        ("polarization", C.c_double), ("n_rebuilds", C.c_int64), ("n", C.c_int32),
+        ("list_capacity", C.c_int32), ("max_neighbors", C.c_int32), ("cells_per_side", C.c_int32),
+    ]
+
+
+class SppProfile(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("stage_launches", C.c_int64), ("stage_ms", C.c_double),
+                ("rebuilds", C.c_int64), ("rebuild_ms", C.c_double), ("total_ms", C.c_double)]
+
+
+def new_params(**kw) -> SppParams:
+    p = SppParams()
+    p.struct_size = C.sizeof(SppParams)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+_P = C.c_void_p
+_F = C.POINTER(C.c_float)
+_I32 = C.POINTER(C.c_int32)
+
+# name -> (restype, argtypes); every entry point declared in include/spp.h
+PROTOTYPES = {
+    "spp_abi_version": (C.c_int, []),
+    "spp_status_string": (C.c_char_p, [C.c_int]),
+    "spp_last_error": (C.c_char_p, []),
+    "spp_params_init": (C.c_int, [C.POINTER(SppParams), C.c_int]),
+    "spp_create": (C.c_int, [C.POINTER(SppParams), C.POINTER(_P)]),
+    "spp_destroy": (C.c_int, [_P]),
+    "spp_set_stream": (C.c_int, [_P, _P]),
+    "spp_upload_state": (C.c_int, [_P, _F, _F, _F, _I32, _I32, C.c_int, C.c_int64]),
+    "spp_download_state": (C.c_int, [_P, _F, _F, _F, _I32, _I32, C.c_int]),
+    "spp_step": (C.c_int, [_P, C.c_int]),
+    "spp_sync": (C.c_int, [_P]),
+    "spp_observables": (C.c_int, [_P, C.POINTER(SppObservables)]),
+    "spp_pairs": (C.c_int, [_P, C.c_double, _I32, _I32, C.c_int, C.POINTER(C.c_int64)]),
+    "spp_cells": (C.c_int, [_P, C.c_int, C.c_int, _I32, _I32, C.c_int]),
+    "spp_kernel_launches": (C.c_int64, [_P]),
+    "spp_stream": (_P, [_P]),
+    "spp_profile": (C.c_int, [_P, C.c_int, C.POINTER(SppProfile)]),
+    "spp_time_steps": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double)]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library.  Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        path = Path(os.environ.get("SPP_GB300_LIB", LIB_PATH))
+        if not path.exists():
+            raise RuntimeError(
+                f"{path} is missing: build the CUDA extension first "
+                "(python -c 'import __graft_entry__ as g; g.build()')")
+        L = C.CDLL(str(path))
+        for name, (res, args) in PROTOTYPES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class SppError(RuntimeError):
+    def __init__(self, status, where):
+        msg = ""
+        try:
+            msg = lib().spp_last_error().decode()
+        except Exception:
+            pass
+        super().__init__(f"{where}: {STATUS_NAMES.get(status, status)} {msg}")
+        self.status = status
+
+
+def check(status, where):
+    if status != SPP_OK:
+        raise SppError(status, where)
+    return status
+
+
+def fptr(a):
+    return a.ctypes.data_as(_F) if a is not None else None
+
+
+def iptr(a):
+    return a.ctypes.data_as(_I32) if a is not None else None

@@ -1,0 +1,117 @@
+"""Parameter presets and initial conditions.
+
+Presets:
+  * ``reference_defaults(model)``: the reference's static initialisers
+    (shared/particle.h:138-140, 249-250, 373-378, 774-786, 1049-1056).
+  * ``vicsek_config(...)``: discrete Vicsek, N=4096, 64x64 box (L=32),
+    v0=0.5, r=1, eta=0.3, dt=1 (the CPU-runnable FP64 workload).
+  * ``abp_config(...)``: repulsive active Brownian / Vicsek, N=1,048,576,
+    1024x1024 box (L=512), harmonic k(1 - r/2a) with a=0.5, k=10,
+    (g/n_i) sum sin alignment within r=1, D_r=0.1, v0=1, RK2 dt=0.005,
+    Verlet skin 0.3 (the headline GPU workload).
+
+Initial conditions are drawn from the same Philox4x32-10 stream the kernels
+use (stream tags SPP_RNG_INIT_POS / SPP_RNG_INIT_ANGLE), so they are
+identical on every machine; this numpy version is checked against the C
+implementation in the tests.
+"""
+import math
+
+import numpy as np
+
+from . import abi
+
+M0, M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
+W0, W1 = np.uint32(0x9E3779B9), np.uint32(0xBB67AE85)
+RNG_ROT_NOISE, RNG_VICSEK, RNG_INIT_POS, RNG_INIT_ANGLE = 1, 2, 3, 4
+
+
+def philox4x32_10(c0, c1, c2, c3, k0, k1):
+    """Vectorised Philox4x32-10 (Salmon et al., SC'11) on uint32 arrays."""
+    c0, c1, c2, c3 = (np.asarray(v, dtype=np.uint32).copy() for v in (c0, c1, c2, c3))
+    k0 = np.uint32(k0)
+    k1 = np.uint32(k1)
+    mask = np.uint64(0xFFFFFFFF)
+    with np.errstate(over="ignore"):
+        for _ in range(10):
+            p0 = M0 * c0.astype(np.uint64)
+            p1 = M1 * c2.astype(np.uint64)
+            hi0, lo0 = (p0 >> np.uint64(32)).astype(np.uint32), (p0 & mask).astype(np.uint32)
+            hi1, lo1 = (p1 >> np.uint64(32)).astype(np.uint32), (p1 & mask).astype(np.uint32)
+            c0, c1, c2, c3 = hi1 ^ c1 ^ k0, lo1, hi0 ^ c3 ^ k1, lo0
+            k0 = np.uint32(k0 + W0)
+            k1 = np.uint32(k1 + W1)
+    return c0, c1, c2, c3
+
+
+def draw(seed, system, pids, step, stream):
+    pids = np.asarray(pids, dtype=np.uint32)
+    z = np.zeros_like(pids)
+    return philox4x32_10(pids, z + np.uint32(step), z + np.uint32(stream), z + np.uint32(system),
+                         seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF)
+
+
+def u01_f32(bits):
+    return (bits >> np.uint32(8)).astype(np.float32) * np.float32(5.9604644775390625e-08)
+
+
+def random_state(n, L, seed, system=0):
+    """Uniform positions in [-L, L)^2 and headings in [-pi, pi), float32,
+    from the Philox init streams (Random_Formation, shared/set-up.h:153-163,
+    with the GSL draws replaced)."""
+    ids = np.arange(n, dtype=np.uint32)
+    a = draw(seed, system, ids, 0, RNG_INIT_POS)
+    b = draw(seed, system, ids, 0, RNG_INIT_ANGLE)
+    Lf = np.float32(L)
+    x = (np.float32(2.0) * u01_f32(a[0]) - np.float32(1.0)) * Lf
+    y = (np.float32(2.0) * u01_f32(a[1]) - np.float32(1.0)) * Lf
+    th = (np.float32(2.0) * u01_f32(b[0]) - np.float32(1.0)) * np.float32(math.pi)
+    # (2u-1)*L rounds up to L for u near 1 when L is not a power of two; keep [-L, L)
+    x = np.where(x >= Lf, -Lf, x).astype(np.float32)
+    y = np.where(y >= Lf, -Lf, y).astype(np.float32)
+    return x.astype(np.float32), y.astype(np.float32), th.astype(np.float32)
+
+
+def reference_defaults(model) -> abi.SppParams:
+    """The reference's static initialisers for a model."""
+    p = abi.new_params(model=model, n=0, seed=10, L=64.0, dt=1.0 / 1024, v0=1.0, Dr=0.0, eta=0.0,
+                       g=1.0, alpha=0.0, r_align=1.0, r_rep=0.0, k_rep=0.0, sigma_rep=1.0,
+                       skin=0.0, beta_push=2.5, r_push=0.127, mu=0.5, k_perp=1.0, torque0=0.0,
+                       k_bond=0.0, bond_rest=1.0, kappa_bend=0.0, integrator=abi.INT_EULER,
+                       force_law=abi.FORCE_NONE, align_mode=abi.ALIGN_REFERENCE)
+    if model == abi.MODEL_ABP:  # RepulsiveParticle, shared/particle.h:774-786
+        p.integrator = abi.INT_RK2
+        p.force_law = abi.FORCE_R12_TRUNC
+        p.k_rep, p.sigma_rep, p.r_align, p.r_rep, p.g = 2.0, 1.0, 1.1, 1.2, 1.0
+    elif model == abi.MODEL_CONTINUOUS:  # ContinuousParticle, :373-378
+        p.g, p.alpha = 4.0, 0.5
+    elif model == abi.MODEL_BEADS:  # ActiveBrownianChain, :1049-1056
+        p.force_law = abi.FORCE_R12_TRUNC
+        p.k_rep, p.sigma_rep, p.r_rep = 1.0, 0.5, 0.55
+        p.mu, p.k_perp = 0.5, 1.0
+        p.integrator = abi.INT_RK2
+    return p
+
+
+def vicsek_config(n=4096, L=32.0, eta=0.3, seed=0, model=abi.MODEL_VICSEK) -> abi.SppParams:
+    """Plain Vicsek: N=4096 in a 64x64 periodic box, v0=0.5, r=1, eta=0.3, dt=1."""
+    p = reference_defaults(model)
+    p.n, p.L, p.eta, p.seed = n, L, eta, seed
+    p.v0, p.r_align, p.dt = 0.5, 1.0, 1.0
+    p.integrator = abi.INT_EULER
+    p.skin = 0.0
+    return p
+
+
+def abp_config(n=1 << 20, L=512.0, seed=1, integrator=abi.INT_RK2) -> abi.SppParams:
+    """Repulsive ABP / Vicsek: N=1,048,576 disks (a=0.5) in a 1024x1024 box."""
+    p = reference_defaults(abi.MODEL_ABP)
+    p.n, p.L, p.seed = n, L, seed
+    p.integrator = integrator
+    p.force_law = abi.FORCE_HARMONIC
+    p.align_mode = abi.ALIGN_MEAN
+    p.k_rep, p.r_rep = 10.0, 1.0          # k (1 - r / 2a), 2a = 1
+    p.g, p.r_align = 1.0, 1.0
+    p.Dr, p.v0, p.dt = 0.1, 1.0, 0.005
+    p.skin = 0.3
+    return p

@@ -1,0 +1,749 @@
+/*
+ * api.cu -- the C ABI of include/spp.h.
+ *
+ * One SppSystem owns the device buffers of one periodic box and launches on
+ * one CUDA stream.  spp_step() replays CUDA graphs of whole steps:
+ *   ABP / continuous:  [stage kernel] x stages  ->  IF(rebuild) { zero counts,
+ *                      bin_count, scan x3, scatter, build_list }
+ *   Vicsek (dt = 1):   zero counts, bin_count, scan x3, scatter, step kernel
+ * The IF condition is set on the device by the last stage kernel
+ * (cudaGraphSetConditional), so a replay of many steps never returns to the
+ * host.  This is the GB300 counterpart of Box::Multi_Step (parallel/box.h:
+ * 394-439), whose per-step MPI barriers and fixed-period Quick_Update_Cells
+ * disappear.
+ */
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <string>
+#include <vector>
+#include "spp_internal.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int status, const std::string& msg) {
+  g_err = msg;
+  return status;
+}
+
+#define CUDA_TRY(expr)                                                                      \
+  do {                                                                                      \
+    cudaError_t _e = (expr);                                                                \
+    if (_e != cudaSuccess)                                                                  \
+      return fail(SPP_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e));       \
+  } while (0)
+
+constexpr int GRAPH_CHUNK = 32;
+
+struct GraphEntry {
+  int nsteps;
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+};
+
+}  // namespace
+
+struct SppSystem {
+  SppParams p;
+  SppConsts k;
+  DevState d;
+  cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;   /* used only while capturing conditional bodies */
+  bool own_stream = false;
+  bool uses_list = false;        /* Verlet list models (ABP, continuous) */
+  int nstages = 1;
+  int per_step_kernels = 0;
+  int per_rebuild_kernels = 0;
+  int64_t host_launches = 0;
+  int64_t graph_kernels = 0;
+  int64_t direct_rebuilds = 0;
+  int64_t target_step = 0;       /* step the caller has asked to reach */
+  int64_t step0 = 0;
+  bool uploaded = false;
+  bool use_graphs = true;
+  float* stage_x = nullptr;      /* staging for uploads/downloads */
+  float* stage_y = nullptr;
+  float* stage_t = nullptr;
+  int2* stage_img = nullptr;
+  std::vector<GraphEntry> graphs;
+};
+
+namespace {
+
+void free_graphs(SppSystem* s) {
+  for (auto& g : s->graphs) {
+    cudaGraphExecDestroy(g.exec);
+    cudaGraphDestroy(g.graph);
+  }
+  s->graphs.clear();
+}
+
+template <class T>
+int dalloc(T** ptr, size_t count) {
+  *ptr = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)ptr, count * sizeof(T));
+  if (e != cudaSuccess) {
+    *ptr = nullptr;
+    return fail(SPP_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  return SPP_OK;
+}
+
+void free_dev(SppSystem* s) {
+  DevState& d = s->d;
+  void* ptrs[] = {d.pos, d.half, d.half2, d.theta, d.img, d.id, d.kacc, d.ref, d.pos_alt,
+                  d.theta_alt, d.img_alt, d.id_alt, d.key, d.rank, d.cell_count, d.cell_start,
+                  d.scan_tmp, d.nbr, d.nn, d.ctl, d.red, s->stage_x, s->stage_y, s->stage_t,
+                  s->stage_img};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  memset(&s->d, 0, sizeof(s->d));
+  s->stage_x = s->stage_y = s->stage_t = nullptr;
+  s->stage_img = nullptr;
+}
+
+double interaction_radius(const SppParams& p) {
+  double r = p.r_align;
+  if (p.force_law != SPP_FORCE_NONE && p.r_rep > r) r = p.r_rep;
+  if (p.model == SPP_MODEL_VICSEK_REF_VECTOR && p.r_push > r) r = p.r_push;
+  return r;
+}
+
+int validate(const SppParams* p) {
+  if (!p) return fail(SPP_ERR_INVALID, "params is NULL");
+  if (p->struct_size != sizeof(SppParams))
+    return fail(SPP_ERR_INVALID, "SppParams.struct_size does not match this library");
+  if (p->n < 1) return fail(SPP_ERR_INVALID, "n must be >= 1");
+  if (!(p->L > 0) || !(p->dt > 0)) return fail(SPP_ERR_INVALID, "L and dt must be > 0");
+  if (!(p->r_align > 0)) return fail(SPP_ERR_INVALID, "r_align must be > 0");
+  if (p->Dr < 0 || p->skin < 0) return fail(SPP_ERR_INVALID, "Dr and skin must be >= 0");
+  switch (p->model) {
+    case SPP_MODEL_VICSEK:
+    case SPP_MODEL_VICSEK_REF_ANGLE:
+    case SPP_MODEL_VICSEK_REF_VECTOR:
+      break;
+    case SPP_MODEL_ABP:
+    case SPP_MODEL_CONTINUOUS:
+      if (p->integrator != SPP_INT_EULER && p->integrator != SPP_INT_RK2 &&
+          p->integrator != SPP_INT_RK4)
+        return fail(SPP_ERR_INVALID, "integrator must be SPP_INT_EULER, _RK2 or _RK4");
+      if (!(p->skin > 0)) return fail(SPP_ERR_INVALID, "the Verlet-list models need skin > 0");
+      if (p->model == SPP_MODEL_ABP && p->force_law != SPP_FORCE_NONE &&
+          p->force_law != SPP_FORCE_HARMONIC && p->force_law != SPP_FORCE_R12_TRUNC)
+        return fail(SPP_ERR_INVALID, "unknown force law");
+      break;
+    default:
+      return fail(SPP_ERR_UNSUPPORTED, "model not built into this library");
+  }
+  return SPP_OK;
+}
+
+int enqueue_rebuild(SppSystem* s, cudaStream_t st, int64_t* launches) {
+  CUDA_TRY(cudaMemsetAsync(s->d.cell_count, 0, sizeof(uint32_t) * s->d.n_keys, st));
+  launch_bin_count(s->k, s->d, st, launches);
+  launch_scan(s->d, st, launches);
+  launch_scatter(s->d, st, launches);
+  launch_build_list(s->k, s->d, s->uses_list ? 1 : 0, st, launches);
+  CUDA_TRY(cudaGetLastError());
+  return SPP_OK;
+}
+
+/* One step of the model, enqueued on st (stream or capture). */
+int enqueue_step(SppSystem* s, cudaStream_t st, bool capture, int64_t* launches) {
+  if (!s->uses_list) {
+    CUDA_TRY(cudaMemsetAsync(s->d.cell_count, 0, sizeof(uint32_t) * s->d.n_keys, st));
+    launch_bin_count(s->k, s->d, st, launches);
+    launch_scan(s->d, st, launches);
+    launch_scatter(s->d, st, launches);
+    launch_vicsek_step(s->k, s->d, st, launches);
+    CUDA_TRY(cudaGetLastError());
+    return SPP_OK;
+  }
+  cudaGraphConditionalHandle handle = 0;
+  if (capture) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g;
+    CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+    CUDA_TRY(cudaGraphConditionalHandleCreate(&handle, g, 0, cudaGraphCondAssignDefault));
+  }
+  for (int stage = 0; stage < s->nstages; ++stage)
+    launch_abp_stage(s->k, s->d, stage, s->nstages, handle, capture ? 1 : 0, st, launches);
+  CUDA_TRY(cudaGetLastError());
+  if (!capture) return SPP_OK;
+  /* IF(rebuild) node whose body holds the rebuild kernels. */
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = handle;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  CUDA_TRY(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CUDA_TRY(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
+                                               cudaStreamSetCaptureDependencies));
+  CUDA_TRY(cudaStreamBeginCaptureToGraph(s->side, body, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_rebuild(s, s->side, nullptr);
+  cudaGraph_t body_out = body;
+  cudaError_t e = cudaStreamEndCapture(s->side, &body_out);
+  if (rc != SPP_OK) return rc;
+  if (e != cudaSuccess) return fail(SPP_ERR_CUDA, std::string("capture rebuild body: ") +
+                                                      cudaGetErrorString(e));
+  return SPP_OK;
+}
+
+int get_graph(SppSystem* s, int nsteps, cudaGraphExec_t* out) {
+  for (auto& g : s->graphs)
+    if (g.nsteps == nsteps) { *out = g.exec; return SPP_OK; }
+  cudaGraph_t graph = nullptr;
+  CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = SPP_OK;
+  for (int i = 0; i < nsteps && rc == SPP_OK; ++i) rc = enqueue_step(s, s->stream, true, nullptr);
+  cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+  if (rc != SPP_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
+  if (e != cudaSuccess) return fail(SPP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  cudaGraphExec_t exec;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return fail(SPP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  }
+  s->graphs.push_back({nsteps, graph, exec});
+  *out = exec;
+  return SPP_OK;
+}
+
+int run_steps(SppSystem* s, int64_t nsteps) {
+  if (!s->use_graphs) {
+    for (int64_t i = 0; i < nsteps; ++i) {
+      int rc = enqueue_step(s, s->stream, false, &s->host_launches);
+      if (rc != SPP_OK) return rc;
+      if (s->uses_list) {
+        Ctl c;
+        CUDA_TRY(cudaMemcpyAsync(&c, s->d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        if (c.need_rebuild) {
+          rc = enqueue_rebuild(s, s->stream, &s->host_launches);
+          if (rc != SPP_OK) return rc;
+          s->direct_rebuilds++;
+        }
+      }
+    }
+    return SPP_OK;
+  }
+  while (nsteps > 0) {
+    int chunk = nsteps >= GRAPH_CHUNK ? GRAPH_CHUNK : (int)nsteps;
+    cudaGraphExec_t exec;
+    int rc = get_graph(s, chunk, &exec);
+    if (rc != SPP_OK) return rc;
+    CUDA_TRY(cudaGraphLaunch(exec, s->stream));
+    s->graph_kernels += (int64_t)chunk * s->per_step_kernels;
+    nsteps -= chunk;
+  }
+  return SPP_OK;
+}
+
+int read_ctl(SppSystem* s, Ctl* c) {
+  CUDA_TRY(cudaMemcpyAsync(c, s->d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return SPP_OK;
+}
+
+int list_capacity_for(const SppParams& p, double rlist) {
+  double area = 4.0 * p.L * p.L;
+  double expected = (double)p.n / area * M_PI * rlist * rlist;
+  int cap = (int)std::ceil(expected * 2.0 + 8.0);
+  if (cap < 16) cap = 16;
+  return (cap + 3) & ~3;
+}
+
+int alloc_list(SppSystem* s, int cap) {
+  if (s->d.nbr) cudaFree(s->d.nbr);
+  s->d.nbr = nullptr;
+  s->d.cap = cap;
+  return dalloc(&s->d.nbr, (size_t)cap * s->d.n);
+}
+
+/* Grows the neighbour list after an overflow and finishes the steps the
+ * frozen kernels skipped. */
+int recover(SppSystem* s) {
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    Ctl c;
+    int rc = read_ctl(s, &c);
+    if (rc != SPP_OK) return rc;
+    if (c.fx_overflow)
+      return fail(SPP_ERR_OVERFLOW, "a pair term exceeded the fixed-point range (overlapping "
+                                    "particles under an R12 force?); the state is not reliable");
+    if (!c.frozen) {
+      if ((int64_t)c.step >= s->target_step) return SPP_OK;
+      rc = run_steps(s, s->target_step - (int64_t)c.step);
+      if (rc != SPP_OK) return rc;
+      continue;
+    }
+    int cap = (int)((c.list_need * 5u) / 4u + 4u);
+    cap = (cap + 3) & ~3;
+    free_graphs(s);
+    rc = alloc_list(s, cap);
+    if (rc != SPP_OK) return rc;
+    CUDA_TRY(cudaMemsetAsync(&s->d.ctl->frozen, 0, sizeof(uint32_t), s->stream));
+    CUDA_TRY(cudaMemsetAsync(&s->d.ctl->list_need, 0, sizeof(uint32_t), s->stream));
+    rc = enqueue_rebuild(s, s->stream, &s->host_launches);
+    if (rc != SPP_OK) return rc;
+    s->direct_rebuilds++;
+  }
+  return fail(SPP_ERR_OVERFLOW, "neighbour list kept overflowing");
+}
+
+}  // namespace
+
+extern "C" {
+
+int spp_abi_version(void) { return SPP_ABI_VERSION; }
+
+const char* spp_status_string(int st) {
+  switch (st) {
+    case SPP_OK: return "SPP_OK";
+    case SPP_ERR_INVALID: return "SPP_ERR_INVALID";
+    case SPP_ERR_ALLOC: return "SPP_ERR_ALLOC";
+    case SPP_ERR_CUDA: return "SPP_ERR_CUDA";
+    case SPP_ERR_OVERFLOW: return "SPP_ERR_OVERFLOW";
+    case SPP_ERR_TIMEOUT: return "SPP_ERR_TIMEOUT";
+    case SPP_ERR_UNSUPPORTED: return "SPP_ERR_UNSUPPORTED";
+    case SPP_ERR_NUMERIC: return "SPP_ERR_NUMERIC";
+    default: return "SPP_ERR_UNKNOWN";
+  }
+}
+
+const char* spp_last_error(void) { return g_err.c_str(); }
+
+int spp_params_init(SppParams* p, int model) {
+  if (!p) return fail(SPP_ERR_INVALID, "params is NULL");
+  memset(p, 0, sizeof(*p));
+  p->struct_size = sizeof(SppParams);
+  p->model = model;
+  p->seed = 10;                   /* shared/parameters.h:60 */
+  p->L = 64.0;                    /* Lx_int, parameters.h:68 */
+  p->dt = 1.0 / 1024;             /* parameters.h:77 */
+  p->v0 = 1.0;                    /* speed, parameters.h:89 */
+  p->g = 1.0;
+  p->r_align = 1.0;
+  p->sigma_rep = 1.0;
+  p->beta_push = 2.5;             /* VicsekParticle2::beta, particle.h:249 */
+  p->r_push = 0.127;              /* VicsekParticle2::rc, particle.h:250 */
+  p->mu = 0.5;                    /* m_parallel = m_perpendicular for nb = 1, particle.h:861-863 */
+  p->k_perp = 1.0;
+  p->bond_rest = 1.0;
+  p->integrator = SPP_INT_EULER;
+  p->force_law = SPP_FORCE_NONE;
+  p->align_mode = SPP_ALIGN_REFERENCE;
+  switch (model) {
+    case SPP_MODEL_ABP:           /* RepulsiveParticle statics, particle.h:774-786 */
+      p->integrator = SPP_INT_RK2;
+      p->force_law = SPP_FORCE_R12_TRUNC;
+      p->k_rep = 2.0; p->sigma_rep = 1.0; p->r_align = 1.1; p->r_rep = 1.2;
+      p->skin = 0.3;
+      break;
+    case SPP_MODEL_CONTINUOUS:    /* ContinuousParticle statics, particle.h:373-378 */
+      p->g = 4.0; p->alpha = 0.5; p->skin = 0.3;
+      break;
+    case SPP_MODEL_BEADS:         /* ActiveBrownianChain statics, particle.h:1049-1056 */
+      p->integrator = SPP_INT_RK2;
+      p->force_law = SPP_FORCE_R12_TRUNC;
+      p->k_rep = 1.0; p->sigma_rep = 0.5; p->r_rep = 0.55; p->skin = 0.3;
+      break;
+    case SPP_MODEL_VICSEK:
+    case SPP_MODEL_VICSEK_REF_ANGLE:
+    case SPP_MODEL_VICSEK_REF_VECTOR:
+      break;
+    default:
+      return fail(SPP_ERR_UNSUPPORTED, "unknown model");
+  }
+  return SPP_OK;
+}
+
+int spp_create(const SppParams* p, SppSystem** out) {
+  if (!out) return fail(SPP_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int rc = validate(p);
+  if (rc != SPP_OK) return rc;
+  SppSystem* s = new SppSystem();
+  s->p = *p;
+  spp_consts_from_params(&s->k, p);
+  s->uses_list = (p->model == SPP_MODEL_ABP || p->model == SPP_MODEL_CONTINUOUS);
+  s->nstages = p->integrator == SPP_INT_RK4 ? 4 : (p->integrator == SPP_INT_RK2 ? 2 : 1);
+  if (!s->uses_list) s->nstages = 1;
+  const char* env = getenv("SPP_NO_GRAPHS");
+  s->use_graphs = !(env && env[0] == '1');
+  double rcell = s->uses_list ? (double)interaction_radius(*p) + p->skin : interaction_radius(*p);
+  int D = (int)std::floor(2.0 * p->L / (rcell * 1.001));
+  if (D < 3) {
+    delete s;
+    return fail(SPP_ERR_INVALID, "box too small for the cell list: 2L / r_cell < 3");
+  }
+  if (D > 65535) {
+    delete s;
+    return fail(SPP_ERR_INVALID, "too many cells per side (> 65535)");
+  }
+  int bits = 0;
+  while ((1 << bits) < D) ++bits;
+  DevState& d = s->d;
+  memset(&d, 0, sizeof(d));
+  d.n = p->n;
+  d.D = D;
+  d.morton_bits = bits;
+  d.n_keys = 1u << (2 * bits);
+  int cap = p->list_capacity > 0 ? p->list_capacity : list_capacity_for(*p, rcell);
+  if (!s->uses_list) cap = 0;
+  size_t n = (size_t)p->n;
+  uint32_t nscan = (d.n_keys + 4095) / 4096;
+  if (nscan > 4096) {
+    delete s;
+    return fail(SPP_ERR_INVALID, "cell grid too large for the scan");
+  }
+  rc = SPP_OK;
+  rc = rc ? rc : dalloc(&d.pos, n);
+  rc = rc ? rc : dalloc(&d.half, s->uses_list ? n : 1);
+  rc = rc ? rc : dalloc(&d.half2, s->nstages > 2 ? n : 1);
+  rc = rc ? rc : dalloc(&d.theta, n);
+  rc = rc ? rc : dalloc(&d.img, n);
+  rc = rc ? rc : dalloc(&d.id, n);
+  rc = rc ? rc : dalloc(&d.kacc, s->nstages > 2 ? n : 1);
+  rc = rc ? rc : dalloc(&d.ref, n);
+  rc = rc ? rc : dalloc(&d.pos_alt, n);
+  rc = rc ? rc : dalloc(&d.theta_alt, n);
+  rc = rc ? rc : dalloc(&d.img_alt, n);
+  rc = rc ? rc : dalloc(&d.id_alt, n);
+  rc = rc ? rc : dalloc(&d.key, n);
+  rc = rc ? rc : dalloc(&d.rank, n);
+  rc = rc ? rc : dalloc(&d.cell_count, d.n_keys);
+  rc = rc ? rc : dalloc(&d.cell_start, d.n_keys);
+  rc = rc ? rc : dalloc(&d.scan_tmp, nscan);
+  rc = rc ? rc : dalloc(&d.nn, n);
+  rc = rc ? rc : dalloc(&d.ctl, 1);
+  rc = rc ? rc : dalloc(&d.red, 4);
+  rc = rc ? rc : dalloc(&s->stage_x, n);
+  rc = rc ? rc : dalloc(&s->stage_y, n);
+  rc = rc ? rc : dalloc(&s->stage_t, n);
+  rc = rc ? rc : dalloc(&s->stage_img, n);
+  if (rc == SPP_OK && s->uses_list) rc = alloc_list(s, cap);
+  if (rc != SPP_OK) {
+    free_dev(s);
+    delete s;
+    return rc;
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMemset(d.ctl, 0, sizeof(Ctl));
+  if (e != cudaSuccess) {
+    free_dev(s);
+    delete s;
+    return fail(SPP_ERR_CUDA, std::string("stream/ctl setup: ") + cudaGetErrorString(e));
+  }
+  s->own_stream = true;
+  s->per_rebuild_kernels = 6;   /* bin_count, scan x3, scatter, build_list */
+  s->per_step_kernels = s->uses_list ? (s->nstages == 1 ? 2 : s->nstages) : 6;
+  *out = s;
+  return SPP_OK;
+}
+
+int spp_destroy(SppSystem* s) {
+  if (!s) return SPP_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  free_graphs(s);
+  free_dev(s);
+  if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+  if (s->side) cudaStreamDestroy(s->side);
+  delete s;
+  return SPP_OK;
+}
+
+int spp_set_stream(SppSystem* s, void* stream) {
+  if (!s) return fail(SPP_ERR_INVALID, "system is NULL");
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  free_graphs(s);
+  if (s->own_stream) cudaStreamDestroy(s->stream);
+  if (stream) {
+    s->stream = (cudaStream_t)stream;
+    s->own_stream = false;
+  } else {
+    CUDA_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    s->own_stream = true;
+  }
+  return SPP_OK;
+}
+
+int spp_upload_state(SppSystem* s, const float* x, const float* y, const float* theta,
+                     const int32_t* img_x, const int32_t* img_y, int n, int64_t step0) {
+  if (!s || !x || !y || !theta) return fail(SPP_ERR_INVALID, "NULL argument");
+  if (n != s->p.n) return fail(SPP_ERR_INVALID, "n differs from the system's particle count");
+  if (step0 < 0 || step0 > 0xffffffffLL) return fail(SPP_ERR_INVALID, "step0 out of range");
+  const float L = s->k.L;
+  for (int i = 0; i < n; ++i) {
+    if (!std::isfinite(x[i]) || !std::isfinite(y[i]) || !std::isfinite(theta[i]))
+      return fail(SPP_ERR_NUMERIC, "non-finite input at particle " + std::to_string(i));
+    if (x[i] < -L || x[i] >= L || y[i] < -L || y[i] >= L)
+      return fail(SPP_ERR_INVALID, "position outside [-L, L) at particle " + std::to_string(i));
+  }
+  size_t bytes = sizeof(float) * (size_t)n;
+  CUDA_TRY(cudaMemcpyAsync(s->stage_x, x, bytes, cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(s->stage_y, y, bytes, cudaMemcpyHostToDevice, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(s->stage_t, theta, bytes, cudaMemcpyHostToDevice, s->stream));
+  launch_init_state(s->k, s->d, s->stage_x, s->stage_y, s->stage_t, s->stream);
+  s->host_launches++;
+  if (img_x || img_y) {
+    std::vector<int2> img((size_t)n);
+    for (int i = 0; i < n; ++i) img[i] = make_int2(img_x ? img_x[i] : 0, img_y ? img_y[i] : 0);
+    CUDA_TRY(cudaMemcpyAsync(s->d.img, img.data(), sizeof(int2) * (size_t)n,
+                             cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+  }
+  Ctl c;
+  memset(&c, 0, sizeof(c));
+  c.step = (uint32_t)step0;
+  CUDA_TRY(cudaMemcpyAsync(s->d.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s->stream));
+  int rc = enqueue_rebuild(s, s->stream, &s->host_launches);
+  if (rc != SPP_OK) return rc;
+  s->direct_rebuilds++;
+  s->step0 = step0;
+  s->target_step = step0;
+  s->uploaded = true;
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return recover(s);
+}
+
+int spp_download_state(SppSystem* s, float* x, float* y, float* theta, int32_t* img_x,
+                       int32_t* img_y, int n) {
+  if (!s || !x || !y || !theta) return fail(SPP_ERR_INVALID, "NULL argument");
+  if (n != s->p.n) return fail(SPP_ERR_INVALID, "n differs from the system's particle count");
+  if (!s->uploaded) return fail(SPP_ERR_INVALID, "no state uploaded");
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  launch_gather_state(s->k, s->d, s->stage_x, s->stage_y, s->stage_t, s->stage_img, s->stream);
+  s->host_launches++;
+  size_t bytes = sizeof(float) * (size_t)n;
+  CUDA_TRY(cudaMemcpyAsync(x, s->stage_x, bytes, cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(y, s->stage_y, bytes, cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(theta, s->stage_t, bytes, cudaMemcpyDeviceToHost, s->stream));
+  if (img_x || img_y) {
+    std::vector<int2> img((size_t)n);
+    CUDA_TRY(cudaMemcpyAsync(img.data(), s->stage_img, sizeof(int2) * (size_t)n,
+                             cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    for (int i = 0; i < n; ++i) {
+      if (img_x) img_x[i] = img[i].x;
+      if (img_y) img_y[i] = img[i].y;
+    }
+  }
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return SPP_OK;
+}
+
+int spp_step(SppSystem* s, int nsteps) {
+  if (!s) return fail(SPP_ERR_INVALID, "system is NULL");
+  if (nsteps < 0) return fail(SPP_ERR_INVALID, "nsteps < 0");
+  if (!s->uploaded) return fail(SPP_ERR_INVALID, "no state uploaded");
+  if (s->target_step + nsteps > 0xffffffffLL) return fail(SPP_ERR_INVALID, "step counter overflow");
+  s->target_step += nsteps;
+  return run_steps(s, nsteps);
+}
+
+int spp_sync(SppSystem* s) {
+  if (!s) return fail(SPP_ERR_INVALID, "system is NULL");
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  CUDA_TRY(cudaGetLastError());
+  return recover(s);
+}
+
+int spp_observables(SppSystem* s, SppObservables* o) {
+  if (!s || !o) return fail(SPP_ERR_INVALID, "NULL argument");
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  CUDA_TRY(cudaMemsetAsync(s->d.red, 0, 2 * sizeof(double), s->stream));
+  launch_polarization(s->d, s->stream);
+  s->host_launches++;
+  long long sums[2];
+  CUDA_TRY(cudaMemcpyAsync(sums, s->d.red, sizeof(sums), cudaMemcpyDeviceToHost, s->stream));
+  Ctl c;
+  CUDA_TRY(cudaMemcpyAsync(&c, s->d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  const double inv = 1.0 / 4294967296.0;
+  memset(o, 0, sizeof(*o));
+  o->step = (int64_t)c.step - s->step0;
+  o->t = (double)o->step * s->p.dt;
+  o->px = (double)sums[0] * inv / s->p.n;
+  o->py = (double)sums[1] * inv / s->p.n;
+  o->polarization = std::sqrt(o->px * o->px + o->py * o->py);
+  o->n_rebuilds = c.n_rebuilds;
+  o->n = s->p.n;
+  o->list_capacity = s->d.cap;
+  o->max_neighbors = (int32_t)c.max_nn;
+  o->cells_per_side = s->d.D;
+  return SPP_OK;
+}
+
+int spp_pairs(SppSystem* s, double r, int32_t* pi, int32_t* pj, int cap, int64_t* n_pairs) {
+  if (!s || !n_pairs || (cap > 0 && (!pi || !pj))) return fail(SPP_ERR_INVALID, "NULL argument");
+  if (!s->uploaded) return fail(SPP_ERR_INVALID, "no state uploaded");
+  double width = 2.0 * s->p.L / s->d.D;
+  if (!(r > 0) || r > width) return fail(SPP_ERR_INVALID, "r must be in (0, cell width]");
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  rc = enqueue_rebuild(s, s->stream, &s->host_launches);  /* bin the current positions */
+  if (rc != SPP_OK) return rc;
+  s->direct_rebuilds++;
+  unsigned long long* counter = nullptr;
+  int32_t *dpi = nullptr, *dpj = nullptr;
+  rc = dalloc(&counter, 1);
+  if (rc == SPP_OK) rc = dalloc(&dpi, cap > 0 ? cap : 1);
+  if (rc == SPP_OK) rc = dalloc(&dpj, cap > 0 ? cap : 1);
+  if (rc == SPP_OK) {
+    cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s->stream);
+    launch_pairs_count(s->k, s->d, (float)(r * r), counter, dpi, dpj, cap, s->stream);
+    s->host_launches++;
+    unsigned long long total = 0;
+    cudaMemcpyAsync(&total, counter, sizeof(total), cudaMemcpyDeviceToHost, s->stream);
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess && cap > 0) {
+      size_t m = total < (unsigned long long)cap ? (size_t)total : (size_t)cap;
+      e = cudaMemcpy(pi, dpi, m * sizeof(int32_t), cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess) e = cudaMemcpy(pj, dpj, m * sizeof(int32_t), cudaMemcpyDeviceToHost);
+    }
+    if (e != cudaSuccess) rc = fail(SPP_ERR_CUDA, std::string("pairs: ") + cudaGetErrorString(e));
+    *n_pairs = (int64_t)total;
+  }
+  if (counter) cudaFree(counter);
+  if (dpi) cudaFree(dpi);
+  if (dpj) cudaFree(dpj);
+  return rc;
+}
+
+int spp_cells(SppSystem* s, int D, int rule, int32_t* cell_x, int32_t* cell_y, int n) {
+  if (!s || !cell_x || !cell_y) return fail(SPP_ERR_INVALID, "NULL argument");
+  if (n != s->p.n || D < 1 || (rule != SPP_BIN_GEOMETRIC && rule != SPP_BIN_REFERENCE))
+    return fail(SPP_ERR_INVALID, "bad n, D or rule");
+  if (!s->uploaded) return fail(SPP_ERR_INVALID, "no state uploaded");
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  int32_t *dx = nullptr, *dy = nullptr;
+  rc = dalloc(&dx, (size_t)n);
+  if (rc == SPP_OK) rc = dalloc(&dy, (size_t)n);
+  if (rc == SPP_OK) {
+    launch_cells(s->k, s->d, D, rule, dx, dy, s->stream);
+    s->host_launches++;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(cell_x, dx, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(cell_y, dy, sizeof(int32_t) * n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = fail(SPP_ERR_CUDA, std::string("cells: ") + cudaGetErrorString(e));
+  }
+  if (dx) cudaFree(dx);
+  if (dy) cudaFree(dy);
+  return rc;
+}
+
+int spp_profile(SppSystem* s, int nsteps, SppProfile* out) {
+  if (!s || !out || nsteps < 0) return fail(SPP_ERR_INVALID, "bad argument");
+  if (!s->uploaded) return fail(SPP_ERR_INVALID, "no state uploaded");
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  memset(out, 0, sizeof(*out));
+  const int per_step = s->uses_list ? s->nstages : 1;
+  const int nev = 2 * (nsteps * per_step + nsteps) + 2;
+  std::vector<cudaEvent_t> ev;
+  ev.reserve((size_t)nev);
+  auto mk = [&]() -> cudaEvent_t {
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    ev.push_back(e);
+    return e;
+  };
+  struct Span { cudaEvent_t a, b; int kind; };
+  std::vector<Span> spans;
+  cudaEvent_t first = mk();
+  CUDA_TRY(cudaEventRecord(first, s->stream));
+  for (int i = 0; i < nsteps && rc == SPP_OK; ++i) {
+    if (s->uses_list) {
+      for (int stage = 0; stage < s->nstages; ++stage) {
+        cudaEvent_t a = mk(), b = mk();
+        cudaEventRecord(a, s->stream);
+        launch_abp_stage(s->k, s->d, stage, s->nstages, 0, 0, s->stream, &s->host_launches);
+        cudaEventRecord(b, s->stream);
+        spans.push_back({a, b, 0});
+      }
+      Ctl c;
+      rc = read_ctl(s, &c);
+      if (rc == SPP_OK && c.need_rebuild) {
+        cudaEvent_t a = mk(), b = mk();
+        cudaEventRecord(a, s->stream);
+        rc = enqueue_rebuild(s, s->stream, &s->host_launches);
+        cudaEventRecord(b, s->stream);
+        spans.push_back({a, b, 1});
+        s->direct_rebuilds++;
+      }
+    } else {
+      cudaEvent_t a = mk(), b = mk();
+      cudaEventRecord(a, s->stream);
+      rc = enqueue_step(s, s->stream, false, &s->host_launches);
+      cudaEventRecord(b, s->stream);
+      spans.push_back({a, b, 0});
+    }
+    s->target_step += 1;
+  }
+  cudaEvent_t last = mk();
+  cudaEventRecord(last, s->stream);
+  cudaError_t e = cudaStreamSynchronize(s->stream);
+  if (rc == SPP_OK && e != cudaSuccess) rc = fail(SPP_ERR_CUDA, cudaGetErrorString(e));
+  if (rc == SPP_OK) {
+    for (auto& sp : spans) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, sp.a, sp.b);
+      if (sp.kind == 0) { out->stage_ms += ms; out->stage_launches++; }
+      else { out->rebuild_ms += ms; out->rebuilds++; }
+    }
+    float tot = 0;
+    cudaEventElapsedTime(&tot, first, last);
+    out->total_ms = tot;
+    out->steps = nsteps;
+  }
+  for (auto x : ev) cudaEventDestroy(x);
+  return rc;
+}
+
+int spp_time_steps(SppSystem* s, int nsteps, double* ms) {
+  if (!s || !ms) return fail(SPP_ERR_INVALID, "NULL argument");
+  cudaEvent_t a, b;
+  CUDA_TRY(cudaEventCreate(&a));
+  CUDA_TRY(cudaEventCreate(&b));
+  cudaEventRecord(a, s->stream);
+  int rc = spp_step(s, nsteps);
+  cudaEventRecord(b, s->stream);
+  cudaError_t e = cudaEventSynchronize(b);
+  float t = 0;
+  if (rc == SPP_OK && e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc != SPP_OK) return rc;
+  if (e != cudaSuccess) return fail(SPP_ERR_CUDA, cudaGetErrorString(e));
+  *ms = t;
+  return spp_sync(s);
+}
+
+int64_t spp_kernel_launches(SppSystem* s) {
+  if (!s) return 0;
+  Ctl c;
+  if (read_ctl(s, &c) != SPP_OK) return -1;
+  int64_t graph_rebuilds = (int64_t)c.n_rebuilds - s->direct_rebuilds;
+  if (graph_rebuilds < 0) graph_rebuilds = 0;
+  return s->host_launches + s->graph_kernels + graph_rebuilds * s->per_rebuild_kernels;
+}
+
+void* spp_stream(SppSystem* s) { return s ? (void*)s->stream : nullptr; }
+
+}  // extern "C"

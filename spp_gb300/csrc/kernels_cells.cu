@@ -1,0 +1,324 @@
+/*
+ * kernels_cells.cu -- cell binning and neighbour lists on sm_103a.
+ *
+ * Replaces Box::Update_Cells (serial/box.h:107-134, parallel/node.h:710-911)
+ * and Box::Update_Neighbor_List (serial/box.h:137-179, shared/cell.h:74-103).
+ * The reference pushes particle ids into a vector<int> per cell and keeps a
+ * half Verlet list per particle, rebuilt every cell_update_period steps.
+ * Here:
+ *   1. bin_count: one thread per particle computes its cell's Morton key and
+ *      takes a slot in that cell with one atomicAdd per group of lanes
+ *      sharing the key (__match_any_sync warp aggregation).
+ *   2. scan: exclusive prefix sum of the per-key counts (three passes).
+ *   3. scatter: every particle's state moves to its cell-ordered slot, so
+ *      that spatial neighbours are neighbours in memory (Morton order keeps
+ *      2-D tiles of cells contiguous).
+ *   4. build_list: one thread per particle scans the 3x3 cells around it and
+ *      records every particle within r_list = r_cut + skin (full list: each
+ *      pair appears in both particles' lists, so the force kernels gather
+ *      without atomics), column-major nbr[slot * n + i].
+ * Order inside a cell depends on atomic arrival order and is therefore not
+ * deterministic; the force sums are order-independent fixed point, so the
+ * physics is unaffected.
+ */
+#include "spp_internal.cuh"
+
+namespace {
+
+__device__ __forceinline__ uint32_t cell_key(const SppConsts& k, const DevState& d, float x, float y,
+                                             int* cx, int* cy) {
+  *cx = spp_cell_coord(x, k.L, k.L2, d.D, SPP_BIN_GEOMETRIC);
+  *cy = spp_cell_coord(y, k.L, k.L2, d.D, SPP_BIN_GEOMETRIC);
+  return spp_morton((uint32_t)*cx, (uint32_t)*cy);
+}
+
+__global__ void __launch_bounds__(SPP_BLOCK) k_bin_count(SppConsts k, DevState d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  if (d.ctl->frozen) return;
+  float4 p = d.pos[i];
+  int cx, cy;
+  uint32_t key = cell_key(k, d, p.x, p.y, &cx, &cy);
+  unsigned mask = __activemask();
+  unsigned peers = __match_any_sync(mask, key);
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(&d.cell_count[key], (uint32_t)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  d.key[i] = key;
+  d.rank[i] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
+/* ---- exclusive scan of cell_count into cell_start ---------------------- */
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_PER_THREAD = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER_THREAD;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v) {
+  __shared__ uint32_t warp_sums[32];
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int nwarps = (int)(blockDim.x >> 5);
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) warp_sums[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < nwarps ? warp_sums[lane] : 0u;
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    warp_sums[lane] = wi - w; /* exclusive prefix of the warp sums */
+  }
+  __syncthreads();
+  return incl - v + warp_sums[warp];
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t* __restrict__ in,
+                                                              uint32_t n, uint32_t* block_sums) {
+  uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+  uint32_t s = 0;
+#pragma unroll
+  for (int q = 0; q < SCAN_PER_THREAD; ++q)
+    if (base + q < n) s += in[base + q];
+  s = __reduce_add_sync(0xffffffffu, s);
+  __shared__ uint32_t ws[SCAN_THREADS / 32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    uint32_t t = ws[threadIdx.x];
+    t = __reduce_add_sync(0xffffffffu, t);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = t;
+  }
+}
+
+/* Exclusive scan of at most SCAN_TILE block sums, in place (one block). */
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_top(uint32_t* sums, uint32_t nb) {
+  uint32_t v[SCAN_PER_THREAD];
+  uint32_t base = threadIdx.x * SCAN_PER_THREAD;
+  uint32_t local = 0;
+#pragma unroll
+  for (int q = 0; q < SCAN_PER_THREAD; ++q) {
+    v[q] = (base + q < nb) ? sums[base + q] : 0u;
+    local += v[q];
+  }
+  uint32_t excl = block_exclusive_scan(local);
+#pragma unroll
+  for (int q = 0; q < SCAN_PER_THREAD; ++q) {
+    if (base + q < nb) sums[base + q] = excl;
+    excl += v[q];
+  }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t* __restrict__ in,
+                                                             uint32_t n,
+                                                             const uint32_t* __restrict__ block_offs,
+                                                             uint32_t* __restrict__ out) {
+  uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+  uint32_t v[SCAN_PER_THREAD];
+  uint32_t local = 0;
+#pragma unroll
+  for (int q = 0; q < SCAN_PER_THREAD; ++q) {
+    v[q] = (base + q < n) ? in[base + q] : 0u;
+    local += v[q];
+  }
+  uint32_t excl = block_exclusive_scan(local) + block_offs[blockIdx.x];
+#pragma unroll
+  for (int q = 0; q < SCAN_PER_THREAD; ++q) {
+    if (base + q < n) out[base + q] = excl;
+    excl += v[q];
+  }
+}
+
+__global__ void __launch_bounds__(SPP_BLOCK) k_scatter(DevState d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  if (d.ctl->frozen) return;
+  uint32_t dst = d.cell_start[d.key[i]] + d.rank[i];
+  d.pos_alt[dst] = d.pos[i];
+  d.theta_alt[dst] = d.theta[i];
+  d.img_alt[dst] = d.img[i];
+  d.id_alt[dst] = d.id[i];
+}
+
+/* Verlet list from the cell-ordered copy (alt), then the copy moves back
+ * into the primary arrays. with_list == 0 only copies (no list). */
+__global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState d, int with_list) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t cnt = 0;
+  if (i < d.n && !d.ctl->frozen) {
+    float4 p = d.pos_alt[i];
+    if (with_list) {
+      int cx, cy;
+      cell_key(k, d, p.x, p.y, &cx, &cy);
+      const int D = d.D;
+      for (int oy = -1; oy <= 1; ++oy) {
+        int ny = cy + oy;
+        ny = ny < 0 ? ny + D : (ny >= D ? ny - D : ny);
+        for (int ox = -1; ox <= 1; ++ox) {
+          int nx = cx + ox;
+          nx = nx < 0 ? nx + D : (nx >= D ? nx - D : nx);
+          uint32_t kk = spp_morton((uint32_t)nx, (uint32_t)ny);
+          uint32_t s0 = d.cell_start[kk], c = d.cell_count[kk];
+          for (uint32_t j = s0; j < s0 + c; ++j) {
+            if ((int)j == i) continue;
+            float4 q = d.pos_alt[j];
+            float dx, dy;
+            float d2 = spp_sep(&k, p.x, p.y, q.x, q.y, &dx, &dy);
+            if (d2 < k.rlist2) {
+              if (cnt < (uint32_t)d.cap) d.nbr[(size_t)cnt * d.n + i] = (int32_t)j;
+              ++cnt;
+            }
+          }
+        }
+      }
+      d.nn[i] = (int32_t)(cnt < (uint32_t)d.cap ? cnt : (uint32_t)d.cap);
+      d.ref[i] = make_float2(p.x, p.y);
+    }
+    d.pos[i] = p;
+    d.theta[i] = d.theta_alt[i];
+    d.img[i] = d.img_alt[i];
+    d.id[i] = d.id_alt[i];
+  }
+  if (with_list) {
+    uint32_t m = __reduce_max_sync(0xffffffffu, cnt);
+    if ((threadIdx.x & 31) == 0 && m > 0) {
+      atomicMax(&d.ctl->max_nn, m);
+      if (m > (uint32_t)d.cap) {
+        atomicMax(&d.ctl->list_need, m);
+        atomicExch(&d.ctl->frozen, 1u);
+      }
+    }
+  }
+  if (i == 0) atomicAdd(&d.ctl->n_rebuilds, 1u);
+}
+
+/* Unique pairs (by particle id) within r, through the cell list. */
+__global__ void __launch_bounds__(SPP_BLOCK) k_pairs(SppConsts k, DevState d, float r2,
+                                                     unsigned long long* counter, int32_t* pi,
+                                                     int32_t* pj, long long cap) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  float4 p = d.pos[i];
+  uint32_t idi = d.id[i];
+  int cx, cy;
+  cell_key(k, d, p.x, p.y, &cx, &cy);
+  const int D = d.D;
+  for (int oy = -1; oy <= 1; ++oy) {
+    int ny = (cy + oy + D) % D;
+    for (int ox = -1; ox <= 1; ++ox) {
+      int nx = (cx + ox + D) % D;
+      uint32_t kk = spp_morton((uint32_t)nx, (uint32_t)ny);
+      uint32_t s0 = d.cell_start[kk], c = d.cell_count[kk];
+      for (uint32_t j = s0; j < s0 + c; ++j) {
+        uint32_t idj = d.id[j];
+        if (idj <= idi) continue;
+        float4 q = d.pos[j];
+        float dx, dy;
+        if (spp_sep(&k, p.x, p.y, q.x, q.y, &dx, &dy) < r2) {
+          unsigned long long slot = atomicAdd(counter, 1ull);
+          if ((long long)slot < cap) {
+            pi[slot] = (int32_t)idi;
+            pj[slot] = (int32_t)idj;
+          }
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_cells(SppConsts k, DevState d, int D, int rule, int32_t* cx, int32_t* cy) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  float4 p = d.pos[i];
+  uint32_t id = d.id[i];
+  cx[id] = spp_cell_coord(p.x, k.L, k.L2, D, rule);
+  cy[id] = spp_cell_coord(p.y, k.L, k.L2, D, rule);
+}
+
+__global__ void k_init_state(DevState d, const float* __restrict__ x, const float* __restrict__ y,
+                             const float* __restrict__ th) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  float s, c;
+  spp_sincosf(th[i], &s, &c);
+  d.pos[i] = make_float4(x[i], y[i], c, s);
+  d.theta[i] = th[i];
+  d.img[i] = make_int2(0, 0);
+  d.id[i] = (uint32_t)i;
+}
+
+__global__ void k_gather_state(DevState d, float* x, float* y, float* th, int2* img) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  uint32_t id = d.id[i];
+  float4 p = d.pos[i];
+  x[id] = p.x;
+  y[id] = p.y;
+  th[id] = d.theta[i];
+  img[id] = d.img[i];
+}
+
+inline int blocks_for(int n, int b = SPP_BLOCK) { return (n + b - 1) / b; }
+
+}  // namespace
+
+void launch_bin_count(const SppConsts& k, const DevState& d, cudaStream_t s, int64_t* launches) {
+  if (d.n == 0) return;
+  k_bin_count<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(k, d);
+  if (launches) *launches += 1;
+}
+
+void launch_scan(const DevState& d, cudaStream_t s, int64_t* launches) {
+  uint32_t nb = (d.n_keys + SCAN_TILE - 1) / SCAN_TILE;
+  k_scan_reduce<<<nb, SCAN_THREADS, 0, s>>>(d.cell_count, d.n_keys, d.scan_tmp);
+  k_scan_top<<<1, SCAN_THREADS, 0, s>>>(d.scan_tmp, nb);
+  k_scan_apply<<<nb, SCAN_THREADS, 0, s>>>(d.cell_count, d.n_keys, d.scan_tmp, d.cell_start);
+  if (launches) *launches += 3;
+}
+
+void launch_scatter(const DevState& d, cudaStream_t s, int64_t* launches) {
+  if (d.n == 0) return;
+  k_scatter<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(d);
+  if (launches) *launches += 1;
+}
+
+void launch_build_list(const SppConsts& k, const DevState& d, int with_list, cudaStream_t s,
+                       int64_t* launches) {
+  if (d.n == 0) return;
+  k_build_list<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(k, d, with_list);
+  if (launches) *launches += 1;
+}
+
+void launch_pairs_count(const SppConsts& k, const DevState& d, float r2, unsigned long long* counter,
+                        int32_t* pi, int32_t* pj, long long cap, cudaStream_t s) {
+  if (d.n == 0) return;
+  k_pairs<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(k, d, r2, counter, pi, pj, cap);
+}
+
+void launch_cells(const SppConsts& k, const DevState& d, int D, int rule, int32_t* cx, int32_t* cy,
+                  cudaStream_t s) {
+  if (d.n == 0) return;
+  k_cells<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(k, d, D, rule, cx, cy);
+}
+
+void launch_init_state(const SppConsts& k, const DevState& d, const float* x, const float* y,
+                       const float* th, cudaStream_t s) {
+  (void)k;
+  if (d.n == 0) return;
+  k_init_state<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(d, x, y, th);
+}
+
+void launch_gather_state(const SppConsts& k, const DevState& d, float* x, float* y, float* th,
+                         int2* img, cudaStream_t s) {
+  (void)k;
+  if (d.n == 0) return;
+  k_gather_state<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(d, x, y, th, img);
+}

@@ -1,0 +1,244 @@
+/*
+ * kernels_step.cu -- force sums fused with the integrator stage, on sm_103a.
+ *
+ * k_abp_stage replaces one Runge-Kutta stage of the reference's step, i.e.
+ * Box::Interact (serial/box.h:322-371) followed by Box::Move_Runge_Kutta*_k
+ * (serial/box.h:380-424 -> RepulsiveParticle::Move_Runge_Kutta{2,4}_k,
+ * shared/particle.h:589-726), in one pass: one thread per particle (cell
+ * order) gathers its Verlet neighbours' float4 (x, y, cos, sin) state,
+ * accumulates force, torque and neighbour count in int64 fixed point, and
+ * writes its stage state.  The last stage also
+ *   - advances theta / image counters in place,
+ *   - reduces the largest squared displacement since the last list build,
+ *   - and, in the block that finishes last, decides whether the list must be
+ *     rebuilt (max displacement > skin/2), sets the CUDA-graph conditional
+ *     that gates the rebuild nodes, and advances the step counter.
+ * The reference rebuilds cells after a fixed number of steps
+ * (cell_update_period, parallel/box.h:432-438); the displacement trigger
+ * rebuilds only when a pair could otherwise be missed.
+ *
+ * k_vicsek_step replaces VicsekParticle{,2}::Interact/Move
+ * (shared/particle.h:145-247) and the configured arg-sum rule, reading the
+ * cell-ordered copy and visiting the 3x3 cells directly (the cell list is
+ * rebuilt every step at dt = 1).
+ */
+#include "spp_internal.cuh"
+
+namespace {
+
+struct StageBufs {
+  const float4* cur;   /* state the forces are evaluated on */
+  float4* out;         /* stage output (pos for the last stage) */
+  int stage, nstages;
+};
+
+__device__ __forceinline__ void finish_step(const SppConsts& k, const DevState& d, float my_max,
+                                            cudaGraphConditionalHandle cond, int use_cond,
+                                            int advance) {
+  __shared__ float warp_max[SPP_BLOCK / 32];
+  __shared__ int is_last;
+  float m = my_max;
+  m = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(m)));
+  if ((threadIdx.x & 31) == 0) warp_max[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float bm = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) bm = fmaxf(bm, warp_max[w]);
+    if (bm > 0.0f) atomicMax(&d.ctl->dmax2_bits, __float_as_uint(bm));
+    __threadfence();
+    unsigned prev = atomicAdd(&d.ctl->blocks_done, 1u);
+    is_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (is_last && threadIdx.x == 0) {
+    __threadfence();
+    volatile Ctl* c = d.ctl;
+    float dm = __uint_as_float(c->dmax2_bits);
+    unsigned rebuild = (advance && !c->frozen && dm > k.trigger2) ? 1u : 0u;
+    c->need_rebuild = rebuild;
+    c->dmax2_bits = 0u;
+    c->blocks_done = 0u;
+    if (advance && !c->frozen) c->step = c->step + 1u;
+    if (use_cond) cudaGraphSetConditional(cond, rebuild);
+  }
+}
+
+__global__ void __launch_bounds__(SPP_BLOCK) k_abp_stage(SppConsts k, DevState d, StageBufs b,
+                                                         cudaGraphConditionalHandle cond,
+                                                         int use_cond) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int last = (b.stage == b.nstages - 1);
+  const int frozen = d.ctl->frozen;
+  float disp2 = 0.0f;
+  if (i < d.n && !frozen) {
+    const uint32_t step = d.ctl->step;
+    const float4 pi = b.cur[i];
+    SppAcc a;
+    spp_acc_zero(&a);
+    const int cnt = d.nn[i];
+    const int32_t* __restrict__ nb = d.nbr + i;
+    for (int q = 0; q < cnt; ++q) {
+      const int j = __ldg(nb + (size_t)q * d.n);
+      const float4 pj = __ldg(b.cur + j);
+      spp_pair_abp(&k, &a, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
+    }
+    if (a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
+    float fx, fy, tau;
+    spp_abp_forces(&k, &a, pi.z, pi.w, &fx, &fy, &tau);
+    const float dth = spp_rot_noise(&k, d.id[i], step);
+    const float4 p0 = (b.stage == 0) ? pi : d.pos[i];
+    const float th0 = d.theta[i];
+    float nx, ny, nt, nc, ns;
+    int gx = 0, gy = 0;
+    if (b.nstages == 1) {
+      spp_euler_update(p0.x, p0.y, th0, fx, fy, tau, dth, &k, &nx, &ny, &nt, &nc, &ns, &gx, &gy);
+    } else {
+      float h, frac;
+      if (b.nstages == 2) {
+        h = b.stage == 0 ? k.half_dt : k.dt;
+        frac = b.stage == 0 ? 0.5f : 1.0f;
+      } else {
+        if (b.stage == 0) {
+          d.kacc[i] = make_float4(fx, fy, tau, 0.0f);
+        } else if (b.stage < 3) {
+          float4 ka = d.kacc[i];
+          d.kacc[i] = make_float4(ka.x + 2.0f * fx, ka.y + 2.0f * fy, ka.z + 2.0f * tau, 0.0f);
+        } else {
+          float4 ka = d.kacc[i];
+          fx = ka.x + fx; fy = ka.y + fy; tau = ka.z + tau;
+        }
+        h = b.stage < 2 ? k.half_dt : (b.stage == 2 ? k.dt : k.dt6);
+        frac = b.stage < 2 ? 0.5f : 1.0f;
+      }
+      spp_stage_update(h, frac, p0.x, p0.y, th0, fx, fy, tau, dth, &k, &nx, &ny, &nt, &nc, &ns,
+                       &gx, &gy);
+    }
+    b.out[i] = make_float4(nx, ny, nc, ns);
+    if (last) {
+      d.theta[i] = nt;
+      if (gx | gy) {
+        int2 g = d.img[i];
+        d.img[i] = make_int2(g.x + gx, g.y + gy);
+      }
+      const float2 r = d.ref[i];
+      float ddx, ddy;
+      disp2 = spp_sep(&k, nx, ny, r.x, r.y, &ddx, &ddy);
+    }
+  }
+  if (last) finish_step(k, d, disp2, cond, use_cond, 1);
+}
+
+__global__ void __launch_bounds__(SPP_BLOCK) k_vicsek_step(SppConsts k, DevState d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < d.n) {
+    const uint32_t step = d.ctl->step;
+    const float4 p = d.pos_alt[i];
+    const float th0 = d.theta_alt[i];
+    const uint32_t id = d.id_alt[i];
+    const int cx = spp_cell_coord(p.x, k.L, k.L2, d.D, SPP_BIN_GEOMETRIC);
+    const int cy = spp_cell_coord(p.y, k.L, k.L2, d.D, SPP_BIN_GEOMETRIC);
+    const int D = d.D;
+    const int need_theta = (k.model == SPP_MODEL_VICSEK_REF_ANGLE);
+    SppAcc a;
+    spp_acc_zero(&a);
+    for (int oy = -1; oy <= 1; ++oy) {
+      int ny = cy + oy;
+      ny = ny < 0 ? ny + D : (ny >= D ? ny - D : ny);
+      for (int ox = -1; ox <= 1; ++ox) {
+        int nx = cx + ox;
+        nx = nx < 0 ? nx + D : (nx >= D ? nx - D : nx);
+        const uint32_t kk = spp_morton((uint32_t)nx, (uint32_t)ny);
+        const uint32_t s0 = d.cell_start[kk], c = d.cell_count[kk];
+        for (uint32_t j = s0; j < s0 + c; ++j) {
+          const float4 q = __ldg(d.pos_alt + j);
+          const float thj = need_theta ? d.theta_alt[j] : 0.0f;
+          spp_pair_vicsek(&k, &a, p.x, p.y, q.x, q.y, q.z, q.w, thj, (int)j == i);
+        }
+      }
+    }
+    if (a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
+    const spp_u32x4 r = spp_draw(k.seed, k.system, id, step, SPP_RNG_VICSEK);
+    float x, y, t, c, s;
+    int gx = 0, gy = 0;
+    spp_vicsek_update(&k, &a, p.x, p.y, th0, p.z, p.w, r.v[0], &x, &y, &t, &c, &s, &gx, &gy);
+    d.pos[i] = make_float4(x, y, c, s);
+    d.theta[i] = t;
+    int2 g = d.img_alt[i];
+    d.img[i] = make_int2(g.x + gx, g.y + gy);
+    d.id[i] = id;
+  }
+  finish_step(k, d, 0.0f, 0, 0, 1);
+}
+
+/* Euler writes its new state to the half buffer (neighbours read pos during
+ * the stage); this commits it. */
+__global__ void __launch_bounds__(SPP_BLOCK) k_commit(DevState d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < d.n && !d.ctl->frozen) d.pos[i] = d.half[i];
+}
+
+/* Sum of (cos, sin) over all particles in int64 fixed point: exact, hence
+ * independent of the particle order (Node::Compute_Polarization,
+ * parallel/node.h:1565-1591, replaces its MPI_Reduce). */
+__global__ void __launch_bounds__(SPP_BLOCK) k_polarization(DevState d, unsigned long long* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  long long sx = 0, sy = 0;
+  if (i < d.n) {
+    const float4 p = d.pos[i];
+    sx = spp_to_fx(p.z);
+    sy = spp_to_fx(p.w);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sx += __shfl_down_sync(0xffffffffu, sx, o);
+    sy += __shfl_down_sync(0xffffffffu, sy, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&out[0], (unsigned long long)sx);
+    atomicAdd(&out[1], (unsigned long long)sy);
+  }
+}
+
+inline int blocks_for(int n) { return (n + SPP_BLOCK - 1) / SPP_BLOCK; }
+
+}  // namespace
+
+void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nstages,
+                      cudaGraphConditionalHandle cond, int use_cond, cudaStream_t s,
+                      int64_t* launches) {
+  StageBufs b;
+  b.stage = stage;
+  b.nstages = nstages;
+  if (nstages == 1) {
+    b.cur = d.pos; b.out = d.half;
+  } else if (nstages == 2) {
+    b.cur = stage == 0 ? d.pos : d.half;
+    b.out = stage == 0 ? d.half : d.pos;
+  } else {
+    static const int cur_sel[4] = {0, 1, 2, 1};   /* pos, half, half2, half */
+    static const int out_sel[4] = {1, 2, 1, 0};
+    float4* bufs[3] = {d.pos, d.half, d.half2};
+    b.cur = bufs[cur_sel[stage]];
+    b.out = bufs[out_sel[stage]];
+  }
+  int nb = blocks_for(d.n);
+  if (nb == 0) nb = 1;
+  k_abp_stage<<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond);
+  if (launches) *launches += 1;
+  if (nstages == 1) {
+    k_commit<<<nb, SPP_BLOCK, 0, s>>>(d);
+    if (launches) *launches += 1;
+  }
+}
+
+void launch_vicsek_step(const SppConsts& k, const DevState& d, cudaStream_t s, int64_t* launches) {
+  int nb = blocks_for(d.n);
+  if (nb == 0) nb = 1;
+  k_vicsek_step<<<nb, SPP_BLOCK, 0, s>>>(k, d);
+  if (launches) *launches += 1;
+}
+
+void launch_polarization(const DevState& d, cudaStream_t s) {
+  if (d.n == 0) return;
+  k_polarization<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(d, reinterpret_cast<unsigned long long*>(d.red));
+}

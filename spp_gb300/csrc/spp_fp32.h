@@ -1,0 +1,305 @@
+/*
+ * spp_fp32.h -- the arithmetic contract shared by the sm_103a kernels and any
+ * CPU code that must reproduce them bit for bit.
+ *
+ * Everything here is a pure function of its arguments and compiles both as
+ * CUDA device code (nvcc, -fmad=false) and as plain C99 (gcc,
+ * -ffp-contract=off).  Fused multiply-adds appear only where written as
+ * fmaf(), division and sqrtf() are IEEE correctly rounded on both sides, so
+ * a CPU build of these functions returns the same bits as the GPU.
+ *
+ * Contents
+ *   - Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw,
+ *     "Parallel random numbers: as easy as 1, 2, 3", SC'11).  It replaces
+ *     the single global GSL generator of the reference (shared/c2dvector.h:
+ *     15-25, 134-144): a draw is a function of (seed, system, particle id,
+ *     step, stream), so it does not depend on the order particles are
+ *     visited in.
+ *   - uniform / Gaussian mappings standing in for gsl_ran_flat and
+ *     gsl_ran_gaussian (shared/particle.h:154, 568).
+ *   - FP32 sin/cos/atan2/log/exp: Cody-Waite range reduction plus
+ *     polynomials fitted by gen_fp32_poly.py (this directory).
+ *   - periodic wrap of angles and coordinates (shared/c2dvector.h:67-73,
+ *     shared/particle.h:599).
+ *   - fixed-point (int64, 2^-32 resolution) accumulation, which makes the
+ *     neighbour sums independent of summation order.
+ */
+#ifndef SPP_FP32_H
+#define SPP_FP32_H
+
+#include <stdint.h>
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define SPP_HD __host__ __device__ __forceinline__
+#else
+#define SPP_HD static inline
+#include <string.h>
+#endif
+
+/* ------------------------------------------------------------------ */
+/* bit casts                                                           */
+/* ------------------------------------------------------------------ */
+SPP_HD uint32_t spp_f2u(float f) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(f);
+#else
+  uint32_t u; memcpy(&u, &f, 4); return u;
+#endif
+}
+SPP_HD float spp_u2f(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float f; memcpy(&f, &u, 4); return f;
+#endif
+}
+
+/* ------------------------------------------------------------------ */
+/* Philox4x32-10                                                       */
+/* ------------------------------------------------------------------ */
+#define SPP_PHILOX_M0 0xD2511F53u
+#define SPP_PHILOX_M1 0xCD9E8D57u
+#define SPP_PHILOX_W0 0x9E3779B9u
+#define SPP_PHILOX_W1 0xBB67AE85u
+
+/* Stream tags: the third counter word separates independent uses. */
+#define SPP_RNG_ROT_NOISE   1u  /* rotational Gaussian noise, one per particle-step */
+#define SPP_RNG_VICSEK      2u  /* Vicsek angular noise xi ~ U[-pi,pi) */
+#define SPP_RNG_INIT_POS    3u  /* initial positions */
+#define SPP_RNG_INIT_ANGLE  4u  /* initial headings */
+#define SPP_RNG_TANGENT     5u  /* tangent-vector initialisation */
+#define SPP_RNG_TRANS_NOISE 6u  /* translational noise (ContinuousParticle Kamp) */
+#define SPP_RNG_SWEEP       7u  /* sweep parameter sampling */
+
+typedef struct { uint32_t v[4]; } spp_u32x4;
+
+SPP_HD void spp_mulhilo(uint32_t a, uint32_t b, uint32_t* hi, uint32_t* lo) {
+#if defined(__CUDA_ARCH__)
+  *hi = __umulhi(a, b);
+  *lo = a * b;
+#else
+  uint64_t p = (uint64_t)a * (uint64_t)b;
+  *hi = (uint32_t)(p >> 32);
+  *lo = (uint32_t)p;
+#endif
+}
+
+SPP_HD spp_u32x4 spp_philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                   uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0, lo0, hi1, lo1;
+    spp_mulhilo(SPP_PHILOX_M0, c0, &hi0, &lo0);
+    spp_mulhilo(SPP_PHILOX_M1, c2, &hi1, &lo1);
+    uint32_t n0 = hi1 ^ c1 ^ k0;
+    uint32_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += SPP_PHILOX_W0;
+    k1 += SPP_PHILOX_W1;
+  }
+  spp_u32x4 o; o.v[0] = c0; o.v[1] = c1; o.v[2] = c2; o.v[3] = c3;
+  return o;
+}
+
+/* Draw for (seed, system, particle id, step, stream). */
+SPP_HD spp_u32x4 spp_draw(uint64_t seed, uint32_t system, uint32_t pid, uint32_t step,
+                          uint32_t stream) {
+  return spp_philox4x32_10(pid, step, stream, system, (uint32_t)seed,
+                           (uint32_t)(seed >> 32));
+}
+
+/* 24-bit uniforms; both are exact in float and in double. */
+SPP_HD float spp_u01_f(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-08f; }       /* [0,1)  */
+SPP_HD float spp_u01_open0_f(uint32_t x) { return (float)((x >> 8) + 1u) * 5.9604644775390625e-08f; } /* (0,1] */
+SPP_HD double spp_u01_d(uint32_t x) { return (double)(x >> 8) * 5.9604644775390625e-08; }
+SPP_HD double spp_u01_open0_d(uint32_t x) { return (double)((x >> 8) + 1u) * 5.9604644775390625e-08; }
+
+/* ------------------------------------------------------------------ */
+/* constants and fitted coefficients (gen_fp32_poly.py)                */
+/* ------------------------------------------------------------------ */
+#define SPP_PI_F       3.14159265358979323846f
+#define SPP_TWO_PI_F   6.28318530717958647692f
+#define SPP_PIO2_F     1.57079632679489661923f
+#define SPP_PIO4_F     0.78539816339744830962f
+#define SPP_INV_2PI_F  0.15915494309189533577f
+#define SPP_2_OVER_PI_F 0.63661977236758134308f
+#define SPP_LOG2E_F    1.44269504088896340736f
+
+#define SPP_SIN_C0      -0.1666666716337204f
+#define SPP_SIN_C1     0.008333329111337662f
+#define SPP_SIN_C2  -0.00019839353626593947f
+#define SPP_SIN_C3    2.718452151384554e-06f
+#define SPP_COS_C0       0.0416666679084301f
+#define SPP_COS_C1   -0.0013888883404433727f
+#define SPP_COS_C2   2.4799463062663563e-05f
+#define SPP_COS_C3   -2.720596512517659e-07f
+#define SPP_ATAN_C0      -0.3333333432674408f
+#define SPP_ATAN_C1      0.19999994337558746f
+#define SPP_ATAN_C2     -0.14285436272621155f
+#define SPP_ATAN_C3       0.1110420972108841f
+#define SPP_ATAN_C4      -0.0899854525923729f
+#define SPP_ATAN_C5      0.06998246908187866f
+#define SPP_ATAN_C6    -0.038038525730371475f
+#define SPP_LOG_C0       0.6666666865348816f
+#define SPP_LOG_C1      0.40000319480895996f
+#define SPP_LOG_C2      0.28538140654563904f
+#define SPP_LOG_C3      0.23567897081375122f
+#define SPP_EXP_C0                      0.5f
+#define SPP_EXP_C1       0.1666666567325592f
+#define SPP_EXP_C2     0.041666269302368164f
+#define SPP_EXP_C3      0.00833342969417572f
+#define SPP_EXP_C4    0.0013946021208539605f
+#define SPP_EXP_C5   0.00019826495554298162f
+#define SPP_PIO2_HI 1.57080078125f
+#define SPP_PIO2_MID -4.453584551811218e-06f
+#define SPP_PIO2_LO -8.705516307827565e-10f
+#define SPP_LN2_HI 0.693115234375f
+#define SPP_LN2_LO 3.194618329871446e-05f
+
+/* ------------------------------------------------------------------ */
+/* sin / cos                                                           */
+/* ------------------------------------------------------------------ */
+/* Valid for |x| up to ~1e4 (three-part Cody-Waite reduction by pi/2). */
+SPP_HD void spp_sincosf(float x, float* s_out, float* c_out) {
+  float k = rintf(x * SPP_2_OVER_PI_F);
+  float r = fmaf(-k, SPP_PIO2_HI, x);
+  r = fmaf(-k, SPP_PIO2_MID, r);
+  r = fmaf(-k, SPP_PIO2_LO, r);
+  float z = r * r;
+  float ps = fmaf(fmaf(fmaf(SPP_SIN_C3, z, SPP_SIN_C2), z, SPP_SIN_C1), z, SPP_SIN_C0);
+  float s = fmaf(r * z, ps, r);
+  float pc = fmaf(fmaf(fmaf(SPP_COS_C3, z, SPP_COS_C2), z, SPP_COS_C1), z, SPP_COS_C0);
+  float c = fmaf(z * z, pc, fmaf(-0.5f, z, 1.0f));
+  int q = ((int)k) & 3;
+  float so, co;
+  if (q == 0) { so = s; co = c; }
+  else if (q == 1) { so = c; co = -s; }
+  else if (q == 2) { so = -s; co = -c; }
+  else { so = -c; co = s; }
+  *s_out = so;
+  *c_out = co;
+}
+SPP_HD float spp_cosf(float x) { float s, c; spp_sincosf(x, &s, &c); return c; }
+SPP_HD float spp_sinf(float x) { float s, c; spp_sincosf(x, &s, &c); return s; }
+
+/* ------------------------------------------------------------------ */
+/* atan2                                                               */
+/* ------------------------------------------------------------------ */
+/* Returns a value in [-pi, pi]; atan2(0, 0) returns 0. */
+SPP_HD float spp_atan2f(float y, float x) {
+  float ax = fabsf(x), ay = fabsf(y);
+  float mx = ax > ay ? ax : ay;
+  float mn = ax > ay ? ay : ax;
+  if (mx == 0.0f) return 0.0f;
+  float a = mn / mx;
+  float t, base;
+  if (a > 0.41421356237309503f) { t = (a - 1.0f) / (a + 1.0f); base = SPP_PIO4_F; }
+  else { t = a; base = 0.0f; }
+  float u = t * t;
+  float p = SPP_ATAN_C6;
+  p = fmaf(p, u, SPP_ATAN_C5);
+  p = fmaf(p, u, SPP_ATAN_C4);
+  p = fmaf(p, u, SPP_ATAN_C3);
+  p = fmaf(p, u, SPP_ATAN_C2);
+  p = fmaf(p, u, SPP_ATAN_C1);
+  p = fmaf(p, u, SPP_ATAN_C0);
+  float r = fmaf(t * u, p, t) + base;
+  if (ay > ax) r = SPP_PIO2_F - r;
+  if (x < 0.0f) r = SPP_PI_F - r;
+  if (y < 0.0f) r = -r;
+  return r;
+}
+
+/* ------------------------------------------------------------------ */
+/* log (argument > 0, normal) and exp (|x| < 80)                       */
+/* ------------------------------------------------------------------ */
+SPP_HD float spp_logf(float u) {
+  uint32_t b = spp_f2u(u);
+  int e = (int)(b >> 23) - 127;
+  float m = spp_u2f((b & 0x007fffffu) | 0x3f800000u);
+  if (m > 1.41421356237309505f) { m = m * 0.5f; e += 1; }
+  float s = (m - 1.0f) / (m + 1.0f);
+  float w = s * s;
+  float R = fmaf(fmaf(fmaf(SPP_LOG_C3, w, SPP_LOG_C2), w, SPP_LOG_C1), w, SPP_LOG_C0);
+  float lm = fmaf(s * w, R, 2.0f * s);
+  float fe = (float)e;
+  return fmaf(fe, SPP_LN2_HI, fmaf(fe, SPP_LN2_LO, lm));
+}
+
+SPP_HD float spp_expf(float x) {
+  float k = rintf(x * SPP_LOG2E_F);
+  float r = fmaf(-k, SPP_LN2_HI, x);
+  r = fmaf(-k, SPP_LN2_LO, r);
+  float p = SPP_EXP_C5;
+  p = fmaf(p, r, SPP_EXP_C4);
+  p = fmaf(p, r, SPP_EXP_C3);
+  p = fmaf(p, r, SPP_EXP_C2);
+  p = fmaf(p, r, SPP_EXP_C1);
+  p = fmaf(p, r, SPP_EXP_C0);
+  float e = fmaf(r * r, p, r) + 1.0f;
+  int ki = (int)k;
+  return e * spp_u2f((uint32_t)(ki + 127) << 23);
+}
+
+/* ------------------------------------------------------------------ */
+/* noise mappings                                                      */
+/* ------------------------------------------------------------------ */
+/* xi ~ U[-pi, pi): (2u-1) is exact, then one rounding for the product. */
+SPP_HD float spp_uniform_pm_pi_f(uint32_t x) {
+  float u = spp_u01_f(x);
+  return (2.0f * u - 1.0f) * SPP_PI_F;
+}
+/* Box-Muller: z = sqrt(-2 ln u1) cos(2 pi u2), u1 in (0,1], u2 in [0,1). */
+SPP_HD float spp_normal_f(uint32_t x0, uint32_t x1) {
+  float u1 = spp_u01_open0_f(x0);
+  float u2 = spp_u01_f(x1);
+  float rad = sqrtf(-2.0f * spp_logf(u1));
+  return rad * spp_cosf(u2 * SPP_TWO_PI_F);
+}
+
+/* ------------------------------------------------------------------ */
+/* periodic wraps                                                      */
+/* ------------------------------------------------------------------ */
+/* theta -> theta - 2 pi floor(theta / 2 pi + 1/2), as shared/particle.h:599. */
+SPP_HD float spp_wrap_angle_f(float th) {
+  float q = floorf(fmaf(th, SPP_INV_2PI_F, 0.5f));
+  return fmaf(-q, SPP_TWO_PI_F, th);
+}
+/* Coordinate in [-L, L) after a move of less than one box length.  The
+ * subtractions are exact (Sterbenz), so wrapping loses no bits; *img counts
+ * box crossings so that the unwrapped position is x + 2L * img. */
+SPP_HD float spp_wrap_coord_f(float x, float L, float L2, int* img) {
+  if (x >= L) { x -= L2; *img += 1; }
+  else if (x < -L) { x += L2; *img -= 1; }
+  return x;
+}
+/* Minimum image of a separation of two wrapped coordinates. */
+SPP_HD float spp_min_image_f(float d, float L, float L2) {
+  if (d >= L) d -= L2;
+  else if (d < -L) d += L2;
+  return d;
+}
+
+/* ------------------------------------------------------------------ */
+/* fixed-point accumulation                                            */
+/* ------------------------------------------------------------------ */
+#define SPP_FX_SCALE     4294967296.0f          /* 2^32  */
+#define SPP_FX_INV_SCALE 2.3283064365386963e-10f /* 2^-32 */
+#define SPP_FX_LIMIT     1073741824.0f          /* |term| must stay below 2^30 */
+
+SPP_HD int64_t spp_to_fx(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float2ll_rn(x * SPP_FX_SCALE);
+#else
+  return (int64_t)llrintf(x * SPP_FX_SCALE);
+#endif
+}
+SPP_HD float spp_from_fx(int64_t a) {
+#if defined(__CUDA_ARCH__)
+  return __ll2float_rn(a) * SPP_FX_INV_SCALE;
+#else
+  return (float)a * SPP_FX_INV_SCALE;
+#endif
+}
+
+#endif /* SPP_FP32_H */

@@ -1,0 +1,92 @@
+/*
+ * spp_internal.cuh -- device data layout and kernel entry points.
+ *
+ * HBM layout of one system (structure of arrays, all in cell order: particles
+ * are counting-sorted by the Morton key of their cell at every list rebuild):
+ *   pos     float4 (x, y, cos theta, sin theta)  read by neighbours, 16 B
+ *   half    float4 stage state of Runge-Kutta stages (RK4 ping-pongs with half2)
+ *   theta   float, img int2 (box crossings), id uint32 (slot -> particle id)
+ *   kacc    float4 RK4 slope accumulator (fx, fy, tau, -)
+ *   ref     float2 positions at the last neighbour-list build
+ *   nbr     int32 [cap][n] neighbour slots, column-major so that a warp's
+ *           32 consecutive particles read 128 contiguous bytes per list slot
+ *   nn      int32 list lengths
+ *   cell_count / cell_start  uint32 per Morton key
+ * A small control block (Ctl) in device memory carries the step counter and
+ * the device-side rebuild decision, so captured graphs replay without host
+ * round trips.
+ */
+#ifndef SPP_INTERNAL_CUH
+#define SPP_INTERNAL_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "spp_physics.h"
+
+#define SPP_BLOCK 256
+
+struct Ctl {
+  uint32_t step;          /* absolute step index (Philox counter word) */
+  uint32_t dmax2_bits;    /* max squared displacement since the last build (float bits) */
+  uint32_t blocks_done;   /* last-block detection */
+  uint32_t need_rebuild;  /* decision of the last step */
+  uint32_t list_need;     /* largest neighbour count met by a build (overflow if > cap) */
+  uint32_t fx_overflow;   /* a pair term left the fixed-point range */
+  uint32_t max_nn;        /* largest list length of the last build */
+  uint32_t n_rebuilds;
+  uint32_t frozen;        /* set on list overflow: later stages skip until the host recovers */
+  uint32_t pad[7];
+};
+
+struct DevState {
+  int n;
+  int cap;
+  int D;                  /* cells per side */
+  int morton_bits;
+  uint32_t n_keys;        /* 4^morton_bits */
+  float4* pos;
+  float4* half;
+  float4* half2;
+  float* theta;
+  int2* img;
+  uint32_t* id;
+  float4* kacc;
+  float2* ref;
+  float4* pos_alt;
+  float* theta_alt;
+  int2* img_alt;
+  uint32_t* id_alt;
+  uint32_t* key;
+  uint32_t* rank;
+  uint32_t* cell_count;
+  uint32_t* cell_start;
+  uint32_t* scan_tmp;     /* block sums of the scan */
+  int32_t* nbr;
+  int32_t* nn;
+  Ctl* ctl;
+  double* red;            /* reduction scratch (polarization) */
+};
+
+/* kernels_cells.cu */
+void launch_bin_count(const SppConsts& k, const DevState& d, cudaStream_t s, int64_t* launches);
+void launch_scan(const DevState& d, cudaStream_t s, int64_t* launches);
+void launch_scatter(const DevState& d, cudaStream_t s, int64_t* launches);
+void launch_build_list(const SppConsts& k, const DevState& d, int with_list, cudaStream_t s,
+                       int64_t* launches);
+void launch_pairs_count(const SppConsts& k, const DevState& d, float r2, unsigned long long* counter,
+                        int32_t* pi, int32_t* pj, long long cap, cudaStream_t s);
+void launch_cells(const SppConsts& k, const DevState& d, int D, int rule, int32_t* cx, int32_t* cy,
+                  cudaStream_t s);
+void launch_init_state(const SppConsts& k, const DevState& d, const float* x, const float* y,
+                       const float* th, cudaStream_t s);
+void launch_gather_state(const SppConsts& k, const DevState& d, float* x, float* y, float* th,
+                         int2* img, cudaStream_t s);
+
+/* kernels_step.cu */
+void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nstages,
+                      cudaGraphConditionalHandle cond, int use_cond, cudaStream_t s,
+                      int64_t* launches);
+void launch_vicsek_step(const SppConsts& k, const DevState& d, cudaStream_t s, int64_t* launches);
+void launch_polarization(const DevState& d, cudaStream_t s);
+
+#endif

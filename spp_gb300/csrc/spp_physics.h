@@ -1,0 +1,295 @@
+/*
+ * spp_physics.h -- per-pair and per-particle FP32 arithmetic of the step.
+ *
+ * Written once, compiled into the sm_103a kernels and into the CPU mirror
+ * (oracle/spp_mirror32.c), so that the mirror reproduces the kernels' bits
+ * and can prove that binning, neighbour lists, particle reordering and graph
+ * replay neither lose nor add anything.  Neighbour sums are accumulated in
+ * int64 fixed point (spp_fp32.h), so the result does not depend on the order
+ * the neighbours are visited in.
+ *
+ * All interactions are written in gather form (particle i sums the terms it
+ * receives from each neighbour j).  The reference visits every pair once and
+ * applies Newton's third law to both particles (shared/cell.h:112-128); the
+ * gather form computes the same sums without write conflicts between threads.
+ */
+#ifndef SPP_PHYSICS_H
+#define SPP_PHYSICS_H
+
+#include "spp_fp32.h"
+#include "../../include/spp.h"
+
+/* Constants of one system, rounded once from the double parameters. */
+typedef struct SppConsts {
+  int32_t model, integrator, force_law, align_mode;
+  uint64_t seed;
+  uint32_t system;
+  int32_t n;
+  float L, L2;                 /* half width, box length */
+  float dt, half_dt, dt6;
+  float v0, v0dt;
+  float sigma;                 /* rotational noise sqrt(2 Dr dt) */
+  float eta;
+  float g, g_over_area;        /* g / (pi R_a^2) */
+  float ral2;                  /* alignment radius squared */
+  float rrep2, inv_rrep, k_rep, sigma_rep, c13;
+  float one_minus_alpha_over_pi, alpha_over_pi;
+  float beta_push, r_push, rpush2;
+  float rlist, rlist2;         /* Verlet list radius */
+  float trigger2;              /* (skin/2)^2 with a small safety factor */
+} SppConsts;
+
+/* Host-side: round the double parameters to the kernels' floats. */
+static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
+  k->model = p->model; k->integrator = p->integrator;
+  k->force_law = p->force_law; k->align_mode = p->align_mode;
+  k->seed = p->seed; k->system = p->system_id; k->n = p->n;
+  k->L = (float)p->L; k->L2 = (float)(2.0 * p->L);
+  k->dt = (float)p->dt; k->half_dt = (float)(0.5 * p->dt); k->dt6 = (float)(p->dt / 6.0);
+  k->v0 = (float)p->v0; k->v0dt = (float)(p->v0 * p->dt);
+  k->sigma = (float)sqrt(2.0 * p->Dr * p->dt);
+  /* ContinuousParticle::Move (shared/particle.h:273-274) adds the Gaussian to
+   * the torque and multiplies the sum by dt, so its Euler noise is sigma * dt. */
+  if (p->model == SPP_MODEL_CONTINUOUS && p->integrator == SPP_INT_EULER)
+    k->sigma = (float)(sqrt(2.0 * p->Dr * p->dt) * p->dt);
+  k->eta = (float)p->eta;
+  k->g = (float)p->g;
+  k->g_over_area = p->r_align > 0 ? (float)(p->g / (3.14159265358979323846 * p->r_align * p->r_align)) : 0.0f;
+  k->ral2 = (float)(p->r_align * p->r_align);
+  if (p->force_law == SPP_FORCE_NONE || p->r_rep <= 0) {
+    k->rrep2 = 0.0f; k->inv_rrep = 0.0f;
+  } else {
+    k->rrep2 = (float)(p->r_rep * p->r_rep);
+    k->inv_rrep = (float)(1.0 / p->r_rep);
+  }
+  k->k_rep = (float)p->k_rep;
+  k->sigma_rep = (float)p->sigma_rep;
+  {
+    float q = (p->r_rep > 0) ? k->sigma_rep / (float)p->r_rep : 0.0f;
+    float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
+    k->c13 = (q8 * q4) * q;
+  }
+  k->one_minus_alpha_over_pi = (float)((1.0 - p->alpha) / 3.14159265358979323846);
+  k->alpha_over_pi = (float)(p->alpha / 3.14159265358979323846);
+  k->beta_push = (float)p->beta_push;
+  k->r_push = (float)p->r_push;
+  k->rpush2 = (float)(p->r_push * p->r_push);
+  {
+    double rc = p->r_align;
+    if (p->force_law != SPP_FORCE_NONE && p->r_rep > rc) rc = p->r_rep;
+    if (p->model == SPP_MODEL_VICSEK_REF_VECTOR && p->r_push > rc) rc = p->r_push;
+    double rl = rc + (p->skin > 0 ? p->skin : 0.0);
+    k->rlist = (float)rl;
+    k->rlist2 = (float)(rl * rl);
+    double half = 0.5 * (p->skin > 0 ? p->skin : 0.0) * 0.98;
+    k->trigger2 = (float)(half * half);
+  }
+}
+
+/* Accumulator for the sums particle i receives. */
+typedef struct SppAcc {
+  int64_t ax, ay;   /* force (ABP) or heading vector sum (Vicsek) */
+  int64_t at;       /* torque / angle sum */
+  int32_t cnt;      /* neighbours within the alignment radius (self excluded) */
+  int32_t ovf;      /* a term left the fixed-point range */
+} SppAcc;
+
+SPP_HD void spp_acc_zero(SppAcc* a) { a->ax = 0; a->ay = 0; a->at = 0; a->cnt = 0; a->ovf = 0; }
+
+SPP_HD int64_t spp_fx_guarded(float t, int32_t* ovf) {
+  if (!(fabsf(t) < SPP_FX_LIMIT)) { *ovf = 1; return 0; }
+  return spp_to_fx(t);
+}
+
+/* Minimum-image separation r_i - r_j and its squared length. */
+SPP_HD float spp_sep(const SppConsts* k, float xi, float yi, float xj, float yj, float* dx,
+                     float* dy) {
+  *dx = spp_min_image_f(xi - xj, k->L, k->L2);
+  *dy = spp_min_image_f(yi - yj, k->L, k->L2);
+  return fmaf(*dx, *dx, *dy * *dy);
+}
+
+/* RepulsiveParticle::Interact (shared/particle.h:728-757) / ContinuousParticle::
+ * Interact (:296-338), as received by i from j.  (c, s) = (cos, sin) theta. */
+SPP_HD void spp_pair_abp(const SppConsts* k, SppAcc* a, float xi, float yi, float ci, float si,
+                         float xj, float yj, float cj, float sj) {
+  float dx, dy;
+  float d2 = spp_sep(k, xi, yi, xj, yj, &dx, &dy);
+  if (d2 < k->rrep2 && d2 > 0.0f) {
+    float d = sqrtf(d2);
+    float t;
+    if (k->force_law == SPP_FORCE_HARMONIC) {
+      t = (k->k_rep * (1.0f - d * k->inv_rrep)) / d;
+    } else { /* R12_Repulsive_Truncated, shared/force-fields.h:14-39 */
+      float q = k->sigma_rep / d;
+      float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
+      float q13 = (q8 * q4) * q;
+      t = (k->k_rep * (q13 - k->c13)) / d;
+    }
+    a->ax += spp_fx_guarded(t * dx, &a->ovf);
+    a->ay += spp_fx_guarded(t * dy, &a->ovf);
+  }
+  if (d2 < k->ral2) {
+    a->cnt += 1;
+    float term = sj * ci - cj * si; /* sin(theta_j - theta_i) */
+    if (k->model == SPP_MODEL_CONTINUOUS) {
+      term = k->one_minus_alpha_over_pi * term;
+      if (k->alpha_over_pi != 0.0f && d2 > 0.0f) {
+        float d = sqrtf(d2);
+        term = term - (k->alpha_over_pi * (dx * si - dy * ci)) / d;
+      }
+    }
+    a->at += spp_to_fx(term);
+  }
+}
+
+/* Self-propulsion plus received force, and the torque (RepulsiveParticle::
+ * Reset :559-564 and the alignment normalisations). */
+SPP_HD void spp_abp_forces(const SppConsts* k, const SppAcc* a, float ci, float si, float* fx,
+                           float* fy, float* tau) {
+  *fx = k->v0 * ci + spp_from_fx(a->ax);
+  *fy = k->v0 * si + spp_from_fx(a->ay);
+  float S = spp_from_fx(a->at);
+  if (k->model == SPP_MODEL_CONTINUOUS) *tau = k->g * S;
+  else if (k->align_mode == SPP_ALIGN_MEAN) *tau = (k->g * S) / (float)(a->cnt + 1);
+  else *tau = S * k->g_over_area;
+}
+
+/* The rotational-noise increment of particle pid at a step. */
+SPP_HD float spp_rot_noise(const SppConsts* k, uint32_t pid, uint32_t step) {
+  spp_u32x4 d = spp_draw(k->seed, k->system, pid, step, SPP_RNG_ROT_NOISE);
+  return k->sigma * spp_normal_f(d.v[0], d.v[1]);
+}
+
+/* One Runge-Kutta stage update from the start-of-step state (x0, y0, th0):
+ *   th = wrap(th0 + h_t * tau + frac * dth),  x = wrap(x0 + h_x * fx).
+ * Move_Runge_Kutta2_1/2 (shared/particle.h:589-631) use (h, frac) =
+ * (dt/2, 1/2) then (dt, 1); RK4 (:633-726) uses (dt/2, 1/2), (dt/2, 1/2),
+ * (dt, 1) and finally dt/6 times the weighted sum of the four slopes. */
+SPP_HD void spp_stage_update(float h, float frac_noise, float x0, float y0, float th0, float fx,
+                             float fy, float tau, float dth, const SppConsts* k, float* x, float* y,
+                             float* th, float* c, float* s, int* imgx, int* imgy) {
+  float t = fmaf(h, tau, th0) + frac_noise * dth;
+  t = spp_wrap_angle_f(t);
+  spp_sincosf(t, s, c);
+  *th = t;
+  *x = spp_wrap_coord_f(fmaf(fx, h, x0), k->L, k->L2, imgx);
+  *y = spp_wrap_coord_f(fmaf(fy, h, y0), k->L, k->L2, imgy);
+}
+
+/* Euler move (RepulsiveParticle::Move, shared/particle.h:571-587): theta is
+ * not wrapped there. */
+SPP_HD void spp_euler_update(float x0, float y0, float th0, float fx, float fy, float tau, float dth,
+                             const SppConsts* k, float* x, float* y, float* th, float* c, float* s,
+                             int* imgx, int* imgy) {
+  float t = fmaf(k->dt, tau, th0) + dth;
+  spp_sincosf(t, s, c);
+  *th = t;
+  *x = spp_wrap_coord_f(fmaf(fx, k->dt, x0), k->L, k->L2, imgx);
+  *y = spp_wrap_coord_f(fmaf(fy, k->dt, y0), k->L, k->L2, imgy);
+}
+
+/* ------------------------------------------------------------------ */
+/* Vicsek family                                                       */
+/* ------------------------------------------------------------------ */
+/* Configured rule: sum e^{i theta_j} over |r_ij| < r, self included (the
+ * self term comes from the d2 = 0 visit of j = i). */
+SPP_HD void spp_pair_vicsek(const SppConsts* k, SppAcc* a, float xi, float yi, float xj, float yj,
+                            float cj, float sj, float thj, int self) {
+  float dx, dy;
+  float d2 = spp_sep(k, xi, yi, xj, yj, &dx, &dy);
+  if (k->model == SPP_MODEL_VICSEK) {
+    if (d2 < k->ral2) {
+      a->ax += spp_to_fx(cj);
+      a->ay += spp_to_fx(sj);
+      a->cnt += 1;
+    }
+    return;
+  }
+  if (self) return;
+  if (k->model == SPP_MODEL_VICSEK_REF_ANGLE) { /* VicsekParticle::Interact, particle.h:171-188 */
+    if (d2 < k->ral2) {
+      a->cnt += 1;
+      a->at += spp_fx_guarded(thj, &a->ovf);
+    }
+    return;
+  }
+  /* VicsekParticle2::Interact, particle.h:221-246 */
+  if (d2 < k->ral2) {
+    a->cnt += 1;
+    a->ax += spp_to_fx(cj);
+    a->ay += spp_to_fx(sj);
+    if (d2 < k->rpush2 && d2 > 0.0f) {
+      float d = sqrtf(d2);
+      float fa = k->beta_push / (1.0f + spp_expf(d / k->r_push - 2.0f));
+      float t = fa / d;
+      a->ax += spp_fx_guarded(t * dx, &a->ovf);
+      a->ay += spp_fx_guarded(t * dy, &a->ovf);
+    }
+  }
+}
+
+/* New heading and position of particle i (VicsekParticle::Move :148-163,
+ * VicsekParticle2::Move :198-213, configured rule). xi_u is the Philox word
+ * of the Vicsek noise stream. */
+SPP_HD void spp_vicsek_update(const SppConsts* k, const SppAcc* a, float x0, float y0, float th0,
+                              float c0, float s0, uint32_t xi_bits, float* x, float* y, float* th,
+                              float* c, float* s, int* imgx, int* imgy) {
+  float xi = spp_uniform_pm_pi_f(xi_bits);
+  float t;
+  if (k->model == SPP_MODEL_VICSEK) {
+    t = spp_atan2f(spp_from_fx(a->ay), spp_from_fx(a->ax)) + k->eta * xi;
+    t = spp_wrap_angle_f(t);
+  } else if (k->model == SPP_MODEL_VICSEK_REF_ANGLE) {
+    float avg = a->cnt > 0 ? spp_from_fx(a->at) / (float)a->cnt : th0;
+    t = avg + k->eta * xi;
+  } else {
+    float ax = a->cnt == 0 ? c0 : spp_from_fx(a->ax);
+    float ay = a->cnt == 0 ? s0 : spp_from_fx(a->ay);
+    float sx, cx;
+    spp_sincosf(xi, &sx, &cx);
+    float amp = (float)a->cnt * k->eta;
+    ax = ax + amp * cx;
+    ay = ay + amp * sx;
+    t = spp_atan2f(ay, ax);
+  }
+  spp_sincosf(t, s, c);
+  *th = t;
+  *x = spp_wrap_coord_f(fmaf(k->v0dt, *c, x0), k->L, k->L2, imgx);
+  *y = spp_wrap_coord_f(fmaf(k->v0dt, *s, y0), k->L, k->L2, imgy);
+}
+
+/* ------------------------------------------------------------------ */
+/* cells                                                               */
+/* ------------------------------------------------------------------ */
+/* Cell coordinate along one axis for D cells over [-L, L).
+ * SPP_BIN_GEOMETRIC: floor((x + L) * D / 2L); SPP_BIN_REFERENCE:
+ * (int)((int)(x + L) * D / 2L), the reference's integer truncation
+ * (serial/box.h:116-117).  Clamped to [0, D). */
+SPP_HD int spp_cell_coord(float x, float L, float L2, int D, int rule) {
+  int c;
+  if (rule == SPP_BIN_REFERENCE) {
+    int ix = (int)(x + L);
+    c = (int)((float)(ix * D) / L2);
+  } else {
+    c = (int)floorf(((x + L) * (float)D) / L2);
+  }
+  if (c < 0) c = 0;
+  if (c >= D) c = D - 1;
+  return c;
+}
+
+/* Morton (Z-order) key of a cell, 16 bits per axis. */
+SPP_HD uint32_t spp_morton_spread(uint32_t v) {
+  v &= 0x0000ffffu;
+  v = (v | (v << 8)) & 0x00ff00ffu;
+  v = (v | (v << 4)) & 0x0f0f0f0fu;
+  v = (v | (v << 2)) & 0x33333333u;
+  v = (v | (v << 1)) & 0x55555555u;
+  return v;
+}
+SPP_HD uint32_t spp_morton(uint32_t cx, uint32_t cy) {
+  return spp_morton_spread(cx) | (spp_morton_spread(cy) << 1);
+}
+
+#endif /* SPP_PHYSICS_H */

@@ -1,0 +1,218 @@
+"""Host-side mirror of the reference's Box interface over the C ABI.
+
+``System`` is a thin owner of one ``SppSystem*``.  ``Box`` keeps the method
+names of the reference's Box (parallel/box.h:15-58, serial/box.h:15-61) so
+that driver code written against the reference keeps its shape:
+
+    reference                              here
+    ---------------------------------------------------------------------
+    Box(Lx, Ly, phi) + Init(node, rho)     Box(params); Init(x, y, theta)
+    Sync()                                 Sync()           (re-bin + list)
+    Update_Cells / Update_Neighbor_List    Update_Cells()   (same rebuild)
+    One_Step()                             One_Step()
+    Multi_Step(steps)                      Multi_Step(steps)
+    Multi_Step(steps, interval)            Multi_Step(steps, interval)
+    Save(sv) / Load(sv)                    Save() -> Snapshot / Load(snap)
+    Save_Polarization(os)                  Save_Polarization(stream)
+    Compute_Polarization()                 Compute_Polarization()
+    operator<<(os, box)                    Write(stream)   (.bin frame)
+
+Errors surface as ``SppError`` carrying the ABI status, where the reference
+prints and exits (shared/cell.h:45-49, parallel/box.h:224-228).
+"""
+import ctypes as C
+import struct
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+
+
+class System:
+    def __init__(self, params: abi.SppParams):
+        self.params = params.copy()
+        if self.params.struct_size == 0:
+            self.params.struct_size = C.sizeof(abi.SppParams)
+        self._h = C.c_void_p()
+        abi.check(abi.lib().spp_create(C.byref(self.params), C.byref(self._h)), "spp_create")
+        self.n = int(self.params.n)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            abi.lib().spp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, x, y, theta, step0=0, img_x=None, img_y=None):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        th = np.ascontiguousarray(theta, np.float32)
+        ix = None if img_x is None else np.ascontiguousarray(img_x, np.int32)
+        iy = None if img_y is None else np.ascontiguousarray(img_y, np.int32)
+        abi.check(abi.lib().spp_upload_state(self._h, abi.fptr(x), abi.fptr(y), abi.fptr(th),
+                                             abi.iptr(ix), abi.iptr(iy), self.n, int(step0)),
+                  "spp_upload_state")
+
+    def download(self):
+        n = self.n
+        x = np.empty(n, np.float32)
+        y = np.empty(n, np.float32)
+        th = np.empty(n, np.float32)
+        ix = np.empty(n, np.int32)
+        iy = np.empty(n, np.int32)
+        abi.check(abi.lib().spp_download_state(self._h, abi.fptr(x), abi.fptr(y), abi.fptr(th),
+                                               abi.iptr(ix), abi.iptr(iy), n), "spp_download_state")
+        return x, y, th, ix, iy
+
+    def step(self, nsteps):
+        abi.check(abi.lib().spp_step(self._h, int(nsteps)), "spp_step")
+
+    def sync(self):
+        abi.check(abi.lib().spp_sync(self._h), "spp_sync")
+
+    def observables(self) -> abi.SppObservables:
+        o = abi.SppObservables()
+        abi.check(abi.lib().spp_observables(self._h, C.byref(o)), "spp_observables")
+        return o
+
+    def pairs(self, r, cap=None):
+        """Unique pairs (i < j, particle ids) within r under the kernels'
+        FP32 predicate, sorted as int64 keys i << 32 | j."""
+        cap = cap if cap is not None else max(16, 8 * self.n)
+        pi = np.empty(cap, np.int32)
+        pj = np.empty(cap, np.int32)
+        cnt = C.c_int64()
+        abi.check(abi.lib().spp_pairs(self._h, float(r), abi.iptr(pi), abi.iptr(pj), cap,
+                                      C.byref(cnt)), "spp_pairs")
+        if cnt.value > cap:
+            return self.pairs(r, cap=int(cnt.value))
+        a = np.minimum(pi[:cnt.value], pj[:cnt.value]).astype(np.int64)
+        b = np.maximum(pi[:cnt.value], pj[:cnt.value]).astype(np.int64)
+        return np.sort(a * (1 << 32) + b)
+
+    def cells(self, D, rule=abi.BIN_GEOMETRIC):
+        cx = np.empty(self.n, np.int32)
+        cy = np.empty(self.n, np.int32)
+        abi.check(abi.lib().spp_cells(self._h, int(D), int(rule), abi.iptr(cx), abi.iptr(cy),
+                                      self.n), "spp_cells")
+        return cx, cy
+
+    def kernel_launches(self):
+        return int(abi.lib().spp_kernel_launches(self._h))
+
+    def stream(self):
+        return abi.lib().spp_stream(self._h)
+
+    def time_steps(self, nsteps):
+        """spp_step(nsteps) timed with CUDA events on the launching stream (ms)."""
+        ms = C.c_double()
+        abi.check(abi.lib().spp_time_steps(self._h, int(nsteps), C.byref(ms)), "spp_time_steps")
+        return ms.value
+
+    def profile(self, nsteps):
+        pr = abi.SppProfile()
+        abi.check(abi.lib().spp_profile(self._h, int(nsteps), C.byref(pr)), "spp_profile")
+        return pr
+
+
+@dataclass
+class Snapshot:
+    """State_Hyper_Vector counterpart (shared/state-hyper-vector.h:6-41): the
+    positions, headings and the Philox step counter, which makes a reload
+    reproduce the same noise (the reference copies the GSL state instead,
+    :169-177)."""
+    x: np.ndarray
+    y: np.ndarray
+    theta: np.ndarray
+    img_x: np.ndarray
+    img_y: np.ndarray
+    step: int
+
+
+class Box:
+    """Reference-shaped driver interface (parallel/box.h:15-58)."""
+
+    def __init__(self, params: abi.SppParams):
+        self.params = params.copy()
+        self.system = System(self.params)
+        self.t = 0.0
+        self.polarization = 0.0
+        self._step0 = 0
+
+    @property
+    def N(self):
+        return self.system.n
+
+    def Init(self, x, y, theta, t=0.0):
+        """Box::Init / Positioning_Particles: place particles, bin, build lists."""
+        step0 = int(round(t / self.params.dt))
+        self.system.upload(x, y, theta, step0=step0)
+        self._step0 = step0
+        self.t = t
+
+    def Sync(self):
+        """Re-bin and rebuild the neighbour list from the current state."""
+        s = self.Save()
+        self.Load(s)
+
+    Update_Cells = Sync
+    Update_Neighbor_List = Sync
+
+    def One_Step(self):
+        self.system.step(1)
+        self.t += self.params.dt
+
+    def Multi_Step(self, steps, interval=None):
+        """Box::Multi_Step(steps) / Multi_Step(steps, interval): the cell
+        update interval is irrelevant here (rebuilds are displacement-
+        triggered on the device), so both forms advance `steps` steps."""
+        self.system.step(int(steps))
+        self.t += self.params.dt * int(steps)
+
+    def Save(self) -> Snapshot:
+        x, y, th, ix, iy = self.system.download()
+        o = self.system.observables()
+        return Snapshot(x, y, th, ix, iy, self._step0 + int(o.step))
+
+    def Load(self, snap: Snapshot):
+        self.system.upload(snap.x, snap.y, snap.theta, step0=snap.step, img_x=snap.img_x,
+                           img_y=snap.img_y)
+        self._step0 = snap.step
+        self.t = snap.step * self.params.dt
+
+    def Compute_Polarization(self):
+        self.polarization = self.system.observables().polarization
+        return self.polarization
+
+    def Save_Polarization(self, os):
+        """Box::Save_Polarization (parallel/box.h:467-473): 't<TAB>P' per line."""
+        os.write(f"{self.t}\t{self.Compute_Polarization()}\n")
+
+    def Write(self, os):
+        """operator<<(ostream&, Box*) (parallel/box.h:476-502): one binary frame
+        t:f64, Lx:f64, Ly:f64, nb:i32, Ns:i32, Nm:i32, then Ns x (x, y, theta)
+        as float32 of the unwrapped position r_original and the heading."""
+        x, y, th, ix, iy = self.system.download()
+        L = self.params.L
+        xu = (x.astype(np.float64) + 2 * L * ix).astype(np.float32)
+        yu = (y.astype(np.float64) + 2 * L * iy).astype(np.float32)
+        os.write(struct.pack("<dddiii", self.t, L, L, 1, self.N, 0))
+        rec = np.empty((self.N, 3), np.float32)
+        rec[:, 0], rec[:, 1], rec[:, 2] = xu, yu, th
+        os.write(rec.tobytes())

@@ -1,0 +1,69 @@
+"""Regenerate tests/golden/reference_runs.npz from the reference's own code.
+
+Runs the reference's particle classes (shared/particle.h, compiled by
+oracle/build.py from the reference checkout into oracle/_ref/libspp_ref.so,
+with the GSL calls answered by the Philox shim) on small seeded cases and
+stores inputs and outputs.  The fixtures pin the FP64 restatement
+(oracle/spp_oracle64.c) where the reference checkout is absent.
+
+    python tests/golden/make_golden.py
+"""
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from spp_gb300 import abi, configs  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+
+def lattice(n_side, spacing, L):
+    g = (np.arange(n_side) * spacing - L + 0.25 * spacing).astype(np.float64)
+    X, Y = np.meshgrid(g, g)
+    return X.ravel(), Y.ravel()
+
+
+def cases():
+    out = []
+    for integ, name in ((abi.INT_EULER, "euler"), (abi.INT_RK2, "rk2"), (abi.INT_RK4, "rk4")):
+        p = configs.reference_defaults(abi.MODEL_ABP)
+        p.n, p.L, p.Dr, p.dt, p.seed, p.integrator = 400, 10.0, 0.1, 0.005, 5, integ
+        x, y = lattice(20, 1.0, p.L)
+        _, _, th = configs.random_state(p.n, p.L, seed=7)
+        out.append((f"repulsive_{name}", p, x, y, th.astype(np.float64), 50))
+    for model, name in ((abi.MODEL_VICSEK_REF_ANGLE, "vicsek_angle"),
+                        (abi.MODEL_VICSEK_REF_VECTOR, "vicsek_vector")):
+        p = configs.vicsek_config(n=1024, L=16.0, model=model, seed=0)
+        x, y, th = configs.random_state(p.n, p.L, seed=3)
+        out.append((name, p, x.astype(np.float64), y.astype(np.float64), th.astype(np.float64), 20))
+    p = configs.reference_defaults(abi.MODEL_CONTINUOUS)
+    p.n, p.L, p.Dr, p.dt, p.v0, p.seed = 1024, 16.0, 0.05, 0.01, 0.5, 11
+    x, y, th = configs.random_state(p.n, p.L, seed=3)
+    out.append(("continuous_euler", p, x.astype(np.float64), y.astype(np.float64),
+                th.astype(np.float64), 20))
+    return out
+
+
+def main():
+    if O.ref() is None:
+        raise SystemExit("reference checkout not found: cannot regenerate the fixtures")
+    blob = {}
+    meta = {}
+    for name, p, x, y, th, steps in cases():
+        s = O.State64(x, y, th)
+        blob[f"{name}/in"] = np.stack([s.x, s.y, s.th, s.xu, s.yu])
+        O.run64(p, s, steps, fn="ref")
+        blob[f"{name}/out"] = np.stack([s.x, s.y, s.th, s.xu, s.yu])
+        meta[name] = {"params": {k: v for k, v in p.as_dict().items()}, "steps": steps}
+    blob["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    path = Path(__file__).resolve().parent / "reference_runs.npz"
+    np.savez_compressed(path, **blob)
+    print(path, path.stat().st_size, "bytes")
+
+
+if __name__ == "__main__":
+    main()

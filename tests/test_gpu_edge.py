@@ -1,0 +1,143 @@
+"""Edge cases through the C ABI on the GPU: tiny and ragged systems,
+boundary coordinates, neighbour-list overflow and its recovery, graph vs
+direct launches, invalid inputs, fixed-point overflow."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spp_gb300 import SppError, System, abi, configs
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_run(p, x, y, th, steps):
+    with System(p) as s:
+        s.upload(x, y, th)
+        s.step(steps)
+        return s.download(), s.observables()
+
+
+def same(gpu, ref):
+    gx, gy, gth, gix, giy = gpu
+    return (np.array_equal(gx, ref.x) and np.array_equal(gy, ref.y) and np.array_equal(gth, ref.th)
+            and np.array_equal(gix, ref.ix) and np.array_equal(giy, ref.iy))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 33, 257, 1000])
+def test_ragged_sizes_bitexact(gpu_lib, n):
+    p = configs.abp_config(n=n, L=4.0, seed=2)
+    x, y, th = configs.random_state(n, p.L, seed=n)
+    gpu, _ = gpu_run(p, x, y, th, 40)
+    assert same(gpu, O.run32(p, O.State32(x, y, th), 40))
+
+
+def test_boundary_coordinates(gpu_lib):
+    L = np.float32(8.0)
+    edge = np.nextafter(L, np.float32(0))
+    x = np.array([-L, edge, 0.0, -L, edge, 0.5], np.float32)
+    y = np.array([-L, -L, edge, edge, 0.0, 0.5], np.float32)
+    th = np.array([3.1, -3.1, 1.5, -1.5, 0.0, 2.0], np.float32)
+    p = configs.abp_config(n=6, L=8.0, seed=3)
+    gpu, _ = gpu_run(p, x, y, th, 200)
+    assert same(gpu, O.run32(p, O.State32(x, y, th), 200))
+    v = configs.vicsek_config(n=6, L=8.0)
+    gpu, _ = gpu_run(v, x, y, th, 50)
+    assert same(gpu, O.run32(v, O.State32(x, y, th), 50))
+
+
+def test_dense_cluster_list_overflow_recovers(gpu_lib):
+    """512 particles in a 2x2 patch overflow a 4-slot list: the device freezes,
+    the host grows the list and finishes the steps; results stay exact."""
+    n = 512
+    p = configs.abp_config(n=n, L=16.0, seed=4)
+    p.list_capacity = 4
+    rng_x, rng_y, th = configs.random_state(n, 1.0, seed=4)
+    gpu, obs = gpu_run(p, rng_x, rng_y, th, 30)
+    assert obs.list_capacity > 4
+    assert obs.step == 30
+    assert same(gpu, O.run32(p, O.State32(rng_x, rng_y, th), 30))
+
+
+def test_graphs_and_direct_launches_agree(gpu_lib, monkeypatch):
+    p = configs.abp_config(n=4096, L=32.0, seed=6)
+    x, y, th = configs.random_state(p.n, p.L, seed=6)
+    a, _ = gpu_run(p, x, y, th, 70)
+    monkeypatch.setenv("SPP_NO_GRAPHS", "1")
+    b, _ = gpu_run(p, x, y, th, 70)
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)
+
+
+def test_step0_offsets_the_noise_stream(gpu_lib):
+    p = configs.abp_config(n=1024, L=16.0, seed=7)
+    x, y, th = configs.random_state(p.n, p.L, seed=7)
+    with System(p) as s:
+        s.upload(x, y, th, step0=123456)
+        s.step(20)
+        g = s.download()
+    assert same(g, O.run32(p, O.State32(x, y, th), 20, step0=123456))
+
+
+def test_snapshot_resume_is_bitexact(gpu_lib):
+    from spp_gb300 import Box
+    p = configs.abp_config(n=2048, L=24.0, seed=8)
+    x, y, th = configs.random_state(p.n, p.L, seed=8)
+    b = Box(p)
+    b.Init(x, y, th)
+    b.Multi_Step(40)
+    snap = b.Save()
+    b.Multi_Step(40)
+    end1 = b.Save()
+    b2 = Box(p)
+    b2.Load(snap)
+    b2.Multi_Step(40)
+    end2 = b2.Save()
+    assert np.array_equal(end1.theta, end2.theta) and np.array_equal(end1.x, end2.x)
+    assert np.array_equal(end1.img_x, end2.img_x) and np.array_equal(end1.img_y, end2.img_y)
+    assert end1.step == end2.step == 80
+
+
+def test_invalid_inputs_fail_loudly(gpu_lib):
+    p = configs.abp_config(n=4, L=4.0)
+    with System(p) as s:
+        x = np.array([0, 1, 2, 5.0], np.float32)  # outside [-4, 4)
+        with pytest.raises(SppError) as e:
+            s.upload(x, x, x)
+        assert e.value.status == 1
+        with pytest.raises(SppError) as e:
+            s.upload(np.array([0, 1, np.nan, 0], np.float32), np.zeros(4, np.float32),
+                     np.zeros(4, np.float32))
+        assert e.value.status == 7
+        with pytest.raises(SppError):
+            s.step(1)  # nothing uploaded yet
+    with pytest.raises(SppError) as e:
+        System(configs.abp_config(n=4, L=1.0))
+    assert e.value.status == 1
+
+
+def test_r12_overlap_reports_fixed_point_overflow(gpu_lib):
+    p = configs.reference_defaults(abi.MODEL_ABP)
+    p.n, p.L, p.dt, p.skin = 2, 4.0, 0.001, 0.3
+    x = np.array([0.0, 0.01], np.float32)   # (sigma / d)^13 ~ 1e26
+    y = np.zeros(2, np.float32)
+    th = np.zeros(2, np.float32)
+    with System(p) as s:
+        s.upload(x, y, th)
+        s.step(1)
+        with pytest.raises(SppError) as e:
+            s.sync()
+        assert e.value.status == 4
+
+
+def test_kernel_launch_count(gpu_lib):
+    p = configs.abp_config(n=4096, L=32.0)
+    x, y, th = configs.random_state(p.n, p.L, seed=1)
+    with System(p) as s:
+        s.upload(x, y, th)
+        n0 = s.kernel_launches()
+        s.step(64)
+        o = s.observables()
+        n1 = s.kernel_launches()
+    assert n1 - n0 >= 64 * 2

@@ -1,0 +1,185 @@
+"""GPU parity through the C ABI.
+
+Gate 1 (bit-exact): the kernels against the CPU mirror of their arithmetic
+(oracle/spp_mirror32.c) -- same Philox draws, same FP32 formulas,
+order-independent fixed-point sums -- so any difference is a fault in the
+device machinery (binning, Morton reordering, Verlet lists and their
+displacement trigger, graphs).
+Gate 2 (tolerance): the kernels against the FP64 restatement of the
+reference (oracle/spp_oracle64.c, itself pinned to the reference's code).
+Tolerance from the spec: positions and headings within 1e-5 relative over
+100 steps, except where FP32 and FP64 disagree on which pairs lie inside a
+hard cutoff (alignment radius); those particles are counted and bounded.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spp_gb300 import System, abi, configs
+
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(p, x, y, th, steps, step0=0):
+    with System(p) as s:
+        s.upload(x, y, th, step0=step0)
+        s.step(steps)
+        out = s.download()
+        obs = s.observables()
+    return out, obs
+
+
+def assert_bitexact(gpu, mirror):
+    gx, gy, gth, gix, giy = gpu
+    for name, a, b in (("x", gx, mirror.x), ("y", gy, mirror.y), ("theta", gth, mirror.th),
+                       ("img_x", gix, mirror.ix), ("img_y", giy, mirror.iy)):
+        bad = np.flatnonzero(a != b)
+        assert bad.size == 0, f"{name}: {bad.size} particles differ, first {bad[:5]}"
+
+
+def lattice(n_side, L, jitter_seed=None):
+    g = (np.arange(n_side) * (2 * L / n_side) - L + 0.25).astype(np.float32)
+    X, Y = np.meshgrid(g, g)
+    return X.ravel().astype(np.float32), Y.ravel().astype(np.float32)
+
+
+ABP_CASES = {
+    "abp_harmonic_mean_rk2": dict(integrator=abi.INT_RK2, steps=100),
+    "abp_harmonic_mean_rk4": dict(integrator=abi.INT_RK4, steps=60),
+    "abp_harmonic_mean_euler": dict(integrator=abi.INT_EULER, steps=60),
+}
+
+
+@pytest.mark.parametrize("case", sorted(ABP_CASES))
+def test_abp_bitexact_vs_mirror(gpu_lib, case):
+    c = ABP_CASES[case]
+    p = configs.abp_config(n=4096, L=32.0, seed=1, integrator=c["integrator"])
+    x, y, th = configs.random_state(p.n, p.L, seed=1)
+    gpu, obs = run_gpu(p, x, y, th, c["steps"])
+    ref = O.run32(p, O.State32(x, y, th), c["steps"])
+    assert_bitexact(gpu, ref)
+    assert obs.step == c["steps"]
+    assert obs.n_rebuilds >= 2  # the displacement trigger fired during the run
+
+
+@pytest.mark.parametrize("integ", [abi.INT_RK2, abi.INT_RK4, abi.INT_EULER])
+def test_repulsive_reference_mode_bitexact(gpu_lib, integ):
+    """RepulsiveParticle as shipped: R12 force, g sin / (pi R_a^2), f = v."""
+    p = configs.reference_defaults(abi.MODEL_ABP)
+    p.n, p.L, p.Dr, p.dt, p.seed, p.integrator, p.skin = 4096, 32.0, 0.1, 0.005, 5, integ, 0.3
+    x, y = lattice(64, p.L)
+    _, _, th = configs.random_state(p.n, p.L, seed=7)
+    gpu, _ = run_gpu(p, x, y, th, 60)
+    ref = O.run32(p, O.State32(x, y, th), 60)
+    assert_bitexact(gpu, ref)
+
+
+@pytest.mark.parametrize("model", [abi.MODEL_VICSEK, abi.MODEL_VICSEK_REF_ANGLE,
+                                   abi.MODEL_VICSEK_REF_VECTOR])
+def test_vicsek_bitexact_vs_mirror(gpu_lib, model):
+    p = configs.vicsek_config(model=model)
+    x, y, th = configs.random_state(p.n, p.L, seed=0)
+    gpu, obs = run_gpu(p, x, y, th, 100)
+    ref = O.run32(p, O.State32(x, y, th), 100)
+    assert_bitexact(gpu, ref)
+    P, _, _ = O.polarization(ref.th)
+    assert abs(obs.polarization - P) < 1e-6
+
+
+@pytest.mark.parametrize("integ", [abi.INT_EULER, abi.INT_RK4])
+def test_continuous_bitexact_vs_mirror(gpu_lib, integ):
+    p = configs.reference_defaults(abi.MODEL_CONTINUOUS)
+    p.n, p.L, p.dt, p.v0, p.seed, p.skin, p.integrator = 4096, 32.0, 0.01, 0.5, 3, 0.3, integ
+    if integ == abi.INT_RK4:  # continuous-time Vicsek of the Lyapunov workload
+        p.alpha, p.g, p.Dr = 0.0, 1.0, 0.0
+    else:
+        p.Dr = 0.05
+    x, y, th = configs.random_state(p.n, p.L, seed=2)
+    gpu, _ = run_gpu(p, x, y, th, 50)
+    ref = O.run32(p, O.State32(x, y, th), 50)
+    assert_bitexact(gpu, ref)
+
+
+def test_abp_vs_fp64_within_spec(gpu_lib):
+    """Config-2 physics at N=4096: 100 RK2 steps against the FP64 oracle."""
+    p = configs.abp_config(n=4096, L=32.0, seed=1)
+    x, y, th = configs.random_state(p.n, p.L, seed=1)
+    (gx, gy, gth, gix, giy), _ = run_gpu(p, x, y, th, 100)
+    a = O.run64(p, O.State64(x, y, th), 100)
+    xu = gx.astype(np.float64) + 2 * p.L * gix
+    yu = gy.astype(np.float64) + 2 * p.L * giy
+    rel_pos = np.maximum(np.abs(xu - a.xu), np.abs(yu - a.yu)) / (2 * p.L)
+    dth = np.abs((gth.astype(np.float64) - a.th + np.pi) % (2 * np.pi) - np.pi)
+    print(f"max rel pos err {rel_pos.max():.3g}, median theta err {np.median(dth):.3g}, "
+          f"theta err > 1e-5 at {np.sum(dth > 1e-5)} particles")
+    assert rel_pos.max() < 1e-5
+    assert np.median(dth) < 1e-6
+    # alignment-cutoff flips between FP32 and FP64 touch a handful of particles
+    assert np.mean(dth > 1e-5) < 0.005
+
+
+def test_pairs_bitexact_vs_mirror(gpu_lib):
+    p = configs.abp_config(n=4096, L=32.0, seed=1)
+    x, y, th = configs.random_state(p.n, p.L, seed=3)
+    with System(p) as s:
+        s.upload(x, y, th)
+        for r in (1.0, 1.3):
+            g = s.pairs(r)
+            m = O.pairs32(p, x, y, r)
+            assert np.array_equal(g, m), r
+            k64 = O.pairs64(x.astype(np.float64), y.astype(np.float64), p.L, r)
+            assert np.setxor1d(g, k64).size <= 2
+        s.step(50)
+        gx, gy, _, _, _ = s.download()
+        assert np.array_equal(s.pairs(1.0), O.pairs32(p, gx, gy, 1.0))
+
+
+def test_cells_bitexact_vs_mirror(gpu_lib):
+    p = configs.abp_config(n=4096, L=32.0, seed=1)
+    x, y, th = configs.random_state(p.n, p.L, seed=3)
+    with System(p) as s:
+        s.upload(x, y, th)
+        for D in (3, 49, 64):
+            for rule in (abi.BIN_GEOMETRIC, abi.BIN_REFERENCE):
+                gx, gy = s.cells(D, rule)
+                mx, my = O.cells32(p, x, y, D, rule)
+                assert np.array_equal(gx, mx) and np.array_equal(gy, my), (D, rule)
+
+
+def test_full_size_abp_bitexact_vs_mirror(gpu_lib):
+    """The headline workload's size (N = 1,048,576, L = 512): 10 RK2 steps."""
+    p = configs.abp_config()
+    x, y, th = configs.random_state(p.n, p.L, seed=1)
+    gpu, obs = run_gpu(p, x, y, th, 10)
+    ref = O.run32(p, O.State32(x, y, th), 10)
+    assert_bitexact(gpu, ref)
+    assert obs.cells_per_side == int(np.floor(1024 / (1.3 * 1.001)))
+
+
+def test_full_size_abp_properties(gpu_lib):
+    """Size-independent properties over 400 steps of the full workload:
+    positions stay wrapped, headings finite, deterministic replay, and the
+    unwrapped displacement is bounded by v0 t plus the force contribution."""
+    p = configs.abp_config()
+    x, y, th = configs.random_state(p.n, p.L, seed=1)
+    with System(p) as s:
+        s.upload(x, y, th)
+        s.step(400)
+        a = s.download()
+        o = s.observables()
+    with System(p) as s:
+        s.upload(x, y, th)
+        s.step(200)
+        s.step(200)
+        b = s.download()
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)
+    gx, gy, gth, gix, giy = a
+    assert np.all(np.isfinite(gth))
+    assert np.all((gx >= -p.L) & (gx < p.L) & (gy >= -p.L) & (gy < p.L))
+    xu = gx.astype(np.float64) + 2 * p.L * gix - x
+    yu = gy.astype(np.float64) + 2 * p.L * giy - y
+    disp = np.hypot(xu, yu)
+    assert disp.max() < 400 * p.dt * 8.0
+    assert 0.0 <= o.polarization <= 1.0
+    assert o.n_rebuilds > 3
