@@ -264,13 +264,13 @@ def run_ours(args):
         hy = torch.from_numpy(y).pin_memory().numpy()
         ht = torch.from_numpy(th).pin_memory().numpy()
         e2e_times = []
-        for k in range(max(3, min(args.steps, 10))):
+        for k in range(0 if args.no_e2e else max(3, min(args.steps, 10))):
             t0 = time.perf_counter()
             s.upload(hx, hy, ht, step0=k * S)
             s.step(S)
             out = s.download()
             e2e_times.append(time.perf_counter() - t0)
-        e2e_value = n * S / statistics.median(e2e_times)
+        e2e_value = n * S / statistics.median(e2e_times) if e2e_times else None
     value = ws * n * S * args.steps / (elapsed_ms / 1e3)
     peak, peak_kind = measured_hbm_peak()
     achieved = ALG_BYTES_PER_PARTICLE_STEP / 2 * n / (stage_avg_ms / 1e3) / 1e9
@@ -351,6 +351,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -118,6 +118,9 @@ typedef struct SppObservables {
   int32_t list_capacity;
   int32_t max_neighbors;  /* largest list length at the last rebuild */
   int32_t cells_per_side;
+  int64_t late_rebuilds;  /* list rebuilds decided only after some particle had moved more than
+                             skin/2 since the previous build: pairs may have been missed (the
+                             time step is too large for the skin) */
 } SppObservables;
 
 typedef struct SppSystem SppSystem;

@@ -94,7 +94,7 @@ int dalloc(T** ptr, size_t count) {
 
 void free_dev(SppSystem* s) {
   DevState& d = s->d;
-  void* ptrs[] = {d.pos, d.half, d.half2, d.theta, d.img, d.id, d.kacc, d.ref, d.pos_alt,
+  void* ptrs[] = {d.pos, d.half, d.half2, d.theta, d.img, d.id, d.kacc, d.dth, d.ref, d.pos_alt,
                   d.theta_alt, d.img_alt, d.id_alt, d.key, d.rank, d.cell_count, d.cell_start,
                   d.scan_tmp, d.nbr, d.nn, d.ctl, d.red, s->stage_x, s->stage_y, s->stage_t,
                   s->stage_img};
@@ -416,6 +416,7 @@ int spp_create(const SppParams* p, SppSystem** out) {
   rc = rc ? rc : dalloc(&d.img, n);
   rc = rc ? rc : dalloc(&d.id, n);
   rc = rc ? rc : dalloc(&d.kacc, s->nstages > 2 ? n : 1);
+  rc = rc ? rc : dalloc(&d.dth, s->nstages > 1 ? n : 1);
   rc = rc ? rc : dalloc(&d.ref, n);
   rc = rc ? rc : dalloc(&d.pos_alt, n);
   rc = rc ? rc : dalloc(&d.theta_alt, n);
@@ -586,6 +587,7 @@ int spp_observables(SppSystem* s, SppObservables* o) {
   o->list_capacity = s->d.cap;
   o->max_neighbors = (int32_t)c.max_nn;
   o->cells_per_side = s->d.D;
+  o->late_rebuilds = c.late_rebuilds;
   return SPP_OK;
 }
 

@@ -35,7 +35,6 @@ __device__ __forceinline__ uint32_t cell_key(const SppConsts& k, const DevState&
 __global__ void __launch_bounds__(SPP_BLOCK) k_bin_count(SppConsts k, DevState d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n) return;
-  if (d.ctl->frozen) return;
   float4 p = d.pos[i];
   int cx, cy;
   uint32_t key = cell_key(k, d, p.x, p.y, &cx, &cy);
@@ -140,7 +139,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t* __r
 __global__ void __launch_bounds__(SPP_BLOCK) k_scatter(DevState d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n) return;
-  if (d.ctl->frozen) return;
   uint32_t dst = d.cell_start[d.key[i]] + d.rank[i];
   d.pos_alt[dst] = d.pos[i];
   d.theta_alt[dst] = d.theta[i];
@@ -149,11 +147,14 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_scatter(DevState d) {
 }
 
 /* Verlet list from the cell-ordered copy (alt), then the copy moves back
- * into the primary arrays. with_list == 0 only copies (no list). */
+ * into the primary arrays. with_list == 0 only copies (no list).  The copy
+ * always completes, even when some list overflows: the overflow only sets
+ * the frozen flag, which stops the stage kernels until the host has grown
+ * the list and rebuilt it. */
 __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState d, int with_list) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t cnt = 0;
-  if (i < d.n && !d.ctl->frozen) {
+  if (i < d.n) {
     float4 p = d.pos_alt[i];
     if (with_list) {
       int cx, cy;

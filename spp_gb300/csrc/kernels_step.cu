@@ -32,60 +32,92 @@ struct StageBufs {
   int stage, nstages;
 };
 
-__device__ __forceinline__ void finish_step(const SppConsts& k, const DevState& d, float my_max,
-                                            cudaGraphConditionalHandle cond, int use_cond,
-                                            int advance) {
-  __shared__ float warp_max[SPP_BLOCK / 32];
+/* End-of-step bookkeeping shared by the step kernels.  Every block reduces
+ * the largest squared displacement since the last list build (my_disp2) and
+ * within this step (my_step2); the block that finishes last decides the
+ * rebuild.  The list stays valid while no two particles together have moved
+ * more than the skin, so the rebuild is scheduled one step ahead: when
+ * max_disp + 2 * max_step_disp exceeds skin/2, i.e. before the next step
+ * could carry a particle past skin/2.  A rebuild decided when some particle
+ * has already passed skin/2 is counted in late_rebuilds (a diagnostic: pairs
+ * may have been missed during that step). */
+__device__ __forceinline__ void finish_step(const SppConsts& k, const DevState& d, float my_disp2,
+                                            float my_step2, cudaGraphConditionalHandle cond,
+                                            int use_cond) {
+  __shared__ float warp_disp[SPP_BLOCK / 32];
+  __shared__ float warp_step[SPP_BLOCK / 32];
   __shared__ int is_last;
-  float m = my_max;
-  m = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(m)));
-  if ((threadIdx.x & 31) == 0) warp_max[threadIdx.x >> 5] = m;
+  const float m1 = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(my_disp2)));
+  const float m2 = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(my_step2)));
+  if ((threadIdx.x & 31) == 0) {
+    warp_disp[threadIdx.x >> 5] = m1;
+    warp_step[threadIdx.x >> 5] = m2;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    float bm = 0.0f;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) bm = fmaxf(bm, warp_max[w]);
-    if (bm > 0.0f) atomicMax(&d.ctl->dmax2_bits, __float_as_uint(bm));
+    float b1 = 0.0f, b2 = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      b1 = fmaxf(b1, warp_disp[w]);
+      b2 = fmaxf(b2, warp_step[w]);
+    }
+    if (b1 > 0.0f) atomicMax(&d.ctl->dmax2_bits, __float_as_uint(b1));
+    if (b2 > 0.0f) atomicMax(&d.ctl->smax2_bits, __float_as_uint(b2));
     __threadfence();
-    unsigned prev = atomicAdd(&d.ctl->blocks_done, 1u);
+    const unsigned prev = atomicAdd(&d.ctl->blocks_done, 1u);
     is_last = (prev == gridDim.x - 1);
   }
   __syncthreads();
   if (is_last && threadIdx.x == 0) {
     __threadfence();
     volatile Ctl* c = d.ctl;
-    float dm = __uint_as_float(c->dmax2_bits);
-    unsigned rebuild = (advance && !c->frozen && dm > k.trigger2) ? 1u : 0u;
+    const int frozen = c->frozen;
+    const float dm = sqrtf(__uint_as_float(c->dmax2_bits));
+    const float sm = sqrtf(__uint_as_float(c->smax2_bits));
+    unsigned rebuild = 0u;
+    if (!frozen && k.half_skin > 0.0f) {
+      rebuild = (dm + 2.0f * sm > k.half_skin) ? 1u : 0u;
+      if (dm > k.half_skin) c->late_rebuilds = c->late_rebuilds + 1u;
+    }
     c->need_rebuild = rebuild;
     c->dmax2_bits = 0u;
+    c->smax2_bits = 0u;
     c->blocks_done = 0u;
-    if (advance && !c->frozen) c->step = c->step + 1u;
+    if (!frozen) c->step = c->step + 1u;
     if (use_cond) cudaGraphSetConditional(cond, rebuild);
   }
 }
 
+template <int LAW, int KIND>
 __global__ void __launch_bounds__(SPP_BLOCK) k_abp_stage(SppConsts k, DevState d, StageBufs b,
                                                          cudaGraphConditionalHandle cond,
                                                          int use_cond) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int last = (b.stage == b.nstages - 1);
   const int frozen = d.ctl->frozen;
-  float disp2 = 0.0f;
+  float disp2 = 0.0f, step2 = 0.0f;
   if (i < d.n && !frozen) {
-    const uint32_t step = d.ctl->step;
     const float4 pi = b.cur[i];
     SppAcc a;
     spp_acc_zero(&a);
     const int cnt = d.nn[i];
     const int32_t* __restrict__ nb = d.nbr + i;
+    const size_t stride = (size_t)d.n;
+#pragma unroll 2
     for (int q = 0; q < cnt; ++q) {
-      const int j = __ldg(nb + (size_t)q * d.n);
+      const int j = __ldg(nb + (size_t)q * stride);
       const float4 pj = __ldg(b.cur + j);
-      spp_pair_abp(&k, &a, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
+      spp_pair_abp_lk(&k, LAW, KIND, &a, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
     }
-    if (a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
+    if (LAW == SPP_FORCE_R12_TRUNC && a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
     float fx, fy, tau;
     spp_abp_forces(&k, &a, pi.z, pi.w, &fx, &fy, &tau);
-    const float dth = spp_rot_noise(&k, d.id[i], step);
+    float dth;
+    if (b.stage == 0) {
+      dth = spp_rot_noise(&k, d.id[i], d.ctl->step);
+      if (b.nstages > 1) d.dth[i] = dth;
+    } else {
+      dth = d.dth[i];
+    }
     const float4 p0 = (b.stage == 0) ? pi : d.pos[i];
     const float th0 = d.theta[i];
     float nx, ny, nt, nc, ns;
@@ -101,10 +133,10 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_abp_stage(SppConsts k, DevState d
         if (b.stage == 0) {
           d.kacc[i] = make_float4(fx, fy, tau, 0.0f);
         } else if (b.stage < 3) {
-          float4 ka = d.kacc[i];
+          const float4 ka = d.kacc[i];
           d.kacc[i] = make_float4(ka.x + 2.0f * fx, ka.y + 2.0f * fy, ka.z + 2.0f * tau, 0.0f);
         } else {
-          float4 ka = d.kacc[i];
+          const float4 ka = d.kacc[i];
           fx = ka.x + fx; fy = ka.y + fy; tau = ka.z + tau;
         }
         h = b.stage < 2 ? k.half_dt : (b.stage == 2 ? k.dt : k.dt6);
@@ -117,15 +149,16 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_abp_stage(SppConsts k, DevState d
     if (last) {
       d.theta[i] = nt;
       if (gx | gy) {
-        int2 g = d.img[i];
+        const int2 g = d.img[i];
         d.img[i] = make_int2(g.x + gx, g.y + gy);
       }
       const float2 r = d.ref[i];
       float ddx, ddy;
       disp2 = spp_sep(&k, nx, ny, r.x, r.y, &ddx, &ddy);
+      step2 = spp_sep(&k, nx, ny, p0.x, p0.y, &ddx, &ddy);
     }
   }
-  if (last) finish_step(k, d, disp2, cond, use_cond, 1);
+  if (last) finish_step(k, d, disp2, step2, cond, use_cond);
 }
 
 __global__ void __launch_bounds__(SPP_BLOCK) k_vicsek_step(SppConsts k, DevState d) {
@@ -167,7 +200,7 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_vicsek_step(SppConsts k, DevState
     d.img[i] = make_int2(g.x + gx, g.y + gy);
     d.id[i] = id;
   }
-  finish_step(k, d, 0.0f, 0, 0, 1);
+  finish_step(k, d, 0.0f, 0.0f, 0, 0);
 }
 
 /* Euler writes its new state to the half buffer (neighbours read pos during
@@ -223,7 +256,22 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
   }
   int nb = blocks_for(d.n);
   if (nb == 0) nb = 1;
-  k_abp_stage<<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond);
+  const int kind = spp_pair_kind(&k);
+#define SPP_STAGE_CASE(L, K)                                                   \
+  if (k.force_law == L && kind == K) {                                        \
+    k_abp_stage<L, K><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond);     \
+  } else
+  SPP_STAGE_CASE(SPP_FORCE_HARMONIC, SPP_KIND_ABP)
+  SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_ABP)
+  SPP_STAGE_CASE(SPP_FORCE_NONE, SPP_KIND_ABP)
+  SPP_STAGE_CASE(SPP_FORCE_NONE, SPP_KIND_CONT)
+  SPP_STAGE_CASE(SPP_FORCE_NONE, SPP_KIND_CONT_ALPHA)
+  SPP_STAGE_CASE(SPP_FORCE_HARMONIC, SPP_KIND_CONT)
+  SPP_STAGE_CASE(SPP_FORCE_HARMONIC, SPP_KIND_CONT_ALPHA)
+  SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_CONT)
+  SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_CONT_ALPHA)
+  {}
+#undef SPP_STAGE_CASE
   if (launches) *launches += 1;
   if (nstages == 1) {
     k_commit<<<nb, SPP_BLOCK, 0, s>>>(d);

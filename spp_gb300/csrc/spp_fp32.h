@@ -241,6 +241,20 @@ SPP_HD float spp_expf(float x) {
   return e * spp_u2f((uint32_t)(ki + 127) << 23);
 }
 
+/* 1/sqrt(x) for normal x > 0: the bit-level initial estimate of Lomont
+ * ("Fast inverse square root", 2003; constant 0x5f375a86, ~3.4% error)
+ * refined by three Newton-Raphson steps y <- y (3/2 - (x/2) y^2) written with
+ * fused multiply-adds; within 2 ulp over the normal range.  One such call
+ * replaces the sqrtf + division of a pair force. */
+SPP_HD float spp_rsqrtf(float x) {
+  float y = spp_u2f(0x5f375a86u - (spp_f2u(x) >> 1));
+  const float h = 0.5f * x;
+  y = y * fmaf(-h * y, y, 1.5f);
+  y = y * fmaf(-h * y, y, 1.5f);
+  y = y * fmaf(-h * y, y, 1.5f);
+  return y;
+}
+
 /* ------------------------------------------------------------------ */
 /* noise mappings                                                      */
 /* ------------------------------------------------------------------ */

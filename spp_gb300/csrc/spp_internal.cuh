@@ -35,7 +35,9 @@ struct Ctl {
   uint32_t max_nn;        /* largest list length of the last build */
   uint32_t n_rebuilds;
   uint32_t frozen;        /* set on list overflow: later stages skip until the host recovers */
-  uint32_t pad[7];
+  uint32_t smax2_bits;    /* max squared displacement during the current step (float bits) */
+  uint32_t late_rebuilds; /* rebuilds decided after some particle had already moved > skin/2 */
+  uint32_t pad[5];
 };
 
 struct DevState {
@@ -51,6 +53,7 @@ struct DevState {
   int2* img;
   uint32_t* id;
   float4* kacc;
+  float* dth;             /* rotational noise of the current step (multi-stage integrators) */
   float2* ref;
   float4* pos_alt;
   float* theta_alt;

@@ -36,7 +36,7 @@ typedef struct SppConsts {
   float one_minus_alpha_over_pi, alpha_over_pi;
   float beta_push, r_push, rpush2;
   float rlist, rlist2;         /* Verlet list radius */
-  float trigger2;              /* (skin/2)^2 with a small safety factor */
+  float half_skin;             /* rebuild threshold on displacements */
 } SppConsts;
 
 /* Host-side: round the double parameters to the kernels' floats. */
@@ -81,8 +81,7 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
     double rl = rc + (p->skin > 0 ? p->skin : 0.0);
     k->rlist = (float)rl;
     k->rlist2 = (float)(rl * rl);
-    double half = 0.5 * (p->skin > 0 ? p->skin : 0.0) * 0.98;
-    k->trigger2 = (float)(half * half);
+    k->half_skin = (float)(0.5 * (p->skin > 0 ? p->skin : 0.0));
   }
 }
 
@@ -109,38 +108,62 @@ SPP_HD float spp_sep(const SppConsts* k, float xi, float yi, float xj, float yj,
   return fmaf(*dx, *dx, *dy * *dy);
 }
 
+/* Alignment-term kinds of the gather loop. */
+#define SPP_KIND_ABP 0          /* sin(theta_j - theta_i), neighbour count */
+#define SPP_KIND_CONT 1         /* (1 - alpha)/pi sin(...)                  */
+#define SPP_KIND_CONT_ALPHA 2   /* ... - alpha (dr x v_i) / (pi d)          */
+
+SPP_HD int spp_pair_kind(const SppConsts* k) {
+  if (k->model != SPP_MODEL_CONTINUOUS) return SPP_KIND_ABP;
+  return k->alpha_over_pi != 0.0f ? SPP_KIND_CONT_ALPHA : SPP_KIND_CONT;
+}
+
 /* RepulsiveParticle::Interact (shared/particle.h:728-757) / ContinuousParticle::
- * Interact (:296-338), as received by i from j.  (c, s) = (cos, sin) theta. */
-SPP_HD void spp_pair_abp(const SppConsts* k, SppAcc* a, float xi, float yi, float ci, float si,
-                         float xj, float yj, float cj, float sj) {
+ * Interact (:296-338), as received by i from j.  (c, s) = (cos, sin) theta.
+ * law and kind are compile-time constants in the kernels (template
+ * arguments), so the branches on them vanish there; the CPU mirror passes
+ * k->force_law and spp_pair_kind(k) and evaluates the same arithmetic.
+ * With r = 1/d from spp_rsqrtf:
+ *   harmonic  k (1 - d / r_rep) dr / d  ->  t = k (r - 1/r_rep),  F = t dr
+ *   R12       A ((sigma/d)^13 - (sigma/r_c)^13) dr / d  ->  t = A (q^13 - c^13) r, q = sigma r */
+SPP_HD void spp_pair_abp_lk(const SppConsts* k, int law, int kind, SppAcc* a, float xi, float yi,
+                            float ci, float si, float xj, float yj, float cj, float sj) {
   float dx, dy;
-  float d2 = spp_sep(k, xi, yi, xj, yj, &dx, &dy);
-  if (d2 < k->rrep2 && d2 > 0.0f) {
-    float d = sqrtf(d2);
-    float t;
-    if (k->force_law == SPP_FORCE_HARMONIC) {
-      t = (k->k_rep * (1.0f - d * k->inv_rrep)) / d;
-    } else { /* R12_Repulsive_Truncated, shared/force-fields.h:14-39 */
-      float q = k->sigma_rep / d;
-      float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
-      float q13 = (q8 * q4) * q;
-      t = (k->k_rep * (q13 - k->c13)) / d;
+  const float d2 = spp_sep(k, xi, yi, xj, yj, &dx, &dy);
+  const int in_rep = (law != SPP_FORCE_NONE) && (d2 < k->rrep2) && (d2 > 0.0f);
+  const int in_al = d2 < k->ral2;
+  if (!(in_rep || in_al)) return;
+  float r = 0.0f;
+  if (in_rep || (kind == SPP_KIND_CONT_ALPHA && in_al && d2 > 0.0f)) r = spp_rsqrtf(d2);
+  if (in_rep) {
+    if (law == SPP_FORCE_HARMONIC) {
+      const float t = k->k_rep * (r - k->inv_rrep);   /* |t dr| <= k: no range guard */
+      a->ax += spp_to_fx(t * dx);
+      a->ay += spp_to_fx(t * dy);
+    } else {
+      const float q = k->sigma_rep * r;
+      const float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
+      const float q13 = (q8 * q4) * q;
+      const float t = (k->k_rep * (q13 - k->c13)) * r;
+      a->ax += spp_fx_guarded(t * dx, &a->ovf);
+      a->ay += spp_fx_guarded(t * dy, &a->ovf);
     }
-    a->ax += spp_fx_guarded(t * dx, &a->ovf);
-    a->ay += spp_fx_guarded(t * dy, &a->ovf);
   }
-  if (d2 < k->ral2) {
+  if (in_al) {
     a->cnt += 1;
     float term = sj * ci - cj * si; /* sin(theta_j - theta_i) */
-    if (k->model == SPP_MODEL_CONTINUOUS) {
+    if (kind != SPP_KIND_ABP) {
       term = k->one_minus_alpha_over_pi * term;
-      if (k->alpha_over_pi != 0.0f && d2 > 0.0f) {
-        float d = sqrtf(d2);
-        term = term - (k->alpha_over_pi * (dx * si - dy * ci)) / d;
-      }
+      if (kind == SPP_KIND_CONT_ALPHA && d2 > 0.0f)
+        term = term - (k->alpha_over_pi * (dx * si - dy * ci)) * r;
     }
     a->at += spp_to_fx(term);
   }
+}
+
+SPP_HD void spp_pair_abp(const SppConsts* k, SppAcc* a, float xi, float yi, float ci, float si,
+                         float xj, float yj, float cj, float sj) {
+  spp_pair_abp_lk(k, k->force_law, spp_pair_kind(k), a, xi, yi, ci, si, xj, yj, cj, sj);
 }
 
 /* Self-propulsion plus received force, and the torque (RepulsiveParticle::
@@ -220,9 +243,10 @@ SPP_HD void spp_pair_vicsek(const SppConsts* k, SppAcc* a, float xi, float yi, f
     a->ax += spp_to_fx(cj);
     a->ay += spp_to_fx(sj);
     if (d2 < k->rpush2 && d2 > 0.0f) {
-      float d = sqrtf(d2);
+      const float r = spp_rsqrtf(d2);
+      const float d = d2 * r;
       float fa = k->beta_push / (1.0f + spp_expf(d / k->r_push - 2.0f));
-      float t = fa / d;
+      float t = fa * r;
       a->ax += spp_fx_guarded(t * dx, &a->ovf);
       a->ay += spp_fx_guarded(t * dy, &a->ovf);
     }

@@ -48,16 +48,30 @@ def test_boundary_coordinates(gpu_lib):
 
 
 def test_dense_cluster_list_overflow_recovers(gpu_lib):
-    """512 particles in a 2x2 patch overflow a 4-slot list: the device freezes,
-    the host grows the list and finishes the steps; results stay exact."""
+    """512 aligning particles (no repulsion) in a 2x2 patch overflow a 4-slot
+    list: the device freezes, the host grows the list and finishes the
+    steps; the result stays bit-exact."""
     n = 512
     p = configs.abp_config(n=n, L=16.0, seed=4)
+    p.force_law = abi.FORCE_NONE
     p.list_capacity = 4
-    rng_x, rng_y, th = configs.random_state(n, 1.0, seed=4)
-    gpu, obs = gpu_run(p, rng_x, rng_y, th, 30)
+    x, y, th = configs.random_state(n, 1.0, seed=4)
+    gpu, obs = gpu_run(p, x, y, th, 30)
     assert obs.list_capacity > 4
-    assert obs.step == 30
-    assert same(gpu, O.run32(p, O.State32(rng_x, rng_y, th), 30))
+    assert obs.max_neighbors > 400
+    assert obs.step == 30 and obs.late_rebuilds == 0
+    assert same(gpu, O.run32(p, O.State32(x, y, th), 30))
+
+
+def test_exploding_cluster_reports_late_rebuilds(gpu_lib):
+    """512 overlapping harmonic disks fly apart at ~15 length units per step,
+    far beyond the skin: the device counts the rebuilds that came too late
+    instead of failing silently."""
+    n = 512
+    p = configs.abp_config(n=n, L=16.0, seed=4)
+    x, y, th = configs.random_state(n, 1.0, seed=4)
+    _, obs = gpu_run(p, x, y, th, 5)
+    assert obs.late_rebuilds > 0
 
 
 def test_graphs_and_direct_launches_agree(gpu_lib, monkeypatch):
