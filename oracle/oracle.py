@@ -39,6 +39,9 @@ def orc():
         L.orc32_cells.argtypes = [_P, _F, _F, C.c_int, C.c_int, _I, _I]
         L.orc32_philox.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.orc32_math.argtypes = [C.c_int, C.c_int, _F, _F, _F]
+        L.orc32_fx_sum.argtypes = [C.c_int, _F, _I, _I, _F]
+        L.orc32_rsqrt.argtypes = [C.c_float]
+        L.orc32_rsqrt.restype = C.c_float
         _orc = L
     return _orc
 
@@ -182,6 +185,17 @@ def philox(ctr, key):
     o = (C.c_uint32 * 4)()
     orc().orc32_philox(c, k, o)
     return tuple(o)
+
+
+def fx_sum(x):
+    x = np.ascontiguousarray(x, np.float32)
+    hi, lo, v = C.c_int32(), C.c_int32(), C.c_float()
+    orc().orc32_fx_sum(len(x), _f(x), C.byref(hi), C.byref(lo), C.byref(v))
+    return hi.value, lo.value, v.value
+
+
+def rsqrt32(x):
+    return float(orc().orc32_rsqrt(float(x)))
 
 
 MATH_FNS = {"sin": 0, "cos": 1, "atan2": 2, "log": 3, "exp": 4, "wrap": 5}

@@ -251,6 +251,14 @@ void orc32_cells(const SppParams* p, const float* x, const float* y, int D, int 
 }
 
 /* Exposed primitives of spp_fp32.h, for the CPU tests of the arithmetic. */
+void orc32_fx_sum(int n, const float* x, int32_t* hi, int32_t* lo, float* value) {
+  spp_fx a = {0, 0};
+  for (int i = 0; i < n; ++i) spp_fx_add(&a, x[i]);
+  *hi = a.hi;
+  *lo = a.lo;
+  *value = spp_fx_value(a);
+}
+float orc32_rsqrt(float x) { return spp_rsqrtf(x); }
 void orc32_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
   spp_u32x4 o = spp_philox4x32_10(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1]);
   memcpy(out, o.v, sizeof(o.v));

@@ -134,6 +134,10 @@ int validate(const SppParams* p) {
       if (p->model == SPP_MODEL_ABP && p->force_law != SPP_FORCE_NONE &&
           p->force_law != SPP_FORCE_HARMONIC && p->force_law != SPP_FORCE_R12_TRUNC)
         return fail(SPP_ERR_INVALID, "unknown force law");
+      /* a harmonic pair term is bounded by k_rep; the fixed-point sums take
+       * terms below 2^16 */
+      if (p->force_law == SPP_FORCE_HARMONIC && !(std::fabs(p->k_rep) < 65536.0))
+        return fail(SPP_ERR_INVALID, "|k_rep| must be < 65536");
       break;
     default:
       return fail(SPP_ERR_UNSUPPORTED, "model not built into this library");
@@ -575,7 +579,7 @@ int spp_observables(SppSystem* s, SppObservables* o) {
   Ctl c;
   CUDA_TRY(cudaMemcpyAsync(&c, s->d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s->stream));
   CUDA_TRY(cudaStreamSynchronize(s->stream));
-  const double inv = 1.0 / 4294967296.0;
+  const double inv = 1.0 / 134217728.0; /* fixed-point units of 2^-27 */
   memset(o, 0, sizeof(*o));
   o->step = (int64_t)c.step - s->step0;
   o->t = (double)o->step * s->p.dt;

@@ -218,8 +218,11 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_polarization(DevState d, unsigned
   long long sx = 0, sy = 0;
   if (i < d.n) {
     const float4 p = d.pos[i];
-    sx = spp_to_fx(p.z);
-    sy = spp_to_fx(p.w);
+    spp_fx a = {0, 0}, b = {0, 0};
+    spp_fx_add(&a, p.z);
+    spp_fx_add(&b, p.w);
+    sx = spp_fx_units(a);
+    sy = spp_fx_units(b);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {

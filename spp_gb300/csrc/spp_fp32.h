@@ -21,8 +21,8 @@
  *     polynomials fitted by gen_fp32_poly.py (this directory).
  *   - periodic wrap of angles and coordinates (shared/c2dvector.h:67-73,
  *     shared/particle.h:599).
- *   - fixed-point (int64, 2^-32 resolution) accumulation, which makes the
- *     neighbour sums independent of summation order.
+ *   - exact fixed-point accumulation (2^-27 resolution) in two int32 parts,
+ *     which makes the neighbour sums independent of summation order.
  */
 #ifndef SPP_FP32_H
 #define SPP_FP32_H
@@ -297,23 +297,42 @@ SPP_HD float spp_min_image_f(float d, float L, float L2) {
 /* ------------------------------------------------------------------ */
 /* fixed-point accumulation                                            */
 /* ------------------------------------------------------------------ */
-#define SPP_FX_SCALE     4294967296.0f          /* 2^32  */
-#define SPP_FX_INV_SCALE 2.3283064365386963e-10f /* 2^-32 */
-#define SPP_FX_LIMIT     1073741824.0f          /* |term| must stay below 2^30 */
+/* A term x (|x| < 2^16) is split exactly into a coarse part, x rounded to a
+ * multiple of 2^-5, and a fine remainder rounded to a multiple of 2^-27; the
+ * integer counts of both parts go to two int32 accumulators.  Integer sums
+ * are exact, so the total does not depend on the order of the terms.  The
+ * split uses only FP32 adds/multiplies and integer subtracts of bit patterns
+ * (the "magic number" rounding: adding 1.5 * 2^k moves x into a binade whose
+ * ulp is the desired grid, and the bit-pattern difference is the integer
+ * count).  Conversions to or from 64-bit integers are avoided on purpose: on
+ * this GPU they execute on the FP64 pipe, which is a small fraction of the
+ * FP32 rate.  Bounds: |x| < 2^16 per term (spp_fx_ok), up to 1024 terms per
+ * accumulator. */
+#define SPP_FX_HI_MAGIC  393216.0f      /* 1.5 * 2^18, ulp 2^-5 */
+#define SPP_FX_LO_MAGIC  12582912.0f    /* 1.5 * 2^23, ulp 1    */
+#define SPP_FX_LO_SCALE  134217728.0f   /* 2^27 */
+#define SPP_FX_INV_LO    7.450580596923828125e-09f /* 2^-27 */
+#define SPP_FX_INV_HI    0.03125f       /* 2^-5 */
+#define SPP_FX_RANGE     65536.0f       /* |term| < 2^16 */
 
-SPP_HD int64_t spp_to_fx(float x) {
-#if defined(__CUDA_ARCH__)
-  return __float2ll_rn(x * SPP_FX_SCALE);
-#else
-  return (int64_t)llrintf(x * SPP_FX_SCALE);
-#endif
+typedef struct { int32_t hi, lo; } spp_fx;
+
+SPP_HD int spp_fx_ok(float x) { return fabsf(x) < SPP_FX_RANGE; }
+
+SPP_HD void spp_fx_add(spp_fx* a, float x) {
+  const float t = x + SPP_FX_HI_MAGIC;          /* x rounded to a multiple of 2^-5 */
+  const float h = t - SPP_FX_HI_MAGIC;          /* exact */
+  const float l = x - h;                        /* exact, |l| <= 2^-6 */
+  const float u = l * SPP_FX_LO_SCALE + SPP_FX_LO_MAGIC; /* round(l * 2^27) */
+  a->hi += (int32_t)(spp_f2u(t) - spp_f2u(SPP_FX_HI_MAGIC));
+  a->lo += (int32_t)(spp_f2u(u) - spp_f2u(SPP_FX_LO_MAGIC));
 }
-SPP_HD float spp_from_fx(int64_t a) {
-#if defined(__CUDA_ARCH__)
-  return __ll2float_rn(a) * SPP_FX_INV_SCALE;
-#else
-  return (float)a * SPP_FX_INV_SCALE;
-#endif
+
+SPP_HD float spp_fx_value(spp_fx a) {
+  return fmaf((float)a.lo, SPP_FX_INV_LO, (float)a.hi * SPP_FX_INV_HI);
 }
+
+/* The exact sum in units of 2^-27 (for reductions across particles). */
+SPP_HD int64_t spp_fx_units(spp_fx a) { return (int64_t)a.hi * 4194304 + (int64_t)a.lo; }
 
 #endif /* SPP_FP32_H */

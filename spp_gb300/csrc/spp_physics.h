@@ -87,17 +87,20 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
 
 /* Accumulator for the sums particle i receives. */
 typedef struct SppAcc {
-  int64_t ax, ay;   /* force (ABP) or heading vector sum (Vicsek) */
-  int64_t at;       /* torque / angle sum */
+  spp_fx ax, ay;    /* force (ABP) or heading vector sum (Vicsek) */
+  spp_fx at;        /* torque / angle sum */
   int32_t cnt;      /* neighbours within the alignment radius (self excluded) */
   int32_t ovf;      /* a term left the fixed-point range */
 } SppAcc;
 
-SPP_HD void spp_acc_zero(SppAcc* a) { a->ax = 0; a->ay = 0; a->at = 0; a->cnt = 0; a->ovf = 0; }
+SPP_HD void spp_acc_zero(SppAcc* a) {
+  a->ax.hi = a->ax.lo = 0; a->ay.hi = a->ay.lo = 0; a->at.hi = a->at.lo = 0;
+  a->cnt = 0; a->ovf = 0;
+}
 
-SPP_HD int64_t spp_fx_guarded(float t, int32_t* ovf) {
-  if (!(fabsf(t) < SPP_FX_LIMIT)) { *ovf = 1; return 0; }
-  return spp_to_fx(t);
+SPP_HD void spp_fx_add_guarded(spp_fx* acc, float t, int32_t* ovf) {
+  if (!spp_fx_ok(t)) { *ovf = 1; return; }
+  spp_fx_add(acc, t);
 }
 
 /* Minimum-image separation r_i - r_j and its squared length. */
@@ -137,16 +140,16 @@ SPP_HD void spp_pair_abp_lk(const SppConsts* k, int law, int kind, SppAcc* a, fl
   if (in_rep || (kind == SPP_KIND_CONT_ALPHA && in_al && d2 > 0.0f)) r = spp_rsqrtf(d2);
   if (in_rep) {
     if (law == SPP_FORCE_HARMONIC) {
-      const float t = k->k_rep * (r - k->inv_rrep);   /* |t dr| <= k: no range guard */
-      a->ax += spp_to_fx(t * dx);
-      a->ay += spp_to_fx(t * dy);
+      const float t = k->k_rep * (r - k->inv_rrep);   /* |t dr| <= k (< 2^16 checked at create) */
+      spp_fx_add(&a->ax, t * dx);
+      spp_fx_add(&a->ay, t * dy);
     } else {
       const float q = k->sigma_rep * r;
       const float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
       const float q13 = (q8 * q4) * q;
       const float t = (k->k_rep * (q13 - k->c13)) * r;
-      a->ax += spp_fx_guarded(t * dx, &a->ovf);
-      a->ay += spp_fx_guarded(t * dy, &a->ovf);
+      spp_fx_add_guarded(&a->ax, t * dx, &a->ovf);
+      spp_fx_add_guarded(&a->ay, t * dy, &a->ovf);
     }
   }
   if (in_al) {
@@ -157,7 +160,7 @@ SPP_HD void spp_pair_abp_lk(const SppConsts* k, int law, int kind, SppAcc* a, fl
       if (kind == SPP_KIND_CONT_ALPHA && d2 > 0.0f)
         term = term - (k->alpha_over_pi * (dx * si - dy * ci)) * r;
     }
-    a->at += spp_to_fx(term);
+    spp_fx_add(&a->at, term);
   }
 }
 
@@ -170,9 +173,9 @@ SPP_HD void spp_pair_abp(const SppConsts* k, SppAcc* a, float xi, float yi, floa
  * Reset :559-564 and the alignment normalisations). */
 SPP_HD void spp_abp_forces(const SppConsts* k, const SppAcc* a, float ci, float si, float* fx,
                            float* fy, float* tau) {
-  *fx = k->v0 * ci + spp_from_fx(a->ax);
-  *fy = k->v0 * si + spp_from_fx(a->ay);
-  float S = spp_from_fx(a->at);
+  *fx = k->v0 * ci + spp_fx_value(a->ax);
+  *fy = k->v0 * si + spp_fx_value(a->ay);
+  float S = spp_fx_value(a->at);
   if (k->model == SPP_MODEL_CONTINUOUS) *tau = k->g * S;
   else if (k->align_mode == SPP_ALIGN_MEAN) *tau = (k->g * S) / (float)(a->cnt + 1);
   else *tau = S * k->g_over_area;
@@ -223,8 +226,8 @@ SPP_HD void spp_pair_vicsek(const SppConsts* k, SppAcc* a, float xi, float yi, f
   float d2 = spp_sep(k, xi, yi, xj, yj, &dx, &dy);
   if (k->model == SPP_MODEL_VICSEK) {
     if (d2 < k->ral2) {
-      a->ax += spp_to_fx(cj);
-      a->ay += spp_to_fx(sj);
+      spp_fx_add(&a->ax, cj);
+      spp_fx_add(&a->ay, sj);
       a->cnt += 1;
     }
     return;
@@ -233,22 +236,22 @@ SPP_HD void spp_pair_vicsek(const SppConsts* k, SppAcc* a, float xi, float yi, f
   if (k->model == SPP_MODEL_VICSEK_REF_ANGLE) { /* VicsekParticle::Interact, particle.h:171-188 */
     if (d2 < k->ral2) {
       a->cnt += 1;
-      a->at += spp_fx_guarded(thj, &a->ovf);
+      spp_fx_add_guarded(&a->at, thj, &a->ovf);
     }
     return;
   }
   /* VicsekParticle2::Interact, particle.h:221-246 */
   if (d2 < k->ral2) {
     a->cnt += 1;
-    a->ax += spp_to_fx(cj);
-    a->ay += spp_to_fx(sj);
+    spp_fx_add(&a->ax, cj);
+    spp_fx_add(&a->ay, sj);
     if (d2 < k->rpush2 && d2 > 0.0f) {
       const float r = spp_rsqrtf(d2);
       const float d = d2 * r;
       float fa = k->beta_push / (1.0f + spp_expf(d / k->r_push - 2.0f));
       float t = fa * r;
-      a->ax += spp_fx_guarded(t * dx, &a->ovf);
-      a->ay += spp_fx_guarded(t * dy, &a->ovf);
+      spp_fx_add_guarded(&a->ax, t * dx, &a->ovf);
+      spp_fx_add_guarded(&a->ay, t * dy, &a->ovf);
     }
   }
 }
@@ -262,14 +265,14 @@ SPP_HD void spp_vicsek_update(const SppConsts* k, const SppAcc* a, float x0, flo
   float xi = spp_uniform_pm_pi_f(xi_bits);
   float t;
   if (k->model == SPP_MODEL_VICSEK) {
-    t = spp_atan2f(spp_from_fx(a->ay), spp_from_fx(a->ax)) + k->eta * xi;
+    t = spp_atan2f(spp_fx_value(a->ay), spp_fx_value(a->ax)) + k->eta * xi;
     t = spp_wrap_angle_f(t);
   } else if (k->model == SPP_MODEL_VICSEK_REF_ANGLE) {
-    float avg = a->cnt > 0 ? spp_from_fx(a->at) / (float)a->cnt : th0;
+    float avg = a->cnt > 0 ? spp_fx_value(a->at) / (float)a->cnt : th0;
     t = avg + k->eta * xi;
   } else {
-    float ax = a->cnt == 0 ? c0 : spp_from_fx(a->ax);
-    float ay = a->cnt == 0 ? s0 : spp_from_fx(a->ay);
+    float ax = a->cnt == 0 ? c0 : spp_fx_value(a->ax);
+    float ay = a->cnt == 0 ? s0 : spp_fx_value(a->ay);
     float sx, cx;
     spp_sincosf(xi, &sx, &cx);
     float amp = (float)a->cnt * k->eta;

@@ -95,3 +95,25 @@ def test_random_state_in_box():
     # a non power-of-two box still lands inside [-L, L)
     x, y, _ = configs.random_state(100000, 13.7, seed=2)
     assert np.all(x < np.float32(13.7)) and np.all(x >= -np.float32(13.7))
+
+
+def test_fixed_point_sum_is_exact_and_order_independent():
+    rng = np.random.default_rng(3)
+    for scale in (1e-6, 1e-2, 1.0, 10.0, 3e3):
+        x = (rng.standard_normal(300) * scale).astype(np.float32)
+        a = O.fx_sum(x)
+        for _ in range(5):
+            assert O.fx_sum(rng.permutation(x)) == a
+        exact = np.sum(np.round(x.astype(np.float64) * 2.0**27)) * 2.0**-27
+        units = a[0] * 2**22 + a[1]
+        # every term is rounded once to the 2^-27 grid; the integer sum is exact
+        assert abs(units * 2.0**-27 - np.sum(x.astype(np.float64))) <= 300 * 2.0**-28 + 1e-12
+        assert abs(units * 2.0**-27 - exact) <= 300 * 2.0**-27
+        assert abs(a[2] - np.sum(x.astype(np.float64))) <= 1e-6 * max(1.0, abs(a[2])) + 300 * 2.0**-27
+
+
+def test_rsqrt_within_two_ulp():
+    for x in np.geomspace(1e-6, 1e6, 20001).astype(np.float32):
+        y = O.rsqrt32(x)
+        e = 1.0 / np.sqrt(np.float64(x))
+        assert abs(y - e) <= 2.0 * np.spacing(np.float32(e))
