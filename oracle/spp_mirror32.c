@@ -6,10 +6,11 @@
  * per-particle formulas come from spp_gb300/csrc/spp_physics.h, the header
  * the kernels compile; everything around them is restated here in the
  * simplest serial form: a plain cell list rebuilt every stage, particles in
- * id order, no Verlet list, no reordering, no graphs.  Because the neighbour
- * sums are order-independent fixed point, the GPU must reproduce these bits
- * exactly; any difference is a fault in binning, lists, reordering or the
- * rebuild trigger.  Its physics is checked independently against the FP64
+ * id order, no Verlet list, no reordering, no graphs.  The neighbour sums
+ * are FP32 in ascending particle id (Verlet models, matching the kernels'
+ * id-sorted lists) or order-independent fixed point (Vicsek models), so the
+ * GPU must reproduce these bits exactly; any difference is a fault in
+ * binning, lists, reordering or the rebuild trigger.  Its physics is checked independently against the FP64
  * restatement (spp_oracle64.c), which is itself pinned to the reference
  * (ref_harness.cpp).
  */
@@ -65,21 +66,39 @@ static double mirror_rcut(const SppParams* p) {
   return r;
 }
 
-/* Sums received by every particle from the state (x, y, c, s). */
+static int cmp_int(const void* a, const void* b) {
+  int x = *(const int*)a, y = *(const int*)b;
+  return (x > y) - (x < y);
+}
+
+/* Sums received by every particle from the state (x, y, c, s), neighbours
+ * taken in ascending particle id (the order of the kernels' sorted lists). */
 static int abp_accumulate(const SppConsts* k, int n, const float* x, const float* y, const float* c,
-                          const float* s, double rcut, SppAcc* acc) {
+                          const float* s, double rcut, SppAccF* acc) {
   mcells cl;
   mcells_build(&cl, n, x, y, k, rcut);
   int ovf = 0;
+  int cap = 64;
+  int* cand = (int*)malloc(sizeof(int) * cap);
   for (int i = 0; i < n; ++i) {
-    SppAcc a;
-    spp_acc_zero(&a);
+    SppAccF a;
+    spp_accf_zero(&a);
+    int m = 0;
     FOR_CANDIDATES(&cl, k, x[i], y[i], n, j, {
-      if (j != i) spp_pair_abp(k, &a, x[i], y[i], c[i], s[i], x[j], y[j], c[j], s[j]);
+      if (j != i) {
+        if (m == cap) { cap *= 2; cand = (int*)realloc(cand, sizeof(int) * cap); }
+        cand[m++] = j;
+      }
     });
+    qsort(cand, (size_t)m, sizeof(int), cmp_int);
+    for (int q = 0; q < m; ++q) {
+      int j = cand[q];
+      spp_pair_abp(k, &a, x[i], y[i], c[i], s[i], x[j], y[j], c[j], s[j]);
+    }
     ovf |= a.ovf;
     acc[i] = a;
   }
+  free(cand);
   mcells_free(&cl);
   return ovf;
 }
@@ -94,7 +113,7 @@ static int abp_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t
   float *hc = (float*)malloc(sizeof(float) * n), *hs = (float*)malloc(sizeof(float) * n);
   float *kx = (float*)malloc(sizeof(float) * n), *ky = (float*)malloc(sizeof(float) * n);
   float* kt = (float*)malloc(sizeof(float) * n);
-  SppAcc* acc = (SppAcc*)malloc(sizeof(SppAcc) * (n > 0 ? n : 1));
+  SppAccF* acc = (SppAccF*)malloc(sizeof(SppAccF) * (n > 0 ? n : 1));
   int rc = SPP_OK;
   for (int i = 0; i < n; ++i) spp_sincosf(th[i], &s[i], &c[i]);
   for (int st = 0; st < nsteps && rc == SPP_OK; ++st) {

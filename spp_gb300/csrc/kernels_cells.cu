@@ -16,10 +16,11 @@
  *   4. build_list: one thread per particle scans the 3x3 cells around it and
  *      records every particle within r_list = r_cut + skin (full list: each
  *      pair appears in both particles' lists, so the force kernels gather
- *      without atomics), column-major nbr[slot * n + i].
+ *      without atomics), column-major nbr[slot * n + i], each list sorted by
+ *      particle id so that the force kernels sum in a reproducible order.
  * Order inside a cell depends on atomic arrival order and is therefore not
- * deterministic; the force sums are order-independent fixed point, so the
- * physics is unaffected.
+ * deterministic; the sorted lists (Verlet models) and the order-independent
+ * fixed-point sums (Vicsek models) keep the physics deterministic.
  */
 #include "spp_internal.cuh"
 
@@ -174,7 +175,18 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
             float dx, dy;
             float d2 = spp_sep(&k, p.x, p.y, q.x, q.y, &dx, &dy);
             if (d2 < k.rlist2) {
-              if (cnt < (uint32_t)d.cap) d.nbr[(size_t)cnt * d.n + i] = (int32_t)j;
+              if (cnt < (uint32_t)d.cap) {
+                /* insertion into the list kept sorted by particle id */
+                const uint32_t idj = d.id_alt[j];
+                int pos = (int)cnt;
+                while (pos > 0) {
+                  const int32_t prev = d.nbr[(size_t)(pos - 1) * d.n + i];
+                  if (d.id_alt[prev] < idj) break;
+                  d.nbr[(size_t)pos * d.n + i] = prev;
+                  --pos;
+                }
+                d.nbr[(size_t)pos * d.n + i] = (int32_t)j;
+              }
               ++cnt;
             }
           }

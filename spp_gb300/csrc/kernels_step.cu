@@ -88,7 +88,7 @@ __device__ __forceinline__ void finish_step(const SppConsts& k, const DevState& 
 }
 
 template <int LAW, int KIND>
-__global__ void __launch_bounds__(SPP_BLOCK) k_abp_stage(SppConsts k, DevState d, StageBufs b,
+__global__ void __launch_bounds__(SPP_BLOCK, 8) k_abp_stage(SppConsts k, DevState d, StageBufs b,
                                                          cudaGraphConditionalHandle cond,
                                                          int use_cond) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -97,8 +97,8 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_abp_stage(SppConsts k, DevState d
   float disp2 = 0.0f, step2 = 0.0f;
   if (i < d.n && !frozen) {
     const float4 pi = b.cur[i];
-    SppAcc a;
-    spp_acc_zero(&a);
+    SppAccF a;
+    spp_accf_zero(&a);
     const int cnt = d.nn[i];
     const int32_t* __restrict__ nb = d.nbr + i;
     const size_t stride = (size_t)d.n;

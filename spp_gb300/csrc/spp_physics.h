@@ -111,6 +111,19 @@ SPP_HD float spp_sep(const SppConsts* k, float xi, float yi, float xj, float yj,
   return fmaf(*dx, *dx, *dy * *dy);
 }
 
+/* Accumulator of the Verlet-list models.  Their neighbour lists are sorted
+ * by particle id at every build, so the terms arrive in ascending id order
+ * and plain FP32 sums are reproducible (the CPU mirror sums the same
+ * contributors in the same order). */
+typedef struct SppAccF {
+  float fx, fy;     /* received force */
+  float tq;         /* received torque sum */
+  int32_t cnt;      /* neighbours within the alignment radius (self excluded) */
+  int32_t ovf;      /* an R12 term left the checked range */
+} SppAccF;
+
+SPP_HD void spp_accf_zero(SppAccF* a) { a->fx = 0.0f; a->fy = 0.0f; a->tq = 0.0f; a->cnt = 0; a->ovf = 0; }
+
 /* Alignment-term kinds of the gather loop. */
 #define SPP_KIND_ABP 0          /* sin(theta_j - theta_i), neighbour count */
 #define SPP_KIND_CONT 1         /* (1 - alpha)/pi sin(...)                  */
@@ -126,10 +139,11 @@ SPP_HD int spp_pair_kind(const SppConsts* k) {
  * law and kind are compile-time constants in the kernels (template
  * arguments), so the branches on them vanish there; the CPU mirror passes
  * k->force_law and spp_pair_kind(k) and evaluates the same arithmetic.
+ * Callers present the neighbours j in ascending particle id.
  * With r = 1/d from spp_rsqrtf:
  *   harmonic  k (1 - d / r_rep) dr / d  ->  t = k (r - 1/r_rep),  F = t dr
  *   R12       A ((sigma/d)^13 - (sigma/r_c)^13) dr / d  ->  t = A (q^13 - c^13) r, q = sigma r */
-SPP_HD void spp_pair_abp_lk(const SppConsts* k, int law, int kind, SppAcc* a, float xi, float yi,
+SPP_HD void spp_pair_abp_lk(const SppConsts* k, int law, int kind, SppAccF* a, float xi, float yi,
                             float ci, float si, float xj, float yj, float cj, float sj) {
   float dx, dy;
   const float d2 = spp_sep(k, xi, yi, xj, yj, &dx, &dy);
@@ -139,18 +153,18 @@ SPP_HD void spp_pair_abp_lk(const SppConsts* k, int law, int kind, SppAcc* a, fl
   float r = 0.0f;
   if (in_rep || (kind == SPP_KIND_CONT_ALPHA && in_al && d2 > 0.0f)) r = spp_rsqrtf(d2);
   if (in_rep) {
+    float t;
     if (law == SPP_FORCE_HARMONIC) {
-      const float t = k->k_rep * (r - k->inv_rrep);   /* |t dr| <= k (< 2^16 checked at create) */
-      spp_fx_add(&a->ax, t * dx);
-      spp_fx_add(&a->ay, t * dy);
+      t = k->k_rep * (r - k->inv_rrep);
     } else {
       const float q = k->sigma_rep * r;
       const float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
       const float q13 = (q8 * q4) * q;
-      const float t = (k->k_rep * (q13 - k->c13)) * r;
-      spp_fx_add_guarded(&a->ax, t * dx, &a->ovf);
-      spp_fx_add_guarded(&a->ay, t * dy, &a->ovf);
+      t = (k->k_rep * (q13 - k->c13)) * r;
+      if (!(fabsf(t * dx) < SPP_FX_RANGE && fabsf(t * dy) < SPP_FX_RANGE)) { a->ovf = 1; t = 0.0f; }
     }
+    a->fx = a->fx + t * dx;
+    a->fy = a->fy + t * dy;
   }
   if (in_al) {
     a->cnt += 1;
@@ -160,22 +174,22 @@ SPP_HD void spp_pair_abp_lk(const SppConsts* k, int law, int kind, SppAcc* a, fl
       if (kind == SPP_KIND_CONT_ALPHA && d2 > 0.0f)
         term = term - (k->alpha_over_pi * (dx * si - dy * ci)) * r;
     }
-    spp_fx_add(&a->at, term);
+    a->tq = a->tq + term;
   }
 }
 
-SPP_HD void spp_pair_abp(const SppConsts* k, SppAcc* a, float xi, float yi, float ci, float si,
+SPP_HD void spp_pair_abp(const SppConsts* k, SppAccF* a, float xi, float yi, float ci, float si,
                          float xj, float yj, float cj, float sj) {
   spp_pair_abp_lk(k, k->force_law, spp_pair_kind(k), a, xi, yi, ci, si, xj, yj, cj, sj);
 }
 
 /* Self-propulsion plus received force, and the torque (RepulsiveParticle::
  * Reset :559-564 and the alignment normalisations). */
-SPP_HD void spp_abp_forces(const SppConsts* k, const SppAcc* a, float ci, float si, float* fx,
+SPP_HD void spp_abp_forces(const SppConsts* k, const SppAccF* a, float ci, float si, float* fx,
                            float* fy, float* tau) {
-  *fx = k->v0 * ci + spp_fx_value(a->ax);
-  *fy = k->v0 * si + spp_fx_value(a->ay);
-  float S = spp_fx_value(a->at);
+  *fx = k->v0 * ci + a->fx;
+  *fy = k->v0 * si + a->fy;
+  float S = a->tq;
   if (k->model == SPP_MODEL_CONTINUOUS) *tau = k->g * S;
   else if (k->align_mode == SPP_ALIGN_MEAN) *tau = (k->g * S) / (float)(a->cnt + 1);
   else *tau = S * k->g_over_area;

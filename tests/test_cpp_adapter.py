@@ -59,4 +59,4 @@ def test_cpp_driver_matches_python(gpu_lib, tmp_path):
     xu = (gx.astype(np.float64) + 2 * L * gix).astype(np.float32)
     assert np.array_equal(rec[:, 0], xu)
     assert np.array_equal(rec[:, 2], gth)
-    assert abs(pol[-1] - P) <= 1e-6 * max(P, 1e-3)  # ostream default precision
+    assert abs(pol[-1] - P) <= 1e-5 * max(P, 1e-3)  # ostream prints 6 significant digits
