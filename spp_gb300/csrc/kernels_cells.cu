@@ -151,16 +151,23 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_scatter(DevState d) {
  * into the primary arrays. with_list == 0 only copies (no list).  The copy
  * always completes, even when some list overflows: the overflow only sets
  * the frozen flag, which stops the stage kernels until the host has grown
- * the list and rebuilt it. */
+ * the list and rebuilt it.
+ * Accepted neighbours are collected as (id << 32 | slot) keys in a per-thread
+ * array, insertion-sorted there (lists hold ~5 entries at unit density) and
+ * written once; lists longer than the array fall back to sorting in place. */
+constexpr int LIST_LOCAL = 48;
+
 __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState d, int with_list) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t cnt = 0;
   if (i < d.n) {
     float4 p = d.pos_alt[i];
     if (with_list) {
+      unsigned long long keys[LIST_LOCAL];
       int cx, cy;
       cell_key(k, d, p.x, p.y, &cx, &cy);
       const int D = d.D;
+      const uint32_t cap = (uint32_t)d.cap;
       for (int oy = -1; oy <= 1; ++oy) {
         int ny = cy + oy;
         ny = ny < 0 ? ny + D : (ny >= D ? ny - D : ny);
@@ -175,24 +182,48 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
             float dx, dy;
             float d2 = spp_sep(&k, p.x, p.y, q.x, q.y, &dx, &dy);
             if (d2 < k.rlist2) {
-              if (cnt < (uint32_t)d.cap) {
-                /* insertion into the list kept sorted by particle id */
-                const uint32_t idj = d.id_alt[j];
+              const unsigned long long key =
+                  ((unsigned long long)d.id_alt[j] << 32) | (unsigned long long)j;
+              if (cnt < (uint32_t)LIST_LOCAL) {
                 int pos = (int)cnt;
-                while (pos > 0) {
+                while (pos > 0 && keys[pos - 1] > key) {
+                  keys[pos] = keys[pos - 1];
+                  --pos;
+                }
+                keys[pos] = key;
+              } else if (cnt < cap) {
+                /* long list: the first LIST_LOCAL keys are still local; keep the
+                 * tail sorted in place in global memory */
+                int pos = (int)cnt;
+                while (pos > LIST_LOCAL) {
                   const int32_t prev = d.nbr[(size_t)(pos - 1) * d.n + i];
-                  if (d.id_alt[prev] < idj) break;
+                  if (d.id_alt[prev] < (uint32_t)(key >> 32)) break;
                   d.nbr[(size_t)pos * d.n + i] = prev;
                   --pos;
                 }
-                d.nbr[(size_t)pos * d.n + i] = (int32_t)j;
+                if (pos == LIST_LOCAL && keys[LIST_LOCAL - 1] > key) {
+                  /* belongs among the local keys: swap with the local maximum */
+                  unsigned long long moved = keys[LIST_LOCAL - 1];
+                  int lp = LIST_LOCAL - 1;
+                  while (lp > 0 && keys[lp - 1] > key) {
+                    keys[lp] = keys[lp - 1];
+                    --lp;
+                  }
+                  keys[lp] = key;
+                  d.nbr[(size_t)pos * d.n + i] = (int32_t)(uint32_t)moved;
+                } else {
+                  d.nbr[(size_t)pos * d.n + i] = (int32_t)j;
+                }
               }
               ++cnt;
             }
           }
         }
       }
-      d.nn[i] = (int32_t)(cnt < (uint32_t)d.cap ? cnt : (uint32_t)d.cap);
+      const uint32_t nloc = cnt < (uint32_t)LIST_LOCAL ? cnt : (uint32_t)LIST_LOCAL;
+      const uint32_t nw = nloc < cap ? nloc : cap;
+      for (uint32_t q = 0; q < nw; ++q) d.nbr[(size_t)q * d.n + i] = (int32_t)(uint32_t)keys[q];
+      d.nn[i] = (int32_t)(cnt < cap ? cnt : cap);
       d.ref[i] = make_float2(p.x, p.y);
     }
     d.pos[i] = p;

@@ -102,11 +102,32 @@ __global__ void __launch_bounds__(SPP_BLOCK, 8) k_abp_stage(SppConsts k, DevStat
     const int cnt = d.nn[i];
     const int32_t* __restrict__ nb = d.nbr + i;
     const size_t stride = (size_t)d.n;
-#pragma unroll 2
-    for (int q = 0; q < cnt; ++q) {
-      const int j = __ldg(nb + (size_t)q * stride);
-      const float4 pj = __ldg(b.cur + j);
-      spp_pair_abp_lk(&k, LAW, KIND, &a, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
+    /* Warps whose particles are all far from the box edges skip the
+     * minimum-image corrections (they would not change any separation). */
+    const int inner = fabsf(pi.x) < k.interior && fabsf(pi.y) < k.interior;
+    const int all_inner = __all_sync(__activemask(), inner);
+    /* the next neighbour's index and state are loaded before the current
+     * pair is evaluated, so the dependent loads overlap the arithmetic */
+    int jn = cnt > 0 ? __ldg(nb) : i;
+    float4 pn = __ldg(b.cur + jn);
+    if (all_inner) {
+      for (int q = 0; q < cnt; ++q) {
+        const float4 pj = pn;
+        if (q + 1 < cnt) {
+          jn = __ldg(nb + (size_t)(q + 1) * stride);
+          pn = __ldg(b.cur + jn);
+        }
+        spp_pair_abp_lkw(&k, LAW, KIND, 0, &a, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
+      }
+    } else {
+      for (int q = 0; q < cnt; ++q) {
+        const float4 pj = pn;
+        if (q + 1 < cnt) {
+          jn = __ldg(nb + (size_t)(q + 1) * stride);
+          pn = __ldg(b.cur + jn);
+        }
+        spp_pair_abp_lkw(&k, LAW, KIND, 1, &a, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
+      }
     }
     if (LAW == SPP_FORCE_R12_TRUNC && a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
     float fx, fy, tau;

@@ -37,6 +37,7 @@ typedef struct SppConsts {
   float beta_push, r_push, rpush2;
   float rlist, rlist2;         /* Verlet list radius */
   float half_skin;             /* rebuild threshold on displacements */
+  float interior;              /* |x|,|y| below this: no list neighbour is across the boundary */
 } SppConsts;
 
 /* Host-side: round the double parameters to the kernels' floats. */
@@ -82,6 +83,7 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
     k->rlist = (float)rl;
     k->rlist2 = (float)(rl * rl);
     k->half_skin = (float)(0.5 * (p->skin > 0 ? p->skin : 0.0));
+    k->interior = (float)(p->L - 2.0 * (rl + (p->skin > 0 ? p->skin : 0.0)));
   }
 }
 
@@ -143,10 +145,16 @@ SPP_HD int spp_pair_kind(const SppConsts* k) {
  * With r = 1/d from spp_rsqrtf:
  *   harmonic  k (1 - d / r_rep) dr / d  ->  t = k (r - 1/r_rep),  F = t dr
  *   R12       A ((sigma/d)^13 - (sigma/r_c)^13) dr / d  ->  t = A (q^13 - c^13) r, q = sigma r */
-SPP_HD void spp_pair_abp_lk(const SppConsts* k, int law, int kind, SppAccF* a, float xi, float yi,
-                            float ci, float si, float xj, float yj, float cj, float sj) {
-  float dx, dy;
-  const float d2 = spp_sep(k, xi, yi, xj, yj, &dx, &dy);
+SPP_HD void spp_pair_abp_lkw(const SppConsts* k, int law, int kind, int wrap, SppAccF* a, float xi,
+                             float yi, float ci, float si, float xj, float yj, float cj, float sj) {
+  float dx, dy, d2;
+  if (wrap) {
+    d2 = spp_sep(k, xi, yi, xj, yj, &dx, &dy);
+  } else { /* both particles far from the boundary: the minimum image is the plain difference */
+    dx = xi - xj;
+    dy = yi - yj;
+    d2 = fmaf(dx, dx, dy * dy);
+  }
   const int in_rep = (law != SPP_FORCE_NONE) && (d2 < k->rrep2) && (d2 > 0.0f);
   const int in_al = d2 < k->ral2;
   if (!(in_rep || in_al)) return;
@@ -180,7 +188,7 @@ SPP_HD void spp_pair_abp_lk(const SppConsts* k, int law, int kind, SppAccF* a, f
 
 SPP_HD void spp_pair_abp(const SppConsts* k, SppAccF* a, float xi, float yi, float ci, float si,
                          float xj, float yj, float cj, float sj) {
-  spp_pair_abp_lk(k, k->force_law, spp_pair_kind(k), a, xi, yi, ci, si, xj, yj, cj, sj);
+  spp_pair_abp_lkw(k, k->force_law, spp_pair_kind(k), 1, a, xi, yi, ci, si, xj, yj, cj, sj);
 }
 
 /* Self-propulsion plus received force, and the torque (RepulsiveParticle::
