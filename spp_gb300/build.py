@@ -15,8 +15,11 @@ from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
-OUT = PKG / "lib" / "libspp_gb300.so"
-BUILD = PKG / "_build"
+# SPP_LIB_OUT / SPP_BUILD_DIR / SPP_NVCC_DEFINES let a launch-shape sweep build
+# variants side by side (e.g. SPP_NVCC_DEFINES="SPP_STAGE_MIN_BLOCKS=8").
+OUT = Path(os.environ.get("SPP_LIB_OUT", PKG / "lib" / "libspp_gb300.so"))
+BUILD = Path(os.environ.get("SPP_BUILD_DIR", PKG / "_build"))
+DEFINES = [f"-D{d}" for d in os.environ.get("SPP_NVCC_DEFINES", "").split() if d]
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -43,7 +46,7 @@ def _compile(src, extra):
     obj = BUILD / (src.stem + ".o")
     deps = [src] + headers()
     if _stale(obj, deps):
-        cmd = [NVCC, *ARCH, *FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+        cmd = [NVCC, *ARCH, *FLAGS, *DEFINES, *extra, "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
