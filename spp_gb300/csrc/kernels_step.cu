@@ -88,7 +88,7 @@ __device__ __forceinline__ void finish_step(const SppConsts& k, const DevState& 
 }
 
 #ifndef SPP_STAGE_MIN_BLOCKS
-#define SPP_STAGE_MIN_BLOCKS 6   /* 6 x 256 threads per SM: 40 registers, no spills */
+#define SPP_STAGE_MIN_BLOCKS 8   /* 8 x 256 threads per SM: 32 registers */
 #endif
 template <int LAW, int KIND>
 __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(SppConsts k, DevState d, StageBufs b,
@@ -100,12 +100,6 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(S
   float disp2 = 0.0f, step2 = 0.0f;
   if (i < d.n && !frozen) {
     const float4 pi = b.cur[i];
-    /* per-particle operands of the update, loaded before the neighbour loop
-     * so that their latency overlaps it */
-    const float th0 = d.theta[i];
-    const float4 p0 = (b.stage == 0) ? pi : d.pos[i];
-    const uint32_t pid = (b.stage == 0) ? d.id[i] : 0u;
-    const float dth_saved = (b.stage == 0) ? 0.0f : d.dth[i];
     SppAccF a;
     spp_accf_zero(&a);
     const int cnt = d.nn[i];
@@ -143,11 +137,13 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(S
     spp_abp_forces(&k, &a, pi.z, pi.w, &fx, &fy, &tau);
     float dth;
     if (b.stage == 0) {
-      dth = spp_rot_noise(&k, pid, d.ctl->step);
+      dth = spp_rot_noise(&k, d.id[i], d.ctl->step);
       if (b.nstages > 1) d.dth[i] = dth;
     } else {
-      dth = dth_saved;
+      dth = d.dth[i];
     }
+    const float4 p0 = (b.stage == 0) ? pi : d.pos[i];
+    const float th0 = d.theta[i];
     float nx, ny, nt, nc, ns;
     int gx = 0, gy = 0;
     if (b.nstages == 1) {
