@@ -195,6 +195,30 @@ int64_t spp_kernel_launches(SppSystem* s);
 /* The cudaStream_t the handle launches on. */
 void* spp_stream(SppSystem* s);
 
+/* ---- pair search that allocates nothing (no counterpart in the reference) ----
+ * For callers that cannot allocate GPU memory themselves or through this
+ * library: a component running under another owner's fixed memory budget
+ * (a host framework with its own pool), or a latency-critical loop where a
+ * cudaMalloc/cudaFree would synchronise the device.  The caller passes its
+ * own device buffers: x, y (n positions, already wrapped into [-L, L)),
+ * pi, pj (room for cap pairs) and count (one int64).  The unique pairs
+ * (i < j, indices into x/y) with |r_ij| < r under the FP32 predicate of
+ * spp_pairs() are written there, and *count receives the total, which may
+ * exceed cap.  Work is enqueued on `stream` (a cudaStream_t, NULL for the
+ * default stream); the results are ready once that stream has completed.
+ * Scratch is one static device array of about 1.8 MB that every GPU loading
+ * this library holds until the process exits; n <= SPP_NOALLOC_MAX_N and at
+ * most SPP_NOALLOC_MAX_CELLS_PER_SIDE^2 cells, larger n is rejected with
+ * SPP_ERR_INVALID.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress, with that device current); make that first
+ * call before any stream capture.  Calls share the array: calls that overlap
+ * on the GPU race and must be ordered by the caller.  Allocates nothing:
+ * no cudaMalloc, cudaFree or allocating library routine is called. */
+#define SPP_NOALLOC_MAX_N 65536
+#define SPP_NOALLOC_MAX_CELLS_PER_SIDE 256
+int spp_pairs_noalloc(const float* x, const float* y, int n, double L, double r, int32_t* pi,
+                      int32_t* pj, int64_t cap, int64_t* count, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,6 +99,8 @@ PROTOTYPES = {
     "spp_stream": (_P, [_P]),
     "spp_profile": (C.c_int, [_P, C.c_int, C.POINTER(SppProfile)]),
     "spp_time_steps": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double)]),
+    "spp_pairs_noalloc": (C.c_int, [_P, _P, C.c_int, C.c_double, C.c_double, _P, _P, C.c_int64,
+                                    _P, _P]),
 }
 
 _lib = None

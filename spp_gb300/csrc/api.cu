@@ -45,6 +45,8 @@ struct GraphEntry {
 
 }  // namespace
 
+void spp_internal_set_error(const char* msg) { g_err = msg ? msg : ""; }
+
 struct SppSystem {
   SppParams p;
   SppConsts k;

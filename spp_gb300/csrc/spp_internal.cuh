@@ -70,6 +70,9 @@ struct DevState {
   double* red;            /* reduction scratch (polarization) */
 };
 
+/* api.cu: sets the message spp_last_error() returns on the calling thread */
+void spp_internal_set_error(const char* msg);
+
 /* kernels_cells.cu */
 void launch_bin_count(const SppConsts& k, const DevState& d, cudaStream_t s, int64_t* launches);
 void launch_scan(const DevState& d, cudaStream_t s, int64_t* launches);
