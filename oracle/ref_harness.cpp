@@ -1,5 +1,5 @@
 /*
- * ORACLE -- test infrastructure only.  Built by oracle/Makefile into
+ * ORACLE -- test infrastructure only.  Built by oracle/build.py into
  * oracle/_ref/libspp_ref.so from the reference's own headers, which are
  * included from the reference checkout (never copied); that library exists
  * only where the reference is present.
@@ -114,6 +114,22 @@ void vicsek_steps(const SppParams* p, int nsteps, int64_t step0, double* x, doub
   store(ps, x, y, th, xu, yu);
 }
 
+/* Interact_Membrane_Beads (parallel/beadbox.h:185-196), restated per ring
+ * with the reference's Spring(). */
+void ring_springs(std::vector<ActiveBrownianChain>& ps, const SppParams* p) {
+  const int M = p->ring_size;
+  for (int r = 0; r < p->n_rings; ++r)
+    for (int m = 0; m < M; ++m) {
+      const int a = r * M + m, b = r * M + (m + 1) % M;
+      C2DVector dr = ps[a].r - ps[b].r;
+      dr.Periodic_Transform();
+      Real d = std::sqrt(dr.Square());
+      C2DVector f = Spring(dr, d, p->bond_rest, p->k_bond);
+      ps[a].f += f;
+      ps[b].f -= f;
+    }
+}
+
 }  // namespace
 
 extern "C" int ref_run(const SppParams* p, int nsteps, int64_t step0, double* x, double* y,
@@ -186,6 +202,42 @@ extern "C" int ref_run(const SppParams* p, int nsteps, int64_t step0, double* x,
           move_all(ps, p, step, [](RepulsiveParticle& q) { q.Move_Runge_Kutta4_3(); });
           interact_all(ps, p->L, rcut);
           move_all(ps, p, step, [](RepulsiveParticle& q) { q.Move_Runge_Kutta4_4(); });
+        }
+      }
+      store(ps, x, y, th, xu, yu);
+      return SPP_OK;
+    }
+    case SPP_MODEL_BEADS: {
+      /* ActiveBrownianChain with nb = 1 (mobilities 0.5, 0.5, 1 from Set_nb,
+       * particle.h:856-864); no bending, no RK4 in the reference. */
+      if (p->force_law != SPP_FORCE_R12_TRUNC || p->kappa_bend != 0.0 || p->mu != 0.5 ||
+          p->k_perp != 1.0 || p->integrator == SPP_INT_RK4)
+        return SPP_ERR_UNSUPPORTED;
+      const int nm = p->n_rings * p->ring_size;
+      std::vector<ActiveBrownianChain> ps(p->n);
+      ActiveBrownianChain::sigma_m = p->sigma_rep;
+      ActiveBrownianChain::repulsion_radius_m = p->r_rep;
+      ActiveBrownianChain::A_p = p->k_rep;
+      ActiveBrownianChain::torque0 = p->torque0;
+      BasicDynamicParticle::Set_Dr(p->Dr);
+      for (int i = 0; i < p->n; ++i) {
+        ps[i].Set_nb(1);
+        ps[i].Set_F0(i < nm ? 0.0 : p->v0 / p->mu);
+      }
+      load(ps, x, y, th, xu, yu);
+      for (int k = 0; k < nsteps; ++k) {
+        int64_t step = step0 + k;
+        if (p->integrator == SPP_INT_EULER) {
+          ring_springs(ps, p);
+          interact_all(ps, p->L, p->r_rep);
+          move_all(ps, p, step, [](ActiveBrownianChain& q) { q.Move(); });
+        } else {
+          ring_springs(ps, p);
+          interact_all(ps, p->L, p->r_rep);
+          move_all(ps, p, step, [](ActiveBrownianChain& q) { q.Move_Runge_Kutta2_1(); });
+          ring_springs(ps, p);
+          interact_all(ps, p->L, p->r_rep);
+          move_all(ps, p, step, [](ActiveBrownianChain& q) { q.Move_Runge_Kutta2_2(); });
         }
       }
       store(ps, x, y, th, xu, yu);

@@ -60,7 +60,7 @@ static void mcells_free(mcells* c) { free(c->head); free(c->next); }
   } while (0)
 
 static double mirror_rcut(const SppParams* p) {
-  double r = p->r_align;
+  double r = p->model == SPP_MODEL_BEADS ? 0.0 : p->r_align;
   if (p->force_law != SPP_FORCE_NONE && p->r_rep > r) r = p->r_rep;
   if (p->model == SPP_MODEL_VICSEK_REF_VECTOR && p->r_push > r) r = p->r_push;
   return r;
@@ -103,6 +103,31 @@ static int abp_accumulate(const SppConsts* k, int n, const float* x, const float
   return ovf;
 }
 
+/* Velocity, angular velocity and noise of body i from its received sums
+ * (ABP/continuous: spp_abp_forces; beads: ring forces + spp_bead_velocity). */
+static void body_rates(const SppConsts* k, int i, const SppAccF* a, const float* cx,
+                       const float* cy, float ci, float si, uint32_t step, float* fx, float* fy,
+                       float* tau, float* dth) {
+  if (k->model == SPP_MODEL_BEADS) {
+    int bead = i < k->n_beads;
+    float rfx = 0.0f, rfy = 0.0f;
+    if (bead) {
+      float px[5], py[5];
+      for (int o = -2; o <= 2; ++o) {
+        uint32_t j = spp_ring_neighbor(k, (uint32_t)i, o);
+        px[o + 2] = cx[j];
+        py[o + 2] = cy[j];
+      }
+      spp_ring_forces(k, px, py, &rfx, &rfy);
+    }
+    spp_bead_velocity(k, !bead, a, rfx, rfy, ci, si, fx, fy, tau);
+    *dth = bead ? 0.0f : spp_rot_noise(k, (uint32_t)i, step);
+  } else {
+    spp_abp_forces(k, a, ci, si, fx, fy, tau);
+    *dth = spp_rot_noise(k, (uint32_t)i, step);
+  }
+}
+
 static int abp_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t step0, float* x,
                      float* y, float* th, int32_t* ix, int32_t* iy) {
   int n = p->n;
@@ -121,9 +146,8 @@ static int abp_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t
     if (p->integrator == SPP_INT_EULER) {
       if (abp_accumulate(k, n, x, y, c, s, rcut, acc)) rc = SPP_ERR_OVERFLOW;
       for (int i = 0; i < n; ++i) {
-        float fx, fy, tau;
-        spp_abp_forces(k, &acc[i], c[i], s[i], &fx, &fy, &tau);
-        float dth = spp_rot_noise(k, (uint32_t)i, step);
+        float fx, fy, tau, dth;
+        body_rates(k, i, &acc[i], x, y, c[i], s[i], step, &fx, &fy, &tau, &dth);
         int gx = ix[i], gy = iy[i];
         spp_euler_update(x[i], y[i], th[i], fx, fy, tau, dth, k, &x[i], &y[i], &th[i], &c[i], &s[i],
                          &gx, &gy);
@@ -142,9 +166,8 @@ static int abp_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t
       float* nc = (float*)malloc(sizeof(float) * n);
       float* ns = (float*)malloc(sizeof(float) * n);
       for (int i = 0; i < n; ++i) {
-        float fx, fy, tau;
-        spp_abp_forces(k, &acc[i], cc[i], cs[i], &fx, &fy, &tau);
-        float dth = spp_rot_noise(k, (uint32_t)i, step);
+        float fx, fy, tau, dth;
+        body_rates(k, i, &acc[i], cx, cy, cc[i], cs[i], step, &fx, &fy, &tau, &dth);
         float h, frac;
         if (nst == 2) {
           h = stage == 0 ? k->half_dt : k->dt;
@@ -226,6 +249,7 @@ int orc32_run(const SppParams* p, int nsteps, int64_t step0, float* x, float* y,
       return vicsek_run32(p, &k, nsteps, step0, x, y, th, ix, iy);
     case SPP_MODEL_ABP:
     case SPP_MODEL_CONTINUOUS:
+    case SPP_MODEL_BEADS:
       return abp_run32(p, &k, nsteps, step0, x, y, th, ix, iy);
     default:
       return SPP_ERR_UNSUPPORTED;

@@ -152,7 +152,7 @@ static void state_free(ostate* s) {
 }
 
 static double interaction_radius(const SppParams* p) {
-  double r = p->r_align;
+  double r = p->model == SPP_MODEL_BEADS ? 0.0 : p->r_align;
   if (p->force_law != SPP_FORCE_NONE && p->r_rep > r) r = p->r_rep;
   if (p->model == SPP_MODEL_VICSEK_REF_VECTOR && p->r_push > r) r = p->r_push;
   return r;
@@ -385,6 +385,135 @@ static void abp_step(ostate* s, int64_t step) {
   }
 }
 
+/* ------------------------------------------------------------------ */
+/* ActiveBrownianChain (nb = 1) bodies + ring membranes                 */
+/* ------------------------------------------------------------------ */
+/* ActiveBrownianChain::Interact for two single-bead bodies, shared/
+ * particle.h:964-984 (R12 with the membrane sigma/cutoff), or the harmonic
+ * law; no alignment. */
+static void bead_pair(void* ctx, int i, int j) {
+  ostate* s = (ostate*)ctx;
+  const SppParams* p = s->p;
+  double dx = pt(s->x[i] - s->x[j], p->L), dy = pt(s->y[i] - s->y[j], p->L);
+  double d = sqrt(dx * dx + dy * dy);
+  if (p->force_law != SPP_FORCE_NONE && d < p->r_rep && d > 0) {
+    double Fx, Fy;
+    if (p->force_law == SPP_FORCE_R12_TRUNC) {
+      r12_trunc(dx, dy, d, p->r_rep, p->sigma_rep, p->k_rep, &Fx, &Fy);
+    } else {
+      double mag = p->k_rep * (1.0 - d / p->r_rep);
+      Fx = mag * dx / d;
+      Fy = mag * dy / d;
+    }
+    s->fx[i] += Fx; s->fy[i] += Fy;
+    s->fx[j] -= Fx; s->fy[j] -= Fy;
+  }
+}
+
+static int n_beads(const SppParams* p) { return p->n_rings * p->ring_size; }
+
+/* ActiveBrownianChain::Reset, particle.h:878-883: torque = torque0, f = F0 v
+ * with F0 = v0 / mu for swimmers (speed v0 = mu F0) and 0 for membrane beads. */
+static void bead_reset(ostate* s) {
+  const SppParams* p = s->p;
+  int nm = n_beads(p);
+  for (int i = 0; i < s->n; ++i) {
+    double F0 = i < nm ? 0.0 : p->v0 / p->mu;
+    s->tq[i] = p->torque0;
+    s->fx[i] = F0 * s->vx[i];
+    s->fy[i] = F0 * s->vy[i];
+  }
+}
+
+/* Interact_Membrane_Beads, parallel/beadbox.h:185-196, per ring: Spring
+ * (force-fields.h:87-97) between i and (i+1) % M; then the bending forces of
+ * E = kappa sum_j (1 - cos phi_j) (no counterpart in the reference). */
+static void ring_forces(ostate* s) {
+  const SppParams* p = s->p;
+  int M = p->ring_size;
+  for (int r = 0; r < p->n_rings; ++r) {
+    int base = r * M;
+    for (int m = 0; m < M; ++m) {
+      int a = base + m, b = base + (m + 1) % M;
+      double dx = pt(s->x[a] - s->x[b], p->L), dy = pt(s->y[a] - s->y[b], p->L);
+      double d = sqrt(dx * dx + dy * dy);
+      double Fx = p->k_bond * (p->bond_rest - d) * dx / d;
+      double Fy = p->k_bond * (p->bond_rest - d) * dy / d;
+      s->fx[a] += Fx; s->fy[a] += Fy;
+      s->fx[b] -= Fx; s->fy[b] -= Fy;
+    }
+    if (p->kappa_bend == 0.0) continue;
+    for (int m = 0; m < M; ++m) {
+      int jm = base + (m + M - 1) % M, j = base + m, jp = base + (m + 1) % M;
+      double ux = pt(s->x[j] - s->x[jm], p->L), uy = pt(s->y[j] - s->y[jm], p->L);
+      double wx = pt(s->x[jp] - s->x[j], p->L), wy = pt(s->y[jp] - s->y[j], p->L);
+      double lu = sqrt(ux * ux + uy * uy), lw = sqrt(wx * wx + wy * wy);
+      double c = (ux * wx + uy * wy) / (lu * lw);
+      double dux = wx / (lu * lw) - c * ux / (lu * lu), duy = wy / (lu * lw) - c * uy / (lu * lu);
+      double dwx = ux / (lu * lw) - c * wx / (lw * lw), dwy = uy / (lu * lw) - c * wy / (lw * lw);
+      double kp = p->kappa_bend;
+      s->fx[jm] -= kp * dux; s->fy[jm] -= kp * duy;
+      s->fx[j] += kp * (dux - dwx); s->fy[j] += kp * (duy - dwy);
+      s->fx[jp] += kp * dwx; s->fy[jp] += kp * dwy;
+    }
+  }
+}
+
+static void bead_stage_forces(ostate* s) {
+  bead_reset(s);
+  ring_forces(s);
+  interact_all(s, bead_pair);
+}
+
+/* Moves of ActiveBrownianChain (particle.h:898-962) with m_parallel =
+ * m_perpendicular = mu: dr = mu f h, dtheta = k_perp torque h (+ noise for
+ * swimmers).  RK4 follows RepulsiveParticle's scheme (:633-726) with these
+ * rates (no reference counterpart for beads).  Membrane beads keep their
+ * heading (F0 = 0 makes it irrelevant to their motion). */
+static void bead_step(ostate* s, int64_t step) {
+  const SppParams* p = s->p;
+  double dt = p->dt, half_dt = 0.5 * dt, dt6 = dt / 6;
+  double sigma = sqrt(2 * p->Dr * dt);
+  int n = s->n, nm = n_beads(p);
+  int nst = p->integrator == SPP_INT_RK4 ? 4 : (p->integrator == SPP_INT_RK2 ? 2 : 1);
+  for (int stage = 0; stage < nst; ++stage) {
+    bead_stage_forces(s);
+    for (int i = 0; i < n; ++i) {
+      int swim = i >= nm;
+      double vx = p->mu * s->fx[i], vy = p->mu * s->fy[i];
+      double om = swim ? p->k_perp * s->tq[i] : 0.0;
+      if (stage == 0) {
+        s->dth[i] = swim ? sigma * orc_normal(p, i, step) : 0.0;
+        s->tho[i] = s->th[i]; s->xo[i] = s->xu[i]; s->yo[i] = s->yu[i];
+      }
+      double h, frac;
+      if (nst == 1) { h = dt; frac = 1; }
+      else if (nst == 2) { h = stage == 0 ? half_dt : dt; frac = stage == 0 ? 0.5 : 1.0; }
+      else {
+        if (stage == 0) { s->k1f_x[i] = vx; s->k1f_y[i] = vy; s->k1t[i] = om; }
+        else if (stage == 1) { s->k2f_x[i] = vx; s->k2f_y[i] = vy; s->k2t[i] = om; }
+        else if (stage == 2) { s->k3f_x[i] = vx; s->k3f_y[i] = vy; s->k3t[i] = om; }
+        else {
+          vx = s->k1f_x[i] + s->k2f_x[i] * 2 + s->k3f_x[i] * 2 + vx;
+          vy = s->k1f_y[i] + s->k2f_y[i] * 2 + s->k3f_y[i] * 2 + vy;
+          om = s->k1t[i] + s->k2t[i] * 2 + s->k3t[i] * 2 + om;
+        }
+        h = stage < 2 ? half_dt : (stage == 2 ? dt : dt6);
+        frac = stage < 2 ? 0.5 : 1.0;
+      }
+      if (swim) {
+        s->th[i] = s->tho[i] + h * om + frac * s->dth[i];
+        if (nst > 1) s->th[i] = wrap_angle(s->th[i]);
+      }
+      double nxu = s->xo[i] + vx * h, nyu = s->yo[i] + vy * h;
+      if (stage == nst - 1) { s->xu[i] = nxu; s->yu[i] = nyu; }
+      s->x[i] = pt(nxu, p->L);
+      s->y[i] = pt(nyu, p->L);
+    }
+    for (int i = 0; i < n; ++i) set_v(s, i);
+  }
+}
+
 /* ContinuousParticle::Move (Euler), shared/particle.h:268-293 */
 static void cont_euler_step(ostate* s, int64_t step) {
   const SppParams* p = s->p;
@@ -465,6 +594,7 @@ int orc64_run(const SppParams* p, int nsteps, int64_t step0, double* x, double* 
       case SPP_MODEL_VICSEK_REF_ANGLE:
       case SPP_MODEL_VICSEK_REF_VECTOR: vicsek_step(&s, step); break;
       case SPP_MODEL_ABP: abp_step(&s, step); break;
+      case SPP_MODEL_BEADS: bead_step(&s, step); break;
       case SPP_MODEL_CONTINUOUS:
         if (p->integrator == SPP_INT_EULER) cont_euler_step(&s, step);
         else abp_step(&s, step);

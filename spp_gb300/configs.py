@@ -115,3 +115,80 @@ def abp_config(n=1 << 20, L=512.0, seed=1, integrator=abi.INT_RK2) -> abi.SppPar
     p.Dr, p.v0, p.dt = 0.1, 1.0, 0.005
     p.skin = 0.3
     return p
+
+
+WCA_CUTOFF = 2.0 ** (1.0 / 6.0)
+
+
+def vesicle_config(n_rings=1024, ring_size=128, swimmers_per_ring=32, L=None, seed=2,
+                   integrator=abi.INT_RK4) -> abi.SppParams:
+    """Ring vesicles with swimmers: n_rings rings of ring_size beads (radius
+    0.5, bonds k = 100 at rest length 1, bending kappa = 10), each enclosing
+    swimmers_per_ring active Brownian swimmers (v0 = 1, D_r = 0.05); a
+    WCA-like truncated r^-12 repulsion (R12_Repulsive_Truncated with
+    sigma = 1, cutoff 2^(1/6)) acts between all bodies; RK4, dt = 0.002.
+
+    The box is sized to 30% area fraction counting each vesicle's enclosed
+    disk of radius R + a, R = 0.5 / sin(pi / M) (set-up.h:299): 1024 rings
+    of 128 beads give a side of 2162 (L = 1081).  Counting bead disks alone
+    would give a box smaller than the rings themselves."""
+    R = 0.5 / math.sin(math.pi / ring_size)
+    if L is None:
+        area = n_rings * math.pi * (R + 0.5) ** 2 / 0.30
+        L = 0.5 * math.sqrt(area)
+    p = reference_defaults(abi.MODEL_BEADS)
+    p.n_rings, p.ring_size = n_rings, ring_size
+    p.n = n_rings * ring_size + n_rings * swimmers_per_ring
+    p.L, p.seed, p.integrator = float(L), seed, integrator
+    p.force_law = abi.FORCE_R12_TRUNC
+    p.sigma_rep, p.r_rep, p.k_rep = 1.0, WCA_CUTOFF, 1.0
+    p.k_bond, p.bond_rest, p.kappa_bend = 100.0, 1.0, 10.0
+    p.mu, p.k_perp, p.torque0 = 0.5, 1.0, 0.0
+    p.v0, p.Dr, p.dt, p.skin = 1.0, 0.05, 0.002, 0.3
+    return p
+
+
+def vesicle_state(p, swimmers_per_ring=None, seed=None):
+    """Rings on a jittered square grid (centres), beads evenly on each ring
+    (Ring_Membrane, shared/set-up.h:292-316), swimmers on a small square
+    lattice (spacing 1.5) around each centre with random headings."""
+    seed = p.seed if seed is None else seed
+    M, nr = p.ring_size, p.n_rings
+    ns = (p.n - nr * M) // max(nr, 1) if swimmers_per_ring is None else swimmers_per_ring
+    L = p.L
+    R = 0.5 * p.bond_rest / math.sin(math.pi / M)
+    G = int(math.ceil(math.sqrt(nr)))
+    spacing = 2 * L / G
+    slack = max(0.0, 0.5 * (spacing - 2 * R - 2.0))
+    ids = np.arange(nr, dtype=np.uint32)
+    jit = draw(seed, 0, ids, 0, RNG_INIT_POS)
+    cx = -L + (np.arange(nr) % G + 0.5) * spacing + (2 * u01_f32(jit[0]).astype(np.float64) - 1) * 0.5 * slack
+    cy = -L + (np.arange(nr) // G + 0.5) * spacing + (2 * u01_f32(jit[1]).astype(np.float64) - 1) * 0.5 * slack
+    ang = 2 * math.pi * np.arange(M) / M
+    bx = (cx[:, None] + R * np.cos(ang)[None, :]).ravel()
+    by = (cy[:, None] + R * np.sin(ang)[None, :]).ravel()
+    bth = np.zeros(nr * M)
+    # swimmer lattice: the ns sites closest to the centre
+    g = np.arange(-12, 13) * 1.5
+    gx, gy = np.meshgrid(g, g)
+    order = np.argsort(gx.ravel() ** 2 + gy.ravel() ** 2 + 1e-6 * gx.ravel(), kind="stable")
+    sx0, sy0 = gx.ravel()[order][:ns], gy.ravel()[order][:ns]
+    if ns and np.max(np.hypot(sx0, sy0)) > R - 2.0:
+        raise ValueError("too many swimmers for the ring size")
+    sid = np.arange(nr * ns, dtype=np.uint32)
+    sw = draw(seed, 0, sid, 0, RNG_INIT_ANGLE)
+    sx = (cx[:, None] + sx0[None, :]).ravel() + 0.2 * (2 * u01_f32(sw[1]).astype(np.float64) - 1)
+    sy = (cy[:, None] + sy0[None, :]).ravel() + 0.2 * (2 * u01_f32(sw[2]).astype(np.float64) - 1)
+    sth = (2 * u01_f32(sw[0]).astype(np.float64) - 1) * math.pi
+    x = np.concatenate([bx, sx])
+    y = np.concatenate([by, sy])
+    th = np.concatenate([bth, sth])
+    # wrap into [-L, L)
+    x = x - 2 * L * np.floor((x + L) / (2 * L))
+    y = y - 2 * L * np.floor((y + L) / (2 * L))
+    x = x.astype(np.float32)
+    y = y.astype(np.float32)
+    Lf = np.float32(L)
+    x = np.where(x >= Lf, -Lf, x).astype(np.float32)
+    y = np.where(y >= Lf, -Lf, y).astype(np.float32)
+    return x, y, th.astype(np.float32)

@@ -96,7 +96,7 @@ int dalloc(T** ptr, size_t count) {
 
 void free_dev(SppSystem* s) {
   DevState& d = s->d;
-  void* ptrs[] = {d.pos, d.half, d.half2, d.theta, d.img, d.id, d.kacc, d.dth, d.ref, d.pos_alt,
+  void* ptrs[] = {d.pos, d.half, d.half2, d.theta, d.img, d.id, d.inv, d.kacc, d.dth, d.ref, d.pos_alt,
                   d.theta_alt, d.img_alt, d.id_alt, d.key, d.rank, d.cell_count, d.cell_start,
                   d.scan_tmp, d.nbr, d.nn, d.ctl, d.red, s->stage_x, s->stage_y, s->stage_t,
                   s->stage_img};
@@ -108,7 +108,7 @@ void free_dev(SppSystem* s) {
 }
 
 double interaction_radius(const SppParams& p) {
-  double r = p.r_align;
+  double r = p.model == SPP_MODEL_BEADS ? 0.0 : p.r_align;
   if (p.force_law != SPP_FORCE_NONE && p.r_rep > r) r = p.r_rep;
   if (p.model == SPP_MODEL_VICSEK_REF_VECTOR && p.r_push > r) r = p.r_push;
   return r;
@@ -127,13 +127,18 @@ int validate(const SppParams* p) {
     case SPP_MODEL_VICSEK_REF_ANGLE:
     case SPP_MODEL_VICSEK_REF_VECTOR:
       break;
+    case SPP_MODEL_BEADS:
+      if (p->n_rings < 0 || (p->n_rings > 0 && p->ring_size < 3) ||
+          (int64_t)p->n_rings * p->ring_size > p->n)
+        return fail(SPP_ERR_INVALID, "membrane rings: need ring_size >= 3 and n_rings*ring_size <= n");
+      /* fall through */
     case SPP_MODEL_ABP:
     case SPP_MODEL_CONTINUOUS:
       if (p->integrator != SPP_INT_EULER && p->integrator != SPP_INT_RK2 &&
           p->integrator != SPP_INT_RK4)
         return fail(SPP_ERR_INVALID, "integrator must be SPP_INT_EULER, _RK2 or _RK4");
       if (!(p->skin > 0)) return fail(SPP_ERR_INVALID, "the Verlet-list models need skin > 0");
-      if (p->model == SPP_MODEL_ABP && p->force_law != SPP_FORCE_NONE &&
+      if (p->model != SPP_MODEL_CONTINUOUS && p->force_law != SPP_FORCE_NONE &&
           p->force_law != SPP_FORCE_HARMONIC && p->force_law != SPP_FORCE_R12_TRUNC)
         return fail(SPP_ERR_INVALID, "unknown force law");
       /* a harmonic pair term is bounded by k_rep; the fixed-point sums take
@@ -383,7 +388,8 @@ int spp_create(const SppParams* p, SppSystem** out) {
   SppSystem* s = new SppSystem();
   s->p = *p;
   spp_consts_from_params(&s->k, p);
-  s->uses_list = (p->model == SPP_MODEL_ABP || p->model == SPP_MODEL_CONTINUOUS);
+  s->uses_list = (p->model == SPP_MODEL_ABP || p->model == SPP_MODEL_CONTINUOUS ||
+                  p->model == SPP_MODEL_BEADS);
   s->nstages = p->integrator == SPP_INT_RK4 ? 4 : (p->integrator == SPP_INT_RK2 ? 2 : 1);
   if (!s->uses_list) s->nstages = 1;
   const char* env = getenv("SPP_NO_GRAPHS");
@@ -421,6 +427,7 @@ int spp_create(const SppParams* p, SppSystem** out) {
   rc = rc ? rc : dalloc(&d.theta, n);
   rc = rc ? rc : dalloc(&d.img, n);
   rc = rc ? rc : dalloc(&d.id, n);
+  if (p->model == SPP_MODEL_BEADS) rc = rc ? rc : dalloc(&d.inv, n);
   rc = rc ? rc : dalloc(&d.kacc, s->nstages > 2 ? n : 1);
   rc = rc ? rc : dalloc(&d.dth, s->nstages > 1 ? n : 1);
   rc = rc ? rc : dalloc(&d.ref, n);

@@ -230,6 +230,7 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
     d.theta[i] = d.theta_alt[i];
     d.img[i] = d.img_alt[i];
     d.id[i] = d.id_alt[i];
+    if (d.inv) d.inv[d.id_alt[i]] = (uint32_t)i;
   }
   if (with_list) {
     uint32_t m = __reduce_max_sync(0xffffffffu, cnt);

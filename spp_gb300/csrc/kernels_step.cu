@@ -134,10 +134,33 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(S
     }
     if (LAW == SPP_FORCE_R12_TRUNC && a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
     float fx, fy, tau;
-    spp_abp_forces(&k, &a, pi.z, pi.w, &fx, &fy, &tau);
+    int turns = 1;
+    uint32_t pid = 0;
+    if (KIND == SPP_KIND_BEADS) {
+      /* membrane beads add their ring forces; positions of the ring
+       * neighbours come from the same stage state, found through id -> slot */
+      pid = d.id[i];
+      float rfx = 0.0f, rfy = 0.0f;
+      const int bead = pid < (uint32_t)k.n_beads;
+      if (bead) {
+        float px[5], py[5];
+#pragma unroll
+        for (int o = -2; o <= 2; ++o) {
+          const uint32_t slot = o == 0 ? (uint32_t)i : d.inv[spp_ring_neighbor(&k, pid, o)];
+          const float4 q = o == 0 ? pi : __ldg(b.cur + slot);
+          px[o + 2] = q.x;
+          py[o + 2] = q.y;
+        }
+        spp_ring_forces(&k, px, py, &rfx, &rfy);
+      }
+      spp_bead_velocity(&k, !bead, &a, rfx, rfy, pi.z, pi.w, &fx, &fy, &tau);
+      turns = !bead;
+    } else {
+      spp_abp_forces(&k, &a, pi.z, pi.w, &fx, &fy, &tau);
+    }
     float dth;
     if (b.stage == 0) {
-      dth = spp_rot_noise(&k, d.id[i], d.ctl->step);
+      dth = turns ? spp_rot_noise(&k, KIND == SPP_KIND_BEADS ? pid : d.id[i], d.ctl->step) : 0.0f;
       if (b.nstages > 1) d.dth[i] = dth;
     } else {
       dth = d.dth[i];
@@ -297,6 +320,9 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
   SPP_STAGE_CASE(SPP_FORCE_HARMONIC, SPP_KIND_CONT_ALPHA)
   SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_CONT)
   SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_CONT_ALPHA)
+  SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_BEADS)
+  SPP_STAGE_CASE(SPP_FORCE_HARMONIC, SPP_KIND_BEADS)
+  SPP_STAGE_CASE(SPP_FORCE_NONE, SPP_KIND_BEADS)
   {}
 #undef SPP_STAGE_CASE
   if (launches) *launches += 1;

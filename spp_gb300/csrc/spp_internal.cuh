@@ -52,6 +52,7 @@ struct DevState {
   float* theta;
   int2* img;
   uint32_t* id;
+  uint32_t* inv;          /* particle id -> slot (ring neighbours of membrane beads) */
   float4* kacc;
   float* dth;             /* rotational noise of the current step (multi-stage integrators) */
   float2* ref;

@@ -38,6 +38,12 @@ typedef struct SppConsts {
   float rlist, rlist2;         /* Verlet list radius */
   float half_skin;             /* rebuild threshold on displacements */
   float interior;              /* |x|,|y| below this: no list neighbour is across the boundary */
+  /* ring membranes + swimmers (SPP_MODEL_BEADS) */
+  int32_t n_beads;             /* bodies [0, n_beads) are membrane beads */
+  int32_t ring_size;
+  float mu;                    /* translational mobility (m_parallel = m_perpendicular) */
+  float ang_drift;             /* k_perp * torque0: intrinsic angular velocity of swimmers */
+  float k_bond, bond_rest, kappa;
 } SppConsts;
 
 /* Host-side: round the double parameters to the kernels' floats. */
@@ -76,13 +82,20 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
   k->r_push = (float)p->r_push;
   k->rpush2 = (float)(p->r_push * p->r_push);
   {
-    double rc = p->r_align;
+    double rc = p->model == SPP_MODEL_BEADS ? 0.0 : p->r_align;
     if (p->force_law != SPP_FORCE_NONE && p->r_rep > rc) rc = p->r_rep;
     if (p->model == SPP_MODEL_VICSEK_REF_VECTOR && p->r_push > rc) rc = p->r_push;
     double rl = rc + (p->skin > 0 ? p->skin : 0.0);
     k->rlist = (float)rl;
     k->rlist2 = (float)(rl * rl);
     k->half_skin = (float)(0.5 * (p->skin > 0 ? p->skin : 0.0));
+    k->n_beads = p->model == SPP_MODEL_BEADS ? p->n_rings * p->ring_size : 0;
+    k->ring_size = p->ring_size;
+    k->mu = (float)p->mu;
+    k->ang_drift = (float)(p->k_perp * p->torque0);
+    k->k_bond = (float)p->k_bond;
+    k->bond_rest = (float)p->bond_rest;
+    k->kappa = (float)p->kappa_bend;
     k->interior = (float)(p->L - 2.0 * (rl + (p->skin > 0 ? p->skin : 0.0)));
   }
 }
@@ -130,8 +143,10 @@ SPP_HD void spp_accf_zero(SppAccF* a) { a->fx = 0.0f; a->fy = 0.0f; a->tq = 0.0f
 #define SPP_KIND_ABP 0          /* sin(theta_j - theta_i), neighbour count */
 #define SPP_KIND_CONT 1         /* (1 - alpha)/pi sin(...)                  */
 #define SPP_KIND_CONT_ALPHA 2   /* ... - alpha (dr x v_i) / (pi d)          */
+#define SPP_KIND_BEADS 3        /* repulsion only (ActiveBrownianChain nb = 1) */
 
 SPP_HD int spp_pair_kind(const SppConsts* k) {
+  if (k->model == SPP_MODEL_BEADS) return SPP_KIND_BEADS;
   if (k->model != SPP_MODEL_CONTINUOUS) return SPP_KIND_ABP;
   return k->alpha_over_pi != 0.0f ? SPP_KIND_CONT_ALPHA : SPP_KIND_CONT;
 }
@@ -156,7 +171,7 @@ SPP_HD void spp_pair_abp_lkw(const SppConsts* k, int law, int kind, int wrap, Sp
     d2 = fmaf(dx, dx, dy * dy);
   }
   const int in_rep = (law != SPP_FORCE_NONE) && (d2 < k->rrep2) && (d2 > 0.0f);
-  const int in_al = d2 < k->ral2;
+  const int in_al = (kind != SPP_KIND_BEADS) && d2 < k->ral2;
   if (!(in_rep || in_al)) return;
   float r = 0.0f;
   if (in_rep || (kind == SPP_KIND_CONT_ALPHA && in_al && d2 > 0.0f)) r = spp_rsqrtf(d2);
@@ -306,6 +321,95 @@ SPP_HD void spp_vicsek_update(const SppConsts* k, const SppAcc* a, float x0, flo
   *th = t;
   *x = spp_wrap_coord_f(fmaf(k->v0dt, *c, x0), k->L, k->L2, imgx);
   *y = spp_wrap_coord_f(fmaf(k->v0dt, *s, y0), k->L, k->L2, imgy);
+}
+
+/* ------------------------------------------------------------------ */
+/* ring membranes (SPP_MODEL_BEADS)                                    */
+/* ------------------------------------------------------------------ */
+/* Ring forces on bead m from its bonds and from the bending of the three
+ * bond angles it takes part in.  px/py hold ring beads m-2 .. m+2 (index 2
+ * is bead m).
+ *   bonds: Spring (shared/force-fields.h:87-97) between consecutive beads,
+ *     as Interact_Membrane_Beads (parallel/beadbox.h:185-196): the force on
+ *     bead m is S(r_m - r_{m-1}) + S(r_m - r_{m+1}), S(dr) = k (rest - d) dr/d.
+ *   bending (no counterpart in the reference): E = kappa sum_j (1 - cos phi_j),
+ *     phi_j the angle between the bonds u = r_j - r_{j-1} and w = r_{j+1} - r_j.
+ *     With c = u.w / (|u||w|), dc/du = w/(|u||w|) - c u/|u|^2 and
+ *     dc/dw = u/(|u||w|) - c w/|w|^2, bead m receives
+ *       kappa dc_{m-1}/dw + kappa (dc_m/du - dc_m/dw) - kappa dc_{m+1}/du. */
+SPP_HD void spp_ring_forces(const SppConsts* k, const float* px, const float* py, float* fx,
+                            float* fy) {
+  float bx[4], by[4], ib[4], b2[4];
+  for (int q = 0; q < 4; ++q) {
+    bx[q] = spp_min_image_f(px[q + 1] - px[q], k->L, k->L2);
+    by[q] = spp_min_image_f(py[q + 1] - py[q], k->L, k->L2);
+    b2[q] = fmaf(bx[q], bx[q], by[q] * by[q]);
+    ib[q] = spp_rsqrtf(b2[q]);
+  }
+  float gx = 0.0f, gy = 0.0f;
+  /* bonds (m-1, m) and (m, m+1): S(b_1) - S(b_2) with S(b) = k (rest - |b|) b / |b| */
+  {
+    const float t1 = k->k_bond * (k->bond_rest * ib[1] - 1.0f);
+    const float t2 = k->k_bond * (k->bond_rest * ib[2] - 1.0f);
+    gx = gx + t1 * bx[1];
+    gy = gy + t1 * by[1];
+    gx = gx - t2 * bx[2];
+    gy = gy - t2 * by[2];
+  }
+  if (k->kappa != 0.0f) {
+    /* angle j = m + q - 1 for q = 0, 1, 2 uses u = b_q, w = b_{q+1} */
+    for (int q = 0; q < 3; ++q) {
+      const float iuw = ib[q] * ib[q + 1];
+      const float c = (bx[q] * bx[q + 1] + by[q] * by[q + 1]) * iuw;
+      const float cu = c * (ib[q] * ib[q]);
+      const float cw = c * (ib[q + 1] * ib[q + 1]);
+      /* dc/du and dc/dw */
+      const float dux = bx[q + 1] * iuw - cu * bx[q];
+      const float duy = by[q + 1] * iuw - cu * by[q];
+      const float dwx = bx[q] * iuw - cw * bx[q + 1];
+      const float dwy = by[q] * iuw - cw * by[q + 1];
+      if (q == 0) {
+        gx = gx + k->kappa * dwx;
+        gy = gy + k->kappa * dwy;
+      } else if (q == 1) {
+        gx = gx + k->kappa * (dux - dwx);
+        gy = gy + k->kappa * (duy - dwy);
+      } else {
+        gx = gx - k->kappa * dux;
+        gy = gy - k->kappa * duy;
+      }
+    }
+  }
+  *fx = gx;
+  *fy = gy;
+}
+
+/* Id of the ring bead at offset o (-2..2) from bead id along its ring. */
+SPP_HD uint32_t spp_ring_neighbor(const SppConsts* k, uint32_t id, int o) {
+  const uint32_t M = (uint32_t)k->ring_size;
+  const uint32_t ring = id / M, m = id % M;
+  const uint32_t mm = (uint32_t)(((int)m + o + (int)M) % (int)M);
+  return ring * M + mm;
+}
+
+/* Velocity and angular velocity of a body of SPP_MODEL_BEADS
+ * (ActiveBrownianChain::Move_Runge_Kutta2_*, shared/particle.h:917-962, with
+ * m_parallel = m_perpendicular = mu as for nb = 1): swimmers move at
+ * v0 (cos, sin) + mu F and turn at k_perp torque0; membrane beads (F0 = 0)
+ * move at mu F and do not turn. */
+SPP_HD void spp_bead_velocity(const SppConsts* k, int swimmer, const SppAccF* a, float rfx,
+                              float rfy, float ci, float si, float* vx, float* vy, float* om) {
+  const float Fx = a->fx + rfx;
+  const float Fy = a->fy + rfy;
+  if (swimmer) {
+    *vx = k->v0 * ci + k->mu * Fx;
+    *vy = k->v0 * si + k->mu * Fy;
+    *om = k->ang_drift;
+  } else {
+    *vx = k->mu * Fx;
+    *vy = k->mu * Fy;
+    *om = 0.0f;
+  }
 }
 
 /* ------------------------------------------------------------------ */

@@ -40,6 +40,16 @@ def cases():
         p = configs.vicsek_config(n=1024, L=16.0, model=model, seed=0)
         x, y, th = configs.random_state(p.n, p.L, seed=3)
         out.append((name, p, x.astype(np.float64), y.astype(np.float64), th.astype(np.float64), 20))
+    for integ, name in ((abi.INT_EULER, "beads_euler"), (abi.INT_RK2, "beads_rk2")):
+        # ActiveBrownianChain (nb = 1) rings + swimmers with the reference's
+        # membrane repulsion (sigma 0.5, cutoff 0.55) and Spring bonds
+        p = configs.vesicle_config(n_rings=4, ring_size=40, swimmers_per_ring=8, L=20.0,
+                                   integrator=integ)
+        x, y, th = configs.vesicle_state(p)  # rings of unit bonds, then stretched below
+        p.sigma_rep, p.r_rep, p.k_rep = 0.5, 0.55, 1.0
+        p.bond_rest, p.k_bond, p.kappa_bend = 0.55, 30.0, 0.0
+        p.Dr, p.dt = 0.2, 0.002
+        out.append((name, p, x.astype(np.float64), y.astype(np.float64), th.astype(np.float64), 60))
     p = configs.reference_defaults(abi.MODEL_CONTINUOUS)
     p.n, p.L, p.Dr, p.dt, p.v0, p.seed = 1024, 16.0, 0.05, 0.01, 0.5, 11
     x, y, th = configs.random_state(p.n, p.L, seed=3)

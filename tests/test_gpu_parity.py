@@ -186,3 +186,38 @@ def test_full_size_abp_properties(gpu_lib):
     assert disp.max() < 400 * p.dt * 8.0
     assert 0.0 <= o.polarization <= 1.0
     assert o.n_rebuilds > 3
+
+
+@pytest.mark.parametrize("integ", [abi.INT_RK2, abi.INT_RK4])
+def test_vesicles_bitexact_vs_mirror(gpu_lib, integ):
+    """Ring membranes (bonds + bending) with swimmers, bit-exact against the mirror."""
+    p = configs.vesicle_config(n_rings=16, ring_size=64, swimmers_per_ring=16, L=48.0,
+                               integrator=integ)
+    x, y, th = configs.vesicle_state(p)
+    gpu, obs = run_gpu(p, x, y, th, 150)
+    ref = O.run32(p, O.State32(x, y, th), 150)
+    assert_bitexact(gpu, ref)
+    assert obs.late_rebuilds == 0
+
+
+def test_vesicles_full_size_bitexact_vs_mirror(gpu_lib):
+    """The full vesicle workload: 1024 rings x 128 beads + 32,768 swimmers, RK4."""
+    p = configs.vesicle_config()
+    x, y, th = configs.vesicle_state(p)
+    gpu, obs = run_gpu(p, x, y, th, 4)
+    ref = O.run32(p, O.State32(x, y, th), 4)
+    assert_bitexact(gpu, ref)
+
+
+def test_vesicles_vs_fp64(gpu_lib):
+    p = configs.vesicle_config(n_rings=16, ring_size=64, swimmers_per_ring=16, L=48.0)
+    x, y, th = configs.vesicle_state(p)
+    (gx, gy, gth, gix, giy), _ = run_gpu(p, x, y, th, 100)
+    a = O.run64(p, O.State64(x, y, th), 100)
+    xu = gx.astype(np.float64) + 2 * p.L * gix
+    yu = gy.astype(np.float64) + 2 * p.L * giy
+    nb = p.n_rings * p.ring_size
+    assert np.max(np.abs(xu - a.xu)) / (2 * p.L) < 1e-5
+    assert np.max(np.abs(yu - a.yu)) / (2 * p.L) < 1e-5
+    dth = np.abs((gth[nb:].astype(np.float64) - a.th[nb:] + np.pi) % (2 * np.pi) - np.pi)
+    assert np.max(dth) < 1e-5
