@@ -173,6 +173,29 @@ int spp_pairs(SppSystem* s, double r, int32_t* pi, int32_t* pj, int cap, int64_t
  * D x D cells under the given SppBinRule (Box::Update_Cells, serial/box.h:107-134). */
 int spp_cells(SppSystem* s, int D, int rule, int32_t* cell_x, int32_t* cell_y, int n);
 
+/* ---- tangent-space Lyapunov spectrum (continuous model) ----
+ * Replaces LyapunovBox (parallel/lyapunovbox.h:11-28): Init_Deviation
+ * (:32-42), Evolution_Reorthonormalize (:128-194) and Lyapunov_Exponent
+ * (:197-255).  The reference evolves k finite perturbations of size 1e-7 as
+ * full clones of the system; here k tangent vectors follow the linearised
+ * integrator (RK2/RK4 of SPP_MODEL_CONTINUOUS with alpha = 0, no
+ * repulsion) and are renormalised every renorm_every steps in FP64
+ * (Gram-Schmidt in Cholesky-QR form, as VectorSet::Renormalize,
+ * shared/vector-set.h:118-127), the log of each stretch summed in FP64. */
+/* k <= 8 tangent vectors of dimension 3n, N(0,1) entries from the Philox
+ * stream keyed by seed, orthonormalised; resets the log-stretch sums. */
+int spp_lyap_init(SppSystem* s, int k, uint64_t seed);
+/* Replaces the tangent vectors ([k][x|y|theta][n], particle-id order)
+ * without renormalising them; resets the sums. */
+int spp_lyap_set_vectors(SppSystem* s, const float* v, int k);
+/* nsteps steps of the base and tangent dynamics, renormalising after every
+ * renorm_every steps and at the end. */
+int spp_lyap_step(SppSystem* s, int nsteps, int renorm_every);
+/* Exponents lambda_a = (sum of log stretches) / elapsed time, a < k. */
+int spp_lyap_exponents(SppSystem* s, double* lambda, int k, double* elapsed);
+/* The current (orthonormal) tangent vectors, [k][x|y|theta][n]. */
+int spp_lyap_vectors(SppSystem* s, float* v, int k);
+
 /* ---- measurement helpers (no reference counterpart) ---- */
 typedef struct SppProfile {
   int64_t steps;          /* steps advanced by the profiling run */

@@ -40,6 +40,13 @@ def orc():
         L.orc32_philox.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.orc32_math.argtypes = [C.c_int, C.c_int, _F, _F, _F]
         L.orc32_fx_sum.argtypes = [C.c_int, _F, _I, _I, _F]
+        L.orc32_renormalize.argtypes = [C.c_int, C.c_int, _F, _D, C.c_int]
+        L.orc32_lyap_init.argtypes = [_P, C.c_int, C.c_uint64, _F]
+        L.orc32_lyap_run.argtypes = [_P, C.c_int, C.c_int64, C.c_int, C.c_int, _F, _F, _F, _I, _I,
+                                     _F, _D]
+        L.orc64_lyap_tangent.argtypes = [_P, C.c_int, C.c_int, C.c_int, _D, _D, _D, _D, _D, _D, _D]
+        L.orc64_lyap_clone.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D,
+                                       _D, _D, _D]
         L.orc32_rsqrt.argtypes = [C.c_float]
         L.orc32_rsqrt.restype = C.c_float
         _orc = L
@@ -196,6 +203,49 @@ def fx_sum(x):
 
 def rsqrt32(x):
     return float(orc().orc32_rsqrt(float(x)))
+
+
+def lyap_init32(p, K, seed):
+    V = np.empty(K * 3 * p.n, np.float32)
+    rc = orc().orc32_lyap_init(C.byref(p), int(K), int(seed), _f(V))
+    if rc:
+        raise RuntimeError(f"mirror lyap init failed {rc}")
+    return V
+
+
+def lyap_run32(p, state: State32, V, nsteps, renorm_every, step0=0):
+    """Mirror of the kernels' base + tangent steps; V ([K*3*n] float32) and
+    the returned log-stretch sums are updated in place."""
+    K = V.size // (3 * p.n)
+    ls = np.zeros(K, np.float64)
+    s = state
+    rc = orc().orc32_lyap_run(C.byref(p), int(nsteps), int(step0), int(renorm_every), K, _f(s.x),
+                              _f(s.y), _f(s.th), _i(s.ix), _i(s.iy), _f(V), _d(ls))
+    if rc:
+        raise RuntimeError(f"mirror lyap run failed {rc}")
+    return ls
+
+
+def lyap_tangent64(p, state: State64, V, nsteps, renorm_every):
+    K = V.size // (3 * p.n)
+    ls = np.zeros(K, np.float64)
+    s = state
+    rc = orc().orc64_lyap_tangent(C.byref(p), int(nsteps), int(renorm_every), K, _d(s.x), _d(s.y),
+                                  _d(s.th), _d(s.xu), _d(s.yu), _d(V), _d(ls))
+    if rc:
+        raise RuntimeError(f"oracle lyap tangent failed {rc}")
+    return ls
+
+
+def lyap_clone64(p, state: State64, V, n_intervals, tau, eps=1e-7):
+    K = V.size // (3 * p.n)
+    ls = np.zeros(K, np.float64)
+    s = state
+    rc = orc().orc64_lyap_clone(C.byref(p), int(n_intervals), int(tau), K, float(eps), _d(s.x),
+                                _d(s.y), _d(s.th), _d(s.xu), _d(s.yu), _d(V), _d(ls))
+    if rc:
+        raise RuntimeError(f"oracle lyap clone failed {rc}")
+    return ls
 
 
 MATH_FNS = {"sin": 0, "cos": 1, "atan2": 2, "log": 3, "exp": 4, "wrap": 5}

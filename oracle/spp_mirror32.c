@@ -319,3 +319,202 @@ void orc32_math(int fn, int n, const float* a, const float* b, float* out) {
     }
   }
 }
+
+/* ------------------------------------------------------------------ */
+/* tangent dynamics + FP64 renormalisation, as the kernels compute them  */
+/* ------------------------------------------------------------------ */
+/* Cholesky-QR pass with the reduction order of k_gram / k_chol / k_apply:
+ * SPP_GRAM_BLOCKS x SPP_GRAM_THREADS threads stride over the elements, a
+ * shuffle-down tree per warp, warps summed in order, blocks summed in order. */
+static int mirror_cholqr_pass(int K, int len, float* V, double* log_stretch, int accumulate) {
+  const int NE = K * (K + 1) / 2;
+  const int stride = SPP_GRAM_BLOCKS * SPP_GRAM_THREADS;
+  static double part[SPP_GRAM_BLOCKS][SPP_GRAM_ENTRIES];
+  double thr[SPP_GRAM_THREADS][SPP_GRAM_ENTRIES];
+  for (int b = 0; b < SPP_GRAM_BLOCKS; ++b) {
+    for (int t = 0; t < SPP_GRAM_THREADS; ++t) {
+      for (int q = 0; q < NE; ++q) thr[t][q] = 0.0;
+      for (int e = b * SPP_GRAM_THREADS + t; e < len; e += stride) {
+        double v[SPP_LYAP_MAX];
+        for (int a = 0; a < K; ++a) v[a] = (double)V[(size_t)a * len + e];
+        for (int a = 0; a < K; ++a)
+          for (int c = 0; c <= a; ++c) thr[t][a * (a + 1) / 2 + c] = thr[t][a * (a + 1) / 2 + c] + v[a] * v[c];
+      }
+    }
+    double warp_part[SPP_GRAM_THREADS / 32][SPP_GRAM_ENTRIES];
+    for (int w = 0; w < SPP_GRAM_THREADS / 32; ++w) {
+      for (int q = 0; q < NE; ++q) {
+        double x[32];
+        for (int l = 0; l < 32; ++l) x[l] = thr[w * 32 + l][q];
+        for (int o = 16; o > 0; o >>= 1) {
+          double y[32];
+          for (int l = 0; l < 32; ++l) y[l] = x[l] + (l + o < 32 ? x[l + o] : x[l]);
+          memcpy(x, y, sizeof(x));
+        }
+        warp_part[w][q] = x[0];
+      }
+    }
+    for (int q = 0; q < NE; ++q) {
+      double x = 0.0;
+      for (int w = 0; w < SPP_GRAM_THREADS / 32; ++w) x = x + warp_part[w][q];
+      part[b][q] = x;
+    }
+  }
+  double G[SPP_GRAM_ENTRIES];
+  for (int q = 0; q < NE; ++q) {
+    double x = 0.0;
+    for (int b = 0; b < SPP_GRAM_BLOCKS; ++b) x = x + part[b][q];
+    G[q] = x;
+  }
+  double rinv[SPP_LYAP_MAX * SPP_LYAP_MAX], lr[SPP_LYAP_MAX];
+  if (spp_cholesky_inverse(K, G, rinv, lr)) return 1;
+  if (accumulate)
+    for (int a = 0; a < K; ++a) log_stretch[a] = log_stretch[a] + lr[a];
+  for (int e = 0; e < len; ++e) {
+    double v[SPP_LYAP_MAX];
+    for (int a = 0; a < K; ++a) v[a] = (double)V[(size_t)a * len + e];
+    for (int a = 0; a < K; ++a) {
+      double x = 0.0;
+      for (int c = 0; c <= a; ++c) x = x + v[c] * rinv[c * SPP_LYAP_MAX + a];
+      V[(size_t)a * len + e] = (float)x;
+    }
+  }
+  return 0;
+}
+
+int orc32_renormalize(int K, int n, float* V, double* log_stretch, int accumulate) {
+  for (int pass = 0; pass < 2; ++pass)
+    if (mirror_cholqr_pass(K, 3 * n, V, log_stretch, accumulate)) return SPP_ERR_NUMERIC;
+  return SPP_OK;
+}
+
+/* The kernels' initial tangent vectors: N(0,1) from the tangent stream,
+ * then orthonormalised. */
+int orc32_lyap_init(const SppParams* p, int K, uint64_t seed, float* V) {
+  int n = p->n;
+  for (int e = 0; e < K * 3 * n; ++e) {
+    int id = e % n, vc = e / n;
+    spp_u32x4 r = spp_draw(seed, p->system_id, (uint32_t)id, (uint32_t)vc, SPP_RNG_TANGENT);
+    V[e] = spp_normal_f(r.v[0], r.v[1]);
+  }
+  double dummy[SPP_LYAP_MAX] = {0};
+  return orc32_renormalize(K, n, V, dummy, 0);
+}
+
+/* Base (continuous model, RK2/RK4) and tangent steps; renormalisation after
+ * every renorm_every steps and at the end (renorm_every <= 0: never). */
+int orc32_lyap_run(const SppParams* p, int nsteps, int64_t step0, int renorm_every, int K, float* x,
+                   float* y, float* th, int32_t* ix, int32_t* iy, float* V, double* log_stretch) {
+  SppConsts k;
+  spp_consts_from_params(&k, p);
+  const int n = p->n;
+  const int nst = p->integrator == SPP_INT_RK4 ? 4 : 2;
+  const double rcut = mirror_rcut(p);
+  float *c = malloc(sizeof(float) * n), *s = malloc(sizeof(float) * n);
+  float *hx = malloc(sizeof(float) * n), *hy = malloc(sizeof(float) * n);
+  float *hc = malloc(sizeof(float) * n), *hs = malloc(sizeof(float) * n);
+  float *kx = malloc(sizeof(float) * n), *ky = malloc(sizeof(float) * n), *kt = malloc(sizeof(float) * n);
+  float *nx = malloc(sizeof(float) * n), *ny = malloc(sizeof(float) * n);
+  float *nc = malloc(sizeof(float) * n), *ns = malloc(sizeof(float) * n);
+  size_t len = (size_t)K * 3 * n;
+  float *ua = malloc(sizeof(float) * len), *ub = malloc(sizeof(float) * len);
+  float *acc = malloc(sizeof(float) * len);
+  SppAccF* A = malloc(sizeof(SppAccF) * n);
+  int* cand = malloc(sizeof(int) * 64);
+  int cap = 64;
+  int rc = SPP_OK;
+  for (int i = 0; i < n; ++i) spp_sincosf(th[i], &s[i], &c[i]);
+  for (int st = 0; st < nsteps && rc == SPP_OK; ++st) {
+    uint32_t step = (uint32_t)(step0 + st);
+    for (int stage = 0; stage < nst; ++stage) {
+      const float *cx = stage == 0 ? x : hx, *cy = stage == 0 ? y : hy;
+      const float *cc = stage == 0 ? c : hc, *cs = stage == 0 ? s : hs;
+      const float* uin = stage == 0 ? V : ((stage & 1) ? ua : ub);
+      float* uout = (stage & 1) ? ub : ua;
+      int last = stage == nst - 1;
+      mcells cl;
+      mcells_build(&cl, n, cx, cy, &k, rcut);
+      /* tangent slopes need the neighbour list at this stage state, in id order */
+      float* slopes = malloc(sizeof(float) * len);
+      for (int i = 0; i < n; ++i) {
+        int m = 0;
+        FOR_CANDIDATES(&cl, &k, cx[i], cy[i], n, j, {
+          if (j != i) {
+            if (m == cap) { cap *= 2; cand = realloc(cand, sizeof(int) * cap); }
+            cand[m++] = j;
+          }
+        });
+        qsort(cand, (size_t)m, sizeof(int), cmp_int);
+        SppAccF a;
+        spp_accf_zero(&a);
+        float tacc[SPP_LYAP_MAX];
+        for (int v = 0; v < K; ++v) tacc[v] = 0.0f;
+        for (int q = 0; q < m; ++q) {
+          int j = cand[q];
+          spp_pair_abp(&k, &a, cx[i], cy[i], cc[i], cs[i], cx[j], cy[j], cc[j], cs[j]);
+          float dx, dy;
+          float d2 = spp_sep(&k, cx[i], cy[i], cx[j], cy[j], &dx, &dy);
+          if (d2 < k.ral2) {
+            float cij = spp_tangent_coupling(cc[i], cs[i], cc[j], cs[j]);
+            for (int v = 0; v < K; ++v)
+              tacc[v] = tacc[v] + cij * (uin[(size_t)(v * 3 + 2) * n + j] - uin[(size_t)(v * 3 + 2) * n + i]);
+          }
+        }
+        A[i] = a;
+        const float gp = k.g * k.one_minus_alpha_over_pi;
+        for (int v = 0; v < K; ++v) {
+          float ui = uin[(size_t)(v * 3 + 2) * n + i];
+          slopes[(size_t)(v * 3 + 0) * n + i] = -k.v0 * cs[i] * ui;
+          slopes[(size_t)(v * 3 + 1) * n + i] = k.v0 * cc[i] * ui;
+          slopes[(size_t)(v * 3 + 2) * n + i] = gp * tacc[v];
+        }
+      }
+      mcells_free(&cl);
+      /* base stage update */
+      for (int i = 0; i < n; ++i) {
+        float fx, fy, tau;
+        spp_abp_forces(&k, &A[i], cc[i], cs[i], &fx, &fy, &tau);
+        float dth = spp_rot_noise(&k, (uint32_t)i, step);
+        float h, frac;
+        if (nst == 2) {
+          h = stage == 0 ? k.half_dt : k.dt;
+          frac = stage == 0 ? 0.5f : 1.0f;
+        } else {
+          if (stage == 0) { kx[i] = fx; ky[i] = fy; kt[i] = tau; }
+          else if (stage < 3) { kx[i] = kx[i] + 2.0f * fx; ky[i] = ky[i] + 2.0f * fy; kt[i] = kt[i] + 2.0f * tau; }
+          else { fx = kx[i] + fx; fy = ky[i] + fy; tau = kt[i] + tau; }
+          h = stage < 2 ? k.half_dt : (stage == 2 ? k.dt : k.dt6);
+          frac = stage < 2 ? 0.5f : 1.0f;
+        }
+        float tnew;
+        int gx = ix[i], gy = iy[i];
+        spp_stage_update(h, frac, x[i], y[i], th[i], fx, fy, tau, dth, &k, &nx[i], &ny[i], &tnew,
+                         &nc[i], &ns[i], &gx, &gy);
+        if (last) { th[i] = tnew; ix[i] = gx; iy[i] = gy; }
+      }
+      /* tangent stage update */
+      for (size_t e = 0; e < len; ++e) {
+        float t0 = V[e];
+        float a = stage == 0 ? 0.0f : acc[e];
+        float uo = 0.0f;
+        spp_tangent_stage_update(&k, stage, nst, slopes[e], &t0, &a, &uo);
+        if (last) V[e] = t0;
+        else uout[e] = uo;
+        if (nst == 4 && stage < 3) acc[e] = a;
+      }
+      free(slopes);
+      if (last) {
+        memcpy(x, nx, sizeof(float) * n); memcpy(y, ny, sizeof(float) * n);
+        memcpy(c, nc, sizeof(float) * n); memcpy(s, ns, sizeof(float) * n);
+      } else {
+        memcpy(hx, nx, sizeof(float) * n); memcpy(hy, ny, sizeof(float) * n);
+        memcpy(hc, nc, sizeof(float) * n); memcpy(hs, ns, sizeof(float) * n);
+      }
+    }
+    if (renorm_every > 0 && ((st + 1) % renorm_every == 0 || st + 1 == nsteps))
+      if (orc32_renormalize(K, n, V, log_stretch, 1)) rc = SPP_ERR_NUMERIC;
+  }
+  free(c); free(s); free(hx); free(hy); free(hc); free(hs); free(kx); free(ky); free(kt);
+  free(nx); free(ny); free(nc); free(ns); free(ua); free(ub); free(acc); free(A); free(cand);
+  return rc;
+}

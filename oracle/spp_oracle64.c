@@ -660,3 +660,195 @@ double orc_polarization(int n, const double* th, double* px, double* py) {
   if (py) *py = sy;
   return sqrt(sx * sx + sy * sy);
 }
+
+/* ------------------------------------------------------------------ */
+/* Lyapunov spectrum                                                   */
+/* ------------------------------------------------------------------ */
+/* Modified Gram-Schmidt on K vectors of length len (VectorSet::
+ * Renormalize(us), shared/vector-set.h:118-127: each vector loses its
+ * projections on the already orthonormalised ones, then is normalised);
+ * log of each norm added to log_stretch[a] (when not NULL) after dividing by
+ * scale. */
+static void mgs(int K, size_t len, double* V, double* log_stretch, double scale) {
+  for (int a = 0; a < K; ++a) {
+    double* va = V + (size_t)a * len;
+    for (int b = 0; b < a; ++b) {
+      const double* vb = V + (size_t)b * len;
+      double dot = 0;
+      for (size_t e = 0; e < len; ++e) dot += vb[e] * va[e];
+      for (size_t e = 0; e < len; ++e) va[e] -= dot * vb[e];
+    }
+    double nn = 0;
+    for (size_t e = 0; e < len; ++e) nn += va[e] * va[e];
+    double nrm = sqrt(nn);
+    for (size_t e = 0; e < len; ++e) va[e] /= nrm;
+    if (log_stretch) log_stretch[a] += log(nrm / scale);
+  }
+}
+
+typedef struct {
+  ostate* s;
+  const double* U;  /* stage tangent input [K][3][n] */
+  double* T;        /* theta slope sums [K][n] */
+  int K;
+} tctx;
+
+/* sum_j cos(th_j - th_i) (u_j - u_i) over pairs within the alignment radius */
+static void tangent_pair(void* ctx, int i, int j) {
+  tctx* c = (tctx*)ctx;
+  ostate* s = c->s;
+  const SppParams* p = s->p;
+  double dx = pt(s->x[i] - s->x[j], p->L), dy = pt(s->y[i] - s->y[j], p->L);
+  if (dx * dx + dy * dy < p->r_align * p->r_align) {
+    double cij = cos(s->th[j] - s->th[i]);
+    int n = s->n;
+    for (int v = 0; v < c->K; ++v) {
+      double ui = c->U[(size_t)(v * 3 + 2) * n + i], uj = c->U[(size_t)(v * 3 + 2) * n + j];
+      c->T[(size_t)v * n + i] += cij * (uj - ui);
+      c->T[(size_t)v * n + j] += cij * (ui - uj);
+    }
+  }
+}
+
+/* Tangent-space estimator in FP64: continuous model (alpha = 0), RK2/RK4
+ * base steps (abp_step's RK schemes) with the tangent vectors advanced by
+ * the derivative of each stage; MGS every renorm_every steps and at the end.
+ * V is [K][x|y|theta][n] (orthonormal on entry). */
+int orc64_lyap_tangent(const SppParams* p, int nsteps, int renorm_every, int K, double* x, double* y,
+                       double* th, double* xu, double* yu, double* V, double* log_stretch) {
+  if (p->model != SPP_MODEL_CONTINUOUS || p->alpha != 0.0 || p->integrator == SPP_INT_EULER)
+    return SPP_ERR_UNSUPPORTED;
+  ostate s;
+  state_alloc(&s, p);
+  int n = p->n;
+  memcpy(s.x, x, sizeof(double) * n); memcpy(s.y, y, sizeof(double) * n);
+  memcpy(s.xu, xu, sizeof(double) * n); memcpy(s.yu, yu, sizeof(double) * n);
+  memcpy(s.th, th, sizeof(double) * n);
+  for (int i = 0; i < n; ++i) set_v(&s, i);
+  size_t len = (size_t)K * 3 * n;
+  double *U = malloc(sizeof(double) * len), *ACC = malloc(sizeof(double) * len);
+  double *T = malloc(sizeof(double) * (size_t)K * n), *SL = malloc(sizeof(double) * len);
+  int nst = p->integrator == SPP_INT_RK4 ? 4 : 2;
+  double dt = p->dt, gp = p->g * (1 - p->alpha) / M_PI;
+  double sigma = sqrt(2 * p->Dr * dt);
+  for (int st = 0; st < nsteps; ++st) {
+    for (int i = 0; i < n; ++i) {
+      s.tho[i] = s.th[i]; s.xo[i] = s.xu[i]; s.yo[i] = s.yu[i];
+      s.dth[i] = sigma * orc_normal(p, i, st);
+    }
+    memcpy(U, V, sizeof(double) * len);
+    for (int stage = 0; stage < nst; ++stage) {
+      /* tangent slopes at this stage state */
+      memset(T, 0, sizeof(double) * (size_t)K * n);
+      tctx c = {&s, U, T, K};
+      ocells cl;
+      cells_build(&cl, n, s.x, s.y, p->L, p->r_align);
+      cells_for_pairs(&cl, n, tangent_pair, &c);
+      cells_free(&cl);
+      for (int v = 0; v < K; ++v)
+        for (int i = 0; i < n; ++i) {
+          double ut = U[(size_t)(v * 3 + 2) * n + i];
+          SL[(size_t)(v * 3 + 0) * n + i] = -p->v0 * sin(s.th[i]) * ut;
+          SL[(size_t)(v * 3 + 1) * n + i] = p->v0 * cos(s.th[i]) * ut;
+          SL[(size_t)(v * 3 + 2) * n + i] = gp * T[(size_t)v * n + i];
+        }
+      /* base stage (forces at the same state) */
+      abp_stage_forces(&s);
+      double h, hw, frac;
+      if (nst == 2) { h = stage == 0 ? 0.5 * dt : dt; hw = h; frac = stage == 0 ? 0.5 : 1.0; }
+      else { h = stage < 2 ? 0.5 * dt : dt; hw = stage == 3 ? dt / 6 : h; frac = stage < 2 ? 0.5 : 1.0; }
+      for (int i = 0; i < n; ++i) {
+        double t = abp_torque(&s, i), fx = s.fx[i], fy = s.fy[i];
+        if (nst == 4) {
+          if (stage == 0) { s.k1f_x[i] = fx; s.k1f_y[i] = fy; s.k1t[i] = t; }
+          else if (stage == 1) { s.k2f_x[i] = fx; s.k2f_y[i] = fy; s.k2t[i] = t; }
+          else if (stage == 2) { s.k3f_x[i] = fx; s.k3f_y[i] = fy; s.k3t[i] = t; }
+          else {
+            t = s.k1t[i] + s.k2t[i] * 2 + s.k3t[i] * 2 + t;
+            fx = s.k1f_x[i] + s.k2f_x[i] * 2 + s.k3f_x[i] * 2 + fx;
+            fy = s.k1f_y[i] + s.k2f_y[i] * 2 + s.k3f_y[i] * 2 + fy;
+          }
+        }
+        s.th[i] = wrap_angle(s.tho[i] + hw * t + frac * s.dth[i]);
+        double nxu = s.xo[i] + fx * hw, nyu = s.yo[i] + fy * hw;
+        if (stage == nst - 1) { s.xu[i] = nxu; s.yu[i] = nyu; }
+        s.x[i] = pt(nxu, p->L); s.y[i] = pt(nyu, p->L);
+      }
+      for (int i = 0; i < n; ++i) set_v(&s, i);
+      /* tangent stage update */
+      for (size_t e = 0; e < len; ++e) {
+        double sl = SL[e];
+        if (nst == 2) {
+          if (stage == 0) U[e] = V[e] + 0.5 * dt * sl;
+          else V[e] = V[e] + dt * sl;
+        } else {
+          if (stage == 0) { ACC[e] = sl; U[e] = V[e] + 0.5 * dt * sl; }
+          else if (stage == 1) { ACC[e] += 2 * sl; U[e] = V[e] + 0.5 * dt * sl; }
+          else if (stage == 2) { ACC[e] += 2 * sl; U[e] = V[e] + dt * sl; }
+          else V[e] = V[e] + dt / 6 * (ACC[e] + sl);
+        }
+      }
+    }
+    if (renorm_every > 0 && ((st + 1) % renorm_every == 0 || st + 1 == nsteps))
+      mgs(K, (size_t)3 * n, V, log_stretch, 1.0);
+  }
+  memcpy(x, s.x, sizeof(double) * n); memcpy(y, s.y, sizeof(double) * n);
+  memcpy(xu, s.xu, sizeof(double) * n); memcpy(yu, s.yu, sizeof(double) * n);
+  memcpy(th, s.th, sizeof(double) * n);
+  free(U); free(ACC); free(T); free(SL);
+  state_free(&s);
+  return SPP_OK;
+}
+
+/* Benettin clone method of LyapunovBox::Evolution_Reorthonormalize
+ * (parallel/lyapunovbox.h:128-194): per interval of tau steps, each
+ * direction u_a (orthonormal, [K][3][n]) seeds a clone base + eps u_a
+ * (Add_Deviation, :46-67); the clones and the base evolve with the full
+ * dynamics; the differences (State_Hyper_Vector::operator-, min image and
+ * wrapped angle) are Gram-Schmidt'ed into the next directions, and
+ * log(|projection| / eps) (the ratio of :177-183) is summed per direction. */
+int orc64_lyap_clone(const SppParams* p, int n_intervals, int tau, int K, double eps, double* x,
+                     double* y, double* th, double* xu, double* yu, double* V, double* log_stretch) {
+  int n = p->n;
+  size_t len = (size_t)3 * n;
+  double *bx = malloc(sizeof(double) * n), *by = malloc(sizeof(double) * n),
+         *bt = malloc(sizeof(double) * n), *bxu = malloc(sizeof(double) * n),
+         *byu = malloc(sizeof(double) * n);
+  double *cx = malloc(sizeof(double) * n), *cy = malloc(sizeof(double) * n),
+         *ct = malloc(sizeof(double) * n), *cxu = malloc(sizeof(double) * n),
+         *cyu = malloc(sizeof(double) * n);
+  int64_t step = 0;
+  int rc = SPP_OK;
+  for (int it = 0; it < n_intervals && rc == SPP_OK; ++it) {
+    memcpy(bx, x, sizeof(double) * n); memcpy(by, y, sizeof(double) * n);
+    memcpy(bt, th, sizeof(double) * n); memcpy(bxu, xu, sizeof(double) * n);
+    memcpy(byu, yu, sizeof(double) * n);
+    rc = orc64_run(p, tau, step, bx, by, bt, bxu, byu);
+    for (int a = 0; a < K && rc == SPP_OK; ++a) {
+      const double* u = V + (size_t)a * len;
+      for (int i = 0; i < n; ++i) {
+        cx[i] = pt(x[i] + eps * u[i], p->L);
+        cy[i] = pt(y[i] + eps * u[n + i], p->L);
+        ct[i] = th[i] + eps * u[2 * n + i];
+        cxu[i] = xu[i] + eps * u[i];
+        cyu[i] = yu[i] + eps * u[n + i];
+      }
+      rc = orc64_run(p, tau, step, cx, cy, ct, cxu, cyu);
+      double* w = V + (size_t)a * len;
+      for (int i = 0; i < n; ++i) {
+        double dth = ct[i] - bt[i];
+        w[i] = pt(cx[i] - bx[i], p->L);
+        w[n + i] = pt(cy[i] - by[i], p->L);
+        w[2 * n + i] = dth - 2 * M_PI * ceil((dth - M_PI) / (2 * M_PI));
+      }
+    }
+    mgs(K, len, V, log_stretch, eps);
+    memcpy(x, bx, sizeof(double) * n); memcpy(y, by, sizeof(double) * n);
+    memcpy(th, bt, sizeof(double) * n); memcpy(xu, bxu, sizeof(double) * n);
+    memcpy(yu, byu, sizeof(double) * n);
+    step += tau;
+  }
+  free(bx); free(by); free(bt); free(bxu); free(byu);
+  free(cx); free(cy); free(ct); free(cxu); free(cyu);
+  return rc;
+}

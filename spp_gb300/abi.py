@@ -99,6 +99,11 @@ PROTOTYPES = {
     "spp_stream": (_P, [_P]),
     "spp_profile": (C.c_int, [_P, C.c_int, C.POINTER(SppProfile)]),
     "spp_time_steps": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double)]),
+    "spp_lyap_init": (C.c_int, [_P, C.c_int, C.c_uint64]),
+    "spp_lyap_set_vectors": (C.c_int, [_P, _F, C.c_int]),
+    "spp_lyap_step": (C.c_int, [_P, C.c_int, C.c_int]),
+    "spp_lyap_exponents": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double)]),
+    "spp_lyap_vectors": (C.c_int, [_P, _F, C.c_int]),
     "spp_pairs_noalloc": (C.c_int, [_P, _P, C.c_int, C.c_double, C.c_double, _P, _P, C.c_int64,
                                     _P, _P]),
 }

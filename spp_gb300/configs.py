@@ -192,3 +192,17 @@ def vesicle_state(p, swimmers_per_ring=None, seed=None):
     x = np.where(x >= Lf, -Lf, x).astype(np.float32)
     y = np.where(y >= Lf, -Lf, y).astype(np.float32)
     return x, y, th.astype(np.float32)
+
+
+def lyapunov_config(n=16384, rho=1.0, seed=3, integrator=abi.INT_RK4) -> abi.SppParams:
+    """Continuous-time Vicsek for the Lyapunov spectrum: N = 16,384 at
+    rho = 1 (L = 64), v0 = 0.5, g = 1, alpha = 0, D_r = 0, r = 1, RK4 with
+    dt = 0.01 (ContinuousParticle, shared/particle.h:254-378, with RK4 in
+    place of its Euler move)."""
+    p = reference_defaults(abi.MODEL_CONTINUOUS)
+    p.n, p.seed, p.integrator = n, seed, integrator
+    p.L = 0.5 * math.sqrt(n / rho)
+    p.v0, p.g, p.alpha, p.Dr, p.r_align, p.dt = 0.5, 1.0, 0.0, 0.0, 1.0, 0.01
+    p.force_law = abi.FORCE_NONE
+    p.skin = 0.3
+    return p

@@ -18,6 +18,7 @@
 #include <string>
 #include <vector>
 #include "spp_internal.cuh"
+#include "spp_lyap.cuh"
 
 namespace {
 
@@ -70,6 +71,12 @@ struct SppSystem {
   float* stage_t = nullptr;
   int2* stage_img = nullptr;
   std::vector<GraphEntry> graphs;
+  /* tangent-space (Lyapunov) estimator */
+  LyapState lyap;
+  bool lyap_on = false;
+  int64_t lyap_steps = 0;        /* steps since spp_lyap_init */
+  int lyap_renorm_every = 10;
+  std::vector<GraphEntry> lyap_graphs;  /* keyed by steps per renormalisation chunk */
 };
 
 namespace {
@@ -92,6 +99,20 @@ int dalloc(T** ptr, size_t count) {
     return fail(SPP_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
   }
   return SPP_OK;
+}
+
+void free_lyap(SppSystem* s) {
+  LyapState& L = s->lyap;
+  void* ptrs[] = {L.t0, L.ua, L.ub, L.acc, L.partial, L.rinv, L.log_stretch, L.error};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  memset(&L, 0, sizeof(L));
+  for (auto& g : s->lyap_graphs) {
+    cudaGraphExecDestroy(g.exec);
+    cudaGraphDestroy(g.graph);
+  }
+  s->lyap_graphs.clear();
+  s->lyap_on = false;
 }
 
 void free_dev(SppSystem* s) {
@@ -283,6 +304,31 @@ int alloc_list(SppSystem* s, int cap) {
   return dalloc(&s->d.nbr, (size_t)cap * s->d.n);
 }
 
+int enqueue_lyap_step(SppSystem* s, cudaStream_t st, bool capture, int64_t* launches);
+
+/* Base + tangent steps with direct launches (recovery path): the rebuild is
+ * decided on the host after each step, renormalisation every
+ * lyap_renorm_every steps and at the end.  Extra renormalisation points
+ * leave the summed log-stretches unchanged (the stretches multiply). */
+int run_lyap_direct(SppSystem* s, int64_t nsteps) {
+  for (int64_t i = 0; i < nsteps; ++i) {
+    int rc = enqueue_lyap_step(s, s->stream, false, &s->host_launches);
+    if (rc != SPP_OK) return rc;
+    Ctl c;
+    CUDA_TRY(cudaMemcpyAsync(&c, s->d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (c.frozen) return SPP_OK;  /* the caller grows the list and comes back */
+    if (c.need_rebuild) {
+      rc = enqueue_rebuild(s, s->stream, &s->host_launches);
+      if (rc != SPP_OK) return rc;
+      s->direct_rebuilds++;
+    }
+    if ((i + 1) % s->lyap_renorm_every == 0 || i + 1 == nsteps)
+      launch_renormalize(s->lyap, 1, s->stream, &s->host_launches);
+  }
+  return SPP_OK;
+}
+
 /* Grows the neighbour list after an overflow and finishes the steps the
  * frozen kernels skipped. */
 int recover(SppSystem* s) {
@@ -295,13 +341,19 @@ int recover(SppSystem* s) {
                                     "particles under an R12 force?); the state is not reliable");
     if (!c.frozen) {
       if ((int64_t)c.step >= s->target_step) return SPP_OK;
-      rc = run_steps(s, s->target_step - (int64_t)c.step);
+      if (s->lyap_on) rc = run_lyap_direct(s, s->target_step - (int64_t)c.step);
+      else rc = run_steps(s, s->target_step - (int64_t)c.step);
       if (rc != SPP_OK) return rc;
       continue;
     }
     int cap = (int)((c.list_need * 5u) / 4u + 4u);
     cap = (cap + 3) & ~3;
     free_graphs(s);
+    for (auto& g : s->lyap_graphs) {
+      cudaGraphExecDestroy(g.exec);
+      cudaGraphDestroy(g.graph);
+    }
+    s->lyap_graphs.clear();
     rc = alloc_list(s, cap);
     if (rc != SPP_OK) return rc;
     CUDA_TRY(cudaMemsetAsync(&s->d.ctl->frozen, 0, sizeof(uint32_t), s->stream));
@@ -311,6 +363,79 @@ int recover(SppSystem* s) {
     s->direct_rebuilds++;
   }
   return fail(SPP_ERR_OVERFLOW, "neighbour list kept overflowing");
+}
+
+/* One step of base + tangent dynamics: each base stage is followed by the
+ * tangent stage evaluated on the same stage state. */
+int enqueue_lyap_step(SppSystem* s, cudaStream_t st, bool capture, int64_t* launches) {
+  cudaGraphConditionalHandle handle = 0;
+  if (capture) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g;
+    CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+    CUDA_TRY(cudaGraphConditionalHandleCreate(&handle, g, 0, cudaGraphCondAssignDefault));
+  }
+  const DevState& d = s->d;
+  for (int stage = 0; stage < s->nstages; ++stage) {
+    const float4* cur;
+    if (s->nstages == 2) cur = stage == 0 ? d.pos : d.half;
+    else {
+      const float4* bufs[3] = {d.pos, d.half, d.half2};
+      static const int cur_sel[4] = {0, 1, 2, 1};
+      cur = bufs[cur_sel[stage]];
+    }
+    launch_abp_stage(s->k, d, stage, s->nstages, handle, capture ? 1 : 0, st, launches);
+    launch_tangent_stage(s->k, d, s->lyap, stage, s->nstages, cur, st, launches);
+  }
+  CUDA_TRY(cudaGetLastError());
+  if (!capture) return SPP_OK;
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = handle;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  CUDA_TRY(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CUDA_TRY(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
+                                               cudaStreamSetCaptureDependencies));
+  CUDA_TRY(cudaStreamBeginCaptureToGraph(s->side, body, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_rebuild(s, s->side, nullptr);
+  cudaGraph_t body_out = body;
+  cudaError_t e = cudaStreamEndCapture(s->side, &body_out);
+  if (rc != SPP_OK) return rc;
+  if (e != cudaSuccess) return fail(SPP_ERR_CUDA, std::string("capture rebuild body: ") +
+                                                      cudaGetErrorString(e));
+  return SPP_OK;
+}
+
+/* Graph of `chunk` base+tangent steps followed by the FP64 renormalisation. */
+int get_lyap_graph(SppSystem* s, int chunk, cudaGraphExec_t* out) {
+  for (auto& g : s->lyap_graphs)
+    if (g.nsteps == chunk) { *out = g.exec; return SPP_OK; }
+  cudaGraph_t graph = nullptr;
+  CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = SPP_OK;
+  for (int i = 0; i < chunk && rc == SPP_OK; ++i) rc = enqueue_lyap_step(s, s->stream, true, nullptr);
+  if (rc == SPP_OK) launch_renormalize(s->lyap, 1, s->stream, nullptr);
+  cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+  if (rc != SPP_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
+  if (e != cudaSuccess) return fail(SPP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  cudaGraphExec_t exec;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return fail(SPP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  }
+  s->lyap_graphs.push_back({chunk, graph, exec});
+  *out = exec;
+  return SPP_OK;
 }
 
 }  // namespace
@@ -472,6 +597,7 @@ int spp_destroy(SppSystem* s) {
   if (!s) return SPP_OK;
   if (s->stream) cudaStreamSynchronize(s->stream);
   free_graphs(s);
+  free_lyap(s);
   free_dev(s);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   if (s->side) cudaStreamDestroy(s->side);
@@ -729,6 +855,103 @@ int spp_profile(SppSystem* s, int nsteps, SppProfile* out) {
   }
   for (auto x : ev) cudaEventDestroy(x);
   return rc;
+}
+
+int spp_lyap_init(SppSystem* s, int K, uint64_t seed) {
+  if (!s) return fail(SPP_ERR_INVALID, "system is NULL");
+  if (!s->uploaded) return fail(SPP_ERR_INVALID, "no state uploaded");
+  if (K < 1 || K > SPP_LYAP_MAX) return fail(SPP_ERR_INVALID, "need 1 <= K <= 8 tangent vectors");
+  if (s->p.model != SPP_MODEL_CONTINUOUS || s->p.alpha != 0.0 || s->p.force_law != SPP_FORCE_NONE)
+    return fail(SPP_ERR_UNSUPPORTED,
+                "the tangent dynamics is built for the continuous model with alpha = 0 and no repulsion");
+  if (s->nstages < 2) return fail(SPP_ERR_UNSUPPORTED, "tangent dynamics needs RK2 or RK4");
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  free_lyap(s);
+  LyapState& L = s->lyap;
+  L.K = K;
+  L.n = s->p.n;
+  size_t len = (size_t)K * 3 * s->p.n;
+  rc = dalloc(&L.t0, len);
+  rc = rc ? rc : dalloc(&L.ua, len);
+  rc = rc ? rc : dalloc(&L.ub, len);
+  rc = rc ? rc : dalloc(&L.acc, len);
+  rc = rc ? rc : dalloc(&L.partial, (size_t)SPP_GRAM_BLOCKS * SPP_GRAM_ENTRIES);
+  rc = rc ? rc : dalloc(&L.rinv, (size_t)SPP_LYAP_MAX * SPP_LYAP_MAX);
+  rc = rc ? rc : dalloc(&L.log_stretch, SPP_LYAP_MAX);
+  rc = rc ? rc : dalloc(&L.error, 1);
+  if (rc != SPP_OK) { free_lyap(s); return rc; }
+  CUDA_TRY(cudaMemsetAsync(L.log_stretch, 0, sizeof(double) * SPP_LYAP_MAX, s->stream));
+  CUDA_TRY(cudaMemsetAsync(L.error, 0, sizeof(uint32_t), s->stream));
+  launch_tangent_init(L, seed, s->p.system_id, s->stream);
+  launch_renormalize(L, 0, s->stream, &s->host_launches);
+  s->host_launches += 1;
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  uint32_t err = 0;
+  CUDA_TRY(cudaMemcpy(&err, L.error, sizeof(err), cudaMemcpyDeviceToHost));
+  if (err) { free_lyap(s); return fail(SPP_ERR_NUMERIC, "initial tangent vectors are dependent"); }
+  s->lyap_on = true;
+  s->lyap_steps = 0;
+  return SPP_OK;
+}
+
+int spp_lyap_set_vectors(SppSystem* s, const float* v, int K) {
+  if (!s || !v) return fail(SPP_ERR_INVALID, "NULL argument");
+  if (!s->lyap_on || K != s->lyap.K) return fail(SPP_ERR_INVALID, "spp_lyap_init with this K first");
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  CUDA_TRY(cudaMemcpy(s->lyap.t0, v, sizeof(float) * (size_t)K * 3 * s->p.n, cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemset(s->lyap.log_stretch, 0, sizeof(double) * SPP_LYAP_MAX));
+  s->lyap_steps = 0;
+  return SPP_OK;
+}
+
+int spp_lyap_step(SppSystem* s, int nsteps, int renorm_every) {
+  if (!s) return fail(SPP_ERR_INVALID, "system is NULL");
+  if (!s->lyap_on) return fail(SPP_ERR_INVALID, "spp_lyap_init first");
+  if (nsteps < 0 || renorm_every < 1) return fail(SPP_ERR_INVALID, "need nsteps >= 0, renorm_every >= 1");
+  s->target_step += nsteps;
+  s->lyap_renorm_every = renorm_every;
+  int64_t left = nsteps;
+  while (left > 0) {
+    int chunk = left >= renorm_every ? renorm_every : (int)left;
+    cudaGraphExec_t exec;
+    int rc = get_lyap_graph(s, chunk, &exec);
+    if (rc != SPP_OK) return rc;
+    CUDA_TRY(cudaGraphLaunch(exec, s->stream));
+    s->graph_kernels += (int64_t)chunk * 2 * s->nstages + 6;
+    s->lyap_steps += chunk;
+    left -= chunk;
+  }
+  return SPP_OK;
+}
+
+int spp_lyap_exponents(SppSystem* s, double* lambda, int K, double* elapsed) {
+  if (!s || !lambda) return fail(SPP_ERR_INVALID, "NULL argument");
+  if (!s->lyap_on || K > s->lyap.K) return fail(SPP_ERR_INVALID, "spp_lyap_init first / K too large");
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  Ctl c;
+  rc = read_ctl(s, &c);
+  if (rc != SPP_OK) return rc;
+  (void)c;
+  double ls[SPP_LYAP_MAX];
+  uint32_t err = 0;
+  CUDA_TRY(cudaMemcpy(ls, s->lyap.log_stretch, sizeof(ls), cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(&err, s->lyap.error, sizeof(err), cudaMemcpyDeviceToHost));
+  if (err) return fail(SPP_ERR_NUMERIC, "tangent vectors became dependent");
+  const double T = (double)s->lyap_steps * s->p.dt;
+  for (int a = 0; a < K; ++a) lambda[a] = T > 0 ? ls[a] / T : 0.0;
+  if (elapsed) *elapsed = T;
+  return SPP_OK;
+}
+
+int spp_lyap_vectors(SppSystem* s, float* v, int K) {
+  if (!s || !v) return fail(SPP_ERR_INVALID, "NULL argument");
+  if (!s->lyap_on || K != s->lyap.K) return fail(SPP_ERR_INVALID, "spp_lyap_init with this K first");
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  CUDA_TRY(cudaMemcpy(v, s->lyap.t0, sizeof(float) * (size_t)K * 3 * s->p.n, cudaMemcpyDeviceToHost));
+  return SPP_OK;
 }
 
 int spp_time_steps(SppSystem* s, int nsteps, double* ms) {

@@ -1,0 +1,204 @@
+/*
+ * kernels_lyap.cu -- tangent dynamics and FP64 renormalisation on sm_103a.
+ *
+ * The reference estimates Lyapunov exponents with k finite perturbations of
+ * the full dynamics (Benettin clones, parallel/lyapunovbox.h:128-194): each
+ * clone is a whole copy of the system, evolved and differenced against the
+ * base run, then Gram-Schmidt renormalised (shared/vector-set.h:118-127).
+ * Here the k tangent vectors are advanced by the linearised integrator next
+ * to the base trajectory:
+ *   k_tangent_stage: after each base stage, one thread per particle gathers
+ *     cos(th_j - th_i) of its neighbours (same id-sorted list, FP32 sums in
+ *     id order) and advances all k vectors through the JVP of that stage.
+ *     Tangent vectors are stored by particle id, [k][x|y|th][n], so the
+ *     cell reordering at list rebuilds does not touch them.
+ *   Renormalisation every m steps, in FP64: a Cholesky-QR pass, done twice
+ *   (the second pass restores orthogonality to working precision):
+ *     k_gram     deterministic block partials of the k x k Gram matrix
+ *     k_chol     one thread: sum of the partials in block order, Cholesky,
+ *                R^{-1}, log R_aa added to the log-stretch sums
+ *     k_apply    V <- V R^{-1}
+ *   The Q and R are those of Gram-Schmidt on the same vectors; the FP64
+ *   accumulation is what the stability of the renormalisation needs.
+ */
+#include "spp_internal.cuh"
+#include "spp_lyap.cuh"
+
+namespace {
+
+template <int K>
+__global__ void __launch_bounds__(SPP_BLOCK) k_tangent_stage(SppConsts k, DevState d, LyapState L,
+                                                             TanStage t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n || d.ctl->frozen) return;
+  const int n = d.n;
+  const uint32_t idi = d.id[i];
+  const float4 pi = t.cur[i];
+  float ui[K], acc[K];
+#pragma unroll
+  for (int v = 0; v < K; ++v) {
+    ui[v] = t.uin[(size_t)(v * 3 + 2) * n + idi];
+    acc[v] = 0.0f;
+  }
+  const int cnt = d.nn[i];
+  for (int q = 0; q < cnt; ++q) {
+    const int j = __ldg(d.nbr + (size_t)q * n + i);
+    const float4 pj = __ldg(t.cur + j);
+    float dx, dy;
+    const float d2 = spp_sep(&k, pi.x, pi.y, pj.x, pj.y, &dx, &dy);
+    if (d2 < k.ral2) {
+      const float cij = spp_tangent_coupling(pi.z, pi.w, pj.z, pj.w);
+      const uint32_t idj = d.id[j];
+#pragma unroll
+      for (int v = 0; v < K; ++v)
+        acc[v] = acc[v] + cij * (t.uin[(size_t)(v * 3 + 2) * n + idj] - ui[v]);
+    }
+  }
+  const float gp = k.g * k.one_minus_alpha_over_pi;
+#pragma unroll
+  for (int v = 0; v < K; ++v) {
+    const float slope[3] = {-k.v0 * pi.w * ui[v], k.v0 * pi.z * ui[v], gp * acc[v]};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t e = (size_t)(v * 3 + c) * n + idi;
+      float t0 = L.t0[e];
+      float a = t.stage == 0 ? 0.0f : L.acc[e];
+      float uo = 0.0f;
+      spp_tangent_stage_update(&k, t.stage, t.nstages, slope[c], &t0, &a, &uo);
+      if (t.stage == t.nstages - 1) L.t0[e] = t0;
+      else t.uout[e] = uo;
+      if (t.nstages == 4 && t.stage < 3) L.acc[e] = a;
+    }
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(SPP_GRAM_THREADS) k_gram(const float* __restrict__ V, int len,
+                                                            double* partial) {
+  double g[SPP_GRAM_ENTRIES];
+#pragma unroll
+  for (int q = 0; q < K * (K + 1) / 2; ++q) g[q] = 0.0;
+  const int stride = SPP_GRAM_BLOCKS * SPP_GRAM_THREADS;
+  for (int e = blockIdx.x * SPP_GRAM_THREADS + threadIdx.x; e < len; e += stride) {
+    double v[K];
+#pragma unroll
+    for (int a = 0; a < K; ++a) v[a] = (double)V[(size_t)a * len + e];
+#pragma unroll
+    for (int a = 0; a < K; ++a)
+#pragma unroll
+      for (int b = 0; b <= a; ++b) g[a * (a + 1) / 2 + b] = g[a * (a + 1) / 2 + b] + v[a] * v[b];
+  }
+  __shared__ double warp_part[SPP_GRAM_THREADS / 32][SPP_GRAM_ENTRIES];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < K * (K + 1) / 2; ++q) {
+    double x = g[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = x + __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) warp_part[warp][q] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < K * (K + 1) / 2) {
+    double x = 0.0;
+    for (int w = 0; w < SPP_GRAM_THREADS / 32; ++w) x = x + warp_part[w][threadIdx.x];
+    partial[(size_t)blockIdx.x * SPP_GRAM_ENTRIES + threadIdx.x] = x;
+  }
+}
+
+__global__ void k_chol(int K, const double* partial, double* rinv, double* log_stretch,
+                       int accumulate, uint32_t* error) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double G[SPP_GRAM_ENTRIES];
+  for (int q = 0; q < K * (K + 1) / 2; ++q) {
+    double x = 0.0;
+    for (int b = 0; b < SPP_GRAM_BLOCKS; ++b) x = x + partial[(size_t)b * SPP_GRAM_ENTRIES + q];
+    G[q] = x;
+  }
+  double lr[SPP_LYAP_MAX];
+  if (spp_cholesky_inverse(K, G, rinv, lr)) {
+    *error = 1u;
+    for (int a = 0; a < SPP_LYAP_MAX * SPP_LYAP_MAX; ++a) rinv[a] = (a % (SPP_LYAP_MAX + 1)) == 0;
+    return;
+  }
+  if (accumulate)
+    for (int a = 0; a < K; ++a) log_stretch[a] = log_stretch[a] + lr[a];
+}
+
+template <int K>
+__global__ void __launch_bounds__(SPP_BLOCK) k_apply(float* V, int len, const double* __restrict__ rinv) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= len) return;
+  double v[K];
+#pragma unroll
+  for (int a = 0; a < K; ++a) v[a] = (double)V[(size_t)a * len + e];
+#pragma unroll
+  for (int a = 0; a < K; ++a) {
+    double x = 0.0;
+#pragma unroll
+    for (int b = 0; b <= a; ++b) x = x + v[b] * rinv[b * SPP_LYAP_MAX + a];
+    V[(size_t)a * len + e] = (float)x;
+  }
+}
+
+/* Gaussian N(0, 1) entries from the Philox tangent stream: component c of
+ * vector v of particle id uses counter (id, v * 3 + c, SPP_RNG_TANGENT). */
+__global__ void k_tangent_init(float* V, int K, int n, uint64_t seed, uint32_t system) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= K * 3 * n) return;
+  const int id = e % n;
+  const int vc = e / n;
+  const spp_u32x4 r = spp_draw(seed, system, (uint32_t)id, (uint32_t)vc, SPP_RNG_TANGENT);
+  V[e] = spp_normal_f(r.v[0], r.v[1]);
+}
+
+}  // namespace
+
+void launch_tangent_init(const LyapState& L, uint64_t seed, uint32_t system, cudaStream_t s) {
+  const int tot = L.K * 3 * L.n;
+  k_tangent_init<<<(tot + SPP_BLOCK - 1) / SPP_BLOCK, SPP_BLOCK, 0, s>>>(L.t0, L.K, L.n, seed, system);
+}
+
+#define SPP_K_DISPATCH(K, CALL) \
+  switch (K) {                  \
+    case 1: CALL(1); break;     \
+    case 2: CALL(2); break;     \
+    case 3: CALL(3); break;     \
+    case 4: CALL(4); break;     \
+    case 5: CALL(5); break;     \
+    case 6: CALL(6); break;     \
+    case 7: CALL(7); break;     \
+    default: CALL(8); break;    \
+  }
+
+void launch_tangent_stage(const SppConsts& k, const DevState& d, const LyapState& L, int stage,
+                          int nstages, const float4* cur, cudaStream_t s, int64_t* launches) {
+  TanStage t;
+  t.cur = cur;
+  t.stage = stage;
+  t.nstages = nstages;
+  /* stage inputs: stage 0 reads t0; RK2/RK4 alternate ua/ub */
+  float* ua = L.ua;
+  float* ub = L.ub;
+  t.uin = stage == 0 ? L.t0 : ((stage & 1) ? ua : ub);
+  t.uout = (stage & 1) ? ub : ua;
+  const int nb = (d.n + SPP_BLOCK - 1) / SPP_BLOCK;
+#define SPP_TAN(KK) k_tangent_stage<KK><<<nb, SPP_BLOCK, 0, s>>>(k, d, L, t)
+  SPP_K_DISPATCH(L.K, SPP_TAN)
+#undef SPP_TAN
+  if (launches) *launches += 1;
+}
+
+void launch_renormalize(const LyapState& L, int accumulate, cudaStream_t s, int64_t* launches) {
+  const int len = 3 * L.n;
+  const int nb = (len + SPP_BLOCK - 1) / SPP_BLOCK;
+  for (int pass = 0; pass < 2; ++pass) {
+#define SPP_GRAM(KK) k_gram<KK><<<SPP_GRAM_BLOCKS, SPP_GRAM_THREADS, 0, s>>>(L.t0, len, L.partial)
+    SPP_K_DISPATCH(L.K, SPP_GRAM)
+#undef SPP_GRAM
+    k_chol<<<1, 32, 0, s>>>(L.K, L.partial, L.rinv, L.log_stretch, accumulate, L.error);
+#define SPP_APPLY(KK) k_apply<KK><<<nb, SPP_BLOCK, 0, s>>>(L.t0, len, L.rinv)
+    SPP_K_DISPATCH(L.K, SPP_APPLY)
+#undef SPP_APPLY
+  }
+  if (launches) *launches += 6;
+}

@@ -324,6 +324,88 @@ SPP_HD void spp_vicsek_update(const SppConsts* k, const SppAcc* a, float x0, flo
 }
 
 /* ------------------------------------------------------------------ */
+/* tangent dynamics (Lyapunov spectrum of the continuous model)        */
+/* ------------------------------------------------------------------ */
+/* Maximum number of tangent vectors carried per system. */
+#define SPP_LYAP_MAX 8
+
+/* The continuous model with alpha = 0 (ContinuousParticle, shared/
+ * particle.h:296-338): dr_i/dt = v0 (cos th_i, sin th_i),
+ * dth_i/dt = g (1 - alpha)/pi sum_{|r_ij| < R} sin(th_j - th_i).  Its
+ * Jacobian-vector product, the cutoff's step ignored (zero almost
+ * everywhere), is
+ *   d(dx_i)/dt  = -v0 sin th_i dth_i,    d(dy_i)/dt = v0 cos th_i dth_i,
+ *   d(dth_i)/dt = g (1 - alpha)/pi sum_j cos(th_j - th_i) (dth_j - dth_i).
+ * The reference estimates exponents with finite perturbations of the full
+ * dynamics instead (parallel/lyapunovbox.h:128-194); this is the linearised
+ * counterpart.  Per-pair term for one tangent vector: */
+SPP_HD float spp_tangent_coupling(float ci, float si, float cj, float sj) {
+  return cj * ci + sj * si; /* cos(th_j - th_i) */
+}
+
+/* One integrator stage of one tangent component, the derivative of the
+ * base stage updates (spp_stage_update / spp_euler_update): slope is the
+ * JVP at the stage state, t0 the component at the start of the step, acc
+ * the RK4 slope sum, uout the input of the next stage. */
+SPP_HD void spp_tangent_stage_update(const SppConsts* k, int stage, int nst, float slope, float* t0,
+                                     float* acc, float* uout) {
+  if (nst == 1) {
+    *t0 = fmaf(k->dt, slope, *t0);
+  } else if (nst == 2) {
+    if (stage == 0) *uout = fmaf(k->half_dt, slope, *t0);
+    else *t0 = fmaf(k->dt, slope, *t0);
+  } else {
+    if (stage == 0) { *acc = slope; *uout = fmaf(k->half_dt, slope, *t0); }
+    else if (stage == 1) { *acc = *acc + 2.0f * slope; *uout = fmaf(k->half_dt, slope, *t0); }
+    else if (stage == 2) { *acc = *acc + 2.0f * slope; *uout = fmaf(k->dt, slope, *t0); }
+    else { *t0 = fmaf(k->dt6, *acc + slope, *t0); }
+  }
+}
+
+/* Gram-matrix layout of the FP64 renormalisation: entries (a, b), b <= a,
+ * packed row by row. */
+#define SPP_GRAM_ENTRIES (SPP_LYAP_MAX * (SPP_LYAP_MAX + 1) / 2)
+#define SPP_GRAM_BLOCKS 64
+#define SPP_GRAM_THREADS 256
+SPP_HD int spp_gram_index(int a, int b) { return a * (a + 1) / 2 + b; }
+
+/* Cholesky G = R^T R (R upper triangular) of a K x K Gram matrix in packed
+ * form, then Rinv = R^{-1}.  Returns 0 on success, 1 if G is not positive
+ * definite (dependent vectors).  log_r[a] = log R_aa, the stretch of vector
+ * a in the Gram-Schmidt sense (the same R as classical Gram-Schmidt,
+ * shared/vector-set.h:118-127, computes). */
+SPP_HD int spp_cholesky_inverse(int K, const double* G, double* Rinv, double* log_r) {
+  double R[SPP_LYAP_MAX][SPP_LYAP_MAX];
+  for (int a = 0; a < K; ++a)
+    for (int b = 0; b < K; ++b) R[a][b] = 0.0;
+  for (int j = 0; j < K; ++j) {
+    double d = G[spp_gram_index(j, j)];
+    for (int q = 0; q < j; ++q) d -= R[q][j] * R[q][j];
+    if (!(d > 0.0)) return 1;
+    const double rjj = sqrt(d);
+    R[j][j] = rjj;
+    for (int c = j + 1; c < K; ++c) {
+      double v = G[spp_gram_index(c, j)];
+      for (int q = 0; q < j; ++q) v -= R[q][j] * R[q][c];
+      R[j][c] = v / rjj;
+    }
+    log_r[j] = log(rjj);
+  }
+  /* upper-triangular inverse, column by column */
+  for (int a = 0; a < K; ++a)
+    for (int b = 0; b < K; ++b) Rinv[a * SPP_LYAP_MAX + b] = 0.0;
+  for (int c = 0; c < K; ++c) {
+    Rinv[c * SPP_LYAP_MAX + c] = 1.0 / R[c][c];
+    for (int r = c - 1; r >= 0; --r) {
+      double v = 0.0;
+      for (int q = r + 1; q <= c; ++q) v += R[r][q] * Rinv[q * SPP_LYAP_MAX + c];
+      Rinv[r * SPP_LYAP_MAX + c] = -v / R[r][r];
+    }
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
 /* ring membranes (SPP_MODEL_BEADS)                                    */
 /* ------------------------------------------------------------------ */
 /* Ring forces on bead m from its bonds and from the bending of the three

@@ -119,6 +119,32 @@ class System:
     def stream(self):
         return abi.lib().spp_stream(self._h)
 
+    # ---- tangent-space Lyapunov spectrum (LyapunovBox counterpart) ----
+    def lyap_init(self, k, seed=3):
+        self._lyap_k = int(k)
+        abi.check(abi.lib().spp_lyap_init(self._h, int(k), int(seed)), "spp_lyap_init")
+
+    def lyap_set_vectors(self, v):
+        v = np.ascontiguousarray(v, np.float32)
+        abi.check(abi.lib().spp_lyap_set_vectors(self._h, abi.fptr(v), self._lyap_k),
+                  "spp_lyap_set_vectors")
+
+    def lyap_step(self, nsteps, renorm_every=10):
+        abi.check(abi.lib().spp_lyap_step(self._h, int(nsteps), int(renorm_every)), "spp_lyap_step")
+
+    def lyap_exponents(self):
+        k = self._lyap_k
+        lam = (C.c_double * k)()
+        T = C.c_double()
+        abi.check(abi.lib().spp_lyap_exponents(self._h, lam, k, C.byref(T)), "spp_lyap_exponents")
+        return np.array(lam[:]), T.value
+
+    def lyap_vectors(self):
+        k = self._lyap_k
+        v = np.empty(k * 3 * self.n, np.float32)
+        abi.check(abi.lib().spp_lyap_vectors(self._h, abi.fptr(v), k), "spp_lyap_vectors")
+        return v.reshape(k, 3, self.n)
+
     def time_steps(self, nsteps):
         """spp_step(nsteps) timed with CUDA events on the launching stream (ms)."""
         ms = C.c_double()

@@ -1,0 +1,65 @@
+"""Tangent-space Lyapunov spectrum on the GPU (continuous Vicsek, RK4): the
+kernels against the CPU mirror of their arithmetic (FP32 tangent stages,
+FP64 Cholesky-QR renormalisation with the same reduction order) and against
+the FP64 restatements of the tangent method and of the reference's clone
+method."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spp_gb300 import System, configs
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_lyap(p, x, y, th, K, seed, steps, m):
+    with System(p) as s:
+        s.upload(x, y, th)
+        s.lyap_init(K, seed)
+        V0 = s.lyap_vectors()
+        s.lyap_step(steps, m)
+        lam, T = s.lyap_exponents()
+        V = s.lyap_vectors()
+        st = s.download()
+    return V0, V, lam, T, st
+
+
+def test_lyap_bitexact_vs_mirror(gpu_lib):
+    p = configs.lyapunov_config(n=2048)
+    x, y, th = configs.random_state(p.n, p.L, seed=3)
+    K, steps, m = 8, 120, 10
+    V0, V, lam, T, (gx, gy, gth, gix, giy) = gpu_lyap(p, x, y, th, K, 3, steps, m)
+    Vm = O.lyap_init32(p, K, 3)
+    assert np.array_equal(V0.ravel(), Vm)
+    sm = O.State32(x, y, th)
+    ls = O.lyap_run32(p, sm, Vm, steps, m)
+    assert np.array_equal(gx, sm.x) and np.array_equal(gth, sm.th)
+    assert np.array_equal(V.ravel(), Vm)
+    # the FP64 logs of the same R_aa (CUDA's log vs libm's: last bits)
+    assert np.allclose(lam * T, ls, rtol=1e-12, atol=1e-12)
+
+
+def test_lyap_exponents_within_two_percent_of_fp64(gpu_lib):
+    p = configs.lyapunov_config(n=1024)
+    x, y, th = configs.random_state(p.n, p.L, seed=3)
+    K, steps, m = 4, 400, 10
+    V0, V, lam, T, _ = gpu_lyap(p, x, y, th, K, 3, steps, m)
+    ls64 = O.lyap_tangent64(p, O.State64(x, y, th), V0.ravel().astype(np.float64), steps, m)
+    lsc = O.lyap_clone64(p, O.State64(x, y, th), V0.ravel().astype(np.float64), steps // m, m)
+    lam64, lamc = ls64 / T, lsc / T
+    print("GPU", lam, "FP64 tangent", lam64, "FP64 clones", lamc)
+    assert np.all(np.abs(lam - lam64) <= 0.02 * np.abs(lam64) + 1e-6)
+    assert np.all(np.abs(lam - lamc) <= 0.02 * np.abs(lamc) + 1e-6)
+
+
+def test_lyap_full_size_bitexact(gpu_lib):
+    """The Lyapunov workload's size: N = 16,384, k = 8, RK4, renormalised every 10 steps."""
+    p = configs.lyapunov_config()
+    x, y, th = configs.random_state(p.n, p.L, seed=3)
+    K, steps, m = 8, 30, 10
+    V0, V, lam, T, _ = gpu_lyap(p, x, y, th, K, 3, steps, m)
+    Vm = O.lyap_init32(p, K, 3)
+    O.lyap_run32(p, O.State32(x, y, th), Vm, steps, m)
+    assert np.array_equal(V.ravel(), Vm)
+    M = V.reshape(K, -1).astype(np.float64)
+    assert np.allclose(M @ M.T, np.eye(K), atol=1e-5)
