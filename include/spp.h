@@ -173,6 +173,47 @@ int spp_pairs(SppSystem* s, double r, int32_t* pi, int32_t* pj, int cap, int64_t
  * D x D cells under the given SppBinRule (Box::Update_Cells, serial/box.h:107-134). */
 int spp_cells(SppSystem* s, int D, int rule, int32_t* cell_x, int32_t* cell_y, int n);
 
+/* ---- batches of independent systems (parameter sweeps) ----
+ * Replaces the task farm of serial/mpi-main.cpp:157-176 (one MPI rank per
+ * realisation, run one after another): every system of a sweep shares one
+ * set of device arrays and one launch per phase of a step.  Vicsek-family
+ * models.  Per system the device keeps the polarization P each step, its
+ * first four moments over a start-up window and its mean over the
+ * stationary part of the run (Compute_Order_Parameters, analyze/analyze.h:
+ * 121-146, computed online). */
+typedef struct SppSweepStats {
+  int64_t steps;            /* steps taken by this system */
+  int32_t active;           /* 1 while stepping; 0 once retired or finished */
+  int32_t reserved;
+  int64_t window_steps;     /* steps inside the start-up window */
+  double p_mean, p_var, p_kurt;   /* moments of P over the window (kurtosis = m4 / var^2) */
+  int64_t stationary_steps; /* samples of P after stationary_from */
+  double p_stationary;      /* their mean */
+  double p2_stationary;     /* mean of P^2 */
+  double p_last;
+} SppSweepStats;
+
+typedef struct SppBatch SppBatch;
+/* systems[s] describes system s (model, n, L, eta, v0, dt, r_align, seed,
+ * system_id -- the Philox counter word keeping systems independent). */
+int spp_batch_create(const SppParams* systems, int n_systems, SppBatch** out);
+int spp_batch_destroy(SppBatch* b);
+/* Start-up window for the moments, start of the stationary average, and the
+ * step count after which a system stops (0 = never). */
+int spp_batch_set_windows(SppBatch* b, int window_steps, int stationary_from, int max_steps);
+/* Positions and headings of all systems concatenated in system order;
+ * resets every system's step counter and statistics. */
+int spp_batch_upload(SppBatch* b, const float* x, const float* y, const float* theta, int total_n);
+int spp_batch_step(SppBatch* b, int nsteps);
+int spp_batch_poll(SppBatch* b, SppSweepStats* out, int n_systems);
+/* Stops the listed systems (retired by the sweep's stopping rule). */
+int spp_batch_retire(SppBatch* b, const int32_t* systems, int count);
+int spp_batch_download(SppBatch* b, float* x, float* y, float* theta, int32_t* img_x,
+                       int32_t* img_y, int total_n);
+int64_t spp_batch_kernel_launches(SppBatch* b);
+/* spp_batch_step bracketed by CUDA events on the batch's stream (ms). */
+int spp_batch_time_steps(SppBatch* b, int nsteps, double* ms);
+
 /* ---- tangent-space Lyapunov spectrum (continuous model) ----
  * Replaces LyapunovBox (parallel/lyapunovbox.h:11-28): Init_Deviation
  * (:32-42), Evolution_Reorthonormalize (:128-194) and Lyapunov_Exponent

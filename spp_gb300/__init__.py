@@ -2,7 +2,7 @@
 particle simulator hamidallaei/SPP, behind the C ABI of include/spp.h."""
 from . import abi, configs
 from .abi import SppError, SppParams, SppObservables, new_params
-from .system import Box, Snapshot, System
+from .system import Batch, Box, Snapshot, System
 
-__all__ = ["abi", "configs", "Box", "Snapshot", "System", "SppError", "SppParams",
+__all__ = ["abi", "configs", "Batch", "Box", "Snapshot", "System", "SppError", "SppParams",
            "SppObservables", "new_params"]

@@ -67,6 +67,14 @@ class SppProfile(C.Structure):
                 ("rebuilds", C.c_int64), ("rebuild_ms", C.c_double), ("total_ms", C.c_double)]
 
 
+class SppSweepStats(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("active", C.c_int32), ("reserved", C.c_int32),
+                ("window_steps", C.c_int64), ("p_mean", C.c_double), ("p_var", C.c_double),
+                ("p_kurt", C.c_double), ("stationary_steps", C.c_int64),
+                ("p_stationary", C.c_double), ("p2_stationary", C.c_double),
+                ("p_last", C.c_double)]
+
+
 def new_params(**kw) -> SppParams:
     p = SppParams()
     p.struct_size = C.sizeof(SppParams)
@@ -99,6 +107,16 @@ PROTOTYPES = {
     "spp_stream": (_P, [_P]),
     "spp_profile": (C.c_int, [_P, C.c_int, C.POINTER(SppProfile)]),
     "spp_time_steps": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double)]),
+    "spp_batch_create": (C.c_int, [C.POINTER(SppParams), C.c_int, C.POINTER(_P)]),
+    "spp_batch_destroy": (C.c_int, [_P]),
+    "spp_batch_set_windows": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
+    "spp_batch_upload": (C.c_int, [_P, _F, _F, _F, C.c_int]),
+    "spp_batch_step": (C.c_int, [_P, C.c_int]),
+    "spp_batch_poll": (C.c_int, [_P, C.POINTER(SppSweepStats), C.c_int]),
+    "spp_batch_retire": (C.c_int, [_P, _I32, C.c_int]),
+    "spp_batch_download": (C.c_int, [_P, _F, _F, _F, _I32, _I32, C.c_int]),
+    "spp_batch_kernel_launches": (C.c_int64, [_P]),
+    "spp_batch_time_steps": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double)]),
     "spp_lyap_init": (C.c_int, [_P, C.c_int, C.c_uint64]),
     "spp_lyap_set_vectors": (C.c_int, [_P, _F, C.c_int]),
     "spp_lyap_step": (C.c_int, [_P, C.c_int, C.c_int]),

@@ -206,3 +206,37 @@ def lyapunov_config(n=16384, rho=1.0, seed=3, integrator=abi.INT_RK4) -> abi.Spp
     p.force_law = abi.FORCE_NONE
     p.skin = 0.3
     return p
+
+
+def sweep_points(n_points=512, n_min=1024, n_max=65536, eta=(0.05, 0.6), rho=(0.25, 2.0),
+                 v0=0.5, seed=4):
+    """Parameter points of the batched Vicsek sweep: N log-uniform in
+    [n_min, n_max], eta and rho uniform, L = sqrt(N) / (2 sqrt(rho)), v0 = 0.5,
+    dt = 1; drawn from the Philox sweep stream (SPP_RNG_SWEEP = 7).  Returns
+    one SppParams per point, system_id = index."""
+    ids = np.arange(n_points, dtype=np.uint32)
+    a = draw(seed, 0, ids, 0, 7)
+    u = [u01_f32(w).astype(np.float64) for w in a]
+    logn = np.log(n_min) + u[0] * (np.log(n_max) - np.log(n_min))
+    N = np.floor(np.exp(logn)).astype(np.int64)
+    etas = eta[0] + u[1] * (eta[1] - eta[0])
+    rhos = rho[0] + u[2] * (rho[1] - rho[0])
+    out = []
+    for s in range(n_points):
+        p = vicsek_config(n=int(N[s]), L=float(0.5 * math.sqrt(N[s] / rhos[s])), eta=float(etas[s]),
+                          seed=seed)
+        p.v0 = v0
+        p.system_id = s
+        out.append(p)
+    return out
+
+
+def sweep_state(points, seed=4):
+    """Uniform positions / headings of every point, concatenated."""
+    xs, ys, ts = [], [], []
+    for p in points:
+        x, y, th = random_state(p.n, p.L, seed=seed, system=p.system_id)
+        xs.append(x)
+        ys.append(y)
+        ts.append(th)
+    return np.concatenate(xs), np.concatenate(ys), np.concatenate(ts)

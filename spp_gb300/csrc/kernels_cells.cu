@@ -321,12 +321,19 @@ void launch_bin_count(const SppConsts& k, const DevState& d, cudaStream_t s, int
   if (launches) *launches += 1;
 }
 
-void launch_scan(const DevState& d, cudaStream_t s, int64_t* launches) {
-  uint32_t nb = (d.n_keys + SCAN_TILE - 1) / SCAN_TILE;
-  k_scan_reduce<<<nb, SCAN_THREADS, 0, s>>>(d.cell_count, d.n_keys, d.scan_tmp);
-  k_scan_top<<<1, SCAN_THREADS, 0, s>>>(d.scan_tmp, nb);
-  k_scan_apply<<<nb, SCAN_THREADS, 0, s>>>(d.cell_count, d.n_keys, d.scan_tmp, d.cell_start);
+void launch_scan_u32(const uint32_t* in, uint32_t n, uint32_t* block_tmp, uint32_t* out,
+                     cudaStream_t s, int64_t* launches) {
+  uint32_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  k_scan_reduce<<<nb, SCAN_THREADS, 0, s>>>(in, n, block_tmp);
+  k_scan_top<<<1, SCAN_THREADS, 0, s>>>(block_tmp, nb);
+  k_scan_apply<<<nb, SCAN_THREADS, 0, s>>>(in, n, block_tmp, out);
   if (launches) *launches += 3;
+}
+
+uint32_t scan_max_elements() { return (uint32_t)SCAN_TILE * (uint32_t)SCAN_TILE; }
+
+void launch_scan(const DevState& d, cudaStream_t s, int64_t* launches) {
+  launch_scan_u32(d.cell_count, d.n_keys, d.scan_tmp, d.cell_start, s, launches);
 }
 
 void launch_scatter(const DevState& d, cudaStream_t s, int64_t* launches) {

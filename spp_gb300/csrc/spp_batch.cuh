@@ -1,0 +1,38 @@
+/* spp_batch.cuh -- device layout of a batch of independent systems. */
+#ifndef SPP_BATCH_CUH
+#define SPP_BATCH_CUH
+#include "spp_internal.cuh"
+
+/* One row of the per-system offset table. */
+struct BatchSys {
+  SppConsts k;            /* the system's constants (box, noise, Philox key and system id) */
+  uint32_t p_off, n;      /* particle range [p_off, p_off + n) */
+  uint32_t c_off, D;      /* cell range [c_off, c_off + D*D), row-major D x D grid */
+  uint32_t active;        /* 0: retired or finished, copied through without work */
+  uint32_t steps;         /* steps taken (the system's Philox step counter) */
+};
+
+/* Per-system accumulators of the polarization P. */
+struct BatchStats {
+  double w1, w2, w3, w4;  /* sums of P^1..P^4 over the first `window` steps */
+  double s1, s2;          /* sums of P, P^2 after `stationary_from` steps */
+  long long ns;           /* number of stationary samples */
+  double p_last;          /* P of the last step */
+  long long sx, sy;       /* fixed-point heading sums of the current step (units 2^-27) */
+};
+
+struct DevBatch {
+  int n_total, n_sys;
+  int window, stationary_from, max_steps;
+  BatchSys* sys;
+  BatchStats* stats;
+  uint32_t* sys_of;       /* particle slot -> system (static: binning stays inside a system's range) */
+  float4 *pos, *pos_alt;
+  float *theta, *theta_alt;
+  int2 *img, *img_alt;
+  uint32_t *id, *id_alt;  /* particle id within its system */
+  uint32_t *key, *rank;
+  uint32_t *cell_count, *cell_start, *scan_tmp;
+  Ctl* ctl;
+};
+#endif

@@ -77,6 +77,11 @@ void spp_internal_set_error(const char* msg);
 /* kernels_cells.cu */
 void launch_bin_count(const SppConsts& k, const DevState& d, cudaStream_t s, int64_t* launches);
 void launch_scan(const DevState& d, cudaStream_t s, int64_t* launches);
+/* exclusive scan of n <= scan_max_elements() counts; block_tmp holds
+ * ceil(n / 4096) entries */
+void launch_scan_u32(const uint32_t* in, uint32_t n, uint32_t* block_tmp, uint32_t* out,
+                     cudaStream_t s, int64_t* launches);
+uint32_t scan_max_elements();
 void launch_scatter(const DevState& d, cudaStream_t s, int64_t* launches);
 void launch_build_list(const SppConsts& k, const DevState& d, int with_list, cudaStream_t s,
                        int64_t* launches);

@@ -242,3 +242,82 @@ class Box:
         rec = np.empty((self.N, 3), np.float32)
         rec[:, 0], rec[:, 1], rec[:, 2] = xu, yu, th
         os.write(rec.tobytes())
+
+
+class Batch:
+    """Many independent Vicsek-family systems in one set of launches
+    (replaces the serial/mpi-main.cpp:157-176 task farm)."""
+
+    def __init__(self, systems):
+        self.params = [q.copy() for q in systems]
+        for q in self.params:
+            if q.struct_size == 0:
+                q.struct_size = C.sizeof(abi.SppParams)
+        arr = (abi.SppParams * len(self.params))(*self.params)
+        self._h = C.c_void_p()
+        abi.check(abi.lib().spp_batch_create(arr, len(self.params), C.byref(self._h)),
+                  "spp_batch_create")
+        self.n_sys = len(self.params)
+        self.sizes = np.array([q.n for q in self.params], np.int64)
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)])
+        self.n_total = int(self.offsets[-1])
+
+    def close(self):
+        if self._h:
+            abi.lib().spp_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_windows(self, window, stationary_from, max_steps):
+        abi.check(abi.lib().spp_batch_set_windows(self._h, int(window), int(stationary_from),
+                                                  int(max_steps)), "spp_batch_set_windows")
+
+    def upload(self, x, y, theta):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        th = np.ascontiguousarray(theta, np.float32)
+        abi.check(abi.lib().spp_batch_upload(self._h, abi.fptr(x), abi.fptr(y), abi.fptr(th),
+                                             self.n_total), "spp_batch_upload")
+
+    def step(self, nsteps):
+        abi.check(abi.lib().spp_batch_step(self._h, int(nsteps)), "spp_batch_step")
+
+    def time_steps(self, nsteps):
+        ms = C.c_double()
+        abi.check(abi.lib().spp_batch_time_steps(self._h, int(nsteps), C.byref(ms)),
+                  "spp_batch_time_steps")
+        return ms.value
+
+    def poll(self):
+        out = (abi.SppSweepStats * self.n_sys)()
+        abi.check(abi.lib().spp_batch_poll(self._h, out, self.n_sys), "spp_batch_poll")
+        return list(out)
+
+    def retire(self, systems):
+        idx = np.ascontiguousarray(systems, np.int32)
+        abi.check(abi.lib().spp_batch_retire(self._h, abi.iptr(idx), len(idx)), "spp_batch_retire")
+
+    def download(self):
+        n = self.n_total
+        x = np.empty(n, np.float32)
+        y = np.empty(n, np.float32)
+        th = np.empty(n, np.float32)
+        ix = np.empty(n, np.int32)
+        iy = np.empty(n, np.int32)
+        abi.check(abi.lib().spp_batch_download(self._h, abi.fptr(x), abi.fptr(y), abi.fptr(th),
+                                               abi.iptr(ix), abi.iptr(iy), n), "spp_batch_download")
+        return x, y, th, ix, iy
+
+    def kernel_launches(self):
+        return int(abi.lib().spp_batch_kernel_launches(self._h))
