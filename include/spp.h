@@ -208,11 +208,34 @@ int spp_batch_step(SppBatch* b, int nsteps);
 int spp_batch_poll(SppBatch* b, SppSweepStats* out, int n_systems);
 /* Stops the listed systems (retired by the sweep's stopping rule). */
 int spp_batch_retire(SppBatch* b, const int32_t* systems, int count);
+/* Restarts retired systems where they stopped (not those past max_steps). */
+int spp_batch_resume(SppBatch* b, const int32_t* systems, int count);
 int spp_batch_download(SppBatch* b, float* x, float* y, float* theta, int32_t* img_x,
                        int32_t* img_y, int total_n);
 int64_t spp_batch_kernel_launches(SppBatch* b);
 /* spp_batch_step bracketed by CUDA events on the batch's stream (ms). */
 int spp_batch_time_steps(SppBatch* b, int nsteps, double* ms);
+
+/* ---- sweep surrogate: ensemble MLP (no counterpart in the reference) ----
+ * E independent networks in -> 128 -> 128 -> 1 (GELU), BF16 weights with
+ * FP32 masters, FP32 accumulation, trained full-batch with Adam on the
+ * device by the library's own forward/backward kernels.  Parameters per
+ * member (spp_mlp_num_params floats): W1[128][in] b1[128] W2[128][128]
+ * b2[128] W3[128] b3; arrays over members are [E][P]. */
+typedef struct SppMlp SppMlp;
+int spp_mlp_create(int ensemble, int in_dim, SppMlp** out);
+int spp_mlp_destroy(SppMlp* m);
+int spp_mlp_num_params(SppMlp* m);
+/* Sets the FP32 masters (and their BF16 copies); resets Adam's moments. */
+int spp_mlp_set_params(SppMlp* m, const float* theta);
+int spp_mlp_get_params(SppMlp* m, float* theta);
+/* y[E][B] for inputs x[B][in]. */
+int spp_mlp_predict(SppMlp* m, const float* x, int B, float* y);
+/* Gradient [E][P] of the mean-squared error over the batch, and the loss per member. */
+int spp_mlp_grad(SppMlp* m, const float* x, const float* t, int B, float* grad, float* loss);
+/* iters Adam steps (beta 0.9 / 0.999, eps 1e-8) at learning rate lr on the
+ * full batch; loss[E] (may be NULL) after the last step. */
+int spp_mlp_train(SppMlp* m, const float* x, const float* t, int B, int iters, float lr, float* loss);
 
 /* ---- tangent-space Lyapunov spectrum (continuous model) ----
  * Replaces LyapunovBox (parallel/lyapunovbox.h:11-28): Init_Deviation

@@ -114,9 +114,18 @@ PROTOTYPES = {
     "spp_batch_step": (C.c_int, [_P, C.c_int]),
     "spp_batch_poll": (C.c_int, [_P, C.POINTER(SppSweepStats), C.c_int]),
     "spp_batch_retire": (C.c_int, [_P, _I32, C.c_int]),
+    "spp_batch_resume": (C.c_int, [_P, _I32, C.c_int]),
     "spp_batch_download": (C.c_int, [_P, _F, _F, _F, _I32, _I32, C.c_int]),
     "spp_batch_kernel_launches": (C.c_int64, [_P]),
     "spp_batch_time_steps": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double)]),
+    "spp_mlp_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(_P)]),
+    "spp_mlp_destroy": (C.c_int, [_P]),
+    "spp_mlp_num_params": (C.c_int, [_P]),
+    "spp_mlp_set_params": (C.c_int, [_P, _F]),
+    "spp_mlp_get_params": (C.c_int, [_P, _F]),
+    "spp_mlp_predict": (C.c_int, [_P, _F, C.c_int, _F]),
+    "spp_mlp_grad": (C.c_int, [_P, _F, _F, C.c_int, _F, _F]),
+    "spp_mlp_train": (C.c_int, [_P, _F, _F, C.c_int, C.c_int, C.c_float, _F]),
     "spp_lyap_init": (C.c_int, [_P, C.c_int, C.c_uint64]),
     "spp_lyap_set_vectors": (C.c_int, [_P, _F, C.c_int]),
     "spp_lyap_step": (C.c_int, [_P, C.c_int, C.c_int]),

@@ -201,7 +201,11 @@ __global__ void k_batch_set_active(DevBatch b, const int32_t* idx, int count, ui
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q < count) {
     const int s = idx[q];
-    if (s >= 0 && s < b.n_sys) b.sys[s].active = value;
+    if (s >= 0 && s < b.n_sys) {
+      /* a system that reached max_steps stays finished */
+      const int finished = b.max_steps > 0 && (int)b.sys[s].steps >= b.max_steps;
+      b.sys[s].active = (value && !finished) ? 1u : 0u;
+    }
   }
 }
 
@@ -497,19 +501,27 @@ int spp_batch_poll(SppBatch* b, SppSweepStats* out, int n_systems) {
   return SPP_OK;
 }
 
-int spp_batch_retire(SppBatch* b, const int32_t* systems, int count) {
+static int batch_set_active(SppBatch* b, const int32_t* systems, int count, uint32_t value) {
   if (!b || (count > 0 && !systems) || count < 0) return bfail(SPP_ERR_INVALID, "bad arguments");
   if (count == 0) return SPP_OK;
   int32_t* d_idx = nullptr;
   int rc = balloc(&d_idx, (size_t)count);
   if (rc != SPP_OK) return rc;
   BCUDA(cudaMemcpyAsync(d_idx, systems, sizeof(int32_t) * count, cudaMemcpyHostToDevice, b->stream));
-  k_batch_set_active<<<nblocks(count), SPP_BLOCK, 0, b->stream>>>(b->d, d_idx, count, 0u);
+  k_batch_set_active<<<nblocks(count), SPP_BLOCK, 0, b->stream>>>(b->d, d_idx, count, value);
   b->launches += 1;
   cudaError_t e = cudaStreamSynchronize(b->stream);
   cudaFree(d_idx);
   if (e != cudaSuccess) return bfail(SPP_ERR_CUDA, cudaGetErrorString(e));
   return SPP_OK;
+}
+
+int spp_batch_retire(SppBatch* b, const int32_t* systems, int count) {
+  return batch_set_active(b, systems, count, 0u);
+}
+
+int spp_batch_resume(SppBatch* b, const int32_t* systems, int count) {
+  return batch_set_active(b, systems, count, 1u);
 }
 
 int spp_batch_download(SppBatch* b, float* x, float* y, float* theta, int32_t* img_x,
