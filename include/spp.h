@@ -231,11 +231,18 @@ int spp_mlp_set_params(SppMlp* m, const float* theta);
 int spp_mlp_get_params(SppMlp* m, float* theta);
 /* y[E][B] for inputs x[B][in]. */
 int spp_mlp_predict(SppMlp* m, const float* x, int B, float* y);
-/* Gradient [E][P] of the mean-squared error over the batch, and the loss per member. */
-int spp_mlp_grad(SppMlp* m, const float* x, const float* t, int B, float* grad, float* loss);
+/* Gradient [E][P] of each member's weighted squared error
+ * L_e = sum_s w[e][s] (y_e(x_s) - t_s)^2 / sum_s w[e][s], and L_e itself.
+ * weights[E][B] may be NULL (the mean-squared error); a member's weights are
+ * finite, >= 0 and not all zero (a zero weight leaves a sample out of that
+ * member's fit, as in K-fold bagging). */
+int spp_mlp_grad(SppMlp* m, const float* x, const float* t, const float* weights, int B, float* grad,
+                 float* loss);
 /* iters Adam steps (beta 0.9 / 0.999, eps 1e-8) at learning rate lr on the
- * full batch; loss[E] (may be NULL) after the last step. */
-int spp_mlp_train(SppMlp* m, const float* x, const float* t, int B, int iters, float lr, float* loss);
+ * full batch with the loss of spp_mlp_grad; loss[E] (may be NULL) after the
+ * last step. */
+int spp_mlp_train(SppMlp* m, const float* x, const float* t, const float* weights, int B, int iters, float lr,
+                  float* loss);
 
 /* ---- tangent-space Lyapunov spectrum (continuous model) ----
  * Replaces LyapunovBox (parallel/lyapunovbox.h:11-28): Init_Deviation

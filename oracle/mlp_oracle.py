@@ -52,12 +52,15 @@ def forward(theta32, x):
     return y, (x, z1, h1, z2, h2, W2, W3)
 
 
-def loss_grad(theta32, x, t):
+def loss_grad(theta32, x, t, w=None):
+    """Weighted squared error sum_s w_s (y_s - t_s)^2 / sum_s w_s (w None:
+    the mean) and its gradient."""
     y, (x, z1, h1, z2, h2, W2, W3) = forward(theta32, x)
     B = len(t)
     t = np.asarray(t, np.float64)
-    loss = np.mean((y - t) ** 2)
-    dy = 2 * (y - t) / B
+    w = np.full(B, 1.0 / B) if w is None else np.asarray(w, np.float64) / np.sum(w)
+    loss = np.sum(w * (y - t) ** 2)
+    dy = 2 * w * (y - t)
     gW3 = h2.T @ dy
     gb3 = dy.sum()
     dz2 = np.outer(dy, W3) * dgelu(z2)

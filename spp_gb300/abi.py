@@ -124,8 +124,8 @@ PROTOTYPES = {
     "spp_mlp_set_params": (C.c_int, [_P, _F]),
     "spp_mlp_get_params": (C.c_int, [_P, _F]),
     "spp_mlp_predict": (C.c_int, [_P, _F, C.c_int, _F]),
-    "spp_mlp_grad": (C.c_int, [_P, _F, _F, C.c_int, _F, _F]),
-    "spp_mlp_train": (C.c_int, [_P, _F, _F, C.c_int, C.c_int, C.c_float, _F]),
+    "spp_mlp_grad": (C.c_int, [_P, _F, _F, _F, C.c_int, _F, _F]),
+    "spp_mlp_train": (C.c_int, [_P, _F, _F, _F, C.c_int, C.c_int, C.c_float, _F]),
     "spp_lyap_init": (C.c_int, [_P, C.c_int, C.c_uint64]),
     "spp_lyap_set_vectors": (C.c_int, [_P, _F, C.c_int]),
     "spp_lyap_step": (C.c_int, [_P, C.c_int, C.c_int]),

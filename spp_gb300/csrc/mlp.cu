@@ -50,8 +50,11 @@ struct MlpDev {
   const __nv_bfloat16* w;   /* [E][P] BF16 copy */
   const float* x;           /* [B][in] */
   const float* t;           /* [B] targets */
+  const float* sw;          /* [E][B] sample weights, each member's summing to 1 */
   float* z1;                /* [E][B][H] pre-activations */
   float* z2;
+  float* h1;                /* [E][B][H] activations gelu(z) */
+  float* h2;
   float* y;                 /* [E][B] */
   float* dz1;               /* [E][B][H] */
   float* dz2;
@@ -74,12 +77,14 @@ __global__ void __launch_bounds__(H) k_mlp_forward(MlpDev m) {
     for (int k = 0; k < in; ++k) z = fmaf(__bfloat162float(w[j * in + k]), m.x[(size_t)s * in + k], z);
     m.z1[((size_t)e * m.B + s) * H + j] = z;
     h1[j] = gelu(z, nullptr);
+    m.h1[((size_t)e * m.B + s) * H + j] = h1[j];
     __syncthreads();
     float z2 = __bfloat162float(w[off_b2(in) + j]);
     const __nv_bfloat16* row = w + off_w2(in) + (size_t)j * H;
     for (int k = 0; k < H; ++k) z2 = fmaf(__bfloat162float(row[k]), h1[k], z2);
     m.z2[((size_t)e * m.B + s) * H + j] = z2;
     h2[j] = gelu(z2, nullptr);
+    m.h2[((size_t)e * m.B + s) * H + j] = h2[j];
     float part = __bfloat162float(w[off_w3(in) + j]) * h2[j];
     for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
     if ((j & 31) == 0) red[j >> 5] = part;
@@ -93,7 +98,8 @@ __global__ void __launch_bounds__(H) k_mlp_forward(MlpDev m) {
   }
 }
 
-/* Per-sample deltas of the mean-squared error L = (1/B) sum (y - t)^2. */
+/* Per-sample deltas of the weighted squared error L_e = sum_s sw[e][s] (y - t)^2
+ * (sw = 1/B without weights: the mean-squared error). */
 __global__ void __launch_bounds__(H) k_mlp_backward(MlpDev m) {
   const int e = blockIdx.y;
   const int s0 = blockIdx.x * CHUNK;
@@ -105,7 +111,7 @@ __global__ void __launch_bounds__(H) k_mlp_backward(MlpDev m) {
     const int s = s0 + q;
     if (s >= m.B) break;
     const size_t es = (size_t)e * m.B + s;
-    const float dy = 2.0f * (m.y[es] - m.t[s]) / (float)m.B;
+    const float dy = 2.0f * m.sw[es] * (m.y[es] - m.t[s]);
     if (j == 0) m.dy[es] = dy;
     float g2;
     gelu(m.z2[es * H + j], &g2);
@@ -140,13 +146,13 @@ __global__ void k_mlp_grad(MlpDev m, float* grad) {
     for (int s = 0; s < m.B; ++s) g += m.dz1[(eb + s) * H + j];
   } else if (q < off_b2(in)) {
     const int j = (q - off_w2(in)) / H, k = (q - off_w2(in)) % H;
-    for (int s = 0; s < m.B; ++s) g = fmaf(m.dz2[(eb + s) * H + j], gelu(m.z1[(eb + s) * H + k], nullptr), g);
+    for (int s = 0; s < m.B; ++s) g = fmaf(m.dz2[(eb + s) * H + j], m.h1[(eb + s) * H + k], g);
   } else if (q < off_w3(in)) {
     const int j = q - off_b2(in);
     for (int s = 0; s < m.B; ++s) g += m.dz2[(eb + s) * H + j];
   } else if (q < off_b3(in)) {
     const int j = q - off_w3(in);
-    for (int s = 0; s < m.B; ++s) g = fmaf(m.dy[eb + s], gelu(m.z2[(eb + s) * H + j], nullptr), g);
+    for (int s = 0; s < m.B; ++s) g = fmaf(m.dy[eb + s], m.h2[(eb + s) * H + j], g);
   } else {
     for (int s = 0; s < m.B; ++s) g += m.dy[eb + s];
   }
@@ -159,9 +165,9 @@ __global__ void k_mlp_loss(MlpDev m, float* loss) {
   float l = 0.0f;
   for (int s = 0; s < m.B; ++s) {
     const float d = m.y[(size_t)e * m.B + s] - m.t[s];
-    l = fmaf(d, d, l);
+    l = fmaf(m.sw[(size_t)e * m.B + s] * d, d, l);
   }
-  loss[e] = l / (float)m.B;
+  loss[e] = l;
 }
 
 /* Adam (Kingma & Ba, 2015) on the FP32 masters; refreshes the BF16 copy. */
@@ -205,18 +211,19 @@ struct SppMlp {
   int64_t adam_t = 0;
   /* scratch sized for the largest batch seen */
   int cap_B = 0;
-  float *x = nullptr, *t = nullptr, *z1 = nullptr, *z2 = nullptr, *y = nullptr;
-  float *dz1 = nullptr, *dz2 = nullptr, *dy = nullptr, *loss = nullptr;
+  float *x = nullptr, *t = nullptr, *z1 = nullptr, *z2 = nullptr, *h1 = nullptr, *h2 = nullptr, *y = nullptr;
+  float *dz1 = nullptr, *dz2 = nullptr, *dy = nullptr, *loss = nullptr, *sw = nullptr;
+  std::vector<float> host_sw;
   cudaStream_t stream = nullptr;
 };
 
 namespace {
 
 void mlp_free_scratch(SppMlp* m) {
-  float* ptrs[] = {m->x, m->t, m->z1, m->z2, m->y, m->dz1, m->dz2, m->dy, m->loss};
+  float* ptrs[] = {m->x, m->t, m->z1, m->z2, m->h1, m->h2, m->y, m->dz1, m->dz2, m->dy, m->loss, m->sw};
   for (float* q : ptrs)
     if (q) cudaFree(q);
-  m->x = m->t = m->z1 = m->z2 = m->y = m->dz1 = m->dz2 = m->dy = m->loss = nullptr;
+  m->x = m->t = m->z1 = m->z2 = m->h1 = m->h2 = m->y = m->dz1 = m->dz2 = m->dy = m->loss = m->sw = nullptr;
   m->cap_B = 0;
 }
 
@@ -225,9 +232,11 @@ int mlp_reserve(SppMlp* m, int B) {
   mlp_free_scratch(m);
   size_t eb = (size_t)m->E * B;
   cudaError_t e = cudaSuccess;
-  float** targets[] = {&m->x, &m->t, &m->z1, &m->z2, &m->y, &m->dz1, &m->dz2, &m->dy, &m->loss};
-  size_t sizes[] = {(size_t)B * m->in, (size_t)B, eb * H, eb * H, eb, eb * H, eb * H, eb, (size_t)m->E};
-  for (int q = 0; q < 9 && e == cudaSuccess; ++q) e = cudaMalloc((void**)targets[q], sizeof(float) * sizes[q]);
+  float** targets[] = {&m->x, &m->t, &m->z1, &m->z2, &m->h1, &m->h2, &m->y,
+                       &m->dz1, &m->dz2, &m->dy, &m->loss, &m->sw};
+  size_t sizes[] = {(size_t)B * m->in, (size_t)B, eb * H, eb * H, eb * H, eb * H, eb,
+                    eb * H, eb * H, eb, (size_t)m->E, eb};
+  for (int q = 0; q < 12 && e == cudaSuccess; ++q) e = cudaMalloc((void**)targets[q], sizeof(float) * sizes[q]);
   if (e != cudaSuccess) {
     mlp_free_scratch(m);
     return mfail(SPP_ERR_ALLOC, std::string("mlp scratch: ") + cudaGetErrorString(e));
@@ -244,8 +253,11 @@ MlpDev mlp_dev(SppMlp* m, int B) {
   d.w = m->w;
   d.x = m->x;
   d.t = m->t;
+  d.sw = m->sw;
   d.z1 = m->z1;
   d.z2 = m->z2;
+  d.h1 = m->h1;
+  d.h2 = m->h2;
   d.y = m->y;
   d.dz1 = m->dz1;
   d.dz2 = m->dz2;
@@ -253,11 +265,33 @@ MlpDev mlp_dev(SppMlp* m, int B) {
   return d;
 }
 
-int mlp_upload(SppMlp* m, const float* x, const float* t, int B) {
+/* Uploads inputs, targets and the sample weights normalised per member
+ * (weights NULL: 1/B each).  Weights must be finite and >= 0 with a positive
+ * sum for every member. */
+int mlp_upload(SppMlp* m, const float* x, const float* t, const float* weights, int B) {
   int rc = mlp_reserve(m, B);
   if (rc != SPP_OK) return rc;
   MCUDA(cudaMemcpyAsync(m->x, x, sizeof(float) * (size_t)B * m->in, cudaMemcpyHostToDevice, m->stream));
-  if (t) MCUDA(cudaMemcpyAsync(m->t, t, sizeof(float) * (size_t)B, cudaMemcpyHostToDevice, m->stream));
+  if (!t) return SPP_OK;
+  MCUDA(cudaMemcpyAsync(m->t, t, sizeof(float) * (size_t)B, cudaMemcpyHostToDevice, m->stream));
+  /* the previous upload of host_sw may still be in flight */
+  MCUDA(cudaStreamSynchronize(m->stream));
+  m->host_sw.assign((size_t)m->E * B, 1.0f / (float)B);
+  if (weights) {
+    for (int e = 0; e < m->E; ++e) {
+      double sum = 0.0;
+      for (int s = 0; s < B; ++s) {
+        const float v = weights[(size_t)e * B + s];
+        if (!(v >= 0.0f) || !std::isfinite(v)) return mfail(SPP_ERR_INVALID, "sample weights must be finite and >= 0");
+        sum += v;
+      }
+      if (!(sum > 0.0)) return mfail(SPP_ERR_INVALID, "every member needs a positive weight sum");
+      for (int s = 0; s < B; ++s)
+        m->host_sw[(size_t)e * B + s] = (float)((double)weights[(size_t)e * B + s] / sum);
+    }
+  }
+  MCUDA(cudaMemcpyAsync(m->sw, m->host_sw.data(), sizeof(float) * m->host_sw.size(), cudaMemcpyHostToDevice,
+                        m->stream));
   return SPP_OK;
 }
 
@@ -336,7 +370,7 @@ int spp_mlp_get_params(SppMlp* m, float* theta) {
 
 int spp_mlp_predict(SppMlp* m, const float* x, int B, float* y) {
   if (!m || !x || !y || B < 1) return mfail(SPP_ERR_INVALID, "bad arguments");
-  int rc = mlp_upload(m, x, nullptr, B);
+  int rc = mlp_upload(m, x, nullptr, nullptr, B);
   if (rc != SPP_OK) return rc;
   mlp_fwd_bwd(m, B, false);
   MCUDA(cudaMemcpyAsync(y, m->y, sizeof(float) * (size_t)m->E * B, cudaMemcpyDeviceToHost, m->stream));
@@ -344,9 +378,10 @@ int spp_mlp_predict(SppMlp* m, const float* x, int B, float* y) {
   return SPP_OK;
 }
 
-int spp_mlp_grad(SppMlp* m, const float* x, const float* t, int B, float* grad, float* loss) {
+int spp_mlp_grad(SppMlp* m, const float* x, const float* t, const float* weights, int B, float* grad,
+                 float* loss) {
   if (!m || !x || !t || B < 1) return mfail(SPP_ERR_INVALID, "bad arguments");
-  int rc = mlp_upload(m, x, t, B);
+  int rc = mlp_upload(m, x, t, weights, B);
   if (rc != SPP_OK) return rc;
   mlp_fwd_bwd(m, B, true);
   MlpDev d = mlp_dev(m, B);
@@ -359,9 +394,10 @@ int spp_mlp_grad(SppMlp* m, const float* x, const float* t, int B, float* grad, 
   return SPP_OK;
 }
 
-int spp_mlp_train(SppMlp* m, const float* x, const float* t, int B, int iters, float lr, float* loss) {
+int spp_mlp_train(SppMlp* m, const float* x, const float* t, const float* weights, int B, int iters, float lr,
+                  float* loss) {
   if (!m || !x || !t || B < 1 || iters < 0) return mfail(SPP_ERR_INVALID, "bad arguments");
-  int rc = mlp_upload(m, x, t, B);
+  int rc = mlp_upload(m, x, t, weights, B);
   if (rc != SPP_OK) return rc;
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   const int tot = m->E * m->P;

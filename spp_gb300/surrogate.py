@@ -5,21 +5,31 @@ realisation per MPI rank (serial/mpi-main.cpp:157-176).  Here all points run
 as one device batch (``Batch``), and an ensemble MLP trained on the sweep's
 own completed runs predicts each point's stationary polarization from its
 parameters and the moments of its polarization over a short start-up
-window.  Points whose ensemble agrees retire after the window; the others,
-and a held-out 10% that judges the surrogate, run to the end.
+window.  Points whose predicted error is small retire after the window; the
+others run to the end, and a held-out 10% runs to the end to judge the
+surrogate.
+
+The ensemble is K-fold bagged: member e is fitted with the completed points
+of fold e left out (weight 0).  A point's error bound is c x (ensemble
+spread), with c a split-conformal multiplier: the ``coverage`` quantile of
+|prediction - full run| / spread over the points that were predicted in an
+earlier round before they ran (before any such points exist, the larger
+out-of-fold multiplier of the fit).  A point retires when its bound is at
+most ``tol``.
 
 Protocol (``run_sweep``):
   1. every point runs ``window`` steps (device-side moments of P);
   2. a pilot subset and the held-out points run to ``max_steps``; their
      stationary P (mean over the second half) are the training targets and
      the judge's ground truth;
-  3. the ensemble is trained on the pilot points (device kernels, Adam);
-  4. remaining points: ensemble mean -> answer if the ensemble spread is
-     below ``spread_threshold``, otherwise the point runs to ``max_steps``
-     (the plain full run is the fallback); the surrogate is retrained on
-     the fallback runs before the answers are final;
-  5. the held-out points compare the surrogate's prediction with their full
-     runs (the judge of its error).
+  3. rounds: fit on all completed non-held-out points; of the points whose
+     bound exceeds ``tol``, the ``run_frac`` with the largest bounds (all of
+     them in the last round) resume and run to the end -- the plain full run
+     is the fallback, and the steps go to the points near the flocking
+     transition;
+  4. the points left when no bound exceeds ``tol`` retire with the ensemble
+     mean of a fit on everything that ran;
+  5. the held-out points compare that fit with their full runs.
 """
 import ctypes as C
 import math
@@ -96,57 +106,102 @@ class Mlp:
         abi.check(abi.lib().spp_mlp_predict(self._h, abi.fptr(x), B, abi.fptr(y)), "spp_mlp_predict")
         return y
 
-    def grad(self, x, t):
+    @staticmethod
+    def _weights(w, E, B):
+        if w is None:
+            return None
+        return np.ascontiguousarray(np.broadcast_to(np.asarray(w, np.float32), (E, B)))
+
+    def grad(self, x, t, weights=None):
+        """Gradient [E][P] and loss [E] of the weighted squared error
+        (weights [E][B] or [B], None = the mean-squared error)."""
         x = np.ascontiguousarray(x, np.float32)
         t = np.ascontiguousarray(t, np.float32)
+        w = self._weights(weights, self.E, x.shape[0])
         g = np.empty((self.E, self.P), np.float32)
         loss = np.empty(self.E, np.float32)
-        abi.check(abi.lib().spp_mlp_grad(self._h, abi.fptr(x), abi.fptr(t), x.shape[0], abi.fptr(g),
-                                         abi.fptr(loss)), "spp_mlp_grad")
+        abi.check(abi.lib().spp_mlp_grad(self._h, abi.fptr(x), abi.fptr(t), abi.fptr(w), x.shape[0],
+                                         abi.fptr(g), abi.fptr(loss)), "spp_mlp_grad")
         return g, loss
 
-    def train(self, x, t, iters=2000, lr=1e-3):
+    def train(self, x, t, iters=2000, lr=1e-3, weights=None):
         x = np.ascontiguousarray(x, np.float32)
         t = np.ascontiguousarray(t, np.float32)
+        w = self._weights(weights, self.E, x.shape[0])
         loss = np.empty(self.E, np.float32)
-        abi.check(abi.lib().spp_mlp_train(self._h, abi.fptr(x), abi.fptr(t), x.shape[0], int(iters),
-                                          float(lr), abi.fptr(loss)), "spp_mlp_train")
+        abi.check(abi.lib().spp_mlp_train(self._h, abi.fptr(x), abi.fptr(t), abi.fptr(w), x.shape[0],
+                                          int(iters), float(lr), abi.fptr(loss)), "spp_mlp_train")
         return loss
 
 
-def raw_features(points, stats):
-    """(eta, rho, v0, log N, mean P, var P, kurtosis P) per point."""
+def features(points, stats):
+    """(eta, rho, v0, log N, mean P, log var P, log kurtosis P) per point,
+    the moments over the start-up window.  Variance and kurtosis span
+    decades across a sweep, so they enter as logarithms."""
     f = np.zeros((len(points), N_FEATURES))
     for s, (p, st) in enumerate(zip(points, stats)):
         rho = p.n / (4.0 * p.L * p.L)
-        f[s] = [p.eta, rho, p.v0, math.log(p.n), st.p_mean, st.p_var, st.p_kurt]
+        f[s] = [p.eta, rho, p.v0, math.log(p.n), st.p_mean, math.log(max(st.p_var, 0.0) + 1e-8),
+                math.log(max(st.p_kurt, 0.0) + 1e-8)]
     return f
+
+
+def kfold(n, k, seed):
+    """Fold index of each of n samples: a seeded permutation dealt into k folds."""
+    fold = np.empty(n, np.int64)
+    fold[np.random.default_rng(seed).permutation(n)] = np.arange(n) % k
+    return fold
 
 
 @dataclass
 class Surrogate:
+    """K-fold bagged ensemble with a conformal error bound (module docstring)."""
     ensemble: int = 5
     seed: int = 4
     iters: int = 3000
     lr: float = 1e-3
+    coverage: float = 0.9
+    spread_floor: float = 1e-3
     mu: np.ndarray = field(default=None)
     sd: np.ndarray = field(default=None)
+    oof_scale: float = math.inf
+    loss: np.ndarray = field(default=None)
     mlp: Mlp = field(default=None)
 
     def _norm(self, f):
         return ((f - self.mu) / self.sd).astype(np.float32)
 
     def fit(self, f, target):
+        """Fits member e with fold e of the samples left out and sets
+        oof_scale, the coverage quantile of |out-of-fold error| / spread."""
+        f = np.asarray(f, np.float64)
+        target = np.asarray(target, np.float64)
+        n, E = len(target), self.ensemble
         self.mu = f.mean(0)
         self.sd = f.std(0) + 1e-9
         if self.mlp is None:
-            self.mlp = Mlp(self.ensemble, f.shape[1], self.seed)
+            self.mlp = Mlp(E, f.shape[1], self.seed)
         else:
-            self.mlp.set_params(init_params(self.ensemble, f.shape[1], self.seed))
-        return self.mlp.train(self._norm(f), np.asarray(target, np.float32), self.iters, self.lr)
+            self.mlp.set_params(init_params(E, f.shape[1], self.seed))
+        fold = kfold(n, E, self.seed)
+        w = (fold[None, :] != np.arange(E)[:, None]).astype(np.float32)
+        if n < 2 * E:
+            w[:] = 1.0  # too few points to leave folds out: plain ensemble, no bound
+        self.loss = self.mlp.train(self._norm(f), target.astype(np.float32), self.iters, self.lr, weights=w)
+        if n < 2 * E:
+            self.oof_scale = math.inf
+            return self.loss
+        y = self.mlp.predict(self._norm(f)).astype(np.float64)
+        oof = y[fold, np.arange(n)]
+        self.oof_scale = float(np.quantile(np.abs(oof - target) / self.floor(y.std(0)), self.coverage))
+        return self.loss
+
+    def floor(self, spread):
+        return np.maximum(spread, self.spread_floor)
 
     def predict(self, f):
-        y = self.mlp.predict(self._norm(f)).astype(np.float64)
+        """(ensemble mean, ensemble spread) per row of f."""
+        y = self.mlp.predict(self._norm(np.asarray(f, np.float64))).astype(np.float64)
         return y.mean(0), y.std(0)
 
 
@@ -154,23 +209,34 @@ class Surrogate:
 class SweepResult:
     p_answer: np.ndarray          # stationary P reported per point
     p_full: np.ndarray            # P of the points run to the end (NaN otherwise)
+    bound: np.ndarray             # error bound of the decision that retired a point (NaN otherwise)
     retired: np.ndarray           # bool: answered by the surrogate
     heldout: np.ndarray           # bool: judge points
     heldout_err: np.ndarray       # |prediction - full run| on the judge points
     particle_steps: int           # work actually done
     particle_steps_plain: int     # work of running every point to the end
+    rounds: int
+    scales: list                  # conformal multiplier of each round
     wall_s: float
     timings: dict
 
 
-def run_sweep(points, max_steps=20000, window=500, pilot_frac=0.3, holdout_frac=0.1,
-              spread_threshold=0.01, surrogate=None, seed=4, x0=None, use_surrogate=True,
+def run_sweep(points, max_steps=20000, window=500, pilot_frac=0.2, holdout_frac=0.1, tol=0.02,
+              max_rounds=3, run_frac=0.3, surrogate=None, seed=4, x0=None, use_surrogate=True,
               chunk=2000):
-    """Runs the sweep described in the module docstring and returns a
-    SweepResult.  With use_surrogate=False every point runs to the end (the
-    plain batched sweep)."""
+    """Runs the sweep and returns a SweepResult.  With use_surrogate=False
+    every point runs to the end (the plain batched sweep).
+
+    Rounds r = 0 .. max_rounds: fit on every completed non-held-out point;
+    the error bound of a remaining point is c x spread, with c the coverage
+    quantile of |prediction - full run| / spread over the points predicted
+    in earlier rounds before they ran (split conformal on fresh residuals;
+    the out-of-fold multiplier, which is larger, before any exist).  Of the
+    points whose bound exceeds tol, the run_frac with the largest bounds run
+    to the end (all of them in the last round); the points left when no
+    bound exceeds tol retire with the mean of a fit on everything run."""
     t_start = time.perf_counter()
-    timings = {}
+    timings = {"runs_s": 0.0, "train_s": 0.0}
     n = len(points)
     rng = np.random.default_rng(seed)
     order = rng.permutation(n)
@@ -183,55 +249,69 @@ def run_sweep(points, max_steps=20000, window=500, pilot_frac=0.3, holdout_frac=
     stationary_from = max_steps // 2
     x, y, th = x0 if x0 is not None else configs.sweep_state(points, seed=seed)
     sizes = np.array([p.n for p in points], np.int64)
+    retired = np.zeros(n, bool)
+    bound = np.full(n, np.nan)
+    heldout_err = np.array([])
+    rounds, scales = 0, []
     with Batch(points) as b:
         b.set_windows(window, stationary_from, max_steps)
         b.upload(x, y, th)
-        t0 = time.perf_counter()
+
+        def run(systems=None):
+            t0 = time.perf_counter()
+            if systems is not None:
+                resume(b, systems)
+            run_until_done(b, chunk)
+            timings["runs_s"] += time.perf_counter() - t0
+
         if use_surrogate:
+            t0 = time.perf_counter()
             b.step(window)
-            st = b.poll()
-            f = raw_features(points, st)
+            timings["runs_s"] += time.perf_counter() - t0
+            f = features(points, b.poll())
             # only the pilot and held-out points continue for now
             b.retire(np.flatnonzero(~(pilot | heldout)))
-        run_until_done(b, chunk)
+        run()
         st = b.poll()
-        timings["runs_s"] = time.perf_counter() - t0
         p_full = np.array([s.p_stationary if s.steps >= max_steps else np.nan for s in st])
-        steps = np.array([s.steps for s in st], np.int64)
-        retired = np.zeros(n, bool)
-        p_answer = p_full.copy()
-        heldout_err = np.array([])
         if use_surrogate:
-            t1 = time.perf_counter()
             sur = surrogate or Surrogate(seed=seed)
-            sur.fit(f[pilot], p_full[pilot])
-            rest = ~(pilot | heldout)
-            mean, spread = sur.predict(f)
-            confident = rest & (spread <= spread_threshold)
-            fallback = rest & ~confident
-            timings["train_s"] = time.perf_counter() - t1
-            # fallback points resume and run to the end
-            if fallback.any():
-                resume(b, np.flatnonzero(fallback))
-                t2 = time.perf_counter()
-                run_until_done(b, chunk)
-                timings["fallback_runs_s"] = time.perf_counter() - t2
-                st = b.poll()
-                for s in np.flatnonzero(fallback):
-                    p_full[s] = st[s].p_stationary
-                    steps[s] = st[s].steps
-                # retrain on everything that ran to the end before answering
-                done = pilot | fallback
-                sur.fit(f[done], p_full[done])
+            remaining = ~(pilot | heldout)
+            fresh = []
+            for r in range(max_rounds + 2):
+                t1 = time.perf_counter()
+                sur.fit(f[np.isfinite(p_full) & ~heldout], p_full[np.isfinite(p_full) & ~heldout])
                 mean, spread = sur.predict(f)
-            retired = confident
-            p_answer = np.where(confident, mean, p_full)
+                timings["train_s"] += time.perf_counter() - t1
+                if r == max_rounds + 1 or not remaining.any():
+                    break
+                rounds += 1
+                scale = float(np.quantile(np.concatenate(fresh), sur.coverage)) if fresh else sur.oof_scale
+                scales.append(scale)
+                bnd = scale * sur.floor(spread)
+                bound[remaining] = bnd[remaining]
+                unsure = np.flatnonzero(remaining & (bnd > tol))
+                if unsure.size == 0:
+                    break
+                if r < max_rounds:
+                    keep = max(1, int(math.ceil(run_frac * unsure.size)))
+                    unsure = unsure[np.argsort(-bnd[unsure], kind="stable")][:keep]
+                run(unsure)
+                st = b.poll()
+                for s in unsure:
+                    p_full[s] = st[s].p_stationary
+                fresh.append(np.abs(mean[unsure] - p_full[unsure]) / sur.floor(spread[unsure]))
+                remaining[unsure] = False
+                bound[unsure] = np.nan
+            retired = remaining
             heldout_err = np.abs(mean[heldout] - p_full[heldout])
+        p_answer = np.where(retired, mean, p_full) if use_surrogate else p_full.copy()
+        steps = np.array([s.steps for s in b.poll()], np.int64)
         wall = time.perf_counter() - t_start
-    return SweepResult(p_answer=p_answer, p_full=p_full, retired=retired, heldout=heldout,
+    return SweepResult(p_answer=p_answer, p_full=p_full, bound=bound, retired=retired, heldout=heldout,
                        heldout_err=heldout_err, particle_steps=int(np.sum(sizes * steps)),
-                       particle_steps_plain=int(np.sum(sizes) * max_steps), wall_s=wall,
-                       timings=timings)
+                       particle_steps_plain=int(np.sum(sizes) * max_steps), rounds=rounds, scales=scales,
+                       wall_s=wall, timings=timings)
 
 
 def run_until_done(b, chunk):

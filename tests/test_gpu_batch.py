@@ -13,8 +13,10 @@ pytestmark = pytest.mark.gpu
 
 def small_points(k=6, seed=9):
     pts = configs.sweep_points(n_points=k, n_min=300, n_max=3000, seed=seed)
-    pts[2].model = abi.MODEL_VICSEK_REF_ANGLE
-    pts[3].model = abi.MODEL_VICSEK_REF_VECTOR
+    if k > 2:
+        pts[2].model = abi.MODEL_VICSEK_REF_ANGLE
+    if k > 3:
+        pts[3].model = abi.MODEL_VICSEK_REF_VECTOR
     return pts
 
 

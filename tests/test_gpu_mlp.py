@@ -59,3 +59,38 @@ def test_training_reduces_loss_and_fits(gpu_lib):
     ye, _ = M.forward(theta[0], x)
     assert np.max(np.abs(y[0] - ye)) < 1e-4
     mlp.close()
+
+
+def test_weighted_gradient_matches_fp64(gpu_lib):
+    """Per-member sample weights (K-fold bagging: zero weight leaves a sample
+    out of that member's fit)."""
+    x, t = data(B=40)
+    mlp = surrogate.Mlp(ensemble=3, seed=11)
+    theta = mlp.params()
+    w = np.random.default_rng(3).uniform(0, 2, (3, 40)).astype(np.float32)
+    w[1, ::4] = 0.0
+    g, loss = mlp.grad(x, t, weights=w)
+    for e in range(3):
+        le, ge = M.loss_grad(theta[e], x, t, w[e])
+        assert abs(loss[e] - le) <= 1e-4 * max(le, 1e-3)
+        assert np.linalg.norm(g[e] - ge) / np.linalg.norm(ge) < 1e-3
+    # a left-out sample does not move member 1's gradient
+    t2 = t.copy()
+    t2[0] += 5.0
+    g2, _ = mlp.grad(x, t2, weights=w)
+    assert np.array_equal(g2[1], g[1]) and not np.array_equal(g2[0], g[0])
+    mlp.close()
+
+
+def test_invalid_weights_are_rejected(gpu_lib):
+    from spp_gb300 import abi
+    x, t = data(B=8)
+    mlp = surrogate.Mlp(ensemble=2, seed=1)
+    w = np.ones((2, 8), np.float32)
+    w[1] = 0.0
+    with pytest.raises(abi.SppError):
+        mlp.grad(x, t, weights=w)
+    w[1] = -1.0
+    with pytest.raises(abi.SppError):
+        mlp.train(x, t, iters=1, weights=w)
+    mlp.close()

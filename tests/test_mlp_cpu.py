@@ -50,3 +50,24 @@ def test_init_params_deterministic_and_scaled():
     W1 = a[0, :128 * 7]
     assert np.abs(W1).max() <= 1 / np.sqrt(7) + 1e-6
     assert not np.array_equal(a[0], a[1])
+
+
+def test_kfold_deals_every_fold():
+    f = surrogate.kfold(23, 5, seed=4)
+    assert np.array_equal(np.bincount(f), [5, 5, 5, 4, 4])
+    assert np.array_equal(f, surrogate.kfold(23, 5, seed=4))
+
+
+def test_oracle_weighted_loss_reduces_to_mean():
+    rng = np.random.default_rng(2)
+    theta = surrogate.init_params(1, 7, seed=5)[0]
+    x = rng.standard_normal((12, 7))
+    t = rng.uniform(0, 1, 12)
+    l0, g0 = M.loss_grad(theta, x, t)
+    l1, g1 = M.loss_grad(theta, x, t, np.full(12, 3.0))
+    assert np.isclose(l0, l1) and np.allclose(g0, g1)
+    w = np.ones(12)
+    w[5] = 0
+    l2, g2 = M.loss_grad(theta, np.delete(x, 5, 0), np.delete(t, 5))
+    l3, g3 = M.loss_grad(theta, x, t, w)
+    assert np.isclose(l2, l3) and np.allclose(g2, g3)
