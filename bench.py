@@ -11,7 +11,11 @@ steps are the workload's 10,000 simulation steps.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Prints one JSON line.  value = particle-steps/s over all ranks (each rank runs
-an independent replica: the sweep-style "replicas only" multi-GPU mode).
+an independent replica: the sweep-style "replicas only" multi-GPU mode).  At
+one GPU the line also carries "sweep": sweep points/hour at |dP| <= 0.02
+against full runs for the 512-point batched Vicsek sweep with the learned
+surrogate, next to the same sweep without it and the plain GPU path run
+point by point.
 """
 import argparse
 import ctypes as C
@@ -207,6 +211,65 @@ def ncu_traffic_per_launch(n):
 
 
 # ---------------------------------------------------------------------------
+# sweep leg: 512-point batched Vicsek sweep with the learned surrogate
+# ---------------------------------------------------------------------------
+SWEEP_TOL = 0.02
+
+
+def sweep_leg(sample_points=24, seed=4):
+    """Sweep points/hour at |dP| <= 0.02 against full runs: the batched
+    sweep steered by the surrogate, the batched sweep without it, and the
+    plain GPU path run point by point (each point alone in its own batch, run
+    to the end; a seeded random sample of points, the mean time per point
+    extrapolated to all of them)."""
+    import numpy as np
+    from spp_gb300 import configs, surrogate
+
+    pts = configs.sweep_points(seed=seed)
+    n = len(pts)
+    plain = surrogate.run_sweep(pts, use_surrogate=False, seed=seed)
+    res = surrogate.run_sweep(pts, tol=SWEEP_TOL, seed=seed)
+    err = np.abs(res.p_answer - plain.p_full)
+    ran = np.isfinite(res.p_full)
+    rng = np.random.default_rng(seed)
+    sample = rng.choice(n, size=min(sample_points, n), replace=False)
+    per_point = []
+    for s in sample:
+        t0 = time.perf_counter()
+        one = surrogate.run_sweep([pts[s]], use_surrogate=False, seed=seed)
+        per_point.append(time.perf_counter() - t0)
+        assert one.p_full[0] == plain.p_full[s], "a point run alone must equal its batched run"
+    mean_pp = float(np.mean(per_point))
+    ret = res.retired
+    pph = lambda wall: n / wall * 3600.0
+    return {
+        "metric": f"sweep points/hour at |dP|<={SWEEP_TOL} vs full runs",
+        "workload": (f"{n} Vicsek points, N log-uniform [1024, 65536] (total {sum(p.n for p in pts):,} "
+                     f"particles), eta U[0.05,0.6], rho U[0.25,2], v0=0.5, dt=1, 20,000 steps, "
+                     f"stationary P over the second half; surrogate 7->128->128->1 GELU, BF16 weights, "
+                     f"ensemble 5, Adam lr 1e-3, window 500 steps, 10% held out, seed {seed}"),
+        "batched_surrogate": {"points_per_hour": pph(res.wall_s), "wall_s": res.wall_s,
+                              "particle_steps": res.particle_steps, "retired": int(ret.sum()),
+                              "rounds": res.rounds, "runs_s": res.timings["runs_s"],
+                              "train_s": res.timings["train_s"]},
+        "batched_plain": {"points_per_hour": pph(plain.wall_s), "wall_s": plain.wall_s,
+                          "particle_steps": plain.particle_steps},
+        "point_by_point": {"points_per_hour": 3600.0 / mean_pp, "mean_s_per_point": mean_pp,
+                           "sampled_points": int(len(sample)),
+                           "sample": "seeded random sample of points, each run alone to 20,000 steps "
+                                     "through the same kernels; mean time per point x all points"},
+        "speedup_vs_point_by_point": (n * mean_pp) / res.wall_s,
+        "accuracy": {"retired_within_tol_frac": float(np.mean(err[ret] <= SWEEP_TOL)) if ret.any() else None,
+                     "retired_err_median": float(np.median(err[ret])) if ret.any() else None,
+                     "retired_err_max": float(np.max(err[ret])) if ret.any() else None,
+                     "all_points_within_tol_frac": float(np.mean(err <= SWEEP_TOL)),
+                     "heldout_err_median": float(np.median(res.heldout_err)),
+                     "heldout_within_tol_frac": float(np.mean(res.heldout_err <= SWEEP_TOL)),
+                     "full_runs_bitexact": bool(np.array_equal(res.p_full[ran], plain.p_full[ran]))},
+    }
+
+
+# ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
 def run_ours(args):
@@ -302,6 +365,8 @@ def run_ours(args):
         "observables": {"polarization": obs.polarization, "rebuilds": obs.n_rebuilds,
                         "max_neighbors": obs.max_neighbors, "list_capacity": obs.list_capacity},
     }
+    if rank == 0 and ws == 1 and not args.no_sweep:
+        line["sweep"] = sweep_leg()
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(sim_steps=2)
     if rank == 0:
@@ -352,6 +417,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the 512-point sweep leg")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

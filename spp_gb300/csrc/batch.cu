@@ -48,74 +48,217 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_batch_bin(DevBatch b) {
   b.rank[i] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
 }
 
+/* Exact fixed-point parts (hi, lo) of a heading's cos and sin, split as the
+ * alignment sums split every term (spp_fx_add).  The scatter computes them
+ * once per particle and step, so the neighbour loop of the vector-sum rule
+ * adds integers only; the sums, being exact, do not depend on the order in
+ * which the candidates are visited. */
+__device__ __forceinline__ int4 fx_parts(float c, float s) {
+  spp_fx a = {0, 0}, b = {0, 0};
+  spp_fx_add(&a, c);
+  spp_fx_add(&b, s);
+  return make_int4(a.hi, a.lo, b.hi, b.lo);
+}
+
 __global__ void __launch_bounds__(SPP_BLOCK) k_batch_scatter(DevBatch b) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.n_total) return;
   const uint32_t dst = b.cell_start[b.key[i]] + b.rank[i];
-  b.pos_alt[dst] = b.pos[i];
+  const float4 p = b.pos[i];
+  b.pos_alt[dst] = p;
+  b.fx_alt[dst] = fx_parts(p.z, p.w);
   b.theta_alt[dst] = b.theta[i];
   b.img_alt[dst] = b.img[i];
   b.id_alt[dst] = b.id[i];
 }
 
+#ifndef SPP_BATCH_UNROLL
+#define SPP_BATCH_UNROLL 2       /* candidates whose loads are issued together */
+#endif
+#ifndef SPP_BATCH_MIN_BLOCKS
+#define SPP_BATCH_MIN_BLOCKS 6   /* resident 256-thread blocks per SM the step kernel is built for */
+#endif
+
+/* Models of the batch step kernel: one rule for all systems of the batch
+ * (the common case), or any mix (runtime dispatch per system). */
+constexpr int BATCH_MIXED = -1;
+
+/* One candidate j of particle i (cell-ordered slot i, position p); q and f
+ * are candidate j's position record and fixed-point heading parts. */
+template <int MODEL>
+__device__ __forceinline__ void visit(const DevBatch& b, const SppConsts& k, int interior, float4 p, int i,
+                                      uint32_t j, float4 q, int4 f, SppAcc* a) {
+  const int model = MODEL == BATCH_MIXED ? k.model : MODEL;
+  if (model == SPP_MODEL_VICSEK) {
+    float dx, dy, d2;
+    if (interior) {
+      dx = p.x - q.x;
+      dy = p.y - q.y;
+      d2 = fmaf(dx, dx, dy * dy);
+    } else {
+      d2 = spp_sep(&k, p.x, p.y, q.x, q.y, &dx, &dy);
+    }
+    if (d2 < k.ral2) {
+      a->ax.hi += f.x;
+      a->ax.lo += f.y;
+      a->ay.hi += f.z;
+      a->ay.lo += f.w;
+      a->cnt += 1;
+    }
+  } else {
+    const float thj = model == SPP_MODEL_VICSEK_REF_ANGLE ? b.theta_alt[j] : 0.0f;
+    spp_pair_vicsek(&k, a, p.x, p.y, q.x, q.y, q.z, q.w, thj, (int)j == i);
+  }
+}
+
+/* Walks a lane's candidate sequence t = 0 .. T-1 (T the warp's longest):
+ * segments of lengths l0, l01 - l0, lt - l01 starting at slots m0, m1 + l0,
+ * m2 + l01; SPP_BATCH_UNROLL candidates per trip with their loads first. */
+template <int MODEL>
+__device__ __forceinline__ void walk(const DevBatch& b, const SppConsts& k, int interior, float4 p, int i, int T,
+                                     int lt, int l0, int l01, uint32_t m0, uint32_t m1, uint32_t m2,
+                                     SppAcc* a) {
+  const int vec = MODEL == BATCH_MIXED ? (k.model == SPP_MODEL_VICSEK) : (MODEL == SPP_MODEL_VICSEK);
+  for (int t0 = 0; t0 < T; t0 += SPP_BATCH_UNROLL) {
+    float4 q[SPP_BATCH_UNROLL];
+    int4 f[SPP_BATCH_UNROLL];
+    uint32_t j[SPP_BATCH_UNROLL];
+#pragma unroll
+    for (int u = 0; u < SPP_BATCH_UNROLL; ++u) {
+      const int t = t0 + u;
+      j[u] = (uint32_t)t + (t < l0 ? m0 : (t < l01 ? m1 : m2));
+      q[u] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      f[u] = make_int4(0, 0, 0, 0);
+      if (t < lt) {
+        if (MODEL == SPP_MODEL_VICSEK) {  /* the vector rule needs the position only */
+          const float2 xy = __ldg(reinterpret_cast<const float2*>(b.pos_alt + j[u]));
+          q[u] = make_float4(xy.x, xy.y, 0.0f, 0.0f);
+        } else {
+          q[u] = __ldg(b.pos_alt + j[u]);
+        }
+        if (vec) f[u] = __ldg(b.fx_alt + j[u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < SPP_BATCH_UNROLL; ++u)
+      if (t0 + u < lt) visit<MODEL>(b, k, interior, p, i, j[u], q[u], f[u], a);
+  }
+}
+
+/* Segments of the candidate sequence of a particle in cell (cx, cy): for each
+ * of the rows cy-1, cy, cy+1 the columns [cx-1, cx+1] clipped to the grid
+ * (wrap = 0), or the one column the periodic wrap adds (wrap = 1: column D-1
+ * for cx = 0, column 0 for cx = D-1, none otherwise). */
+__device__ __forceinline__ void segments(const DevBatch& b, const BatchSys* S, int cx, int cy, int wrap,
+                                         uint32_t* m0, uint32_t* m1, uint32_t* m2, int* l0, int* l01,
+                                         int* lt) {
+  const int D = (int)S->D;
+  int ca, cb;
+  if (!wrap) {
+    ca = cx > 0 ? cx - 1 : 0;
+    cb = cx < D - 1 ? cx + 1 : D - 1;
+  } else {
+    ca = cb = cx == 0 ? D - 1 : 0;
+  }
+  const int none = wrap && cx != 0 && cx != D - 1;
+  uint32_t lo[3], hi[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    int ny = cy + r - 1;
+    ny = ny < 0 ? ny + D : (ny >= D ? ny - D : ny);
+    const uint32_t row = S->c_off + (uint32_t)ny * (uint32_t)D;
+    lo[r] = hi[r] = 0;
+    if (!none) {
+      lo[r] = b.cell_start[row + (uint32_t)ca];
+      hi[r] = b.cell_start[row + (uint32_t)cb] + b.cell_count[row + (uint32_t)cb];
+    }
+  }
+  *m0 = lo[0];
+  *l0 = (int)(hi[0] - lo[0]);
+  *l01 = *l0 + (int)(hi[1] - lo[1]);
+  *lt = *l01 + (int)(hi[2] - lo[2]);
+  *m1 = lo[1] - (uint32_t)*l0;   /* slot = t + m1 for l0 <= t < l01 (wraps as unsigned) */
+  *m2 = lo[2] - (uint32_t)*l01;
+}
+
 /* One Vicsek step of every active system (VicsekParticle{,2}::Interact/Move,
  * shared/particle.h:145-247, or the arg-sum rule), from the cell-ordered
- * copy back into the primary arrays; per-system heading sums for P. */
-__global__ void __launch_bounds__(SPP_BLOCK) k_batch_step(DevBatch b) {
+ * copy back into the primary arrays; per-system heading sums for P.
+ *
+ * Candidates: the 3x3 cells around a particle are, per grid row, one run of
+ * consecutive keys (row-major keys), i.e. one contiguous range of the
+ * cell-ordered arrays; a lane walks its three row ranges as one flattened
+ * sequence, and the warp runs the longest lane's count, so lanes diverge only
+ * in the length of their sequences.  The cell that the periodic wrap adds to
+ * a row (a particle in the first or last column) is walked in a second pass,
+ * entered only by warps that have such a lane.  A warp whose particles all
+ * sit in interior cells (no wrap in any candidate) takes plain differences
+ * instead of minimum images: for such pairs the two are the same number. */
+template <int MODEL>
+__global__ void __launch_bounds__(SPP_BLOCK, SPP_BATCH_MIN_BLOCKS) k_batch_step(DevBatch b) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   long long ux = 0, uy = 0;
   int s = -1;
+  int active = 0;
+  const BatchSys* S = nullptr;
+  float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   if (i < b.n_total) {
     s = batch_sys(b, i);
-    const BatchSys& S = b.sys[s];
-    const float4 p = b.pos_alt[i];
+    S = &b.sys[s];
+    active = (int)S->active;
+    p = b.pos_alt[i];
+  }
+  int cx = 0, cy = 0, interior = 1, edge = 0;
+  uint32_t m0 = 0, m1 = 0, m2 = 0;
+  int l0 = 0, l01 = 0, lt = 0;
+  if (active) {
+    const int D = (int)S->D;
+    cx = spp_cell_coord(p.x, S->k.L, S->k.L2, D, SPP_BIN_GEOMETRIC);
+    cy = spp_cell_coord(p.y, S->k.L, S->k.L2, D, SPP_BIN_GEOMETRIC);
+    /* |dx|, |dy| < 2 cell widths <= L for D >= 4: no image is ever nearer */
+    interior = (D >= 4 && cx >= 1 && cx <= D - 2 && cy >= 1 && cy <= D - 2);
+    edge = (cx == 0 || cx == D - 1);
+    segments(b, S, cx, cy, 0, &m0, &m1, &m2, &l0, &l01, &lt);
+  }
+  const int all_interior = __all_sync(0xffffffffu, interior);
+  const int any_edge = __any_sync(0xffffffffu, edge);
+  const int T = (int)__reduce_max_sync(0xffffffffu, (unsigned)lt);
+  SppAcc a;
+  spp_acc_zero(&a);
+  if (active) walk<MODEL>(b, S->k, all_interior, p, i, T, lt, l0, l01, m0, m1, m2, &a);
+  if (any_edge) {
+    lt = 0;
+    if (active) segments(b, S, cx, cy, 1, &m0, &m1, &m2, &l0, &l01, &lt);
+    const int WT = (int)__reduce_max_sync(0xffffffffu, (unsigned)lt);
+    if (active) walk<MODEL>(b, S->k, 0, p, i, WT, lt, l0, l01, m0, m1, m2, &a);
+  }
+  if (active) {
+    const SppConsts& k = S->k;
+    if (a.ovf) atomicOr(&b.ctl->fx_overflow, 1u);
     const float th0 = b.theta_alt[i];
     const uint32_t id = b.id_alt[i];
-    float4 out = p;
-    float t = th0;
-    int2 g = b.img_alt[i];
-    if (S.active) {
-      const SppConsts& k = S.k;
-      const int D = (int)S.D;
-      const int cx = spp_cell_coord(p.x, k.L, k.L2, D, SPP_BIN_GEOMETRIC);
-      const int cy = spp_cell_coord(p.y, k.L, k.L2, D, SPP_BIN_GEOMETRIC);
-      const int need_theta = (k.model == SPP_MODEL_VICSEK_REF_ANGLE);
-      SppAcc a;
-      spp_acc_zero(&a);
-      for (int oy = -1; oy <= 1; ++oy) {
-        int ny = cy + oy;
-        ny = ny < 0 ? ny + D : (ny >= D ? ny - D : ny);
-        for (int ox = -1; ox <= 1; ++ox) {
-          int nx = cx + ox;
-          nx = nx < 0 ? nx + D : (nx >= D ? nx - D : nx);
-          const uint32_t kk = S.c_off + (uint32_t)ny * S.D + (uint32_t)nx;
-          const uint32_t s0 = b.cell_start[kk], c = b.cell_count[kk];
-          for (uint32_t j = s0; j < s0 + c; ++j) {
-            const float4 q = __ldg(b.pos_alt + j);
-            const float thj = need_theta ? b.theta_alt[j] : 0.0f;
-            spp_pair_vicsek(&k, &a, p.x, p.y, q.x, q.y, q.z, q.w, thj, (int)j == i);
-          }
-        }
-      }
-      if (a.ovf) atomicOr(&b.ctl->fx_overflow, 1u);
-      const spp_u32x4 r = spp_draw(k.seed, k.system, id, S.steps, SPP_RNG_VICSEK);
-      float x, y, c, sn;
-      int gx = 0, gy = 0;
-      spp_vicsek_update(&k, &a, p.x, p.y, th0, p.z, p.w, r.v[0], &x, &y, &t, &c, &sn, &gx, &gy);
-      out = make_float4(x, y, c, sn);
-      g = make_int2(g.x + gx, g.y + gy);
-      spp_fx hx = {0, 0}, hy = {0, 0};
-      spp_fx_add(&hx, c);
-      spp_fx_add(&hy, sn);
-      ux = spp_fx_units(hx);
-      uy = spp_fx_units(hy);
-    } else {
-      s = -1;  /* inactive: no contribution */
-    }
-    b.pos[i] = out;
+    const spp_u32x4 r = spp_draw(k.seed, k.system, id, S->steps, SPP_RNG_VICSEK);
+    float x, y, c, sn, t;
+    int gx = 0, gy = 0;
+    spp_vicsek_update(&k, &a, p.x, p.y, th0, p.z, p.w, r.v[0], &x, &y, &t, &c, &sn, &gx, &gy);
+    const int2 g = b.img_alt[i];
+    b.pos[i] = make_float4(x, y, c, sn);
     b.theta[i] = t;
-    b.img[i] = g;
+    b.img[i] = make_int2(g.x + gx, g.y + gy);
     b.id[i] = id;
+    spp_fx hx = {0, 0}, hy = {0, 0};
+    spp_fx_add(&hx, c);
+    spp_fx_add(&hy, sn);
+    ux = spp_fx_units(hx);
+    uy = spp_fx_units(hy);
+  } else {
+    if (i < b.n_total) {  /* retired or finished: copied through */
+      b.pos[i] = p;
+      b.theta[i] = b.theta_alt[i];
+      b.img[i] = b.img_alt[i];
+      b.id[i] = b.id_alt[i];
+    }
+    s = -1;  /* no contribution */
   }
   /* heading sums: one atomic per group of lanes of the same system (a tree
    * when the whole warp is one system, the common case) */
@@ -235,6 +378,7 @@ struct SppBatch {
   std::vector<cudaGraph_t> graph_defs;
   int64_t launches = 0;
   bool uploaded = false;
+  int model = -1;  /* the one model of all systems, or -1 for a mix */
 };
 
 namespace {
@@ -257,7 +401,7 @@ void batch_free(SppBatch* b) {
   b->graph_defs.clear();
   DevBatch& d = b->d;
   void* ptrs[] = {d.sys, d.stats, d.sys_of, d.pos, d.pos_alt, d.theta, d.theta_alt, d.img,
-                  d.img_alt, d.id, d.id_alt, d.key, d.rank, d.cell_count, d.cell_start,
+                  d.img_alt, d.id, d.id_alt, d.key, d.rank, d.cell_count, d.cell_start, d.fx_alt,
                   d.scan_tmp, d.ctl, b->stage_x, b->stage_y, b->stage_t, b->stage_img};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -273,7 +417,12 @@ int enqueue_batch_step(SppBatch* b, cudaStream_t st) {
   k_batch_bin<<<nb, SPP_BLOCK, 0, st>>>(d);
   launch_scan_u32(d.cell_count, b->n_keys, d.scan_tmp, d.cell_start, st, nullptr);
   k_batch_scatter<<<nb, SPP_BLOCK, 0, st>>>(d);
-  k_batch_step<<<nb, SPP_BLOCK, 0, st>>>(d);
+  switch (b->model) {
+    case SPP_MODEL_VICSEK: k_batch_step<SPP_MODEL_VICSEK><<<nb, SPP_BLOCK, 0, st>>>(d); break;
+    case SPP_MODEL_VICSEK_REF_ANGLE: k_batch_step<SPP_MODEL_VICSEK_REF_ANGLE><<<nb, SPP_BLOCK, 0, st>>>(d); break;
+    case SPP_MODEL_VICSEK_REF_VECTOR: k_batch_step<SPP_MODEL_VICSEK_REF_VECTOR><<<nb, SPP_BLOCK, 0, st>>>(d); break;
+    default: k_batch_step<BATCH_MIXED><<<nb, SPP_BLOCK, 0, st>>>(d); break;
+  }
   k_batch_finish<<<nblocks(d.n_sys), SPP_BLOCK, 0, st>>>(d);
   BCUDA(cudaGetLastError());
   return SPP_OK;
@@ -329,6 +478,7 @@ int spp_batch_create(const SppParams* systems, int n_systems, SppBatch** out) {
       delete b;
       return bfail(SPP_ERR_INVALID, "system " + std::to_string(s) + ": box too small (2L/r < 3)");
     }
+    b->model = s == 0 ? p.model : (b->model == p.model ? b->model : -1);
     BatchSys& S = b->host_sys[(size_t)s];
     memset(&S, 0, sizeof(S));
     spp_consts_from_params(&S.k, &p);
@@ -364,6 +514,7 @@ int spp_batch_create(const SppParams* systems, int n_systems, SppBatch** out) {
   rc = rc ? rc : balloc(&d.theta_alt, n);
   rc = rc ? rc : balloc(&d.img, n);
   rc = rc ? rc : balloc(&d.img_alt, n);
+  rc = rc ? rc : balloc(&d.fx_alt, n);
   rc = rc ? rc : balloc(&d.id, n);
   rc = rc ? rc : balloc(&d.id_alt, n);
   rc = rc ? rc : balloc(&d.key, n);

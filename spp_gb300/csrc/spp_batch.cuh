@@ -30,6 +30,7 @@ struct DevBatch {
   float4 *pos, *pos_alt;
   float *theta, *theta_alt;
   int2 *img, *img_alt;
+  int4* fx_alt;           /* fixed-point (cos hi, cos lo, sin hi, sin lo) of the cell-ordered copy */
   uint32_t *id, *id_alt;  /* particle id within its system */
   uint32_t *key, *rank;
   uint32_t *cell_count, *cell_start, *scan_tmp;
