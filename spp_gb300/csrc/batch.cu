@@ -27,16 +27,25 @@
 
 namespace {
 
-__device__ __forceinline__ int batch_sys(const DevBatch& b, int i) { return (int)b.sys_of[i]; }
+/* Compact particle index t -> (system, slot). */
+__device__ __forceinline__ int act_slot(const DevBatch& b, int t, int* s) {
+  *s = (int)b.act_sys[t];
+  return t + b.sact[*s].a_corr;
+}
 
+/* Keys are compact cell indices: a system's D x D row-major grid starts at
+ * its a_coff, so the scan runs over the cells of active systems only and a
+ * system's cell starts, plus its a_corr, are slots of its own particle range. */
 __global__ void __launch_bounds__(SPP_BLOCK) k_batch_bin(DevBatch b) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= b.n_total) return;
-  const BatchSys& S = b.sys[batch_sys(b, i)];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.n_act) return;
+  int s;
+  const int i = act_slot(b, t, &s);
+  const BatchSys& S = b.sys[s];
   const float4 p = b.pos[i];
   const int cx = spp_cell_coord(p.x, S.k.L, S.k.L2, (int)S.D, SPP_BIN_GEOMETRIC);
   const int cy = spp_cell_coord(p.y, S.k.L, S.k.L2, (int)S.D, SPP_BIN_GEOMETRIC);
-  const uint32_t key = S.c_off + (uint32_t)cy * S.D + (uint32_t)cx;
+  const uint32_t key = b.sact[s].a_coff + (uint32_t)cy * S.D + (uint32_t)cx;
   const unsigned mask = __activemask();
   const unsigned peers = __match_any_sync(mask, key);
   const int lane = threadIdx.x & 31;
@@ -44,8 +53,8 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_batch_bin(DevBatch b) {
   uint32_t base = 0;
   if (lane == leader) base = atomicAdd(&b.cell_count[key], (uint32_t)__popc(peers));
   base = __shfl_sync(peers, base, leader);
-  b.key[i] = key;
-  b.rank[i] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+  b.key[t] = key;
+  b.rank[t] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
 }
 
 /* Exact fixed-point parts (hi, lo) of a heading's cos and sin, split as the
@@ -61,9 +70,11 @@ __device__ __forceinline__ int4 fx_parts(float c, float s) {
 }
 
 __global__ void __launch_bounds__(SPP_BLOCK) k_batch_scatter(DevBatch b) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= b.n_total) return;
-  const uint32_t dst = b.cell_start[b.key[i]] + b.rank[i];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= b.n_act) return;
+  int s;
+  const int i = act_slot(b, t, &s);
+  const uint32_t dst = b.cell_start[b.key[t]] + b.rank[t] + (uint32_t)b.sact[s].a_corr;
   const float4 p = b.pos[i];
   b.pos_alt[dst] = p;
   b.fx_alt[dst] = fx_parts(p.z, p.w);
@@ -149,8 +160,8 @@ __device__ __forceinline__ void walk(const DevBatch& b, const SppConsts& k, int 
  * of the rows cy-1, cy, cy+1 the columns [cx-1, cx+1] clipped to the grid
  * (wrap = 0), or the one column the periodic wrap adds (wrap = 1: column D-1
  * for cx = 0, column 0 for cx = D-1, none otherwise). */
-__device__ __forceinline__ void segments(const DevBatch& b, const BatchSys* S, int cx, int cy, int wrap,
-                                         uint32_t* m0, uint32_t* m1, uint32_t* m2, int* l0, int* l01,
+__device__ __forceinline__ void segments(const DevBatch& b, const BatchSys* S, SysAct A, int cx, int cy,
+                                         int wrap, uint32_t* m0, uint32_t* m1, uint32_t* m2, int* l0, int* l01,
                                          int* lt) {
   const int D = (int)S->D;
   int ca, cb;
@@ -166,11 +177,11 @@ __device__ __forceinline__ void segments(const DevBatch& b, const BatchSys* S, i
   for (int r = 0; r < 3; ++r) {
     int ny = cy + r - 1;
     ny = ny < 0 ? ny + D : (ny >= D ? ny - D : ny);
-    const uint32_t row = S->c_off + (uint32_t)ny * (uint32_t)D;
+    const uint32_t row = A.a_coff + (uint32_t)ny * (uint32_t)D;
     lo[r] = hi[r] = 0;
     if (!none) {
-      lo[r] = b.cell_start[row + (uint32_t)ca];
-      hi[r] = b.cell_start[row + (uint32_t)cb] + b.cell_count[row + (uint32_t)cb];
+      lo[r] = b.cell_start[row + (uint32_t)ca] + (uint32_t)A.a_corr;
+      hi[r] = b.cell_start[row + (uint32_t)cb] + b.cell_count[row + (uint32_t)cb] + (uint32_t)A.a_corr;
     }
   }
   *m0 = lo[0];
@@ -196,15 +207,17 @@ __device__ __forceinline__ void segments(const DevBatch& b, const BatchSys* S, i
  * instead of minimum images: for such pairs the two are the same number. */
 template <int MODEL>
 __global__ void __launch_bounds__(SPP_BLOCK, SPP_BATCH_MIN_BLOCKS) k_batch_step(DevBatch b) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   long long ux = 0, uy = 0;
-  int s = -1;
+  int s = -1, i = -1;
   int active = 0;
   const BatchSys* S = nullptr;
+  SysAct A = {0u, 0};
   float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  if (i < b.n_total) {
-    s = batch_sys(b, i);
+  if (t < b.n_act) {
+    i = act_slot(b, t, &s);
     S = &b.sys[s];
+    A = b.sact[s];
     active = (int)S->active;
     p = b.pos_alt[i];
   }
@@ -218,7 +231,7 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_BATCH_MIN_BLOCKS) k_batch_step(
     /* |dx|, |dy| < 2 cell widths <= L for D >= 4: no image is ever nearer */
     interior = (D >= 4 && cx >= 1 && cx <= D - 2 && cy >= 1 && cy <= D - 2);
     edge = (cx == 0 || cx == D - 1);
-    segments(b, S, cx, cy, 0, &m0, &m1, &m2, &l0, &l01, &lt);
+    segments(b, S, A, cx, cy, 0, &m0, &m1, &m2, &l0, &l01, &lt);
   }
   const int all_interior = __all_sync(0xffffffffu, interior);
   const int any_edge = __any_sync(0xffffffffu, edge);
@@ -228,7 +241,7 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_BATCH_MIN_BLOCKS) k_batch_step(
   if (active) walk<MODEL>(b, S->k, all_interior, p, i, T, lt, l0, l01, m0, m1, m2, &a);
   if (any_edge) {
     lt = 0;
-    if (active) segments(b, S, cx, cy, 1, &m0, &m1, &m2, &l0, &l01, &lt);
+    if (active) segments(b, S, A, cx, cy, 1, &m0, &m1, &m2, &l0, &l01, &lt);
     const int WT = (int)__reduce_max_sync(0xffffffffu, (unsigned)lt);
     if (active) walk<MODEL>(b, S->k, 0, p, i, WT, lt, l0, l01, m0, m1, m2, &a);
   }
@@ -252,7 +265,7 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_BATCH_MIN_BLOCKS) k_batch_step(
     ux = spp_fx_units(hx);
     uy = spp_fx_units(hy);
   } else {
-    if (i < b.n_total) {  /* retired or finished: copied through */
+    if (i >= 0) {  /* finished since the compact space was built: copied through */
       b.pos[i] = p;
       b.theta[i] = b.theta_alt[i];
       b.img[i] = b.img_alt[i];
@@ -317,6 +330,11 @@ __global__ void k_batch_finish(DevBatch b) {
   if (b.max_steps > 0 && (int)t >= b.max_steps) S.active = 0u;
 }
 
+__global__ void k_batch_flags(DevBatch b) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < b.n_sys) b.flags[s] = b.sys[s].active;
+}
+
 __global__ void k_batch_init(DevBatch b, const float* x, const float* y, const float* th) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.n_total) return;
@@ -379,6 +397,8 @@ struct SppBatch {
   int64_t launches = 0;
   bool uploaded = false;
   int model = -1;  /* the one model of all systems, or -1 for a mix */
+  std::vector<uint32_t> act_flags;  /* the active set the compact launch space was built for */
+  bool act_valid = false;
 };
 
 namespace {
@@ -402,7 +422,8 @@ void batch_free(SppBatch* b) {
   DevBatch& d = b->d;
   void* ptrs[] = {d.sys, d.stats, d.sys_of, d.pos, d.pos_alt, d.theta, d.theta_alt, d.img,
                   d.img_alt, d.id, d.id_alt, d.key, d.rank, d.cell_count, d.cell_start, d.fx_alt,
-                  d.scan_tmp, d.ctl, b->stage_x, b->stage_y, b->stage_t, b->stage_img};
+                  d.scan_tmp, d.ctl, d.act_sys, d.sact, d.flags, b->stage_x, b->stage_y, b->stage_t,
+                  b->stage_img};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   memset(&b->d, 0, sizeof(b->d));
@@ -412,10 +433,10 @@ void batch_free(SppBatch* b) {
 
 int enqueue_batch_step(SppBatch* b, cudaStream_t st) {
   const DevBatch& d = b->d;
-  BCUDA(cudaMemsetAsync(d.cell_count, 0, sizeof(uint32_t) * b->n_keys, st));
-  const int nb = nblocks(d.n_total);
+  BCUDA(cudaMemsetAsync(d.cell_count, 0, sizeof(uint32_t) * (size_t)d.n_act_keys, st));
+  const int nb = nblocks(d.n_act);
   k_batch_bin<<<nb, SPP_BLOCK, 0, st>>>(d);
-  launch_scan_u32(d.cell_count, b->n_keys, d.scan_tmp, d.cell_start, st, nullptr);
+  launch_scan_u32(d.cell_count, (uint32_t)d.n_act_keys, d.scan_tmp, d.cell_start, st, nullptr);
   k_batch_scatter<<<nb, SPP_BLOCK, 0, st>>>(d);
   switch (b->model) {
     case SPP_MODEL_VICSEK: k_batch_step<SPP_MODEL_VICSEK><<<nb, SPP_BLOCK, 0, st>>>(d); break;
@@ -429,6 +450,51 @@ int enqueue_batch_step(SppBatch* b, cudaStream_t st) {
 }
 
 constexpr int BATCH_GRAPH_CHUNK = 32;
+
+void batch_drop_graphs(SppBatch* b) {
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.second);
+  for (auto g : b->graph_defs) cudaGraphDestroy(g);
+  b->graphs.clear();
+  b->graph_defs.clear();
+}
+
+/* Reads the active flags and, when the set of active systems changed since
+ * the compact launch space was built, rebuilds it (and the step graphs,
+ * whose launch sizes depend on it). */
+int batch_refresh_active(SppBatch* b) {
+  DevBatch& d = b->d;
+  const int ns = d.n_sys;
+  k_batch_flags<<<nblocks(ns), SPP_BLOCK, 0, b->stream>>>(d);
+  b->launches += 1;
+  std::vector<uint32_t> flags((size_t)ns);
+  BCUDA(cudaMemcpyAsync(flags.data(), d.flags, sizeof(uint32_t) * ns, cudaMemcpyDeviceToHost, b->stream));
+  BCUDA(cudaStreamSynchronize(b->stream));
+  if (b->act_valid && flags == b->act_flags) return SPP_OK;
+  std::vector<SysAct> sact((size_t)ns);
+  std::vector<uint32_t> act_sys;
+  act_sys.reserve((size_t)d.n_total);
+  uint32_t a_poff = 0, a_coff = 0;
+  for (int s = 0; s < ns; ++s) {
+    const BatchSys& S = b->host_sys[(size_t)s];
+    sact[(size_t)s] = {0u, 0};
+    if (!flags[(size_t)s]) continue;
+    sact[(size_t)s] = {a_coff, (int32_t)S.p_off - (int32_t)a_poff};
+    act_sys.insert(act_sys.end(), S.n, (uint32_t)s);
+    a_poff += S.n;
+    a_coff += S.D * S.D;
+  }
+  BCUDA(cudaMemcpyAsync(d.sact, sact.data(), sizeof(SysAct) * ns, cudaMemcpyHostToDevice, b->stream));
+  if (a_poff)
+    BCUDA(cudaMemcpyAsync(d.act_sys, act_sys.data(), sizeof(uint32_t) * a_poff, cudaMemcpyHostToDevice,
+                          b->stream));
+  BCUDA(cudaStreamSynchronize(b->stream));
+  batch_drop_graphs(b);
+  d.n_act = (int)a_poff;
+  d.n_act_keys = (int)a_coff;
+  b->act_flags = flags;
+  b->act_valid = true;
+  return SPP_OK;
+}
 
 int batch_graph(SppBatch* b, int nsteps, cudaGraphExec_t* out) {
   for (auto& g : b->graphs)
@@ -451,6 +517,21 @@ int batch_graph(SppBatch* b, int nsteps, cudaGraphExec_t* out) {
   *out = exec;
   return SPP_OK;
 }
+
+int batch_step_enqueue(SppBatch* b, int nsteps) {
+  if (b->d.n_act == 0) return SPP_OK;  /* nothing active */
+  while (nsteps > 0) {
+    int chunk = nsteps >= BATCH_GRAPH_CHUNK ? BATCH_GRAPH_CHUNK : nsteps;
+    cudaGraphExec_t exec;
+    int rc = batch_graph(b, chunk, &exec);
+    if (rc != SPP_OK) return rc;
+    BCUDA(cudaGraphLaunch(exec, b->stream));
+    b->launches += (int64_t)chunk * 7;
+    nsteps -= chunk;
+  }
+  return SPP_OK;
+}
+
 
 }  // namespace
 
@@ -523,6 +604,9 @@ int spp_batch_create(const SppParams* systems, int n_systems, SppBatch** out) {
   rc = rc ? rc : balloc(&d.cell_start, (size_t)c_off);
   rc = rc ? rc : balloc(&d.scan_tmp, ((size_t)c_off + 4095) / 4096 + 1);
   rc = rc ? rc : balloc(&d.ctl, 1);
+  rc = rc ? rc : balloc(&d.act_sys, n);
+  rc = rc ? rc : balloc(&d.sact, (size_t)n_systems);
+  rc = rc ? rc : balloc(&d.flags, (size_t)n_systems);
   rc = rc ? rc : balloc(&b->stage_x, n);
   rc = rc ? rc : balloc(&b->stage_y, n);
   rc = rc ? rc : balloc(&b->stage_t, n);
@@ -604,16 +688,9 @@ int spp_batch_upload(SppBatch* b, const float* x, const float* y, const float* t
 int spp_batch_step(SppBatch* b, int nsteps) {
   if (!b || nsteps < 0) return bfail(SPP_ERR_INVALID, "bad arguments");
   if (!b->uploaded) return bfail(SPP_ERR_INVALID, "no state uploaded");
-  while (nsteps > 0) {
-    int chunk = nsteps >= BATCH_GRAPH_CHUNK ? BATCH_GRAPH_CHUNK : nsteps;
-    cudaGraphExec_t exec;
-    int rc = batch_graph(b, chunk, &exec);
-    if (rc != SPP_OK) return rc;
-    BCUDA(cudaGraphLaunch(exec, b->stream));
-    b->launches += (int64_t)chunk * 7;
-    nsteps -= chunk;
-  }
-  return SPP_OK;
+  int rc = batch_refresh_active(b);
+  if (rc != SPP_OK) return rc;
+  return batch_step_enqueue(b, nsteps);
 }
 
 int spp_batch_poll(SppBatch* b, SppSweepStats* out, int n_systems) {
@@ -703,11 +780,21 @@ int64_t spp_batch_kernel_launches(SppBatch* b) { return b ? b->launches : 0; }
 
 int spp_batch_time_steps(SppBatch* b, int nsteps, double* ms) {
   if (!b || !ms) return bfail(SPP_ERR_INVALID, "NULL argument");
+  if (!b->uploaded || nsteps < 0) return bfail(SPP_ERR_INVALID, "no state uploaded or bad step count");
+  int rc = batch_refresh_active(b);
+  if (rc != SPP_OK) return rc;
+  if (b->d.n_act > 0) {  /* capture outside the timed region */
+    cudaGraphExec_t exec;
+    rc = batch_graph(b, nsteps >= BATCH_GRAPH_CHUNK ? BATCH_GRAPH_CHUNK : nsteps, &exec);
+    if (rc == SPP_OK && nsteps % BATCH_GRAPH_CHUNK && nsteps > BATCH_GRAPH_CHUNK)
+      rc = batch_graph(b, nsteps % BATCH_GRAPH_CHUNK, &exec);
+    if (rc != SPP_OK) return rc;
+  }
   cudaEvent_t e0, e1;
   BCUDA(cudaEventCreate(&e0));
   BCUDA(cudaEventCreate(&e1));
   cudaEventRecord(e0, b->stream);
-  int rc = spp_batch_step(b, nsteps);
+  rc = batch_step_enqueue(b, nsteps);
   cudaEventRecord(e1, b->stream);
   cudaError_t e = cudaEventSynchronize(e1);
   float t = 0;

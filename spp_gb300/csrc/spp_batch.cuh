@@ -21,6 +21,13 @@ struct BatchStats {
   long long sx, sy;       /* fixed-point heading sums of the current step (units 2^-27) */
 };
 
+/* Per system: where it sits in the compact launch space of the active
+ * systems (rebuilt by the host when the set of active systems changes). */
+struct SysAct {
+  uint32_t a_coff;        /* first cell of the system in the compact cell space */
+  int32_t a_corr;         /* slot = compact particle index + a_corr */
+};
+
 struct DevBatch {
   int n_total, n_sys;
   int window, stationary_from, max_steps;
@@ -35,5 +42,12 @@ struct DevBatch {
   uint32_t *key, *rank;
   uint32_t *cell_count, *cell_start, *scan_tmp;
   Ctl* ctl;
+  /* compact launch space: the particles and cells of the systems that were
+   * active when the host last looked; binning, scan, scatter and step run
+   * over these only */
+  int n_act, n_act_keys;
+  uint32_t* act_sys;      /* compact particle index -> system */
+  SysAct* sact;           /* [n_sys] */
+  uint32_t* flags;        /* [n_sys] snapshot of the active flags (k_batch_flags) */
 };
 #endif

@@ -323,5 +323,4 @@ def run_until_done(b, chunk):
 
 
 def resume(b, systems):
-    idx = np.ascontiguousarray(systems, np.int32)
-    abi.check(abi.lib().spp_batch_resume(b._h, abi.iptr(idx), len(idx)), "spp_batch_resume")
+    b.resume(systems)

@@ -305,8 +305,14 @@ class Batch:
         return list(out)
 
     def retire(self, systems):
+        """Stops the given systems; they leave the launch space at the next step."""
         idx = np.ascontiguousarray(systems, np.int32)
         abi.check(abi.lib().spp_batch_retire(self._h, abi.iptr(idx), len(idx)), "spp_batch_retire")
+
+    def resume(self, systems):
+        """Restarts retired systems (not those that reached max_steps) where they stopped."""
+        idx = np.ascontiguousarray(systems, np.int32)
+        abi.check(abi.lib().spp_batch_resume(self._h, abi.iptr(idx), len(idx)), "spp_batch_resume")
 
     def download(self):
         n = self.n_total

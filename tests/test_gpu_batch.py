@@ -91,3 +91,46 @@ def test_batch_retire_freezes_a_system(gpu_lib):
     s2 = slice(b.offsets[2], b.offsets[3])
     m = O.run32(p, O.State32(x[s2], y[s2], th[s2]), 35)
     assert np.array_equal(end[2][s2], m.th)
+
+
+def test_retired_systems_leave_the_launch_space_and_resume_exactly(gpu_lib):
+    """Retire and resume change the compact launch space (the particles and
+    cells of the active systems); every system still evolves exactly as it
+    would alone for the steps it was active."""
+    pts = small_points(k=6)
+    x, y, th = configs.sweep_state(pts, seed=9)
+    with Batch(pts) as b:
+        b.upload(x, y, th)
+        b.step(10)
+        b.retire([0, 2, 5])
+        b.step(25)
+        b.resume([0, 5])
+        b.step(15)
+        gx, gy, gth, gix, giy = b.download()
+        st = b.poll()
+        launches = b.kernel_launches()
+    expect = {0: 25, 1: 50, 2: 10, 3: 50, 4: 50, 5: 25}
+    for s, p in enumerate(pts):
+        sl = slice(b.offsets[s], b.offsets[s + 1])
+        assert st[s].steps == expect[s], s
+        m = O.run32(p, O.State32(x[sl], y[sl], th[sl]), expect[s])
+        assert np.array_equal(gx[sl], m.x) and np.array_equal(gth[sl], m.th), s
+        assert np.array_equal(gix[sl], m.ix) and np.array_equal(giy[sl], m.iy), s
+    assert launches > 0
+
+
+def test_all_retired_batch_steps_nothing(gpu_lib):
+    pts = small_points(k=3)
+    x, y, th = configs.sweep_state(pts, seed=9)
+    with Batch(pts) as b:
+        b.upload(x, y, th)
+        b.step(5)
+        b.retire([0, 1, 2])
+        b.step(7)
+        st = b.poll()
+        gx = b.download()[0]
+    assert [q.steps for q in st] == [5, 5, 5]
+    for s, p in enumerate(pts):
+        sl = slice(b.offsets[s], b.offsets[s + 1])
+        m = O.run32(p, O.State32(x[sl], y[sl], th[sl]), 5)
+        assert np.array_equal(gx[sl], m.x)
