@@ -173,6 +173,43 @@ int spp_pairs(SppSystem* s, double r, int32_t* pi, int32_t* pj, int cap, int64_t
  * D x D cells under the given SppBinRule (Box::Update_Cells, serial/box.h:107-134). */
 int spp_cells(SppSystem* s, int D, int rule, int32_t* cell_x, int32_t* cell_y, int n);
 
+/* ---- order parameters and pair statistics ----
+ * The reference computes these offline from saved frames:
+ * Compute_Order_Parameters (analyze/analyze.h:121-146) with the error bar of
+ * Stat::Compute / Find_Correlation_Length (analyze/statistics.h:35-82), and
+ * Pair_Distribution (analyze/analyze.h:365-424).  Here the frames come from
+ * the device. */
+typedef struct SppOrderStats {
+  int64_t samples;
+  double mean, mean_square, variance, std, min, max;
+  double corr_len;          /* first lag whose normalised autocorrelation is < 0.01 (T/2 - 1 if none) */
+  double error;             /* sqrt(variance * corr_len / samples) */
+  double sigma2;            /* variance * area (analyze.h:144) */
+  double p4_mean;           /* mean of P^4 */
+  double binder;            /* 1 - <P^4> / (3 <P^2>^2) */
+  double binder_reference;  /* 1 - <P^4> / (3 <P^2>), as analyze.h:145 writes it */
+} SppOrderStats;
+/* Statistics of a polarization series p[0..T-1] (host computation, T >= 2);
+ * area = the box area (2L)^2 for sigma2. */
+int spp_order_parameters(const double* p, int T, double area, SppOrderStats* out);
+/* Advances the system nframes x every steps and records P after every
+ * `every` steps (px, py may be NULL).  P is the exact fixed-point heading sum
+ * of spp_observables. */
+int spp_polarization_series(SppSystem* s, int nframes, int every, double* p, double* px, double* py);
+/* Radial pair histogram of the current state: counts[b] = number of ordered
+ * pairs (i != j) with minimum-image distance d < r_max and
+ * b = min(nbins - 1, (int)(d / (r_max / nbins))) in FP32.  r_max <= 2L/3,
+ * 1 <= nbins <= 4096.  g(r) = counts[b] / (N rho pi ((r+dr)^2 - r^2)). */
+int spp_radial_distribution(SppSystem* s, double r_max, int nbins, uint64_t* counts);
+/* Pair_Distribution (analyze/analyze.h:365-424) of the current state: for
+ * ordered pairs (j, k), j != k, the plain (not minimum-image) difference
+ * dr = r_k - r_j in the frame of j's heading, t_y = v_j . dr and
+ * t_x = v_j.y dr.x - v_j.x dr.y; pairs with |t_x| < lx and |t_y| < ly add
+ * one to counts[x * gy + y], x = (int)(gx ((t_x / lx) + 1) / 2),
+ * y = (int)(gy ((t_y / ly) + 1) / 2), in FP32.  sqrt(lx^2 + ly^2) <= 2L/3,
+ * 1 <= gx, gy and gx * gy <= 65536. */
+int spp_pair_distribution(SppSystem* s, double lx, double ly, int gx, int gy, uint64_t* counts);
+
 /* ---- batches of independent systems (parameter sweeps) ----
  * Replaces the task farm of serial/mpi-main.cpp:157-176 (one MPI rank per
  * realisation, run one after another): every system of a sweep shares one
@@ -191,6 +228,9 @@ typedef struct SppSweepStats {
   double p_stationary;      /* their mean */
   double p2_stationary;     /* mean of P^2 */
   double p_last;
+  double p4_stationary;     /* mean of P^4 */
+  double binder;            /* 1 - <P^4> / (3 <P^2>^2) over the stationary samples */
+  double binder_reference;  /* 1 - <P^4> / (3 <P^2>), as analyze/analyze.h:145 writes it */
 } SppSweepStats;
 
 typedef struct SppBatch SppBatch;

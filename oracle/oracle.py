@@ -15,6 +15,7 @@ from . import build as _build
 _D = C.POINTER(C.c_double)
 _F = C.POINTER(C.c_float)
 _I = C.POINTER(C.c_int32)
+_U64 = C.POINTER(C.c_uint64)
 _P = C.POINTER(abi.SppParams)
 
 _orc = None
@@ -48,6 +49,9 @@ def orc():
         L.orc64_lyap_clone.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D,
                                        _D, _D, _D]
         L.orc32_rsqrt.argtypes = [C.c_float]
+        L.orc32_radial.argtypes = [_F, _F, C.c_int, C.c_double, C.c_double, C.c_int, _U64]
+        L.orc32_pair_distribution.argtypes = [_F, _F, _F, _F, C.c_int, C.c_double, C.c_double, C.c_int,
+                                              C.c_int, _U64]
         L.orc32_rsqrt.restype = C.c_float
         _orc = L
     return _orc
@@ -79,6 +83,10 @@ def _f(a):
 
 def _i(a):
     return a.ctypes.data_as(_I)
+
+
+def _u64(a):
+    return a.ctypes.data_as(_U64)
 
 
 class State64:
@@ -136,6 +144,24 @@ def pairs64(x, y, L, r, cap=None):
     if cnt > cap:
         return pairs64(x, y, L, r, cap=int(cnt))
     return _sorted_pairs(pi[:cnt], pj[:cnt])
+
+
+def radial32(x, y, L, r_max, nbins):
+    """Ordered-pair radial histogram, FP32 as spp_radial_distribution computes it (O(N^2))."""
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    out = np.zeros(nbins, np.uint64)
+    orc().orc32_radial(_f(x), _f(y), len(x), float(L), float(r_max), int(nbins), _u64(out))
+    return out
+
+
+def pair_distribution32(x, y, c, s, lx, ly, gx, gy):
+    """Body-frame histogram [gx][gy], FP32 as spp_pair_distribution computes it (O(N^2))."""
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (x, y, c, s)]
+    out = np.zeros(gx * gy, np.uint64)
+    orc().orc32_pair_distribution(*[_f(a) for a in arrs], len(arrs[0]), float(lx), float(ly), int(gx),
+                                  int(gy), _u64(out))
+    return out.reshape(gx, gy)
 
 
 def pairs32(p, x, y, r, cap=None):

@@ -518,3 +518,47 @@ int orc32_lyap_run(const SppParams* p, int nsteps, int64_t step0, int renorm_eve
   free(nx); free(ny); free(nc); free(ns); free(ua); free(ub); free(acc); free(A); free(cand);
   return rc;
 }
+
+/* ---------------------------------------------------------------- */
+/* pair histograms of the observables (spp_radial_distribution,      */
+/* spp_pair_distribution), all ordered pairs, same FP32 expressions  */
+/* ---------------------------------------------------------------- */
+void orc32_radial(const float* x, const float* y, int n, double L, double r_max, int nbins,
+                  uint64_t* counts) {
+  const float Lf = (float)L, L2 = (float)(2.0 * L);
+  const float rm = (float)r_max, r2max = rm * rm, dr = rm / (float)nbins;
+  for (int b = 0; b < nbins; ++b) counts[b] = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      if (j == i) continue;
+      const float dx = spp_min_image_f(x[i] - x[j], Lf, L2);
+      const float dy = spp_min_image_f(y[i] - y[j], Lf, L2);
+      const float d2 = fmaf(dx, dx, dy * dy);
+      if (d2 < r2max) {
+        int b = (int)(sqrtf(d2) / dr);
+        b = b < nbins ? b : nbins - 1;
+        counts[b]++;
+      }
+    }
+}
+
+void orc32_pair_distribution(const float* x, const float* y, const float* c, const float* s, int n,
+                             double lx, double ly, int gx, int gy, uint64_t* counts) {
+  const float lxf = (float)lx, lyf = (float)ly;
+  for (int b = 0; b < gx * gy; ++b) counts[b] = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      if (j == i) continue;
+      const float dx = x[j] - x[i];
+      const float dy = y[j] - y[i];
+      const float ty = c[i] * dx + s[i] * dy;
+      const float tx = s[i] * dx - c[i] * dy;
+      if (fabsf(tx) < lxf && fabsf(ty) < lyf) {
+        int bx = (int)((float)gx * ((tx / lxf) + 1.0f) / 2.0f);
+        int by = (int)((float)gy * ((ty / lyf) + 1.0f) / 2.0f);
+        bx = bx < gx ? bx : gx - 1;
+        by = by < gy ? by : gy - 1;
+        counts[(size_t)bx * gy + by]++;
+      }
+    }
+}

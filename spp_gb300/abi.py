@@ -72,7 +72,15 @@ class SppSweepStats(C.Structure):
                 ("window_steps", C.c_int64), ("p_mean", C.c_double), ("p_var", C.c_double),
                 ("p_kurt", C.c_double), ("stationary_steps", C.c_int64),
                 ("p_stationary", C.c_double), ("p2_stationary", C.c_double),
-                ("p_last", C.c_double)]
+                ("p_last", C.c_double), ("p4_stationary", C.c_double), ("binder", C.c_double),
+                ("binder_reference", C.c_double)]
+
+
+class SppOrderStats(C.Structure):
+    _fields_ = [("samples", C.c_int64), ("mean", C.c_double), ("mean_square", C.c_double),
+                ("variance", C.c_double), ("std", C.c_double), ("min", C.c_double), ("max", C.c_double),
+                ("corr_len", C.c_double), ("error", C.c_double), ("sigma2", C.c_double),
+                ("p4_mean", C.c_double), ("binder", C.c_double), ("binder_reference", C.c_double)]
 
 
 def new_params(**kw) -> SppParams:
@@ -86,6 +94,8 @@ def new_params(**kw) -> SppParams:
 _P = C.c_void_p
 _F = C.POINTER(C.c_float)
 _I32 = C.POINTER(C.c_int32)
+_D = C.POINTER(C.c_double)
+_U64 = C.POINTER(C.c_uint64)
 
 # name -> (restype, argtypes); every entry point declared in include/spp.h
 PROTOTYPES = {
@@ -118,6 +128,10 @@ PROTOTYPES = {
     "spp_batch_download": (C.c_int, [_P, _F, _F, _F, _I32, _I32, C.c_int]),
     "spp_batch_kernel_launches": (C.c_int64, [_P]),
     "spp_batch_time_steps": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double)]),
+    "spp_order_parameters": (C.c_int, [_D, C.c_int, C.c_double, C.POINTER(SppOrderStats)]),
+    "spp_polarization_series": (C.c_int, [_P, C.c_int, C.c_int, _D, _D, _D]),
+    "spp_radial_distribution": (C.c_int, [_P, C.c_double, C.c_int, _U64]),
+    "spp_pair_distribution": (C.c_int, [_P, C.c_double, C.c_double, C.c_int, C.c_int, _U64]),
     "spp_mlp_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(_P)]),
     "spp_mlp_destroy": (C.c_int, [_P]),
     "spp_mlp_num_params": (C.c_int, [_P]),

@@ -440,6 +440,20 @@ int get_lyap_graph(SppSystem* s, int chunk, cudaGraphExec_t* out) {
 
 }  // namespace
 
+/* Internal view of a system for the observables (observables.cu). */
+int spp_internal_view(SppSystem* s, DevState* d, SppConsts* k, cudaStream_t* st) {
+  if (!s) return fail(SPP_ERR_INVALID, "system is NULL");
+  if (!s->uploaded) return fail(SPP_ERR_INVALID, "no state uploaded");
+  *d = s->d;
+  *k = s->k;
+  *st = s->stream;
+  return SPP_OK;
+}
+
+void spp_internal_count_launches(SppSystem* s, int n) {
+  if (s) s->host_launches += n;
+}
+
 extern "C" {
 
 int spp_abi_version(void) { return SPP_ABI_VERSION; }

@@ -323,6 +323,7 @@ __global__ void k_batch_finish(DevBatch b) {
   if ((int)t > b.stationary_from) {
     T.s1 += P;
     T.s2 += P * P;
+    T.s4 += (P * P) * (P * P);
     T.ns += 1;
   }
   T.p_last = P;
@@ -724,6 +725,11 @@ int spp_batch_poll(SppBatch* b, SppSweepStats* out, int n_systems) {
     if (T.ns > 0) {
       o.p_stationary = T.s1 / T.ns;
       o.p2_stationary = T.s2 / T.ns;
+      o.p4_stationary = T.s4 / T.ns;
+      if (o.p2_stationary > 0) {
+        o.binder = 1.0 - o.p4_stationary / (3.0 * o.p2_stationary * o.p2_stationary);
+        o.binder_reference = 1.0 - o.p4_stationary / (3.0 * o.p2_stationary);
+      }
     }
   }
   return SPP_OK;

@@ -343,3 +343,8 @@ void launch_polarization(const DevState& d, cudaStream_t s) {
   if (d.n == 0) return;
   k_polarization<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(d, reinterpret_cast<unsigned long long*>(d.red));
 }
+
+void launch_polarization_into(const DevState& d, unsigned long long* sums, cudaStream_t s) {
+  if (d.n == 0) return;
+  k_polarization<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(d, sums);
+}

@@ -15,7 +15,7 @@ struct BatchSys {
 /* Per-system accumulators of the polarization P. */
 struct BatchStats {
   double w1, w2, w3, w4;  /* sums of P^1..P^4 over the first `window` steps */
-  double s1, s2;          /* sums of P, P^2 after `stationary_from` steps */
+  double s1, s2, s4;      /* sums of P, P^2, P^4 after `stationary_from` steps */
   long long ns;           /* number of stationary samples */
   double p_last;          /* P of the last step */
   long long sx, sy;       /* fixed-point heading sums of the current step (units 2^-27) */

@@ -71,6 +71,11 @@ struct DevState {
   double* red;            /* reduction scratch (polarization) */
 };
 
+/* api.cu: the device state, constants and stream of an uploaded system
+ * (observables.cu), and the host-launch counter */
+int spp_internal_view(SppSystem* s, DevState* d, SppConsts* k, cudaStream_t* st);
+void spp_internal_count_launches(SppSystem* s, int n);
+
 /* api.cu: sets the message spp_last_error() returns on the calling thread */
 void spp_internal_set_error(const char* msg);
 
@@ -100,5 +105,7 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
                       int64_t* launches);
 void launch_vicsek_step(const SppConsts& k, const DevState& d, cudaStream_t s, int64_t* launches);
 void launch_polarization(const DevState& d, cudaStream_t s);
+/* the two fixed-point heading sums added into sums[0..1] (zeroed by the caller) */
+void launch_polarization_into(const DevState& d, unsigned long long* sums, cudaStream_t s);
 
 #endif

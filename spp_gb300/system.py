@@ -151,6 +151,31 @@ class System:
         abi.check(abi.lib().spp_time_steps(self._h, int(nsteps), C.byref(ms)), "spp_time_steps")
         return ms.value
 
+    def polarization_series(self, nframes, every=1):
+        """Advances nframes x every steps, P after every `every` steps
+        (returns p, px, py as float64 arrays)."""
+        p = np.empty(nframes, np.float64)
+        px = np.empty(nframes, np.float64)
+        py = np.empty(nframes, np.float64)
+        D = lambda a: a.ctypes.data_as(abi._D)
+        abi.check(abi.lib().spp_polarization_series(self._h, int(nframes), int(every), D(p), D(px), D(py)),
+                  "spp_polarization_series")
+        return p, px, py
+
+    def radial_distribution(self, r_max, nbins):
+        """Ordered-pair counts of minimum-image distances < r_max in nbins bins."""
+        out = np.zeros(nbins, np.uint64)
+        abi.check(abi.lib().spp_radial_distribution(self._h, float(r_max), int(nbins),
+                                                     out.ctypes.data_as(abi._U64)), "spp_radial_distribution")
+        return out
+
+    def pair_distribution(self, lx, ly, gx, gy):
+        """Body-frame pair counts [gx][gy] (the reference's Pair_Distribution)."""
+        out = np.zeros(gx * gy, np.uint64)
+        abi.check(abi.lib().spp_pair_distribution(self._h, float(lx), float(ly), int(gx), int(gy),
+                                                   out.ctypes.data_as(abi._U64)), "spp_pair_distribution")
+        return out.reshape(gx, gy)
+
     def profile(self, nsteps):
         pr = abi.SppProfile()
         abi.check(abi.lib().spp_profile(self._h, int(nsteps), C.byref(pr)), "spp_profile")

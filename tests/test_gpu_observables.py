@@ -1,0 +1,108 @@
+"""Device observables against the FP32 mirror (bit-exact counts) and against
+per-step readouts: the radial and body-frame pair histograms of a state,
+the recorded polarization series, and the batch's stationary Binder
+cumulants."""
+import numpy as np
+import pytest
+
+from oracle import analysis_oracle as A
+from oracle import oracle as O
+from spp_gb300 import Batch, System, configs, observables
+
+pytestmark = pytest.mark.gpu
+
+
+def vicsek_system(n=4096, L=32.0, eta=0.3, seed=0):
+    p = configs.vicsek_config(n=n, L=L, eta=eta, seed=seed)
+    x, y, th = configs.random_state(n, L, seed=seed)
+    return p, x, y, th
+
+
+def test_pair_histograms_bitexact_vs_mirror(gpu_lib):
+    p, x, y, th = vicsek_system()
+    with System(p) as s:
+        s.upload(x, y, th)
+        s.step(40)
+        gx, gy, gth, _, _ = s.download()
+        rad = s.radial_distribution(5.0, 50)
+        pd = s.pair_distribution(2.0, 3.0, 20, 30)
+    assert np.array_equal(rad, O.radial32(gx, gy, p.L, 5.0, 50))
+    c, sn = O.math32("cos", gth), O.math32("sin", gth)
+    assert np.array_equal(pd, O.pair_distribution32(gx, gy, c, sn, 2.0, 3.0, 20, 30))
+    # the FP64 restatement of the reference's Pair_Distribution on the same frame
+    ref = A.pair_distribution(gx, gy, gth, 2.0, 3.0, 20, 30)
+    assert abs(int(pd.sum()) - int(ref.sum())) <= 4 and np.abs(pd.astype(np.int64) - ref).sum() <= 12
+
+
+def test_radial_distribution_large_system_properties(gpu_lib):
+    """N = 1M ABP state: ordered-pair counts are even per unordered pair, the
+    disks' repulsion depletes the core, and g(r) -> 1 at larger r."""
+    n, L = 1 << 20, 512.0
+    p = configs.abp_config(n=n, L=L, seed=1)
+    x, y, th = configs.random_state(n, L, seed=1)
+    with System(p) as s:
+        s.upload(x, y, th)
+        s.step(400)
+        counts = s.radial_distribution(4.0, 40)
+    assert int(counts.sum()) % 2 == 0
+    r, g = observables.radial_g(counts, n, L, 4.0)
+    assert g[:3].mean() < 0.9 and np.all(np.abs(g[-10:] - 1) < 0.1)
+
+
+def test_polarization_series_matches_stepwise_readout(gpu_lib):
+    p, x, y, th = vicsek_system(n=2048, L=24.0, eta=0.2, seed=3)
+    with System(p) as a:
+        a.upload(x, y, th)
+        pa, pxa, pya = a.polarization_series(30, every=5)
+    pb = []
+    with System(p) as b:
+        b.upload(x, y, th)
+        for _ in range(30):
+            b.step(5)
+            pb.append(b.observables().polarization)
+    assert np.array_equal(pa, np.array(pb))
+    st = observables.order_parameters(pa, area=4 * p.L * p.L)
+    assert st["mean"] == pytest.approx(pa.mean(), rel=1e-12)
+    assert 0 <= st["corr_len"] < 15
+
+
+def test_polarization_series_of_abp_recovers_overflowing_lists(gpu_lib):
+    """A series over a run that outgrows its neighbour list: every frame is
+    read after the list was grown and the frozen steps re-run."""
+    n, L = 4096, 24.0
+    p = configs.abp_config(n=n, L=L, seed=2)
+    p.list_capacity = 4
+    x, y, th = configs.random_state(n, L, seed=2)
+    with System(p) as a:
+        a.upload(x, y, th)
+        pa, _, _ = a.polarization_series(10, every=20)
+    q = configs.abp_config(n=n, L=L, seed=2)
+    with System(q) as b:
+        b.upload(x, y, th)
+        pb = []
+        for _ in range(10):
+            b.step(20)
+            pb.append(b.observables().polarization)
+    assert np.array_equal(pa, np.array(pb))
+
+
+def test_batch_binder_matches_series(gpu_lib):
+    pts = configs.sweep_points(n_points=3, n_min=300, n_max=1200, seed=5)
+    x, y, th = configs.sweep_state(pts, seed=5)
+    W, S0, T = 10, 20, 60
+    with Batch(pts) as b:
+        b.set_windows(W, S0, T)
+        b.upload(x, y, th)
+        b.step(T)
+        st = b.poll()
+    for s, p in enumerate(pts):
+        sl = slice(b.offsets[s], b.offsets[s + 1])
+        state = O.State32(x[sl], y[sl], th[sl])
+        P = []
+        for t in range(T):
+            O.run32(p, state, 1, step0=t)
+            P.append(A.frame_polarization(state.th))
+        P = np.array(P[S0:])
+        m2, m4 = np.mean(P ** 2), np.mean(P ** 4)
+        assert st[s].binder == pytest.approx(1 - m4 / (3 * m2 * m2), abs=1e-6)
+        assert st[s].binder_reference == pytest.approx(1 - m4 / (3 * m2), abs=1e-6)
