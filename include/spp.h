@@ -209,6 +209,18 @@ int spp_radial_distribution(SppSystem* s, double r_max, int nbins, uint64_t* cou
  * y = (int)(gy ((t_y / ly) + 1) / 2), in FP32.  sqrt(lx^2 + ly^2) <= 2L/3,
  * 1 <= gx, gy and gx * gy <= 65536. */
 int spp_pair_distribution(SppSystem* s, double lx, double ly, int gx, int gy, uint64_t* counts);
+/* Shape of each ring vesicle of a bead model (Box::Compute_All_Variables,
+ * parallel/beadbox.h:325-434, which does this for the one membrane of a
+ * box): centre of mass, gyration tensor xx = <x^2> - <x>^2 (and yy, xy),
+ * its eigenvalues, Rg = sqrt(xx + yy) and asphericity
+ * Delta = ((l1 - l2) / (l1 + l2))^2, of the ring's beads (mb_) and of the
+ * swimmers of the ring (sw_: the swimmers_per_ring consecutive swimmers
+ * placed in it), from the unwrapped positions.  out[n_rings]. */
+typedef struct SppRingShape {
+  double mb_cm_x, mb_cm_y, mb_xx, mb_yy, mb_xy, mb_lambda1, mb_lambda2, mb_Rg, mb_Delta;
+  double sw_cm_x, sw_cm_y, sw_xx, sw_yy, sw_xy, sw_lambda1, sw_lambda2, sw_Rg, sw_Delta;
+} SppRingShape;
+int spp_ring_shapes(SppSystem* s, SppRingShape* out, int n_rings);
 
 /* ---- batches of independent systems (parameter sweeps) ----
  * Replaces the task farm of serial/mpi-main.cpp:157-176 (one MPI rank per

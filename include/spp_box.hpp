@@ -121,13 +121,17 @@ class Box {
   }
 
   // operator<<(ostream&, Box*) (parallel/box.h:476-502): t, Lx, Ly as
-  // doubles, nb, Ns, Nm as int32, then Ns x (x, y, theta) float32 with x, y
-  // the unwrapped position r_original (RepulsiveParticle::Write, shared/
-  // particle.h:759-764).
+  // doubles (Lx = Ly = the half-width L), nb, Ns, Nm as int32, then the Nm
+  // membrane beads (the first n_rings x ring_size particles of a bead model)
+  // as (x, y) float32 (C2DVector::write, shared/c2dvector.h:175-184) and the
+  // Ns swimmers as (x, y, theta) float32 (RepulsiveParticle::Write, shared/
+  // particle.h:759-764); x, y are the unwrapped positions r_original.
   friend std::ostream& operator<<(std::ostream& os, Box& box) {
     State s = box.Save();
     double L = box.p_.L;
-    int32_t nb = 1, Ns = box.N, Nm = 0;
+    int32_t nb = 1;
+    int32_t Nm = box.p_.model == SPP_MODEL_BEADS ? box.p_.n_rings * box.p_.ring_size : 0;
+    int32_t Ns = box.N - Nm;
     os.write(reinterpret_cast<const char*>(&box.t), sizeof(double));
     os.write(reinterpret_cast<const char*>(&L), sizeof(double));
     os.write(reinterpret_cast<const char*>(&L), sizeof(double));
@@ -137,7 +141,7 @@ class Box {
     for (int i = 0; i < box.N; ++i) {
       float rec[3] = {(float)(s.x[i] + 2.0 * L * s.img_x[i]), (float)(s.y[i] + 2.0 * L * s.img_y[i]),
                       s.theta[i]};
-      os.write(reinterpret_cast<const char*>(rec), sizeof(rec));
+      os.write(reinterpret_cast<const char*>(rec), (i < Nm ? 2 : 3) * sizeof(float));
     }
     return os;
   }

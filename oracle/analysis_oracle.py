@@ -104,3 +104,21 @@ def radial_counts(x, y, L, r_max, nbins):
         b = np.minimum((d[d < r_max] / dr).astype(np.int64), nbins - 1)
         np.add.at(counts, b, 1)
     return counts
+
+
+def ring_shape(x, y):
+    """Box::Compute_All_Variables' shape quantities (parallel/beadbox.h:
+    402-428) of one set of unwrapped points: cm, xx, yy, xy, lambda1,
+    lambda2, Rg, Delta (FP64)."""
+    x = np.asarray(x, np.float64)
+    y = np.asarray(y, np.float64)
+    n = len(x)
+    cx, cy = x.sum() / n, y.sum() / n
+    xx = (x * x).sum() / n - cx * cx
+    yy = (y * y).sum() / n - cy * cy
+    xy = (x * y).sum() / n - cx * cy
+    root = math.sqrt((xx - yy) ** 2 + 4 * xy * xy)
+    l1 = 0.5 * (xx + yy) + 0.5 * root
+    l2 = 0.5 * (xx + yy) - 0.5 * root
+    return dict(cm_x=cx, cm_y=cy, xx=xx, yy=yy, xy=xy, lambda1=l1, lambda2=l2, Rg=math.sqrt(xx + yy),
+                Delta=((l1 - l2) / (l1 + l2)) ** 2)

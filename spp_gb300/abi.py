@@ -76,6 +76,11 @@ class SppSweepStats(C.Structure):
                 ("binder_reference", C.c_double)]
 
 
+class SppRingShape(C.Structure):
+    _fields_ = [(f"{pre}_{k}", C.c_double) for pre in ("mb", "sw")
+                for k in ("cm_x", "cm_y", "xx", "yy", "xy", "lambda1", "lambda2", "Rg", "Delta")]
+
+
 class SppOrderStats(C.Structure):
     _fields_ = [("samples", C.c_int64), ("mean", C.c_double), ("mean_square", C.c_double),
                 ("variance", C.c_double), ("std", C.c_double), ("min", C.c_double), ("max", C.c_double),
@@ -132,6 +137,7 @@ PROTOTYPES = {
     "spp_polarization_series": (C.c_int, [_P, C.c_int, C.c_int, _D, _D, _D]),
     "spp_radial_distribution": (C.c_int, [_P, C.c_double, C.c_int, _U64]),
     "spp_pair_distribution": (C.c_int, [_P, C.c_double, C.c_double, C.c_int, C.c_int, _U64]),
+    "spp_ring_shapes": (C.c_int, [_P, C.POINTER(SppRingShape), C.c_int]),
     "spp_mlp_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(_P)]),
     "spp_mlp_destroy": (C.c_int, [_P]),
     "spp_mlp_num_params": (C.c_int, [_P]),

@@ -1,0 +1,52 @@
+"""Bit-exact checkpoint and resume of a system.
+
+Replaces the reference's restart path -- a saved frame read back by
+operator>>(istream&, Box*) (parallel/box.h:505-524) and re-placed by
+Positioning_Particles (:155-218) -- which cannot continue the same noise,
+since the GSL generator state is not saved.  A checkpoint here holds the
+parameters, the wrapped positions with their box-crossing counters, the
+headings and the Philox step counter: the noise of a step is a function of
+(seed, system, particle, step), so a resumed run continues bit for bit.
+File: a numpy .npz archive (params as the raw SppParams bytes)."""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .system import Snapshot, System
+
+FORMAT = 1
+
+
+def save(path, system: System, step=None):
+    """Writes the system's parameters and state; step = the Philox step
+    counter of the state (default: the steps the system has taken since its
+    upload plus the upload's step0)."""
+    x, y, th, ix, iy = system.download()
+    if step is None:
+        step = system.step0 + int(system.observables().step)
+    raw = bytes(C.string_at(C.addressof(system.params), C.sizeof(system.params)))
+    np.savez(path, format=FORMAT, params=np.frombuffer(raw, np.uint8), x=x, y=y, theta=th, img_x=ix,
+             img_y=iy, step=np.int64(step))
+
+
+def load(path):
+    """(SppParams, Snapshot) of a checkpoint file."""
+    with np.load(path) as z:
+        if int(z["format"]) != FORMAT:
+            raise ValueError(f"unknown checkpoint format {int(z['format'])}")
+        raw = z["params"].tobytes()
+        if len(raw) != C.sizeof(abi.SppParams):
+            raise ValueError("checkpoint was written with a different SppParams layout")
+        p = abi.SppParams.from_buffer_copy(raw)
+        snap = Snapshot(z["x"].copy(), z["y"].copy(), z["theta"].copy(), z["img_x"].copy(), z["img_y"].copy(),
+                        int(z["step"]))
+    return p, snap
+
+
+def resume(path) -> System:
+    """A new system holding the checkpointed state, ready to continue."""
+    p, snap = load(path)
+    s = System(p)
+    s.upload(snap.x, snap.y, snap.theta, step0=snap.step, img_x=snap.img_x, img_y=snap.img_y)
+    return s

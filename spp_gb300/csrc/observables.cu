@@ -137,6 +137,54 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_obs_pairdist(Grid g, float lx, fl
   }
 }
 
+/* Per ring: sums of x, y, x^2, y^2, xy of the unwrapped positions of its
+ * beads (block 2r) and of its swimmers (block 2r + 1), in FP64 with a fixed
+ * reduction tree.  Slot of particle id q: inv[q]. */
+__global__ void __launch_bounds__(SPP_BLOCK) k_obs_ring_sums(DevState d, SppConsts k, int n_rings, int ring_size,
+                                                             int sw_per_ring, double* sums) {
+  __shared__ double red[5][SPP_BLOCK];
+  const int ring = blockIdx.x >> 1, part = blockIdx.x & 1;
+  const int first = part == 0 ? ring * ring_size : n_rings * ring_size + ring * sw_per_ring;
+  const int count = part == 0 ? ring_size : sw_per_ring;
+  double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int q = threadIdx.x; q < count; q += blockDim.x) {
+    const uint32_t slot = d.inv[first + q];
+    const float4 p = d.pos[slot];
+    const int2 g = d.img[slot];
+    const double x = (double)p.x + (double)k.L2 * (double)g.x;
+    const double y = (double)p.y + (double)k.L2 * (double)g.y;
+    a[0] += x;
+    a[1] += y;
+    a[2] += x * x;
+    a[3] += y * y;
+    a[4] += x * y;
+  }
+  for (int c = 0; c < 5; ++c) red[c][threadIdx.x] = a[c];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int c = 0; c < 5; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 5) sums[(size_t)blockIdx.x * 5 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+/* The reference's formulas (beadbox.h:402-428) from the five sums of n points. */
+void shape_from_sums(const double* m, int n, double* cm_x, double* cm_y, double* xx, double* yy, double* xy,
+                     double* l1, double* l2, double* rg, double* delta) {
+  *cm_x = m[0] / n;
+  *cm_y = m[1] / n;
+  *xx = (m[2] / n) - *cm_x * *cm_x;
+  *yy = (m[3] / n) - *cm_y * *cm_y;
+  *xy = (m[4] / n) - *cm_x * *cm_y;
+  const double root = std::sqrt((*xx - *yy) * (*xx - *yy) + 4 * *xy * *xy);
+  *l1 = 0.5 * (*xx + *yy) + 0.5 * root;
+  *l2 = 0.5 * (*xx + *yy) - 0.5 * root;
+  *rg = std::sqrt(*xx + *yy);
+  const double dl = (*l1 - *l2) / (*l1 + *l2);
+  *delta = dl * dl;
+}
+
 inline int nblk(int n) { return (n + SPP_BLOCK - 1) / SPP_BLOCK; }
 
 /* Sorts the system's current positions into a grid of cells at least `range`
@@ -315,6 +363,42 @@ int spp_pair_distribution(SppSystem* s, double lx, double ly, int gx, int gy, ui
   if (dc) cudaFree(dc);
   grid_free(&g);
   if (e != cudaSuccess) return ofail(SPP_ERR_CUDA, std::string("pair distribution: ") + cudaGetErrorString(e));
+  return SPP_OK;
+}
+
+int spp_ring_shapes(SppSystem* s, SppRingShape* out, int n_rings) {
+  if (!s || !out) return ofail(SPP_ERR_INVALID, "NULL argument");
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  DevState d;
+  SppConsts k;
+  cudaStream_t st;
+  rc = spp_internal_view(s, &d, &k, &st);
+  if (rc != SPP_OK) return rc;
+  if (k.model != SPP_MODEL_BEADS || k.n_beads <= 0 || k.ring_size <= 0)
+    return ofail(SPP_ERR_INVALID, "ring shapes need a bead model with rings");
+  const int nr = k.n_beads / k.ring_size;
+  if (n_rings != nr) return ofail(SPP_ERR_INVALID, "n_rings differs from the system's ring count");
+  const int sw = (d.n - k.n_beads) / nr;
+  double* sums = nullptr;
+  OCUDA(cudaMalloc((void**)&sums, sizeof(double) * 10 * (size_t)nr));
+  k_obs_ring_sums<<<2 * nr, SPP_BLOCK, 0, st>>>(d, k, nr, k.ring_size, sw, sums);
+  spp_internal_count_launches(s, 1);
+  std::vector<double> h(10 * (size_t)nr);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), sums, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(sums);
+  if (e != cudaSuccess) return ofail(SPP_ERR_CUDA, std::string("ring shapes: ") + cudaGetErrorString(e));
+  for (int r = 0; r < nr; ++r) {
+    SppRingShape& o = out[r];
+    memset(&o, 0, sizeof(o));
+    shape_from_sums(&h[10 * (size_t)r], k.ring_size, &o.mb_cm_x, &o.mb_cm_y, &o.mb_xx, &o.mb_yy, &o.mb_xy,
+                    &o.mb_lambda1, &o.mb_lambda2, &o.mb_Rg, &o.mb_Delta);
+    if (sw > 0)
+      shape_from_sums(&h[10 * (size_t)r + 5], sw, &o.sw_cm_x, &o.sw_cm_y, &o.sw_xx, &o.sw_yy, &o.sw_xy,
+                      &o.sw_lambda1, &o.sw_lambda2, &o.sw_Rg, &o.sw_Delta);
+  }
   return SPP_OK;
 }
 

@@ -21,7 +21,6 @@ Errors surface as ``SppError`` carrying the ABI status, where the reference
 prints and exits (shared/cell.h:45-49, parallel/box.h:224-228).
 """
 import ctypes as C
-import struct
 from dataclasses import dataclass
 
 import numpy as np
@@ -37,6 +36,7 @@ class System:
         self._h = C.c_void_p()
         abi.check(abi.lib().spp_create(C.byref(self.params), C.byref(self._h)), "spp_create")
         self.n = int(self.params.n)
+        self.step0 = 0
 
     @property
     def handle(self):
@@ -68,6 +68,7 @@ class System:
         abi.check(abi.lib().spp_upload_state(self._h, abi.fptr(x), abi.fptr(y), abi.fptr(th),
                                              abi.iptr(ix), abi.iptr(iy), self.n, int(step0)),
                   "spp_upload_state")
+        self.step0 = int(step0)
 
     def download(self):
         n = self.n
@@ -176,6 +177,16 @@ class System:
                                                    out.ctypes.data_as(abi._U64)), "spp_pair_distribution")
         return out.reshape(gx, gy)
 
+    def ring_shapes(self):
+        """Per ring vesicle: shape of the membrane (mb_*) and of its swimmers
+        (sw_*) -- centre of mass, gyration tensor, eigenvalues, Rg, asphericity
+        (Box::Compute_All_Variables, parallel/beadbox.h:325-434).  Returns a
+        dict of arrays."""
+        nr = int(self.params.n_rings)
+        out = (abi.SppRingShape * nr)()
+        abi.check(abi.lib().spp_ring_shapes(self._h, out, nr), "spp_ring_shapes")
+        return {name: np.array([getattr(o, name) for o in out]) for name, _ in abi.SppRingShape._fields_}
+
     def profile(self, nsteps):
         pr = abi.SppProfile()
         abi.check(abi.lib().spp_profile(self._h, int(nsteps), C.byref(pr)), "spp_profile")
@@ -257,16 +268,12 @@ class Box:
 
     def Write(self, os):
         """operator<<(ostream&, Box*) (parallel/box.h:476-502): one binary frame
-        t:f64, Lx:f64, Ly:f64, nb:i32, Ns:i32, Nm:i32, then Ns x (x, y, theta)
-        as float32 of the unwrapped position r_original and the heading."""
+        in the reference's format (spp_gb300.binfile): header t, Lx, Ly, nb,
+        Ns, Nm, then membrane beads (x, y) and swimmers (x, y, theta) as
+        float32, positions unwrapped (r_original)."""
+        from . import binfile
         x, y, th, ix, iy = self.system.download()
-        L = self.params.L
-        xu = (x.astype(np.float64) + 2 * L * ix).astype(np.float32)
-        yu = (y.astype(np.float64) + 2 * L * iy).astype(np.float32)
-        os.write(struct.pack("<dddiii", self.t, L, L, 1, self.N, 0))
-        rec = np.empty((self.N, 3), np.float32)
-        rec[:, 0], rec[:, 1], rec[:, 2] = xu, yu, th
-        os.write(rec.tobytes())
+        os.write(binfile.state_frame(self.params, self.t, x, y, th, ix, iy))
 
 
 class Batch:

@@ -59,4 +59,8 @@ def test_cpp_driver_matches_python(gpu_lib, tmp_path):
     xu = (gx.astype(np.float64) + 2 * L * gix).astype(np.float32)
     assert np.array_equal(rec[:, 0], xu)
     assert np.array_equal(rec[:, 2], gth)
+    # the frame reads back through the reference-format reader
+    from spp_gb300 import binfile
+    (frame,) = binfile.read_frames(raw)
+    assert frame.healthy and np.array_equal(frame.x, xu) and np.array_equal(frame.theta, gth)
     assert abs(pol[-1] - P) <= 1e-5 * max(P, 1e-3)  # ostream prints 6 significant digits

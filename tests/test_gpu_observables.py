@@ -106,3 +106,51 @@ def test_batch_binder_matches_series(gpu_lib):
         m2, m4 = np.mean(P ** 2), np.mean(P ** 4)
         assert st[s].binder == pytest.approx(1 - m4 / (3 * m2 * m2), abs=1e-6)
         assert st[s].binder_reference == pytest.approx(1 - m4 / (3 * m2), abs=1e-6)
+
+
+def test_system_frames_read_back(gpu_lib, tmp_path):
+    """Frames written from the device state (vesicles: membrane beads and
+    swimmers) read back through the reference-format reader."""
+    from spp_gb300 import binfile
+    p = configs.vesicle_config(n_rings=16, ring_size=64, swimmers_per_ring=8)
+    x, y, th = configs.vesicle_state(p)
+    path = tmp_path / "traj.bin"
+    nm = p.n_rings * p.ring_size
+    with System(p) as s, open(path, "wb") as f:
+        s.upload(x, y, th)
+        states = []
+        for _ in range(3):
+            s.step(50)
+            binfile.write_system_frame(f, s)
+            states.append(s.download())
+    frames = binfile.read_frames(path)
+    assert len(frames) == 3
+    for fr, (gx, gy, gth, gix, giy) in zip(frames, states):
+        xu = (gx.astype(np.float64) + 2 * p.L * gix).astype(np.float32)
+        assert fr.healthy and len(fr.mx) == nm and np.array_equal(fr.mx, xu[:nm])
+        assert np.array_equal(fr.x, xu[nm:]) and np.array_equal(fr.theta, gth[nm:])
+    assert [fr.t for fr in frames] == pytest.approx([50 * p.dt, 100 * p.dt, 150 * p.dt])
+
+
+def test_ring_shapes_match_fp64(gpu_lib):
+    p = configs.vesicle_config(n_rings=16, ring_size=64, swimmers_per_ring=8)
+    x, y, th = configs.vesicle_state(p)
+    with System(p) as s:
+        s.upload(x, y, th)
+        s.step(200)
+        shapes = s.ring_shapes()
+        gx, gy, _, gix, giy = s.download()
+    xu = gx.astype(np.float64) + 2 * p.L * gix
+    yu = gy.astype(np.float64) + 2 * p.L * giy
+    M, nr = p.ring_size, p.n_rings
+    sw = (p.n - nr * M) // nr
+    for r in range(nr):
+        mb = A.ring_shape(xu[r * M:(r + 1) * M], yu[r * M:(r + 1) * M])
+        q0 = nr * M + r * sw
+        swd = A.ring_shape(xu[q0:q0 + sw], yu[q0:q0 + sw])
+        for key, v in mb.items():
+            assert shapes["mb_" + key][r] == pytest.approx(v, rel=1e-7, abs=1e-7), key
+        for key, v in swd.items():
+            assert shapes["sw_" + key][r] == pytest.approx(v, rel=1e-7, abs=1e-7), key
+        # a ring of 64 beads at rest length 1 stays near-circular: R ~ 10.2, Delta small
+        assert 9.0 < shapes["mb_Rg"][r] < 11.5 and shapes["mb_Delta"][r] < 0.05
