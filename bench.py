@@ -409,6 +409,89 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# the other configurations (one JSON line each; not the headline)
+# ---------------------------------------------------------------------------
+def other_workload(args):
+    """Throughput of configurations 1, 3, 4 and 5 on one GPU: plain Vicsek
+    N=4096 (32 B/particle-step), vesicles with swimmers (163,840 bodies, RK4,
+    ~260 B/body-step), the Lyapunov spectrum (N=16,384, k=8 tangent vectors,
+    ~2,550 B/particle-step) and the 512-point sweep.  Effective bandwidth =
+    algorithmic bytes x rate (the working sets are L2-resident)."""
+    import numpy as np
+    import torch
+    from spp_gb300 import System, configs
+
+    peak, peak_kind = measured_hbm_peak()
+    w = args.workload
+    if w == "sweep":
+        line = {"metric": "sweep points/hour at |dP|<=0.02 vs full runs", "n_gpus": 1, "data": "synthetic"}
+        line.update(sweep_leg())
+        line["value"] = line["batched_surrogate"]["points_per_hour"]
+        line["unit"] = "points/hour"
+        line["higher_is_better"] = True
+        print(json.dumps(line), flush=True)
+        return
+    if w == "vicsek":
+        p = configs.vicsek_config()
+        x, y, th = configs.random_state(p.n, p.L, seed=0)
+        chunk, alg, unit = 2000, 32, "particle-steps/s"
+        desc = "plain Vicsek (arg-sum rule), N=4096, L=32, v0=0.5, r=1, eta=0.3, dt=1, 2000 steps per bench step"
+    elif w == "vesicles":
+        p = configs.vesicle_config()
+        x, y, th = configs.vesicle_state(p)
+        chunk, alg, unit = 200, 260, "body-steps/s"
+        desc = ("1024 ring vesicles x 128 beads + 32 swimmers each (163,840 bodies), bonds k=100, bending "
+                "kappa=10, WCA-like R12, RK4 dt=0.002, L=1081 (30% area fraction by enclosed area); 200 "
+                "steps per bench step")
+    elif w == "lyapunov":
+        p = configs.lyapunov_config()
+        x, y, th = configs.random_state(p.n, p.L, seed=3)
+        chunk, alg, unit = 100, 2550, "particle-steps/s"
+        desc = ("continuous Vicsek N=16,384, L=64, RK4 dt=0.01, k=8 tangent vectors, linearised RK4, "
+                "FP64 Gram-Schmidt every 10 steps; 100 steps per bench step")
+    else:
+        raise SystemExit(f"unknown workload {w}")
+    with System(p) as s:
+        s.upload(x, y, th)
+        times = []
+        if w == "lyapunov":
+            s.lyap_init(8, seed=3)
+            for _ in range(args.warmup):
+                s.lyap_step(chunk, renorm_every=10)
+            s.sync()
+            for _ in range(args.steps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                s.lyap_step(chunk, renorm_every=10)
+                s.sync()
+                times.append((time.perf_counter() - t0) * 1e3)
+            lam, T = s.lyap_exponents()
+            extra = {"lyapunov_exponents": [float(v) for v in lam], "time_span": T,
+                     "timing": "host wall clock around spp_lyap_step + spp_sync"}
+        else:
+            for _ in range(args.warmup):
+                s.step(chunk)
+            s.sync()
+            for _ in range(args.steps):
+                times.append(s.time_steps(chunk))
+            extra = {"timing": "CUDA events on the system's stream (spp_time_steps)",
+                     "polarization": s.observables().polarization}
+    ms = float(np.sum(times))
+    value = p.n * chunk * args.steps / (ms / 1e3)
+    achieved = alg * value / 1e9
+    line = {"metric": unit, "workload": w, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "ms_per_sim_step": ms / args.steps / chunk,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic (Philox-seeded)",
+            "config": {"workload": desc, "n": int(p.n)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "alg_bytes_per_unit": alg,
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                         "note": "effective bandwidth of the whole step; working set L2-resident"}}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -418,11 +501,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-sweep", action="store_true", help="skip the 512-point sweep leg")
+    ap.add_argument("--workload", default="abp", choices=["abp", "vicsek", "vesicles", "lyapunov", "sweep"],
+                    help="abp: the headline line (default); the others print their own line")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "abp":
+        other_workload(args)
     else:
         run_ours(args)
 
