@@ -103,7 +103,7 @@ int dalloc(T** ptr, size_t count) {
 
 void free_lyap(SppSystem* s) {
   LyapState& L = s->lyap;
-  void* ptrs[] = {L.t0, L.ua, L.ub, L.acc, L.partial, L.rinv, L.log_stretch, L.error};
+  void* ptrs[] = {L.t0, L.ua, L.ub, L.acc, L.uslot, L.partial, L.rinv, L.log_stretch, L.error};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   memset(&L, 0, sizeof(L));
@@ -305,6 +305,7 @@ int alloc_list(SppSystem* s, int cap) {
 }
 
 int enqueue_lyap_step(SppSystem* s, cudaStream_t st, bool capture, int64_t* launches);
+int launch_lyap_chunks(SppSystem* s, int64_t nsteps);
 
 /* Base + tangent steps with direct launches (recovery path): the rebuild is
  * decided on the host after each step, renormalisation every
@@ -330,9 +331,13 @@ int run_lyap_direct(SppSystem* s, int64_t nsteps) {
 }
 
 /* Grows the neighbour list after an overflow and finishes the steps the
- * frozen kernels skipped. */
+ * frozen kernels skipped.  A system whose density keeps growing (flocks
+ * without repulsion) may overflow again after some progress; recovery goes
+ * on while the steps advance and gives up after 8 overflows in a row at the
+ * same step. */
 int recover(SppSystem* s) {
-  for (int attempt = 0; attempt < 8; ++attempt) {
+  int64_t last_frozen_step = -1;
+  for (int stalls = 0; stalls < 8;) {
     Ctl c;
     int rc = read_ctl(s, &c);
     if (rc != SPP_OK) return rc;
@@ -341,13 +346,19 @@ int recover(SppSystem* s) {
                                     "particles under an R12 force?); the state is not reliable");
     if (!c.frozen) {
       if ((int64_t)c.step >= s->target_step) return SPP_OK;
-      if (s->lyap_on) rc = run_lyap_direct(s, s->target_step - (int64_t)c.step);
+      if (s->lyap_on && s->use_graphs) rc = launch_lyap_chunks(s, s->target_step - (int64_t)c.step);
+      else if (s->lyap_on) rc = run_lyap_direct(s, s->target_step - (int64_t)c.step);
       else rc = run_steps(s, s->target_step - (int64_t)c.step);
       if (rc != SPP_OK) return rc;
       continue;
     }
-    int cap = (int)((c.list_need * 5u) / 4u + 4u);
-    cap = (cap + 3) & ~3;
+    if ((int64_t)c.step <= last_frozen_step) ++stalls;
+    else stalls = 0;
+    last_frozen_step = (int64_t)c.step;
+    int64_t need = (int64_t)c.list_need * 5 / 4 + 4;
+    if (need < (int64_t)s->d.cap + 4) need = (int64_t)s->d.cap + 4;
+    if (need > (int64_t)s->d.n + 4) need = (int64_t)s->d.n + 4;
+    int cap = (int)((need + 3) & ~(int64_t)3);
     free_graphs(s);
     for (auto& g : s->lyap_graphs) {
       cudaGraphExecDestroy(g.exec);
@@ -435,6 +446,26 @@ int get_lyap_graph(SppSystem* s, int chunk, cudaGraphExec_t* out) {
   }
   s->lyap_graphs.push_back({chunk, graph, exec});
   *out = exec;
+  return SPP_OK;
+}
+
+/* Graphs of renorm_every base + tangent steps, each closed by the FP64
+ * renormalisation.  Also the recovery path after a list overflow: the steps
+ * the frozen kernels skipped are run again the same way (the chunk ends of
+ * the re-run are extra renormalisation points, which leave the summed
+ * log-stretches unchanged). */
+int launch_lyap_chunks(SppSystem* s, int64_t nsteps) {
+  const int every = s->lyap_renorm_every > 0 ? s->lyap_renorm_every : 10;
+  int64_t left = nsteps;
+  while (left > 0) {
+    int chunk = left >= every ? every : (int)left;
+    cudaGraphExec_t exec;
+    int rc = get_lyap_graph(s, chunk, &exec);
+    if (rc != SPP_OK) return rc;
+    CUDA_TRY(cudaGraphLaunch(exec, s->stream));
+    s->graph_kernels += (int64_t)chunk * 3 * s->nstages + 6;
+    left -= chunk;
+  }
   return SPP_OK;
 }
 
@@ -890,6 +921,7 @@ int spp_lyap_init(SppSystem* s, int K, uint64_t seed) {
   rc = rc ? rc : dalloc(&L.ua, len);
   rc = rc ? rc : dalloc(&L.ub, len);
   rc = rc ? rc : dalloc(&L.acc, len);
+  rc = rc ? rc : dalloc(&L.uslot, tangent_slot_floats(K, s->p.n));
   rc = rc ? rc : dalloc(&L.partial, (size_t)SPP_GRAM_BLOCKS * SPP_GRAM_ENTRIES);
   rc = rc ? rc : dalloc(&L.rinv, (size_t)SPP_LYAP_MAX * SPP_LYAP_MAX);
   rc = rc ? rc : dalloc(&L.log_stretch, SPP_LYAP_MAX);
@@ -897,6 +929,7 @@ int spp_lyap_init(SppSystem* s, int K, uint64_t seed) {
   if (rc != SPP_OK) { free_lyap(s); return rc; }
   CUDA_TRY(cudaMemsetAsync(L.log_stretch, 0, sizeof(double) * SPP_LYAP_MAX, s->stream));
   CUDA_TRY(cudaMemsetAsync(L.error, 0, sizeof(uint32_t), s->stream));
+  CUDA_TRY(cudaMemsetAsync(L.uslot, 0, sizeof(float) * tangent_slot_floats(K, s->p.n), s->stream));
   launch_tangent_init(L, seed, s->p.system_id, s->stream);
   launch_renormalize(L, 0, s->stream, &s->host_launches);
   s->host_launches += 1;
@@ -925,18 +958,8 @@ int spp_lyap_step(SppSystem* s, int nsteps, int renorm_every) {
   if (nsteps < 0 || renorm_every < 1) return fail(SPP_ERR_INVALID, "need nsteps >= 0, renorm_every >= 1");
   s->target_step += nsteps;
   s->lyap_renorm_every = renorm_every;
-  int64_t left = nsteps;
-  while (left > 0) {
-    int chunk = left >= renorm_every ? renorm_every : (int)left;
-    cudaGraphExec_t exec;
-    int rc = get_lyap_graph(s, chunk, &exec);
-    if (rc != SPP_OK) return rc;
-    CUDA_TRY(cudaGraphLaunch(exec, s->stream));
-    s->graph_kernels += (int64_t)chunk * 2 * s->nstages + 6;
-    s->lyap_steps += chunk;
-    left -= chunk;
-  }
-  return SPP_OK;
+  s->lyap_steps += nsteps;
+  return launch_lyap_chunks(s, nsteps);
 }
 
 int spp_lyap_exponents(SppSystem* s, double* lambda, int K, double* elapsed) {

@@ -7,9 +7,10 @@
  * base run, then Gram-Schmidt renormalised (shared/vector-set.h:118-127).
  * Here the k tangent vectors are advanced by the linearised integrator next
  * to the base trajectory:
- *   k_tangent_stage: after each base stage, one thread per particle gathers
- *     cos(th_j - th_i) of its neighbours (same id-sorted list, FP32 sums in
- *     id order) and advances all k vectors through the JVP of that stage.
+ *   k_tangent_stage: after each base stage, one thread per (particle,
+ *     vector) gathers cos(th_j - th_i) of its neighbours (same id-sorted
+ *     list, FP32 sums in id order) and advances its vector through the JVP
+ *     of that stage.
  *     Tangent vectors are stored by particle id, [k][x|y|th][n], so the
  *     cell reordering at list rebuilds does not touch them.
  *   Renormalisation every m steps, in FP64: a Cholesky-QR pass, done twice
@@ -26,38 +27,70 @@
 
 namespace {
 
-template <int K>
-__global__ void __launch_bounds__(SPP_BLOCK) k_tangent_stage(SppConsts k, DevState d, LyapState L,
-                                                             TanStage t) {
+/* Vectors are handled in groups of 4: uslot holds, per slot, the heading
+ * components of all vectors padded to a multiple of 4, so a neighbour's
+ * components for one group are one float4 load. */
+constexpr int TAN_GROUP = 4;
+constexpr int TAN_BLOCK = 128;
+
+__host__ __device__ inline int tan_padded(int K) { return (K + TAN_GROUP - 1) / TAN_GROUP * TAN_GROUP; }
+
+/* The heading components of the stage input, gathered into slot order:
+ * uslot[i][v] = u[v][theta][id_i] (v < K; the padding stays 0). */
+__global__ void __launch_bounds__(SPP_BLOCK) k_tangent_gather(DevState d, int K, const float* uin, float* uslot) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = blockIdx.y;
+  if (i >= d.n) return;
+  uslot[(size_t)i * tan_padded(K) + v] = uin[(size_t)(v * 3 + 2) * d.n + d.id[i]];
+}
+
+/* One thread per (particle slot, group of 4 tangent vectors), blockIdx.y the
+ * group: a small system (N = 16,384) still spreads over the GPU, a
+ * neighbour's components for the group are one float4 load, and the sum over
+ * neighbours for each vector is the same FP32 expression in the same
+ * (id-sorted list) order as with one vector per thread. */
+__global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevState d, LyapState L, TanStage t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v0 = blockIdx.y * TAN_GROUP;
   if (i >= d.n || d.ctl->frozen) return;
   const int n = d.n;
+  const int KP = tan_padded(L.K);
   const uint32_t idi = d.id[i];
   const float4 pi = t.cur[i];
-  float ui[K], acc[K];
-#pragma unroll
-  for (int v = 0; v < K; ++v) {
-    ui[v] = t.uin[(size_t)(v * 3 + 2) * n + idi];
-    acc[v] = 0.0f;
-  }
+  const float4 ui = *reinterpret_cast<const float4*>(L.uslot + (size_t)i * KP + v0);
+  float acc[TAN_GROUP] = {0.0f, 0.0f, 0.0f, 0.0f};
   const int cnt = d.nn[i];
+  const int32_t* __restrict__ nb = d.nbr + i;
+  /* the next neighbour's index, state and components are loaded before the
+   * current one is used */
+  int jn = cnt > 0 ? __ldg(nb) : i;
+  float4 pn = __ldg(t.cur + jn);
+  float4 un = __ldg(reinterpret_cast<const float4*>(L.uslot + (size_t)jn * KP + v0));
   for (int q = 0; q < cnt; ++q) {
-    const int j = __ldg(d.nbr + (size_t)q * n + i);
-    const float4 pj = __ldg(t.cur + j);
+    const float4 pj = pn;
+    const float4 uj = un;
+    if (q + 1 < cnt) {
+      jn = __ldg(nb + (size_t)(q + 1) * n);
+      pn = __ldg(t.cur + jn);
+      un = __ldg(reinterpret_cast<const float4*>(L.uslot + (size_t)jn * KP + v0));
+    }
     float dx, dy;
     const float d2 = spp_sep(&k, pi.x, pi.y, pj.x, pj.y, &dx, &dy);
     if (d2 < k.ral2) {
       const float cij = spp_tangent_coupling(pi.z, pi.w, pj.z, pj.w);
-      const uint32_t idj = d.id[j];
-#pragma unroll
-      for (int v = 0; v < K; ++v)
-        acc[v] = acc[v] + cij * (t.uin[(size_t)(v * 3 + 2) * n + idj] - ui[v]);
+      acc[0] = acc[0] + cij * (uj.x - ui.x);
+      acc[1] = acc[1] + cij * (uj.y - ui.y);
+      acc[2] = acc[2] + cij * (uj.z - ui.z);
+      acc[3] = acc[3] + cij * (uj.w - ui.w);
     }
   }
   const float gp = k.g * k.one_minus_alpha_over_pi;
+  const float uiv[TAN_GROUP] = {ui.x, ui.y, ui.z, ui.w};
 #pragma unroll
-  for (int v = 0; v < K; ++v) {
-    const float slope[3] = {-k.v0 * pi.w * ui[v], k.v0 * pi.z * ui[v], gp * acc[v]};
+  for (int u = 0; u < TAN_GROUP; ++u) {
+    const int v = v0 + u;
+    if (v >= L.K) break;
+    const float slope[3] = {-k.v0 * pi.w * uiv[u], k.v0 * pi.z * uiv[u], gp * acc[u]};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const size_t e = (size_t)(v * 3 + c) * n + idi;
@@ -105,15 +138,21 @@ __global__ void __launch_bounds__(SPP_GRAM_THREADS) k_gram(const float* __restri
   }
 }
 
+/* One block of SPP_GRAM_ENTRIES threads: thread q sums entry q of the block
+ * partials in block order; thread 0 factors. */
 __global__ void k_chol(int K, const double* partial, double* rinv, double* log_stretch,
                        int accumulate, uint32_t* error) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double G[SPP_GRAM_ENTRIES];
-  for (int q = 0; q < K * (K + 1) / 2; ++q) {
+  __shared__ double Gs[SPP_GRAM_ENTRIES];
+  const int q = threadIdx.x;
+  if (q < K * (K + 1) / 2) {
     double x = 0.0;
     for (int b = 0; b < SPP_GRAM_BLOCKS; ++b) x = x + partial[(size_t)b * SPP_GRAM_ENTRIES + q];
-    G[q] = x;
+    Gs[q] = x;
   }
+  __syncthreads();
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double G[SPP_GRAM_ENTRIES];
+  for (int e = 0; e < K * (K + 1) / 2; ++e) G[e] = Gs[e];
   double lr[SPP_LYAP_MAX];
   if (spp_cholesky_inverse(K, G, rinv, lr)) {
     *error = 1u;
@@ -153,6 +192,8 @@ __global__ void k_tangent_init(float* V, int K, int n, uint64_t seed, uint32_t s
 
 }  // namespace
 
+size_t tangent_slot_floats(int K, int n) { return (size_t)tan_padded(K) * (size_t)n; }
+
 void launch_tangent_init(const LyapState& L, uint64_t seed, uint32_t system, cudaStream_t s) {
   const int tot = L.K * 3 * L.n;
   k_tangent_init<<<(tot + SPP_BLOCK - 1) / SPP_BLOCK, SPP_BLOCK, 0, s>>>(L.t0, L.K, L.n, seed, system);
@@ -181,11 +222,11 @@ void launch_tangent_stage(const SppConsts& k, const DevState& d, const LyapState
   float* ub = L.ub;
   t.uin = stage == 0 ? L.t0 : ((stage & 1) ? ua : ub);
   t.uout = (stage & 1) ? ub : ua;
-  const int nb = (d.n + SPP_BLOCK - 1) / SPP_BLOCK;
-#define SPP_TAN(KK) k_tangent_stage<KK><<<nb, SPP_BLOCK, 0, s>>>(k, d, L, t)
-  SPP_K_DISPATCH(L.K, SPP_TAN)
-#undef SPP_TAN
-  if (launches) *launches += 1;
+  const dim3 ggrid((unsigned)((d.n + SPP_BLOCK - 1) / SPP_BLOCK), (unsigned)L.K);
+  k_tangent_gather<<<ggrid, SPP_BLOCK, 0, s>>>(d, L.K, t.uin, L.uslot);
+  const dim3 tgrid((unsigned)((d.n + TAN_BLOCK - 1) / TAN_BLOCK), (unsigned)(tan_padded(L.K) / TAN_GROUP));
+  k_tangent_stage<<<tgrid, TAN_BLOCK, 0, s>>>(k, d, L, t);
+  if (launches) *launches += 2;
 }
 
 void launch_renormalize(const LyapState& L, int accumulate, cudaStream_t s, int64_t* launches) {
@@ -195,7 +236,7 @@ void launch_renormalize(const LyapState& L, int accumulate, cudaStream_t s, int6
 #define SPP_GRAM(KK) k_gram<KK><<<SPP_GRAM_BLOCKS, SPP_GRAM_THREADS, 0, s>>>(L.t0, len, L.partial)
     SPP_K_DISPATCH(L.K, SPP_GRAM)
 #undef SPP_GRAM
-    k_chol<<<1, 32, 0, s>>>(L.K, L.partial, L.rinv, L.log_stretch, accumulate, L.error);
+    k_chol<<<1, SPP_GRAM_ENTRIES, 0, s>>>(L.K, L.partial, L.rinv, L.log_stretch, accumulate, L.error);
 #define SPP_APPLY(KK) k_apply<KK><<<nb, SPP_BLOCK, 0, s>>>(L.t0, len, L.rinv)
     SPP_K_DISPATCH(L.K, SPP_APPLY)
 #undef SPP_APPLY

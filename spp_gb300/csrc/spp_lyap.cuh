@@ -10,6 +10,7 @@ struct LyapState {
   float* ua;              /* stage inputs (RK2/RK4) */
   float* ub;
   float* acc;             /* RK4 slope sums */
+  float* uslot;           /* the stage input's heading components in slot order, [n][K padded to 4] */
   double* partial;        /* Gram partials [SPP_GRAM_BLOCKS][SPP_GRAM_ENTRIES] */
   double* rinv;           /* R^{-1}, [SPP_LYAP_MAX][SPP_LYAP_MAX] */
   double* log_stretch;    /* running sums of log R_aa, FP64 */
@@ -27,5 +28,7 @@ void launch_tangent_stage(const SppConsts& k, const DevState& d, const LyapState
                           int nstages, const float4* cur, cudaStream_t s, int64_t* launches);
 void launch_renormalize(const LyapState& L, int accumulate, cudaStream_t s, int64_t* launches);
 void launch_tangent_init(const LyapState& L, uint64_t seed, uint32_t system, cudaStream_t s);
+/* floats of LyapState::uslot for K vectors of n particles */
+size_t tangent_slot_floats(int K, int n);
 
 #endif

@@ -176,3 +176,18 @@ def test_checkpoint_file_resume_is_bitexact(gpu_lib, tmp_path):
         end_b = b.download()
     for u, v in zip(end_a, end_b):
         assert np.array_equal(u, v)
+
+
+def test_densifying_flocks_keep_recovering(gpu_lib):
+    """Continuous Vicsek without noise or repulsion: flocks densify, the
+    neighbour list overflows again and again as the run goes on; recovery
+    keeps growing it, and the run stays bit-exact."""
+    p = configs.lyapunov_config(n=1024)
+    x, y, th = configs.random_state(p.n, p.L, seed=3)
+    with System(p) as s:
+        s.upload(x, y, th)
+        s.step(1050)
+        g = s.download()
+        o = s.observables()
+    assert o.step == 1050 and o.list_capacity > 16
+    assert same(g, O.run32(p, O.State32(x, y, th), 1050))

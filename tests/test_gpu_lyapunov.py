@@ -63,3 +63,27 @@ def test_lyap_full_size_bitexact(gpu_lib):
     assert np.array_equal(V.ravel(), Vm)
     M = V.reshape(K, -1).astype(np.float64)
     assert np.allclose(M @ M.T, np.eye(K), atol=1e-5)
+
+
+def test_lyap_through_list_overflows(gpu_lib):
+    """A run whose neighbour list overflows (a small initial capacity) is
+    recovered with the same step graphs: the base trajectory stays bit-exact
+    and the exponents agree with an overflow-free run (the recovery only adds
+    renormalisation points)."""
+    p = configs.lyapunov_config(n=2048)
+    x, y, th = configs.random_state(p.n, p.L, seed=4)
+    q = configs.lyapunov_config(n=2048)
+    q.list_capacity = 4
+    K, steps, m = 4, 200, 10
+    _, _, lam_a, Ta, st_a = gpu_lyap(p, x, y, th, K, 4, steps, m)
+    with System(q) as s:
+        s.upload(x, y, th)
+        s.lyap_init(K, 4)
+        s.lyap_step(steps, m)
+        lam_b, Tb = s.lyap_exponents()
+        st_b = s.download()
+        grown = s.observables().list_capacity
+    assert grown > 4 and Ta == Tb
+    for u, v in zip(st_a, st_b):
+        assert np.array_equal(u, v)
+    assert np.allclose(lam_a, lam_b, rtol=1e-4, atol=1e-6)
