@@ -198,16 +198,17 @@ def measured_hbm_peak():
 
 
 def ncu_traffic_per_launch(n):
-    """DRAM bytes per k_abp_stage launch from the committed ncu summary,
-    scaled from the captured size to n particles."""
-    f = ROOT / "profiles" / "abp_stage_traffic.json"
+    """DRAM bytes per k_abp_stage launch from the committed ncu summary
+    (profiles/k_abp_stage_abp1M_rk2.md, the line 'dram bytes per launch:
+    <bytes> at n=<n>'), scaled to n particles."""
+    f = ROOT / "profiles" / "k_abp_stage_abp1M_rk2.md"
     if not f.exists():
         return None
-    try:
-        d = json.loads(f.read_text())
-        return float(d["dram_bytes_per_launch"]) * n / float(d["n"])
-    except Exception:
+    import re
+    m = re.search(r"dram bytes per launch:\s*([0-9.eE+]+)\s*at n=([0-9]+)", f.read_text())
+    if not m:
         return None
+    return float(m.group(1)) * n / float(m.group(2))
 
 
 # ---------------------------------------------------------------------------

@@ -61,40 +61,67 @@ struct MlpDev {
   float* dy;                /* [E][B] */
 };
 
+/* W2 of one member in shared memory, row-major with a padded row stride of
+ * H + 2 BF16 (65 words): a warp reading a column (forward: row j per thread)
+ * or a row (backward: column j per thread) hits 32 different banks. */
+constexpr int W2S = H + 2;
+
+__device__ __forceinline__ void load_w2(const __nv_bfloat16* w2, __nv_bfloat16* w2s) {
+  for (int idx = threadIdx.x; idx < H * H; idx += blockDim.x) w2s[(idx / H) * W2S + (idx % H)] = w2[idx];
+}
+
+/* One block per (member, chunk of CHUNK samples), one thread per hidden unit.
+ * The layer sums run over k in order for every sample, as FP32 FMAs on the
+ * BF16 weights. */
 __global__ void __launch_bounds__(H) k_mlp_forward(MlpDev m) {
   const int e = blockIdx.y;
   const int s0 = blockIdx.x * CHUNK;
   const int j = threadIdx.x;
   const int in = m.in, P = n_params(in);
   const __nv_bfloat16* w = m.w + (size_t)e * P;
-  __shared__ float h1[H];
-  __shared__ float h2[H];
-  __shared__ float red[H / 32];
-  for (int q = 0; q < CHUNK; ++q) {
+  __shared__ __nv_bfloat16 w2s[H * W2S];
+  __shared__ float h1s[CHUNK][H];
+  __shared__ float red[CHUNK][H / 32];
+  load_w2(w + off_w2(in), w2s);
+  const int nq = m.B - s0 < CHUNK ? m.B - s0 : CHUNK;
+  const float b1j = __bfloat162float(w[off_b1(in) + j]);
+  for (int q = 0; q < nq; ++q) {
     const int s = s0 + q;
-    if (s >= m.B) break;
-    float z = __bfloat162float(w[off_b1(in) + j]);
+    float z = b1j;
     for (int k = 0; k < in; ++k) z = fmaf(__bfloat162float(w[j * in + k]), m.x[(size_t)s * in + k], z);
-    m.z1[((size_t)e * m.B + s) * H + j] = z;
-    h1[j] = gelu(z, nullptr);
-    m.h1[((size_t)e * m.B + s) * H + j] = h1[j];
-    __syncthreads();
-    float z2 = __bfloat162float(w[off_b2(in) + j]);
-    const __nv_bfloat16* row = w + off_w2(in) + (size_t)j * H;
-    for (int k = 0; k < H; ++k) z2 = fmaf(__bfloat162float(row[k]), h1[k], z2);
-    m.z2[((size_t)e * m.B + s) * H + j] = z2;
-    h2[j] = gelu(z2, nullptr);
-    m.h2[((size_t)e * m.B + s) * H + j] = h2[j];
-    float part = __bfloat162float(w[off_w3(in) + j]) * h2[j];
+    const size_t es = ((size_t)e * m.B + s) * H + j;
+    m.z1[es] = z;
+    const float h = gelu(z, nullptr);
+    h1s[q][j] = h;
+    m.h1[es] = h;
+  }
+  __syncthreads();
+  float z2[CHUNK];
+  const float b2j = __bfloat162float(w[off_b2(in) + j]);
+#pragma unroll
+  for (int q = 0; q < CHUNK; ++q) z2[q] = b2j;
+  for (int k = 0; k < H; ++k) {
+    const float wv = __bfloat162float(w2s[j * W2S + k]);
+#pragma unroll
+    for (int q = 0; q < CHUNK; ++q) z2[q] = fmaf(wv, h1s[q < nq ? q : 0][k], z2[q]);
+  }
+  const float w3j = __bfloat162float(w[off_w3(in) + j]);
+#pragma unroll
+  for (int q = 0; q < CHUNK; ++q) {
+    if (q >= nq) break;
+    const size_t es = ((size_t)e * m.B + s0 + q) * H + j;
+    m.z2[es] = z2[q];
+    const float h2 = gelu(z2[q], nullptr);
+    m.h2[es] = h2;
+    float part = w3j * h2;
     for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
-    if ((j & 31) == 0) red[j >> 5] = part;
-    __syncthreads();
-    if (j == 0) {
-      float yy = __bfloat162float(w[off_b3(in)]);
-      for (int q2 = 0; q2 < H / 32; ++q2) yy += red[q2];
-      m.y[(size_t)e * m.B + s] = yy;
-    }
-    __syncthreads();
+    if ((j & 31) == 0) red[q][j >> 5] = part;
+  }
+  __syncthreads();
+  if (j < nq) {
+    float yy = __bfloat162float(w[off_b3(in)]);
+    for (int q2 = 0; q2 < H / 32; ++q2) yy += red[j][q2];
+    m.y[(size_t)e * m.B + s0 + j] = yy;
   }
 }
 
@@ -106,31 +133,78 @@ __global__ void __launch_bounds__(H) k_mlp_backward(MlpDev m) {
   const int j = threadIdx.x;
   const int in = m.in, P = n_params(in);
   const __nv_bfloat16* w = m.w + (size_t)e * P;
-  __shared__ float dz2s[H];
-  for (int q = 0; q < CHUNK; ++q) {
+  __shared__ __nv_bfloat16 w2s[H * W2S];
+  __shared__ float dz2s[CHUNK][H];
+  load_w2(w + off_w2(in), w2s);
+  const int nq = m.B - s0 < CHUNK ? m.B - s0 : CHUNK;
+  const float w3j = __bfloat162float(w[off_w3(in) + j]);
+  for (int q = 0; q < nq; ++q) {
     const int s = s0 + q;
-    if (s >= m.B) break;
     const size_t es = (size_t)e * m.B + s;
     const float dy = 2.0f * m.sw[es] * (m.y[es] - m.t[s]);
     if (j == 0) m.dy[es] = dy;
     float g2;
     gelu(m.z2[es * H + j], &g2);
-    const float dz2 = dy * __bfloat162float(w[off_w3(in) + j]) * g2;
+    const float dz2 = dy * w3j * g2;
     m.dz2[es * H + j] = dz2;
-    dz2s[j] = dz2;
-    __syncthreads();
-    /* dh1[j] = sum_r W2[r][j] dz2[r] */
-    float dh1 = 0.0f;
-    for (int r = 0; r < H; ++r) dh1 = fmaf(__bfloat162float(w[off_w2(in) + (size_t)r * H + j]), dz2s[r], dh1);
+    dz2s[q][j] = dz2;
+  }
+  __syncthreads();
+  /* dh1[j] = sum_r W2[r][j] dz2[r], r in order */
+  float dh1[CHUNK];
+#pragma unroll
+  for (int q = 0; q < CHUNK; ++q) dh1[q] = 0.0f;
+  for (int r = 0; r < H; ++r) {
+    const float wv = __bfloat162float(w2s[r * W2S + j]);
+#pragma unroll
+    for (int q = 0; q < CHUNK; ++q) dh1[q] = fmaf(wv, dz2s[q < nq ? q : 0][r], dh1[q]);
+  }
+#pragma unroll
+  for (int q = 0; q < CHUNK; ++q) {
+    if (q >= nq) break;
+    const size_t es = (size_t)e * m.B + s0 + q;
     float g1;
     gelu(m.z1[es * H + j], &g1);
-    m.dz1[es * H + j] = dh1 * g1;
-    __syncthreads();
+    m.dz1[es * H + j] = dh1[q] * g1;
   }
 }
 
-/* One thread per (member, parameter): the gradient summed over the samples
- * in order. */
+/* Gradient of W2 (H x H per member): one block per (member, GW_ROWS rows),
+ * one thread per column k, the samples streamed through shared memory in
+ * chunks; each entry is summed over the samples in order. */
+constexpr int GW_ROWS = 16;
+constexpr int GW_SAMPLES = 32;
+
+__global__ void __launch_bounds__(H) k_mlp_grad_w2(MlpDev m, float* grad) {
+  const int e = blockIdx.y;
+  const int j0 = blockIdx.x * GW_ROWS;
+  const int k = threadIdx.x;
+  const int in = m.in, P = n_params(in);
+  __shared__ float hs[GW_SAMPLES][H];
+  __shared__ float dzs[GW_SAMPLES][GW_ROWS];
+  float acc[GW_ROWS];
+#pragma unroll
+  for (int r = 0; r < GW_ROWS; ++r) acc[r] = 0.0f;
+  const size_t eb = (size_t)e * m.B;
+  for (int c0 = 0; c0 < m.B; c0 += GW_SAMPLES) {
+    const int nc = m.B - c0 < GW_SAMPLES ? m.B - c0 : GW_SAMPLES;
+    for (int ss = 0; ss < nc; ++ss) hs[ss][k] = m.h1[(eb + c0 + ss) * H + k];
+    for (int idx = k; idx < nc * GW_ROWS; idx += H)
+      dzs[idx / GW_ROWS][idx % GW_ROWS] = m.dz2[(eb + c0 + idx / GW_ROWS) * H + j0 + idx % GW_ROWS];
+    __syncthreads();
+    for (int ss = 0; ss < nc; ++ss) {
+      const float hk = hs[ss][k];
+#pragma unroll
+      for (int r = 0; r < GW_ROWS; ++r) acc[r] = fmaf(dzs[ss][r], hk, acc[r]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < GW_ROWS; ++r) grad[(size_t)e * P + off_w2(in) + (size_t)(j0 + r) * H + k] = acc[r];
+}
+
+/* One thread per (member, parameter) outside W2: the gradient summed over
+ * the samples in order. */
 __global__ void k_mlp_grad(MlpDev m, float* grad) {
   const int in = m.in, P = n_params(in);
   const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -145,8 +219,7 @@ __global__ void k_mlp_grad(MlpDev m, float* grad) {
     const int j = q - off_b1(in);
     for (int s = 0; s < m.B; ++s) g += m.dz1[(eb + s) * H + j];
   } else if (q < off_b2(in)) {
-    const int j = (q - off_w2(in)) / H, k = (q - off_w2(in)) % H;
-    for (int s = 0; s < m.B; ++s) g = fmaf(m.dz2[(eb + s) * H + j], m.h1[(eb + s) * H + k], g);
+    return;  /* W2: k_mlp_grad_w2 */
   } else if (q < off_w3(in)) {
     const int j = q - off_b2(in);
     for (int s = 0; s < m.B; ++s) g += m.dz2[(eb + s) * H + j];
@@ -170,11 +243,16 @@ __global__ void k_mlp_loss(MlpDev m, float* loss) {
   loss[e] = l;
 }
 
-/* Adam (Kingma & Ba, 2015) on the FP32 masters; refreshes the BF16 copy. */
+/* Adam (Kingma & Ba, 2015) on the FP32 masters; refreshes the BF16 copy.
+ * The bias corrections of step t are bias[*tix] = (1 - b1^t, 1 - b2^t),
+ * tabulated on the host for the steps of one training call. */
 __global__ void k_mlp_adam(int count, float* master, __nv_bfloat16* w, const float* grad, float* mom,
-                           float* vel, float lr, float b1, float b2, float eps, float c1, float c2) {
+                           float* vel, float lr, float b1, float b2, float eps, const float2* bias,
+                           const int* tix) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
+  const float2 c = bias[*tix];
+  const float c1 = c.x, c2 = c.y;
   const float g = grad[i];
   const float mm = b1 * mom[i] + (1.0f - b1) * g;
   const float vv = b2 * vel[i] + (1.0f - b2) * g * g;
@@ -184,6 +262,8 @@ __global__ void k_mlp_adam(int count, float* master, __nv_bfloat16* w, const flo
   master[i] = th;
   w[i] = __float2bfloat16_rn(th);
 }
+
+__global__ void k_mlp_next(int* tix) { *tix += 1; }
 
 __global__ void k_mlp_cast(int count, const float* master, __nv_bfloat16* w) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -215,11 +295,27 @@ struct SppMlp {
   float *dz1 = nullptr, *dz2 = nullptr, *dy = nullptr, *loss = nullptr, *sw = nullptr;
   std::vector<float> host_sw;
   cudaStream_t stream = nullptr;
+  /* Adam bias corrections of one training call, and the index of the step */
+  float2* bias = nullptr;
+  int bias_cap = 0;
+  int* tix = nullptr;
+  /* graphs of TRAIN_GRAPH_ITERS training iterations, keyed by (B, lr) */
+  struct TrainGraph { int B; float lr; cudaGraph_t graph; cudaGraphExec_t exec; };
+  std::vector<TrainGraph> graphs;
 };
 
 namespace {
 
+void mlp_drop_graphs(SppMlp* m) {
+  for (auto& g : m->graphs) {
+    cudaGraphExecDestroy(g.exec);
+    cudaGraphDestroy(g.graph);
+  }
+  m->graphs.clear();
+}
+
 void mlp_free_scratch(SppMlp* m) {
+  mlp_drop_graphs(m);
   float* ptrs[] = {m->x, m->t, m->z1, m->z2, m->h1, m->h2, m->y, m->dz1, m->dz2, m->dy, m->loss, m->sw};
   for (float* q : ptrs)
     if (q) cudaFree(q);
@@ -303,6 +399,38 @@ void mlp_fwd_bwd(SppMlp* m, int B, bool backward) {
   k_mlp_backward<<<grid, H, 0, m->stream>>>(d);
   const long long tot = (long long)m->E * m->P;
   k_mlp_grad<<<(unsigned)((tot + 255) / 256), 256, 0, m->stream>>>(d, m->grad);
+  k_mlp_grad_w2<<<dim3(H / GW_ROWS, m->E), H, 0, m->stream>>>(d, m->grad);
+}
+
+constexpr float ADAM_B1 = 0.9f, ADAM_B2 = 0.999f, ADAM_EPS = 1e-8f;
+constexpr int TRAIN_GRAPH_ITERS = 50;
+
+/* One training iteration: gradient, Adam with the bias correction at
+ * bias[*tix], next step index. */
+void mlp_train_iter(SppMlp* m, int B, float lr) {
+  mlp_fwd_bwd(m, B, true);
+  const int tot = m->E * m->P;
+  k_mlp_adam<<<(tot + 255) / 256, 256, 0, m->stream>>>(tot, m->master, m->w, m->grad, m->mom, m->vel, lr,
+                                                       ADAM_B1, ADAM_B2, ADAM_EPS, m->bias, m->tix);
+  k_mlp_next<<<1, 1, 0, m->stream>>>(m->tix);
+}
+
+int mlp_train_graph(SppMlp* m, int B, float lr, cudaGraphExec_t* out) {
+  for (auto& g : m->graphs)
+    if (g.B == B && g.lr == lr) { *out = g.exec; return SPP_OK; }
+  cudaGraph_t graph = nullptr;
+  MCUDA(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+  for (int it = 0; it < TRAIN_GRAPH_ITERS; ++it) mlp_train_iter(m, B, lr);
+  MCUDA(cudaStreamEndCapture(m->stream, &graph));
+  cudaGraphExec_t exec;
+  cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return mfail(SPP_ERR_CUDA, std::string("training graph: ") + cudaGetErrorString(e));
+  }
+  m->graphs.push_back({B, lr, graph, exec});
+  *out = exec;
+  return SPP_OK;
 }
 
 }  // namespace
@@ -341,6 +469,7 @@ int spp_mlp_destroy(SppMlp* m) {
   cudaStreamSynchronize(m->stream);
   mlp_free_scratch(m);
   cudaFree(m->master); cudaFree(m->w); cudaFree(m->mom); cudaFree(m->vel); cudaFree(m->grad);
+  cudaFree(m->bias); cudaFree(m->tix);
   cudaStreamDestroy(m->stream);
   delete m;
   return SPP_OK;
@@ -399,15 +528,37 @@ int spp_mlp_train(SppMlp* m, const float* x, const float* t, const float* weight
   if (!m || !x || !t || B < 1 || iters < 0) return mfail(SPP_ERR_INVALID, "bad arguments");
   int rc = mlp_upload(m, x, t, weights, B);
   if (rc != SPP_OK) return rc;
-  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-  const int tot = m->E * m->P;
-  for (int it = 0; it < iters; ++it) {
-    mlp_fwd_bwd(m, B, true);
-    m->adam_t += 1;
-    const float c1 = 1.0f - (float)std::pow((double)b1, (double)m->adam_t);
-    const float c2 = 1.0f - (float)std::pow((double)b2, (double)m->adam_t);
-    k_mlp_adam<<<(tot + 255) / 256, 256, 0, m->stream>>>(tot, m->master, m->w, m->grad, m->mom, m->vel, lr,
-                                                         b1, b2, eps, c1, c2);
+  if (iters > 0) {
+    /* the bias corrections of steps adam_t + 1 .. adam_t + iters */
+    if (iters > m->bias_cap) {
+      mlp_drop_graphs(m);  /* they hold the old table's address */
+      cudaFree(m->bias);
+      m->bias = nullptr;
+      m->bias_cap = 0;
+      const int cap = iters > 4096 ? iters : 4096;
+      MCUDA(cudaMalloc((void**)&m->bias, sizeof(float2) * cap));
+      m->bias_cap = cap;
+    }
+    if (!m->tix) MCUDA(cudaMalloc((void**)&m->tix, sizeof(int)));
+    MCUDA(cudaStreamSynchronize(m->stream));  /* the previous table may still be read */
+    std::vector<float2> table((size_t)iters);
+    for (int it = 0; it < iters; ++it) {
+      const double t = (double)(m->adam_t + 1 + it);
+      table[(size_t)it] = make_float2(1.0f - (float)std::pow((double)ADAM_B1, t),
+                                      1.0f - (float)std::pow((double)ADAM_B2, t));
+    }
+    MCUDA(cudaMemcpyAsync(m->bias, table.data(), sizeof(float2) * iters, cudaMemcpyHostToDevice, m->stream));
+    MCUDA(cudaMemsetAsync(m->tix, 0, sizeof(int), m->stream));
+    int done = 0;
+    if (iters >= TRAIN_GRAPH_ITERS) {
+      cudaGraphExec_t exec;
+      rc = mlp_train_graph(m, B, lr, &exec);
+      if (rc != SPP_OK) return rc;
+      for (; done + TRAIN_GRAPH_ITERS <= iters; done += TRAIN_GRAPH_ITERS) MCUDA(cudaGraphLaunch(exec, m->stream));
+    }
+    for (; done < iters; ++done) mlp_train_iter(m, B, lr);
+    m->adam_t += iters;
+    MCUDA(cudaStreamSynchronize(m->stream));  /* the host table goes out of scope */
   }
   MCUDA(cudaGetLastError());
   if (loss) {

@@ -222,7 +222,7 @@ class SweepResult:
 
 
 def run_sweep(points, max_steps=20000, window=500, pilot_frac=0.2, holdout_frac=0.1, tol=0.02,
-              max_rounds=3, run_frac=0.3, surrogate=None, seed=4, x0=None, use_surrogate=True,
+              max_rounds=2, run_frac=0.5, surrogate=None, seed=4, x0=None, use_surrogate=True,
               chunk=2000):
     """Runs the sweep and returns a SweepResult.  With use_surrogate=False
     every point runs to the end (the plain batched sweep).
