@@ -425,6 +425,31 @@ def other_workload(args):
 
     peak, peak_kind = measured_hbm_peak()
     w = args.workload
+    if w == "batch64":
+        # the small case the kernel captures use: 64 sweep points stepped 40
+        # times, then 60 surrogate training iterations on 300 samples
+        from spp_gb300 import Batch, surrogate
+        pts = configs.sweep_points(n_points=64)
+        x, y, th = configs.sweep_state(pts, seed=4)
+        with Batch(pts) as b:
+            b.set_windows(500, 10000, 20000)
+            b.upload(x, y, th)
+            ms = b.time_steps(40)
+        rng = np.random.default_rng(0)
+        f = rng.standard_normal((300, 7)).astype(np.float32)
+        t = rng.uniform(0, 1, 300).astype(np.float32)
+        mlp = surrogate.Mlp(5, 7, 4)
+        t0 = time.perf_counter()
+        mlp.train(f, t, iters=60, lr=1e-3)
+        train_ms = (time.perf_counter() - t0) * 1e3
+        mlp.close()
+        n = sum(p.n for p in pts)
+        print(json.dumps({"metric": "particle-steps/s", "workload": "batch64", "value": n * 40 / (ms / 1e3),
+                          "unit": "particle-steps/s", "n_gpus": 1, "ms_per_step": ms / 40,
+                          "config": {"workload": f"64 sweep points ({n:,} particles), 40 steps; "
+                                                 "60 training iterations of the 5-member surrogate on 300 samples"},
+                          "train_ms_per_iteration": train_ms / 60}), flush=True)
+        return
     if w == "sweep":
         line = {"metric": "sweep points/hour at |dP|<=0.02 vs full runs", "n_gpus": 1, "data": "synthetic"}
         line.update(sweep_leg())
@@ -502,7 +527,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-sweep", action="store_true", help="skip the 512-point sweep leg")
-    ap.add_argument("--workload", default="abp", choices=["abp", "vicsek", "vesicles", "lyapunov", "sweep"],
+    ap.add_argument("--workload", default="abp",
+                    choices=["abp", "vicsek", "vesicles", "lyapunov", "sweep", "batch64"],
                     help="abp: the headline line (default); the others print their own line")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
