@@ -355,8 +355,10 @@ int recover(SppSystem* s) {
     if ((int64_t)c.step <= last_frozen_step) ++stalls;
     else stalls = 0;
     last_frozen_step = (int64_t)c.step;
-    int64_t need = (int64_t)c.list_need * 5 / 4 + 4;
-    if (need < (int64_t)s->d.cap + 4) need = (int64_t)s->d.cap + 4;
+    /* densities that grew once tend to keep growing (flocking): grow by at
+     * least half the current capacity, so that a long run regrows rarely */
+    int64_t need = (int64_t)c.list_need * 3 / 2 + 8;
+    if (need < (int64_t)s->d.cap * 3 / 2 + 4) need = (int64_t)s->d.cap * 3 / 2 + 4;
     if (need > (int64_t)s->d.n + 4) need = (int64_t)s->d.n + 4;
     int cap = (int)((need + 3) & ~(int64_t)3);
     free_graphs(s);
