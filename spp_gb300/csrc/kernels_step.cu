@@ -87,6 +87,10 @@ __device__ __forceinline__ void finish_step(const SppConsts& k, const DevState& 
   }
 }
 
+#ifndef SPP_STAGE_GROUP
+#define SPP_STAGE_GROUP 3        /* neighbours whose loads are issued together (1: one-ahead prefetch) */
+#endif
+
 #ifndef SPP_STAGE_MIN_BLOCKS
 #define SPP_STAGE_MIN_BLOCKS 8   /* 8 x 256 threads per SM: 32 registers */
 #endif
@@ -109,6 +113,27 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(S
      * minimum-image corrections (they would not change any separation). */
     const int inner = fabsf(pi.x) < k.interior && fabsf(pi.y) < k.interior;
     const int all_inner = __all_sync(__activemask(), inner);
+#if SPP_STAGE_GROUP > 1
+    /* list entries and neighbour states are loaded SPP_STAGE_GROUP at a time
+     * (independent loads in flight), the pairs evaluated in list order */
+    for (int q0 = 0; q0 < cnt; q0 += SPP_STAGE_GROUP) {
+      int jg[SPP_STAGE_GROUP];
+      float4 pg[SPP_STAGE_GROUP];
+#pragma unroll
+      for (int u = 0; u < SPP_STAGE_GROUP; ++u) jg[u] = q0 + u < cnt ? __ldg(nb + (size_t)(q0 + u) * stride) : i;
+#pragma unroll
+      for (int u = 0; u < SPP_STAGE_GROUP; ++u) pg[u] = __ldg(b.cur + jg[u]);
+#pragma unroll
+      for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
+        if (q0 + u < cnt) {
+          if (all_inner)
+            spp_pair_abp_lkw(&k, LAW, KIND, 0, &a, pi.x, pi.y, pi.z, pi.w, pg[u].x, pg[u].y, pg[u].z, pg[u].w);
+          else
+            spp_pair_abp_lkw(&k, LAW, KIND, 1, &a, pi.x, pi.y, pi.z, pi.w, pg[u].x, pg[u].y, pg[u].z, pg[u].w);
+        }
+      }
+    }
+#else
     /* the next neighbour's index and state are loaded before the current
      * pair is evaluated, so the dependent loads overlap the arithmetic */
     int jn = cnt > 0 ? __ldg(nb) : i;
@@ -132,6 +157,7 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(S
         spp_pair_abp_lkw(&k, LAW, KIND, 1, &a, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
       }
     }
+#endif
     if (LAW == SPP_FORCE_R12_TRUNC && a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
     float fx, fy, tau;
     int turns = 1;
