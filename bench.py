@@ -327,12 +327,14 @@ def run_ours(args):
         hx = torch.from_numpy(x).pin_memory().numpy()
         hy = torch.from_numpy(y).pin_memory().numpy()
         ht = torch.from_numpy(th).pin_memory().numpy()
+        pinned_out = tuple(torch.empty(n, dtype=dt).pin_memory().numpy()
+                           for dt in (torch.float32, torch.float32, torch.float32, torch.int32, torch.int32))
         e2e_times = []
         for k in range(0 if args.no_e2e else max(3, min(args.steps, 10))):
             t0 = time.perf_counter()
             s.upload(hx, hy, ht, step0=k * S)
             s.step(S)
-            out = s.download()
+            out = s.download(out=pinned_out)
             e2e_times.append(time.perf_counter() - t0)
         e2e_value = n * S / statistics.median(e2e_times) if e2e_times else None
     value = ws * n * S * args.steps / (elapsed_ms / 1e3)
@@ -362,7 +364,7 @@ def run_ours(args):
         "rebuild": {"avg_ms": rebuild_avg_ms, "per_200_steps": prof.rebuilds},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * n,
                 "d2h_bytes_per_step": 20 * n,
-                "path": "spp_upload_state (pinned host) + spp_step(200) + spp_download_state"},
+                "path": "spp_upload_state (pinned host) + spp_step(200) + spp_download_state (pinned host)"},
         "observables": {"polarization": obs.polarization, "rebuilds": obs.n_rebuilds,
                         "max_neighbors": obs.max_neighbors, "list_capacity": obs.list_capacity},
     }

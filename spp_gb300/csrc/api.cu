@@ -672,37 +672,42 @@ int spp_upload_state(SppSystem* s, const float* x, const float* y, const float* 
   if (!s || !x || !y || !theta) return fail(SPP_ERR_INVALID, "NULL argument");
   if (n != s->p.n) return fail(SPP_ERR_INVALID, "n differs from the system's particle count");
   if (step0 < 0 || step0 > 0xffffffffLL) return fail(SPP_ERR_INVALID, "step0 out of range");
-  const float L = s->k.L;
-  for (int i = 0; i < n; ++i) {
-    if (!std::isfinite(x[i]) || !std::isfinite(y[i]) || !std::isfinite(theta[i]))
-      return fail(SPP_ERR_NUMERIC, "non-finite input at particle " + std::to_string(i));
-    if (x[i] < -L || x[i] >= L || y[i] < -L || y[i] >= L)
-      return fail(SPP_ERR_INVALID, "position outside [-L, L) at particle " + std::to_string(i));
-  }
+  /* the inputs are checked on the device, where they are placed
+   * (k_init_state); the upload is refused, and the system left without a
+   * state, if any value is non-finite or any position lies outside [-L, L) */
+  s->uploaded = false;
   size_t bytes = sizeof(float) * (size_t)n;
   CUDA_TRY(cudaMemcpyAsync(s->stage_x, x, bytes, cudaMemcpyHostToDevice, s->stream));
   CUDA_TRY(cudaMemcpyAsync(s->stage_y, y, bytes, cudaMemcpyHostToDevice, s->stream));
   CUDA_TRY(cudaMemcpyAsync(s->stage_t, theta, bytes, cudaMemcpyHostToDevice, s->stream));
-  launch_init_state(s->k, s->d, s->stage_x, s->stage_y, s->stage_t, s->stream);
-  s->host_launches++;
+  int32_t* img_dev = nullptr;
   if (img_x || img_y) {
-    std::vector<int2> img((size_t)n);
-    for (int i = 0; i < n; ++i) img[i] = make_int2(img_x ? img_x[i] : 0, img_y ? img_y[i] : 0);
-    CUDA_TRY(cudaMemcpyAsync(s->d.img, img.data(), sizeof(int2) * (size_t)n,
-                             cudaMemcpyHostToDevice, s->stream));
-    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    img_dev = reinterpret_cast<int32_t*>(s->stage_img);  /* 2n int32: x counters, then y counters */
+    if (img_x) CUDA_TRY(cudaMemcpyAsync(img_dev, img_x, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s->stream));
+    else CUDA_TRY(cudaMemsetAsync(img_dev, 0, sizeof(int32_t) * n, s->stream));
+    if (img_y) CUDA_TRY(cudaMemcpyAsync(img_dev + n, img_y, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s->stream));
+    else CUDA_TRY(cudaMemsetAsync(img_dev + n, 0, sizeof(int32_t) * n, s->stream));
   }
   Ctl c;
   memset(&c, 0, sizeof(c));
   c.step = (uint32_t)step0;
+  c.bad_nonfinite = 0xffffffffu;
+  c.bad_range = 0xffffffffu;
   CUDA_TRY(cudaMemcpyAsync(s->d.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s->stream));
+  launch_init_state(s->k, s->d, s->stage_x, s->stage_y, s->stage_t, img_dev, s->stream);
+  s->host_launches++;
   int rc = enqueue_rebuild(s, s->stream, &s->host_launches);
   if (rc != SPP_OK) return rc;
   s->direct_rebuilds++;
+  rc = read_ctl(s, &c);
+  if (rc != SPP_OK) return rc;
+  if (c.bad_nonfinite != 0xffffffffu)
+    return fail(SPP_ERR_NUMERIC, "non-finite input at particle " + std::to_string(c.bad_nonfinite));
+  if (c.bad_range != 0xffffffffu)
+    return fail(SPP_ERR_INVALID, "position outside [-L, L) at particle " + std::to_string(c.bad_range));
   s->step0 = step0;
   s->target_step = step0;
   s->uploaded = true;
-  CUDA_TRY(cudaStreamSynchronize(s->stream));
   return recover(s);
 }
 
@@ -713,22 +718,15 @@ int spp_download_state(SppSystem* s, float* x, float* y, float* theta, int32_t* 
   if (!s->uploaded) return fail(SPP_ERR_INVALID, "no state uploaded");
   int rc = spp_sync(s);
   if (rc != SPP_OK) return rc;
-  launch_gather_state(s->k, s->d, s->stage_x, s->stage_y, s->stage_t, s->stage_img, s->stream);
+  int32_t* img_dev = reinterpret_cast<int32_t*>(s->stage_img);  /* 2n int32: x, then y */
+  launch_gather_state(s->k, s->d, s->stage_x, s->stage_y, s->stage_t, img_dev, s->stream);
   s->host_launches++;
   size_t bytes = sizeof(float) * (size_t)n;
   CUDA_TRY(cudaMemcpyAsync(x, s->stage_x, bytes, cudaMemcpyDeviceToHost, s->stream));
   CUDA_TRY(cudaMemcpyAsync(y, s->stage_y, bytes, cudaMemcpyDeviceToHost, s->stream));
   CUDA_TRY(cudaMemcpyAsync(theta, s->stage_t, bytes, cudaMemcpyDeviceToHost, s->stream));
-  if (img_x || img_y) {
-    std::vector<int2> img((size_t)n);
-    CUDA_TRY(cudaMemcpyAsync(img.data(), s->stage_img, sizeof(int2) * (size_t)n,
-                             cudaMemcpyDeviceToHost, s->stream));
-    CUDA_TRY(cudaStreamSynchronize(s->stream));
-    for (int i = 0; i < n; ++i) {
-      if (img_x) img_x[i] = img[i].x;
-      if (img_y) img_y[i] = img[i].y;
-    }
-  }
+  if (img_x) CUDA_TRY(cudaMemcpyAsync(img_x, img_dev, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s->stream));
+  if (img_y) CUDA_TRY(cudaMemcpyAsync(img_y, img_dev + n, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s->stream));
   CUDA_TRY(cudaStreamSynchronize(s->stream));
   return SPP_OK;
 }

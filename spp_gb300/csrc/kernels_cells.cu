@@ -288,19 +288,27 @@ __global__ void k_cells(SppConsts k, DevState d, int D, int rule, int32_t* cx, i
   cy[id] = spp_cell_coord(p.y, k.L, k.L2, D, rule);
 }
 
-__global__ void k_init_state(DevState d, const float* __restrict__ x, const float* __restrict__ y,
-                             const float* __restrict__ th) {
+/* Places the uploaded state (particle-id order) and checks it: the smallest
+ * index with a non-finite value and the smallest with a position outside
+ * [-L, L) go to the control block, which the host reads before it accepts
+ * the upload.  Invalid values stay bounded in what follows: cell
+ * coordinates are clamped, and comparisons with NaN are false. */
+__global__ void k_init_state(SppConsts k, DevState d, const float* __restrict__ x, const float* __restrict__ y,
+                             const float* __restrict__ th, const int32_t* __restrict__ img_xy) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n) return;
+  const float xi = x[i], yi = y[i], ti = th[i];
+  if (!isfinite(xi) || !isfinite(yi) || !isfinite(ti)) atomicMin(&d.ctl->bad_nonfinite, (uint32_t)i);
+  else if (!(xi >= -k.L && xi < k.L && yi >= -k.L && yi < k.L)) atomicMin(&d.ctl->bad_range, (uint32_t)i);
   float s, c;
-  spp_sincosf(th[i], &s, &c);
-  d.pos[i] = make_float4(x[i], y[i], c, s);
-  d.theta[i] = th[i];
-  d.img[i] = make_int2(0, 0);
+  spp_sincosf(ti, &s, &c);
+  d.pos[i] = make_float4(xi, yi, c, s);
+  d.theta[i] = ti;
+  d.img[i] = img_xy ? make_int2(img_xy[i], img_xy[d.n + i]) : make_int2(0, 0);
   d.id[i] = (uint32_t)i;
 }
 
-__global__ void k_gather_state(DevState d, float* x, float* y, float* th, int2* img) {
+__global__ void k_gather_state(DevState d, float* x, float* y, float* th, int32_t* img_xy) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n) return;
   uint32_t id = d.id[i];
@@ -308,7 +316,9 @@ __global__ void k_gather_state(DevState d, float* x, float* y, float* th, int2* 
   x[id] = p.x;
   y[id] = p.y;
   th[id] = d.theta[i];
-  img[id] = d.img[i];
+  const int2 g = d.img[i];
+  img_xy[id] = g.x;
+  img_xy[d.n + id] = g.y;
 }
 
 inline int blocks_for(int n, int b = SPP_BLOCK) { return (n + b - 1) / b; }
@@ -362,15 +372,14 @@ void launch_cells(const SppConsts& k, const DevState& d, int D, int rule, int32_
 }
 
 void launch_init_state(const SppConsts& k, const DevState& d, const float* x, const float* y,
-                       const float* th, cudaStream_t s) {
-  (void)k;
+                       const float* th, const int32_t* img_xy, cudaStream_t s) {
   if (d.n == 0) return;
-  k_init_state<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(d, x, y, th);
+  k_init_state<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(k, d, x, y, th, img_xy);
 }
 
 void launch_gather_state(const SppConsts& k, const DevState& d, float* x, float* y, float* th,
-                         int2* img, cudaStream_t s) {
+                         int32_t* img_xy, cudaStream_t s) {
   (void)k;
   if (d.n == 0) return;
-  k_gather_state<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(d, x, y, th, img);
+  k_gather_state<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(d, x, y, th, img_xy);
 }

@@ -37,7 +37,9 @@ struct Ctl {
   uint32_t frozen;        /* set on list overflow: later stages skip until the host recovers */
   uint32_t smax2_bits;    /* max squared displacement during the current step (float bits) */
   uint32_t late_rebuilds; /* rebuilds decided after some particle had already moved > skin/2 */
-  uint32_t pad[5];
+  uint32_t bad_nonfinite; /* smallest index of an uploaded particle with a non-finite value (or ~0) */
+  uint32_t bad_range;     /* smallest index of an uploaded position outside [-L, L) (or ~0) */
+  uint32_t pad[3];
 };
 
 struct DevState {
@@ -94,10 +96,13 @@ void launch_pairs_count(const SppConsts& k, const DevState& d, float r2, unsigne
                         int32_t* pi, int32_t* pj, long long cap, cudaStream_t s);
 void launch_cells(const SppConsts& k, const DevState& d, int D, int rule, int32_t* cx, int32_t* cy,
                   cudaStream_t s);
+/* Also checks the inputs (finite, positions in [-L, L)) into Ctl::bad_*;
+ * img_xy (may be NULL): 2n int32 box-crossing counters, x then y. */
 void launch_init_state(const SppConsts& k, const DevState& d, const float* x, const float* y,
-                       const float* th, cudaStream_t s);
+                       const float* th, const int32_t* img_xy, cudaStream_t s);
+/* img_xy: 2n int32, x counters then y counters (particle-id order) */
 void launch_gather_state(const SppConsts& k, const DevState& d, float* x, float* y, float* th,
-                         int2* img, cudaStream_t s);
+                         int32_t* img_xy, cudaStream_t s);
 
 /* kernels_step.cu */
 void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nstages,

@@ -70,13 +70,22 @@ class System:
                   "spp_upload_state")
         self.step0 = int(step0)
 
-    def download(self):
+    def download(self, out=None):
+        """(x, y, theta, img_x, img_y) in particle-id order; out = five arrays
+        (float32, float32, float32, int32, int32, length n) to fill instead of
+        new ones, e.g. pinned host buffers."""
         n = self.n
-        x = np.empty(n, np.float32)
-        y = np.empty(n, np.float32)
-        th = np.empty(n, np.float32)
-        ix = np.empty(n, np.int32)
-        iy = np.empty(n, np.int32)
+        if out is not None:
+            x, y, th, ix, iy = out
+            for a, dt in zip(out, (np.float32, np.float32, np.float32, np.int32, np.int32)):
+                if a.dtype != dt or a.shape != (n,) or not a.flags.c_contiguous:
+                    raise ValueError("download buffers must be contiguous arrays of length n")
+        else:
+            x = np.empty(n, np.float32)
+            y = np.empty(n, np.float32)
+            th = np.empty(n, np.float32)
+            ix = np.empty(n, np.int32)
+            iy = np.empty(n, np.int32)
         abi.check(abi.lib().spp_download_state(self._h, abi.fptr(x), abi.fptr(y), abi.fptr(th),
                                                abi.iptr(ix), abi.iptr(iy), n), "spp_download_state")
         return x, y, th, ix, iy

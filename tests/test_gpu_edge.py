@@ -191,3 +191,28 @@ def test_densifying_flocks_keep_recovering(gpu_lib):
         o = s.observables()
     assert o.step == 1050 and o.list_capacity > 16
     assert same(g, O.run32(p, O.State32(x, y, th), 1050))
+
+
+def test_rejected_upload_then_valid_upload_and_download_into_buffers(gpu_lib):
+    """Inputs are checked on the device as they are placed: a bad upload is
+    refused (the system holds no state until a good one), and the smallest
+    bad index is reported.  Downloads can fill caller buffers."""
+    p = configs.abp_config(n=4096, L=32.0, seed=5)
+    x, y, th = configs.random_state(p.n, p.L, seed=5)
+    bad = x.copy()
+    bad[[700, 2000]] = 40.0
+    with System(p) as s:
+        with pytest.raises(SppError) as e:
+            s.upload(bad, y, th)
+        assert e.value.status == 1 and "particle 700" in str(e.value)
+        with pytest.raises(SppError):
+            s.step(1)
+        s.upload(x, y, th)
+        s.step(10)
+        ref = s.download()
+        out = tuple(np.empty(p.n, dt) for dt in (np.float32, np.float32, np.float32, np.int32, np.int32))
+        got = s.download(out=out)
+        assert all(a is b for a, b in zip(got, out))
+        for u, v in zip(ref, got):
+            assert np.array_equal(u, v)
+    assert same(ref, O.run32(p, O.State32(x, y, th), 10))
