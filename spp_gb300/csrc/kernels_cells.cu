@@ -155,15 +155,22 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_scatter(DevState d) {
  * Accepted neighbours are collected as (id << 32 | slot) keys in a per-thread
  * array, insertion-sorted there (lists hold ~5 entries at unit density) and
  * written once; lists longer than the array fall back to sorting in place. */
-constexpr int LIST_LOCAL = 48;
+#ifndef SPP_LIST_LOCAL
+#define SPP_LIST_LOCAL 16
+#endif
+/* keys kept in shared memory per thread (column threadIdx.x of a
+ * [LIST_LOCAL][SPP_BLOCK] array: conflict-free), the rest of a longer list
+ * sorted in place in global memory */
+constexpr int LIST_LOCAL = SPP_LIST_LOCAL;
 
 __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState d, int with_list) {
+  __shared__ unsigned long long skeys[LIST_LOCAL][SPP_BLOCK];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t cnt = 0;
   if (i < d.n) {
     float4 p = d.pos_alt[i];
     if (with_list) {
-      unsigned long long keys[LIST_LOCAL];
+#define keys(q) skeys[(q)][threadIdx.x]
       int cx, cy;
       cell_key(k, d, p.x, p.y, &cx, &cy);
       const int D = d.D;
@@ -186,11 +193,11 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
                   ((unsigned long long)d.id_alt[j] << 32) | (unsigned long long)j;
               if (cnt < (uint32_t)LIST_LOCAL) {
                 int pos = (int)cnt;
-                while (pos > 0 && keys[pos - 1] > key) {
-                  keys[pos] = keys[pos - 1];
+                while (pos > 0 && keys(pos - 1) > key) {
+                  keys(pos) = keys(pos - 1);
                   --pos;
                 }
-                keys[pos] = key;
+                keys(pos) = key;
               } else if (cnt < cap) {
                 /* long list: the first LIST_LOCAL keys are still local; keep the
                  * tail sorted in place in global memory */
@@ -201,15 +208,15 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
                   d.nbr[(size_t)pos * d.n + i] = prev;
                   --pos;
                 }
-                if (pos == LIST_LOCAL && keys[LIST_LOCAL - 1] > key) {
+                if (pos == LIST_LOCAL && keys(LIST_LOCAL - 1) > key) {
                   /* belongs among the local keys: swap with the local maximum */
-                  unsigned long long moved = keys[LIST_LOCAL - 1];
+                  unsigned long long moved = keys(LIST_LOCAL - 1);
                   int lp = LIST_LOCAL - 1;
-                  while (lp > 0 && keys[lp - 1] > key) {
-                    keys[lp] = keys[lp - 1];
+                  while (lp > 0 && keys(lp - 1) > key) {
+                    keys(lp) = keys(lp - 1);
                     --lp;
                   }
-                  keys[lp] = key;
+                  keys(lp) = key;
                   d.nbr[(size_t)pos * d.n + i] = (int32_t)(uint32_t)moved;
                 } else {
                   d.nbr[(size_t)pos * d.n + i] = (int32_t)j;
@@ -222,9 +229,10 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
       }
       const uint32_t nloc = cnt < (uint32_t)LIST_LOCAL ? cnt : (uint32_t)LIST_LOCAL;
       const uint32_t nw = nloc < cap ? nloc : cap;
-      for (uint32_t q = 0; q < nw; ++q) d.nbr[(size_t)q * d.n + i] = (int32_t)(uint32_t)keys[q];
+      for (uint32_t q = 0; q < nw; ++q) d.nbr[(size_t)q * d.n + i] = (int32_t)(uint32_t)keys(q);
       d.nn[i] = (int32_t)(cnt < cap ? cnt : cap);
       d.ref[i] = make_float2(p.x, p.y);
+#undef keys
     }
     d.pos[i] = p;
     d.theta[i] = d.theta_alt[i];
