@@ -66,6 +66,12 @@ enum SppAlignMode {
   SPP_ALIGN_MEAN = 1       /* (g / n_i) sum sin(theta_j - theta_i), n_i counts self (shared/particle.h:561) */
 };
 
+/* Rotational noise of the swimmers of SPP_MODEL_BEADS. */
+enum SppRotNoise {
+  SPP_NOISE_GAUSSIAN = 0,  /* sqrt(2 Dr dt) N(0,1) per step (ActiveBrownianChain::Noise_Gen, particle.h:891-894) */
+  SPP_NOISE_TUMBLE = 1     /* run and tumble (RTPChain::Noise_Gen, particle.h:1085-1103) */
+};
+
 enum SppBinRule {
   SPP_BIN_GEOMETRIC = 0,   /* cell = floor((x + L) D / 2L) */
   SPP_BIN_REFERENCE = 1    /* cell = (int)((int)(x + L) * D / 2L), serial/box.h:116-117 */
@@ -106,6 +112,11 @@ typedef struct SppParams {
   double k_bond;          /* ring bond stiffness (Spring amplitude, force-fields.h:87-97) */
   double bond_rest;       /* ring bond rest length */
   double kappa_bend;      /* bending stiffness on consecutive bond angles */
+  int32_t rot_noise;      /* enum SppRotNoise (swimmers of SPP_MODEL_BEADS) */
+  int32_t reserved;
+  double tumble_rate;     /* RTPChain::lambda: a tumble starts with probability rate * dt per step */
+  double tumble_time;     /* RTPChain::t_tumble: a tumble lasts while its elapsed time < t_tumble */
+  double tumble_torque;   /* RTPChain::torque_tumble: dtheta = k_perp dt (+-1) torque_tumble per step */
 } SppParams;
 
 typedef struct SppObservables {

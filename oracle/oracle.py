@@ -49,6 +49,8 @@ def orc():
         L.orc64_lyap_clone.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D,
                                        _D, _D, _D]
         L.orc32_rsqrt.argtypes = [C.c_float]
+        L.orc32_tumble_steps.argtypes = [_P]
+        L.orc32_tumble_steps.restype = C.c_int32
         L.orc32_radial.argtypes = [_F, _F, C.c_int, C.c_double, C.c_double, C.c_int, _U64]
         L.orc32_pair_distribution.argtypes = [_F, _F, _F, _F, C.c_int, C.c_double, C.c_double, C.c_int,
                                               C.c_int, _U64]
@@ -144,6 +146,14 @@ def pairs64(x, y, L, r, cap=None):
     if cnt > cap:
         return pairs64(x, y, L, r, cap=int(cnt))
     return _sorted_pairs(pi[:cnt], pj[:cnt])
+
+
+def tumble_steps(p):
+    """Length in steps of a run-and-tumble tumble, as the kernels count it."""
+    q = p.copy()
+    q.model = abi.MODEL_BEADS
+    q.rot_noise = abi.NOISE_TUMBLE
+    return int(orc().orc32_tumble_steps(C.byref(q)))
 
 
 def radial32(x, y, L, r_max, nbins):

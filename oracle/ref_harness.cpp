@@ -116,7 +116,8 @@ void vicsek_steps(const SppParams* p, int nsteps, int64_t step0, double* x, doub
 
 /* Interact_Membrane_Beads (parallel/beadbox.h:185-196), restated per ring
  * with the reference's Spring(). */
-void ring_springs(std::vector<ActiveBrownianChain>& ps, const SppParams* p) {
+template <class P>
+void ring_springs(std::vector<P>& ps, const SppParams* p) {
   const int M = p->ring_size;
   for (int r = 0; r < p->n_rings; ++r)
     for (int m = 0; m < M; ++m) {
@@ -128,6 +129,40 @@ void ring_springs(std::vector<ActiveBrownianChain>& ps, const SppParams* p) {
       ps[a].f += f;
       ps[b].f -= f;
     }
+}
+
+template <class P>
+int chain_steps(const SppParams* p, int nsteps, int64_t step0, double* x, double* y, double* th,
+                double* xu, double* yu) {
+  const int nm = p->n_rings * p->ring_size;
+  std::vector<P> ps(p->n);
+  ActiveBrownianChain::sigma_m = p->sigma_rep;
+  ActiveBrownianChain::repulsion_radius_m = p->r_rep;
+  ActiveBrownianChain::A_p = p->k_rep;
+  ActiveBrownianChain::torque0 = p->torque0;
+  BasicDynamicParticle::Set_Dr(p->Dr);
+  for (int i = 0; i < p->n; ++i) {
+    ps[i].Set_nb(1);
+    ps[i].Set_F0(i < nm ? 0.0 : p->v0 / p->mu);
+  }
+  load(ps, x, y, th, xu, yu);
+  for (int k = 0; k < nsteps; ++k) {
+    int64_t step = step0 + k;
+    if (p->integrator == SPP_INT_EULER) {
+      ring_springs(ps, p);
+      interact_all(ps, p->L, p->r_rep);
+      move_all(ps, p, step, [](P& q) { q.Move(); });
+    } else {
+      ring_springs(ps, p);
+      interact_all(ps, p->L, p->r_rep);
+      move_all(ps, p, step, [](P& q) { q.Move_Runge_Kutta2_1(); });
+      ring_springs(ps, p);
+      interact_all(ps, p->L, p->r_rep);
+      move_all(ps, p, step, [](P& q) { q.Move_Runge_Kutta2_2(); });
+    }
+  }
+  store(ps, x, y, th, xu, yu);
+  return SPP_OK;
 }
 
 }  // namespace
@@ -209,39 +244,18 @@ extern "C" int ref_run(const SppParams* p, int nsteps, int64_t step0, double* x,
     }
     case SPP_MODEL_BEADS: {
       /* ActiveBrownianChain with nb = 1 (mobilities 0.5, 0.5, 1 from Set_nb,
-       * particle.h:856-864); no bending, no RK4 in the reference. */
+       * particle.h:856-864), or its run-and-tumble subclass RTPChain
+       * (:1061-1108); no bending, no RK4 in the reference. */
       if (p->force_law != SPP_FORCE_R12_TRUNC || p->kappa_bend != 0.0 || p->mu != 0.5 ||
           p->k_perp != 1.0 || p->integrator == SPP_INT_RK4)
         return SPP_ERR_UNSUPPORTED;
-      const int nm = p->n_rings * p->ring_size;
-      std::vector<ActiveBrownianChain> ps(p->n);
-      ActiveBrownianChain::sigma_m = p->sigma_rep;
-      ActiveBrownianChain::repulsion_radius_m = p->r_rep;
-      ActiveBrownianChain::A_p = p->k_rep;
-      ActiveBrownianChain::torque0 = p->torque0;
-      BasicDynamicParticle::Set_Dr(p->Dr);
-      for (int i = 0; i < p->n; ++i) {
-        ps[i].Set_nb(1);
-        ps[i].Set_F0(i < nm ? 0.0 : p->v0 / p->mu);
+      if (p->rot_noise == SPP_NOISE_TUMBLE) {
+        RTPChain::lambda = p->tumble_rate;
+        RTPChain::t_tumble = p->tumble_time;
+        RTPChain::torque_tumble = p->tumble_torque;
+        return chain_steps<RTPChain>(p, nsteps, step0, x, y, th, xu, yu);
       }
-      load(ps, x, y, th, xu, yu);
-      for (int k = 0; k < nsteps; ++k) {
-        int64_t step = step0 + k;
-        if (p->integrator == SPP_INT_EULER) {
-          ring_springs(ps, p);
-          interact_all(ps, p->L, p->r_rep);
-          move_all(ps, p, step, [](ActiveBrownianChain& q) { q.Move(); });
-        } else {
-          ring_springs(ps, p);
-          interact_all(ps, p->L, p->r_rep);
-          move_all(ps, p, step, [](ActiveBrownianChain& q) { q.Move_Runge_Kutta2_1(); });
-          ring_springs(ps, p);
-          interact_all(ps, p->L, p->r_rep);
-          move_all(ps, p, step, [](ActiveBrownianChain& q) { q.Move_Runge_Kutta2_2(); });
-        }
-      }
-      store(ps, x, y, th, xu, yu);
-      return SPP_OK;
+      return chain_steps<ActiveBrownianChain>(p, nsteps, step0, x, y, th, xu, yu);
     }
     default:
       return SPP_ERR_UNSUPPORTED;

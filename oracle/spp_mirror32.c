@@ -139,20 +139,34 @@ static int abp_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t
   float *kx = (float*)malloc(sizeof(float) * n), *ky = (float*)malloc(sizeof(float) * n);
   float* kt = (float*)malloc(sizeof(float) * n);
   SppAccF* acc = (SppAccF*)malloc(sizeof(SppAccF) * (n > 0 ? n : 1));
+  /* run and tumble: the swimmers' states (all running at the start of the
+   * call) and the step's dtheta, drawn once per step as the kernels do */
+  int32_t* tstate = k->tumble ? (int32_t*)calloc((size_t)(n > 0 ? n : 1), sizeof(int32_t)) : NULL;
+  float* tdth = k->tumble ? (float*)malloc(sizeof(float) * (n > 0 ? n : 1)) : NULL;
   int rc = SPP_OK;
   for (int i = 0; i < n; ++i) spp_sincosf(th[i], &s[i], &c[i]);
   for (int st = 0; st < nsteps && rc == SPP_OK; ++st) {
     uint32_t step = (uint32_t)(step0 + st);
+    if (k->tumble)
+      for (int i = 0; i < n; ++i)
+        tdth[i] = i < k->n_beads ? 0.0f : spp_tumble_noise(k, (uint32_t)i, step, &tstate[i]);
     if (p->integrator == SPP_INT_EULER) {
+      /* every body's rates from the state at the start of the step (ring
+       * forces read the neighbours' old positions), then all moves */
       if (abp_accumulate(k, n, x, y, c, s, rcut, acc)) rc = SPP_ERR_OVERFLOW;
       for (int i = 0; i < n; ++i) {
         float fx, fy, tau, dth;
         body_rates(k, i, &acc[i], x, y, c[i], s[i], step, &fx, &fy, &tau, &dth);
+        if (k->tumble) dth = tdth[i];
         int gx = ix[i], gy = iy[i];
-        spp_euler_update(x[i], y[i], th[i], fx, fy, tau, dth, k, &x[i], &y[i], &th[i], &c[i], &s[i],
+        float nt, ncs, nsn;
+        spp_euler_update(x[i], y[i], th[i], fx, fy, tau, dth, k, &hx[i], &hy[i], &nt, &ncs, &nsn,
                          &gx, &gy);
+        kx[i] = nt; hc[i] = ncs; hs[i] = nsn;
         ix[i] = gx; iy[i] = gy;
       }
+      memcpy(x, hx, sizeof(float) * n); memcpy(y, hy, sizeof(float) * n);
+      memcpy(th, kx, sizeof(float) * n); memcpy(c, hc, sizeof(float) * n); memcpy(s, hs, sizeof(float) * n);
       continue;
     }
     int nst = p->integrator == SPP_INT_RK4 ? 4 : 2;
@@ -168,6 +182,7 @@ static int abp_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t
       for (int i = 0; i < n; ++i) {
         float fx, fy, tau, dth;
         body_rates(k, i, &acc[i], cx, cy, cc[i], cs[i], step, &fx, &fy, &tau, &dth);
+        if (k->tumble) dth = tdth[i];
         float h, frac;
         if (nst == 2) {
           h = stage == 0 ? k->half_dt : k->dt;
@@ -196,6 +211,7 @@ static int abp_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t
     }
   }
   free(c); free(s); free(hx); free(hy); free(hc); free(hs); free(kx); free(ky); free(kt); free(acc);
+  free(tstate); free(tdth);
   return rc;
 }
 
@@ -561,4 +577,11 @@ void orc32_pair_distribution(const float* x, const float* y, const float* c, con
         counts[(size_t)bx * gy + by]++;
       }
     }
+}
+
+/* The kernels' run-and-tumble constants for p (spp_consts_from_params). */
+int32_t orc32_tumble_steps(const SppParams* p) {
+  SppConsts k;
+  spp_consts_from_params(&k, p);
+  return k.tumble_steps;
 }

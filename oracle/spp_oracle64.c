@@ -126,6 +126,8 @@ typedef struct {
   double *avx, *avy, *ath;        /* Vicsek averages */
   double *tho, *xo, *yo, *dth;    /* theta_old, r_old, dtheta */
   double *k1f_x, *k1f_y, *k1t, *k2f_x, *k2f_y, *k2t, *k3f_x, *k3f_y, *k3t;
+  int* tflag;                     /* RTPChain::tumble_flag */
+  double* telapsed;               /* RTPChain::tumble_elapesed_time */
 } ostate;
 
 static double* dalloc(int n) { return (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double)); }
@@ -142,8 +144,12 @@ static void state_alloc(ostate* s, const SppParams* p) {
   s->k1f_x = dalloc(n); s->k1f_y = dalloc(n); s->k1t = dalloc(n);
   s->k2f_x = dalloc(n); s->k2f_y = dalloc(n); s->k2t = dalloc(n);
   s->k3f_x = dalloc(n); s->k3f_y = dalloc(n); s->k3t = dalloc(n);
+  s->tflag = (int*)calloc((size_t)(n > 0 ? n : 1), sizeof(int));
+  s->telapsed = dalloc(n);
 }
 static void state_free(ostate* s) {
+  free(s->tflag);
+  free(s->telapsed);
   double* arr[] = {s->x, s->y, s->xu, s->yu, s->th, s->vx, s->vy, s->fx, s->fy, s->tq,
                    s->avx, s->avy, s->ath, s->tho, s->xo, s->yo, s->dth,
                    s->k1f_x, s->k1f_y, s->k1t, s->k2f_x, s->k2f_y, s->k2t, s->k3f_x, s->k3f_y, s->k3t};
@@ -470,6 +476,29 @@ static void bead_stage_forces(ostate* s) {
  * swimmers).  RK4 follows RepulsiveParticle's scheme (:633-726) with these
  * rates (no reference counterpart for beads).  Membrane beads keep their
  * heading (F0 = 0 makes it irrelevant to their motion). */
+/* RTPChain::Noise_Gen (shared/particle.h:1085-1103): a running swimmer
+ * starts a tumble of random sign with probability lambda dt; a tumble lasts
+ * while its elapsed time, accumulated in steps of dt, is < t_tumble. */
+static double tumble_noise(ostate* s, int i, int64_t step) {
+  const SppParams* p = s->p;
+  if (s->tflag[i] == 0) {
+    double u = spp_u01_d(spp_draw(p->seed, p->system_id, (uint32_t)i, (uint32_t)step, SPP_RNG_TUMBLE).v[0]);
+    if (u < p->tumble_rate * p->dt) {
+      double u2 = spp_u01_d(spp_draw(p->seed, p->system_id, (uint32_t)i, (uint32_t)step, SPP_RNG_TUMBLE_SIGN).v[0]);
+      s->tflag[i] = 2 * (int)(unsigned long)(u2 * 2.0) - 1;
+      s->telapsed[i] += p->dt;
+    }
+  } else {
+    if (s->telapsed[i] < p->tumble_time) {
+      s->telapsed[i] += p->dt;
+    } else {
+      s->telapsed[i] = 0;
+      s->tflag[i] = 0;
+    }
+  }
+  return p->k_perp * p->dt * s->tflag[i] * p->tumble_torque;
+}
+
 static void bead_step(ostate* s, int64_t step) {
   const SppParams* p = s->p;
   double dt = p->dt, half_dt = 0.5 * dt, dt6 = dt / 6;
@@ -483,7 +512,9 @@ static void bead_step(ostate* s, int64_t step) {
       double vx = p->mu * s->fx[i], vy = p->mu * s->fy[i];
       double om = swim ? p->k_perp * s->tq[i] : 0.0;
       if (stage == 0) {
-        s->dth[i] = swim ? sigma * orc_normal(p, i, step) : 0.0;
+        if (!swim) s->dth[i] = 0.0;
+        else if (p->rot_noise == SPP_NOISE_TUMBLE) s->dth[i] = tumble_noise(s, i, step);
+        else s->dth[i] = sigma * orc_normal(p, i, step);
         s->tho[i] = s->th[i]; s->xo[i] = s->xu[i]; s->yo[i] = s->yu[i];
       }
       double h, frac;

@@ -18,6 +18,7 @@ STATUS_NAMES = {0: "SPP_OK", 1: "SPP_ERR_INVALID", 2: "SPP_ERR_ALLOC", 3: "SPP_E
 
 MODEL_VICSEK, MODEL_VICSEK_REF_ANGLE, MODEL_VICSEK_REF_VECTOR = 0, 1, 2
 MODEL_CONTINUOUS, MODEL_ABP, MODEL_BEADS = 3, 4, 5
+NOISE_GAUSSIAN, NOISE_TUMBLE = 0, 1
 INT_EULER, INT_RK2, INT_RK4 = 1, 2, 4
 FORCE_NONE, FORCE_HARMONIC, FORCE_R12_TRUNC = 0, 1, 2
 ALIGN_REFERENCE, ALIGN_MEAN = 0, 1
@@ -35,7 +36,8 @@ class SppParams(C.Structure):
         ("r_rep", C.c_double), ("k_rep", C.c_double), ("sigma_rep", C.c_double),
         ("skin", C.c_double), ("beta_push", C.c_double), ("r_push", C.c_double),
         ("mu", C.c_double), ("k_perp", C.c_double), ("torque0", C.c_double),
-        ("k_bond", C.c_double), ("bond_rest", C.c_double), ("kappa_bend", C.c_double),
+        ("k_bond", C.c_double), ("bond_rest", C.c_double), ("kappa_bend", C.c_double), ("rot_noise", C.c_int32), ("reserved", C.c_int32),
+                ("tumble_rate", C.c_double), ("tumble_time", C.c_double), ("tumble_torque", C.c_double),
     ]
 
     def copy(self):

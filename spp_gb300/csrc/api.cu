@@ -119,7 +119,7 @@ void free_dev(SppSystem* s) {
   DevState& d = s->d;
   void* ptrs[] = {d.pos, d.half, d.half2, d.theta, d.img, d.id, d.inv, d.kacc, d.dth, d.ref, d.pos_alt,
                   d.theta_alt, d.img_alt, d.id_alt, d.key, d.rank, d.cell_count, d.cell_start,
-                  d.scan_tmp, d.nbr, d.nn, d.ctl, d.red, s->stage_x, s->stage_y, s->stage_t,
+                  d.scan_tmp, d.nbr, d.nn, d.tumble, d.ctl, d.red, s->stage_x, s->stage_y, s->stage_t,
                   s->stage_img};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -143,6 +143,16 @@ int validate(const SppParams* p) {
   if (!(p->L > 0) || !(p->dt > 0)) return fail(SPP_ERR_INVALID, "L and dt must be > 0");
   if (!(p->r_align > 0)) return fail(SPP_ERR_INVALID, "r_align must be > 0");
   if (p->Dr < 0 || p->skin < 0) return fail(SPP_ERR_INVALID, "Dr and skin must be >= 0");
+  if (p->rot_noise != SPP_NOISE_GAUSSIAN && p->rot_noise != SPP_NOISE_TUMBLE)
+    return fail(SPP_ERR_INVALID, "rot_noise must be SPP_NOISE_GAUSSIAN or SPP_NOISE_TUMBLE");
+  if (p->rot_noise == SPP_NOISE_TUMBLE) {
+    if (p->model != SPP_MODEL_BEADS)
+      return fail(SPP_ERR_UNSUPPORTED, "run and tumble is built for SPP_MODEL_BEADS swimmers (RTPChain)");
+    if (!(p->tumble_rate >= 0) || !std::isfinite(p->tumble_rate) || !std::isfinite(p->tumble_time) ||
+        !std::isfinite(p->tumble_torque) || p->tumble_time / p->dt > 2.0e9)
+      return fail(SPP_ERR_INVALID, "tumble_rate >= 0, finite tumble_time / tumble_torque, "
+                                   "tumble_time / dt < 2e9");
+  }
   switch (p->model) {
     case SPP_MODEL_VICSEK:
     case SPP_MODEL_VICSEK_REF_ANGLE:
@@ -527,6 +537,11 @@ int spp_params_init(SppParams* p, int model) {
   p->integrator = SPP_INT_EULER;
   p->force_law = SPP_FORCE_NONE;
   p->align_mode = SPP_ALIGN_REFERENCE;
+  /* RTPChain statics, particle.h:1106-1108 (used with SPP_NOISE_TUMBLE) */
+  p->rot_noise = SPP_NOISE_GAUSSIAN;
+  p->tumble_rate = 0.1;
+  p->tumble_time = 10 * 0.1;
+  p->tumble_torque = 1.0;
   switch (model) {
     case SPP_MODEL_ABP:           /* RepulsiveParticle statics, particle.h:774-786 */
       p->integrator = SPP_INT_RK2;
@@ -600,6 +615,7 @@ int spp_create(const SppParams* p, SppSystem** out) {
   rc = rc ? rc : dalloc(&d.img, n);
   rc = rc ? rc : dalloc(&d.id, n);
   if (p->model == SPP_MODEL_BEADS) rc = rc ? rc : dalloc(&d.inv, n);
+  if (s->k.tumble) rc = rc ? rc : dalloc(&d.tumble, n);
   rc = rc ? rc : dalloc(&d.kacc, s->nstages > 2 ? n : 1);
   rc = rc ? rc : dalloc(&d.dth, s->nstages > 1 ? n : 1);
   rc = rc ? rc : dalloc(&d.ref, n);
@@ -694,6 +710,8 @@ int spp_upload_state(SppSystem* s, const float* x, const float* y, const float* 
   c.bad_nonfinite = 0xffffffffu;
   c.bad_range = 0xffffffffu;
   CUDA_TRY(cudaMemcpyAsync(s->d.ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s->stream));
+  /* every swimmer starts running (RTPChain::RTPChain, particle.h:1078-1083) */
+  if (s->d.tumble) CUDA_TRY(cudaMemsetAsync(s->d.tumble, 0, sizeof(int32_t) * (size_t)n, s->stream));
   launch_init_state(s->k, s->d, s->stage_x, s->stage_y, s->stage_t, img_dev, s->stream);
   s->host_launches++;
   int rc = enqueue_rebuild(s, s->stream, &s->host_launches);

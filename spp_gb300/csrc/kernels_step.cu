@@ -186,7 +186,13 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(S
     }
     float dth;
     if (b.stage == 0) {
-      dth = turns ? spp_rot_noise(&k, KIND == SPP_KIND_BEADS ? pid : d.id[i], d.ctl->step) : 0.0f;
+      if (!turns) {
+        dth = 0.0f;
+      } else if (KIND == SPP_KIND_BEADS && k.tumble) {
+        dth = spp_tumble_noise(&k, pid, d.ctl->step, d.tumble + pid);
+      } else {
+        dth = spp_rot_noise(&k, KIND == SPP_KIND_BEADS ? pid : d.id[i], d.ctl->step);
+      }
       if (b.nstages > 1) d.dth[i] = dth;
     } else {
       dth = d.dth[i];

@@ -71,6 +71,11 @@ SPP_HD float spp_u2f(uint32_t u) {
 #define SPP_RNG_TANGENT     5u  /* tangent-vector initialisation */
 #define SPP_RNG_TRANS_NOISE 6u  /* translational noise (ContinuousParticle Kamp) */
 #define SPP_RNG_SWEEP       7u  /* sweep parameter sampling */
+/* Run and tumble: the start test and the direction of a tumble, the first
+ * and second draw of RTPChain::Noise_Gen (shared/particle.h:1089, 1092) in
+ * the per-(particle, step) stream order the tests' GSL stand-in uses. */
+#define SPP_RNG_TUMBLE      SPP_RNG_VICSEK
+#define SPP_RNG_TUMBLE_SIGN 101u
 
 typedef struct { uint32_t v[4]; } spp_u32x4;
 

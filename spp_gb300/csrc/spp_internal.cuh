@@ -69,6 +69,7 @@ struct DevState {
   uint32_t* scan_tmp;     /* block sums of the scan */
   int32_t* nbr;
   int32_t* nn;
+  int32_t* tumble;        /* run-and-tumble state by particle id (SPP_NOISE_TUMBLE), else NULL */
   Ctl* ctl;
   double* red;            /* reduction scratch (polarization) */
 };

@@ -44,6 +44,15 @@ typedef struct SppConsts {
   float mu;                    /* translational mobility (m_parallel = m_perpendicular) */
   float ang_drift;             /* k_perp * torque0: intrinsic angular velocity of swimmers */
   float k_bond, bond_rest, kappa;
+  /* run and tumble (SPP_NOISE_TUMBLE): a tumble starts when the 24-bit
+   * uniform of the start draw is < tumble_u24, i.e. exactly when the
+   * reference's double u < rate * dt; it lasts tumble_steps steps, the count
+   * of dt additions after which the reference's double elapsed time first
+   * reaches t_tumble; each tumbling step turns by +-tumble_dth */
+  int32_t tumble;
+  uint32_t tumble_u24;
+  int32_t tumble_steps;
+  float tumble_dth;
 } SppConsts;
 
 /* Host-side: round the double parameters to the kernels' floats. */
@@ -97,6 +106,22 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
     k->bond_rest = (float)p->bond_rest;
     k->kappa = (float)p->kappa_bend;
     k->interior = (float)(p->L - 2.0 * (rl + (p->skin > 0 ? p->skin : 0.0)));
+  }
+  k->tumble = (p->model == SPP_MODEL_BEADS && p->rot_noise == SPP_NOISE_TUMBLE) ? 1 : 0;
+  k->tumble_u24 = 0u;
+  k->tumble_steps = 0;
+  k->tumble_dth = 0.0f;
+  if (k->tumble) {
+    const double thr = ceil((p->tumble_rate * p->dt) * 16777216.0);  /* 2^24 */
+    k->tumble_u24 = thr <= 0.0 ? 0u : (thr >= 16777216.0 ? 16777216u : (uint32_t)thr);
+    double e = 0.0;
+    int32_t c = 0;
+    while (e < p->tumble_time && c < 0x7fffffff) {
+      e += p->dt;
+      ++c;
+    }
+    k->tumble_steps = c;
+    k->tumble_dth = (float)((p->k_perp * p->dt) * p->tumble_torque);
   }
 }
 
@@ -216,6 +241,27 @@ SPP_HD void spp_abp_forces(const SppConsts* k, const SppAccF* a, float ci, float
   if (k->model == SPP_MODEL_CONTINUOUS) *tau = k->g * S;
   else if (k->align_mode == SPP_ALIGN_MEAN) *tau = (k->g * S) / (float)(a->cnt + 1);
   else *tau = S * k->g_over_area;
+}
+
+/* RTPChain::Noise_Gen (shared/particle.h:1085-1103) on an integer state: 0
+ * while running, +-c while tumbling (c = dt additions to the elapsed time so
+ * far).  Returns the step's dtheta and updates the state. */
+SPP_HD float spp_tumble_noise(const SppConsts* k, uint32_t pid, uint32_t step, int32_t* state) {
+  int32_t s = *state;
+  if (s == 0) {
+    const uint32_t u = spp_draw(k->seed, k->system, pid, step, SPP_RNG_TUMBLE).v[0] >> 8;
+    if (u < k->tumble_u24) {
+      /* 2 * gsl_rng_uniform_int(r, 2) - 1: -1 when the uniform is < 1/2 */
+      const uint32_t v = spp_draw(k->seed, k->system, pid, step, SPP_RNG_TUMBLE_SIGN).v[0] >> 8;
+      s = v < (1u << 23) ? -1 : 1;
+    }
+  } else {
+    const int32_t c = s < 0 ? -s : s;
+    if (c < k->tumble_steps) s = s < 0 ? s - 1 : s + 1;
+    else s = 0;
+  }
+  *state = s;
+  return s == 0 ? 0.0f : (s < 0 ? -k->tumble_dth : k->tumble_dth);
 }
 
 /* The rotational-noise increment of particle pid at a step. */

@@ -27,6 +27,20 @@ def lattice(n_side, spacing, L):
     return X.ravel(), Y.ravel()
 
 
+def rtp_case(integ):
+    """RTPChain (run and tumble) swimmers inside rings: tumbles start often
+    (rate 20, dt 0.002) and last 0.03 (15 steps)."""
+    p = configs.vesicle_config(n_rings=4, ring_size=40, swimmers_per_ring=8, L=20.0,
+                               integrator=integ, seed=9)
+    x, y, th = configs.vesicle_state(p)
+    p.sigma_rep, p.r_rep, p.k_rep = 0.5, 0.55, 1.0
+    p.bond_rest, p.k_bond, p.kappa_bend = 0.55, 30.0, 0.0
+    p.dt = 0.002
+    p.rot_noise = abi.NOISE_TUMBLE
+    p.tumble_rate, p.tumble_time, p.tumble_torque = 20.0, 0.03, 3.0
+    return p, x.astype(np.float64), y.astype(np.float64), th.astype(np.float64)
+
+
 def cases():
     out = []
     for integ, name in ((abi.INT_EULER, "euler"), (abi.INT_RK2, "rk2"), (abi.INT_RK4, "rk4")):
@@ -50,6 +64,8 @@ def cases():
         p.bond_rest, p.k_bond, p.kappa_bend = 0.55, 30.0, 0.0
         p.Dr, p.dt = 0.2, 0.002
         out.append((name, p, x.astype(np.float64), y.astype(np.float64), th.astype(np.float64), 60))
+    for integ, name in ((abi.INT_EULER, "rtp_euler"), (abi.INT_RK2, "rtp_rk2")):
+        out.append((name, *rtp_case(integ), 80))
     p = configs.reference_defaults(abi.MODEL_CONTINUOUS)
     p.n, p.L, p.Dr, p.dt, p.v0, p.seed = 1024, 16.0, 0.05, 0.01, 0.5, 11
     x, y, th = configs.random_state(p.n, p.L, seed=3)

@@ -221,3 +221,47 @@ def test_vesicles_vs_fp64(gpu_lib):
     assert np.max(np.abs(yu - a.yu)) / (2 * p.L) < 1e-5
     dth = np.abs((gth[nb:].astype(np.float64) - a.th[nb:] + np.pi) % (2 * np.pi) - np.pi)
     assert np.max(dth) < 1e-5
+
+
+@pytest.mark.parametrize("integ", [abi.INT_EULER, abi.INT_RK2, abi.INT_RK4])
+def test_run_and_tumble_bitexact_vs_mirror(gpu_lib, integ):
+    """RTPChain swimmers (run and tumble) inside ring membranes: the tumble
+    states live by particle id on the device and advance once per step."""
+    p = configs.vesicle_config(n_rings=16, ring_size=64, swimmers_per_ring=16, L=48.0,
+                               integrator=integ, seed=9)
+    x, y, th = configs.vesicle_state(p)
+    p.rot_noise = abi.NOISE_TUMBLE
+    p.tumble_rate, p.tumble_time, p.tumble_torque = 20.0, 0.03, 3.0
+    if integ == abi.INT_EULER:
+        p.dt = 0.0005  # the stiff bonds and bending need a smaller first-order step
+    gpu, _ = run_gpu(p, x, y, th, 200)
+    ref = O.run32(p, O.State32(x, y, th), 200)
+    assert_bitexact(gpu, ref)
+    nb = p.n_rings * p.ring_size
+    assert np.abs(gpu[2][nb:] - th[nb:]).max() > 0.1
+
+
+def test_run_and_tumble_fraction_of_time_tumbling(gpu_lib):
+    """Many free swimmers: the stationary share of tumbling swimmers is
+    rate * T / (1 + rate * T) with T the tumble length (the geometric
+    waiting time of the start draws)."""
+    p = configs.vesicle_config(n_rings=0, ring_size=3, swimmers_per_ring=0, L=200.0, seed=4)
+    p.n = 40000
+    p.force_law = abi.FORCE_NONE  # random placement: no overlapping pairs to resolve
+    x, y, th = configs.random_state(p.n, p.L, seed=4)
+    p.rot_noise = abi.NOISE_TUMBLE
+    p.tumble_rate, p.tumble_time, p.tumble_torque, p.dt = 5.0, 0.1, 2.0, 0.002
+    K = O.tumble_steps(p)
+    with System(p) as s:
+        s.upload(x, y, th)
+        s.step(2000)
+        t1 = s.download()[2].astype(np.float64)
+        s.step(1)
+        t2 = s.download()[2].astype(np.float64)
+    dth = np.abs(((t2 - t1) + np.pi) % (2 * np.pi) - np.pi)
+    turning = dth > 0.5 * p.k_perp * p.dt * p.tumble_torque
+    rate_dt = p.tumble_rate * p.dt
+    # per step: a running swimmer starts with probability rate*dt; a tumble
+    # turns for K steps (start step included) and resets on the next
+    expect = K / (K + 1 + 1 / rate_dt - 1)
+    assert abs(turning.mean() - expect) < 0.02, (turning.mean(), expect)

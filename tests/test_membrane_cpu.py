@@ -4,6 +4,7 @@ passive deformed ring relaxes (energy decreases, shape rounds)."""
 import math
 
 import numpy as np
+import pytest
 
 from oracle import oracle as O
 from spp_gb300 import abi, configs
@@ -85,3 +86,44 @@ def test_mirror_tracks_fp64_vesicles():
     m = O.run32(p, O.State32(x, y, th), 100)
     xu = m.x.astype(np.float64) + 2 * p.L * m.ix
     assert np.max(np.abs(xu - a.xu)) / (2 * p.L) < 1e-6
+
+
+def _rtp(integ):
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    from make_golden import rtp_case
+    return rtp_case(integ)
+
+
+@pytest.mark.parametrize("integ", [abi.INT_EULER, abi.INT_RK2, abi.INT_RK4])
+def test_mirror_tumbles_like_fp64(integ):
+    """Run and tumble: the kernels' integer schedule (a start threshold on
+    the 24-bit uniform, a tumble length counted in steps) makes the same
+    decisions as the reference's double-precision rule, so the FP32 mirror
+    stays within FP32 rounding of the FP64 restatement; one differing
+    decision would cost a whole tumble step of turning (>= 0.006 rad here)."""
+    p, x, y, th = _rtp(integ)
+    th0 = th.copy()
+    s32 = O.State32(x, y, th)
+    O.run32(p, s32, 300)
+    a = O.State64(x.copy(), y.copy(), th.copy())
+    O.run64(p, a, 300)
+    nb = p.n_rings * p.ring_size
+    d = np.abs(((s32.th[nb:].astype(np.float64) - a.th[nb:]) + np.pi) % (2 * np.pi) - np.pi)
+    assert d.max() < 1e-4
+    assert np.abs(a.th[nb:] - th0[nb:]).max() > 0.1
+
+
+def test_tumble_schedule_constants():
+    """The step count of a tumble replays the reference's accumulation of dt
+    in double (tumble_elapesed_time, particle.h:1092-1100)."""
+    p, _, _, _ = _rtp(abi.INT_RK2)
+    for t_tumble, dt in ((0.03, 0.002), (1.0, 0.1), (0.0, 0.01), (0.3, 0.1)):
+        e, c = 0.0, 0
+        while e < t_tumble:
+            e += dt
+            c += 1
+        q = p.copy()
+        q.tumble_time, q.dt = t_tumble, dt
+        assert O.tumble_steps(q) == c
