@@ -117,7 +117,18 @@ typedef struct SppParams {
   double tumble_rate;     /* RTPChain::lambda: a tumble starts with probability rate * dt per step */
   double tumble_time;     /* RTPChain::t_tumble: a tumble lasts while its elapsed time < t_tumble */
   double tumble_torque;   /* RTPChain::torque_tumble: dtheta = k_perp dt (+-1) torque_tumble per step */
+  /* Multi-bead swimmers of SPP_MODEL_BEADS (ActiveBrownianChain with nb > 1,
+   * shared/particle.h:856-876, 964-1012).  With chain_beads = 1 every body is
+   * a single bead and the fields below are unused. */
+  int32_t chain_beads;    /* beads per swimmer (nb), 1 .. SPP_MAX_CHAIN_BEADS */
+  int32_t reserved2;
+  double bead_separation; /* ActiveBrownianChain::separation: distance between a swimmer's beads */
+  double sigma_chain;     /* ActiveBrownianChain::sigma_p: R12 sigma of bead pairs that involve a chain */
+  double r_chain;         /* ActiveBrownianChain::repulsion_radius: their cutoff */
 } SppParams;
+
+/* Largest chain_beads. */
+#define SPP_MAX_CHAIN_BEADS 8
 
 typedef struct SppObservables {
   int64_t step;           /* steps taken since upload */
@@ -144,6 +155,14 @@ const char* spp_last_error(void);
 /* Fill defaults for a model: the static initialisers of shared/particle.h
  * (e.g. RepulsiveParticle A_p=2, sigma_p=1, R_a=1.1, r_c=1.2, :774-786). */
 int spp_params_init(SppParams* p, int model);
+/* Mobilities of a swimmer of nb beads (ActiveBrownianChain::Set_nb,
+ * shared/particle.h:856-876): out = {m_parallel, m_perpendicular,
+ * k_perpendicular}.  nb = 1 gives {0.5, 0.5, 1}; nb > 1 the prolate-body
+ * formulas of the aspect ratio 1 / ((separation (nb - 1) / sigma) + 1).  A
+ * chain swimmer's speed is v0 = m_parallel F0, its intrinsic angular
+ * velocity k_perpendicular torque0 (Set_R0: torque0 = m_parallel F0 /
+ * (k_perpendicular R0)). */
+int spp_chain_mobility(int nb, double separation, double sigma, double* out3);
 
 /* ---- one system ---- */
 /* Box constructor + Init (parallel/box.h:69-88, 123-151): validates the

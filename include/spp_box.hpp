@@ -129,7 +129,8 @@ class Box {
   friend std::ostream& operator<<(std::ostream& os, Box& box) {
     State s = box.Save();
     double L = box.p_.L;
-    int32_t nb = 1;
+    // the first swimmer's chain length (particle[Nm].nb)
+    int32_t nb = box.p_.model == SPP_MODEL_BEADS && box.p_.chain_beads > 1 ? box.p_.chain_beads : 1;
     int32_t Nm = box.p_.model == SPP_MODEL_BEADS ? box.p_.n_rings * box.p_.ring_size : 0;
     int32_t Ns = box.N - Nm;
     os.write(reinterpret_cast<const char*>(&box.t), sizeof(double));

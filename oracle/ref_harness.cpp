@@ -140,24 +140,33 @@ int chain_steps(const SppParams* p, int nsteps, int64_t step0, double* x, double
   ActiveBrownianChain::repulsion_radius_m = p->r_rep;
   ActiveBrownianChain::A_p = p->k_rep;
   ActiveBrownianChain::torque0 = p->torque0;
+  /* chain statics (particle.h:1050-1054), read by Set_nb and Interact */
+  ActiveBrownianChain::sigma_p = p->sigma_chain;
+  ActiveBrownianChain::repulsion_radius = p->r_chain;
+  ActiveBrownianChain::separation = p->bead_separation;
   BasicDynamicParticle::Set_Dr(p->Dr);
+  const int nb = p->chain_beads > 1 ? p->chain_beads : 1;
+  double rcut = p->r_rep;
+  if (nb > 1 && (nb - 1) * p->bead_separation + p->r_chain > rcut)
+    rcut = (nb - 1) * p->bead_separation + p->r_chain;
   for (int i = 0; i < p->n; ++i) {
-    ps[i].Set_nb(1);
-    ps[i].Set_F0(i < nm ? 0.0 : p->v0 / p->mu);
+    ps[i].Set_nb(i < nm ? 1 : nb);
+    /* speed v0 = m_parallel F0 */
+    ps[i].Set_F0(i < nm ? 0.0 : (nb > 1 ? p->v0 / ps[i].m_parallel : p->v0 / p->mu));
   }
   load(ps, x, y, th, xu, yu);
   for (int k = 0; k < nsteps; ++k) {
     int64_t step = step0 + k;
     if (p->integrator == SPP_INT_EULER) {
       ring_springs(ps, p);
-      interact_all(ps, p->L, p->r_rep);
+      interact_all(ps, p->L, rcut);
       move_all(ps, p, step, [](P& q) { q.Move(); });
     } else {
       ring_springs(ps, p);
-      interact_all(ps, p->L, p->r_rep);
+      interact_all(ps, p->L, rcut);
       move_all(ps, p, step, [](P& q) { q.Move_Runge_Kutta2_1(); });
       ring_springs(ps, p);
-      interact_all(ps, p->L, p->r_rep);
+      interact_all(ps, p->L, rcut);
       move_all(ps, p, step, [](P& q) { q.Move_Runge_Kutta2_2(); });
     }
   }

@@ -59,12 +59,7 @@ static void mcells_free(mcells* c) { free(c->head); free(c->next); }
     }                                                                                \
   } while (0)
 
-static double mirror_rcut(const SppParams* p) {
-  double r = p->model == SPP_MODEL_BEADS ? 0.0 : p->r_align;
-  if (p->force_law != SPP_FORCE_NONE && p->r_rep > r) r = p->r_rep;
-  if (p->model == SPP_MODEL_VICSEK_REF_VECTOR && p->r_push > r) r = p->r_push;
-  return r;
-}
+static double mirror_rcut(const SppParams* p) { return spp_interaction_range(p); }
 
 static int cmp_int(const void* a, const void* b) {
   int x = *(const int*)a, y = *(const int*)b;
@@ -91,9 +86,16 @@ static int abp_accumulate(const SppConsts* k, int n, const float* x, const float
       }
     });
     qsort(cand, (size_t)m, sizeof(int), cmp_int);
+    const int chain = spp_pair_kind(k) == SPP_KIND_CHAIN;
+    const int nbi = chain && i >= k->n_beads ? k->chain_nb : 1;
     for (int q = 0; q < m; ++q) {
       int j = cand[q];
-      spp_pair_abp(k, &a, x[i], y[i], c[i], s[i], x[j], y[j], c[j], s[j]);
+      if (chain) {
+        const int nbj = j >= k->n_beads ? k->chain_nb : 1;
+        spp_pair_chain(k, k->force_law, 1, &a, nbi, nbj, x[i], y[i], c[i], s[i], x[j], y[j], c[j], s[j]);
+      } else {
+        spp_pair_abp(k, &a, x[i], y[i], c[i], s[i], x[j], y[j], c[j], s[j]);
+      }
     }
     ovf |= a.ovf;
     acc[i] = a;
@@ -106,8 +108,8 @@ static int abp_accumulate(const SppConsts* k, int n, const float* x, const float
 /* Velocity, angular velocity and noise of body i from its received sums
  * (ABP/continuous: spp_abp_forces; beads: ring forces + spp_bead_velocity). */
 static void body_rates(const SppConsts* k, int i, const SppAccF* a, const float* cx,
-                       const float* cy, float ci, float si, uint32_t step, float* fx, float* fy,
-                       float* tau, float* dth) {
+                       const float* cy, float ci, float si, uint32_t step, const float* tdth,
+                       float th0, int euler, float* fx, float* fy, float* tau, float* dth) {
   if (k->model == SPP_MODEL_BEADS) {
     int bead = i < k->n_beads;
     float rfx = 0.0f, rfy = 0.0f;
@@ -120,8 +122,17 @@ static void body_rates(const SppConsts* k, int i, const SppAccF* a, const float*
       }
       spp_ring_forces(k, px, py, &rfx, &rfy);
     }
-    spp_bead_velocity(k, !bead, a, rfx, rfy, ci, si, fx, fy, tau);
-    *dth = bead ? 0.0f : spp_rot_noise(k, (uint32_t)i, step);
+    *dth = bead ? 0.0f : (tdth ? tdth[i] : spp_rot_noise(k, (uint32_t)i, step));
+    if (!bead && k->chain_nb > 1) {
+      spp_chain_velocity(k, a, ci, si, ci, si, fx, fy, tau);
+      if (euler) { /* Move() projects on the heading after the turn */
+        float wc, ws;
+        spp_sincosf(spp_euler_theta(k, th0, *tau, *dth), &ws, &wc);
+        spp_chain_velocity(k, a, ci, si, wc, ws, fx, fy, tau);
+      }
+    } else {
+      spp_bead_velocity(k, !bead, a, rfx, rfy, ci, si, fx, fy, tau);
+    }
   } else {
     spp_abp_forces(k, a, ci, si, fx, fy, tau);
     *dth = spp_rot_noise(k, (uint32_t)i, step);
@@ -156,8 +167,7 @@ static int abp_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t
       if (abp_accumulate(k, n, x, y, c, s, rcut, acc)) rc = SPP_ERR_OVERFLOW;
       for (int i = 0; i < n; ++i) {
         float fx, fy, tau, dth;
-        body_rates(k, i, &acc[i], x, y, c[i], s[i], step, &fx, &fy, &tau, &dth);
-        if (k->tumble) dth = tdth[i];
+        body_rates(k, i, &acc[i], x, y, c[i], s[i], step, tdth, th[i], 1, &fx, &fy, &tau, &dth);
         int gx = ix[i], gy = iy[i];
         float nt, ncs, nsn;
         spp_euler_update(x[i], y[i], th[i], fx, fy, tau, dth, k, &hx[i], &hy[i], &nt, &ncs, &nsn,
@@ -181,8 +191,7 @@ static int abp_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t
       float* ns = (float*)malloc(sizeof(float) * n);
       for (int i = 0; i < n; ++i) {
         float fx, fy, tau, dth;
-        body_rates(k, i, &acc[i], cx, cy, cc[i], cs[i], step, &fx, &fy, &tau, &dth);
-        if (k->tumble) dth = tdth[i];
+        body_rates(k, i, &acc[i], cx, cy, cc[i], cs[i], step, tdth, th[i], 0, &fx, &fy, &tau, &dth);
         float h, frac;
         if (nst == 2) {
           h = stage == 0 ? k->half_dt : k->dt;

@@ -157,11 +157,35 @@ static void state_free(ostate* s) {
   free(s->nb);
 }
 
+static int chain_nb(const SppParams* p) {
+  return p->model == SPP_MODEL_BEADS && p->chain_beads > 1 ? p->chain_beads : 1;
+}
+
 static double interaction_radius(const SppParams* p) {
   double r = p->model == SPP_MODEL_BEADS ? 0.0 : p->r_align;
   if (p->force_law != SPP_FORCE_NONE && p->r_rep > r) r = p->r_rep;
   if (p->model == SPP_MODEL_VICSEK_REF_VECTOR && p->r_push > r) r = p->r_push;
+  /* two chains interact while some bead pair is within r_chain: centres up
+   * to (nb - 1) separation + r_chain apart */
+  if (chain_nb(p) > 1 && p->force_law != SPP_FORCE_NONE) {
+    double reach = (chain_nb(p) - 1) * p->bead_separation + p->r_chain;
+    if (reach > r) r = reach;
+  }
   return r;
+}
+
+/* ActiveBrownianChain::Set_nb, shared/particle.h:856-876: m_parallel,
+ * m_perpendicular, k_perpendicular of a body of nb beads. */
+static void chain_mobility(int nb, double separation, double sigma_p, double* mpar, double* mperp,
+                           double* kperp) {
+  if (nb == 1) { *mpar = 0.5; *mperp = 0.5; *kperp = 1; return; }
+  double aspect_ratio = 1 / ((separation * (nb - 1) / sigma_p) + 1);
+  double e2 = 1 - aspect_ratio * aspect_ratio;
+  double e = sqrt(e2);
+  double L = log((1 + e) / (1 - e));
+  *mpar = 1.0;
+  *mperp = 0.5 * (2 * e + (3 * e2 - 1) * L) / ((1 + e2) * L - 2 * e);
+  *kperp = 6 / (1 + aspect_ratio * aspect_ratio) / sigma_p / sigma_p;
 }
 
 /* ------------------------------------------------------------------ */
@@ -418,13 +442,60 @@ static void bead_pair(void* ctx, int i, int j) {
 
 static int n_beads(const SppParams* p) { return p->n_rings * p->ring_size; }
 
+/* Beads of body i: membrane beads have one, swimmers chain_beads. */
+static int body_nb(const SppParams* p, int i) { return i < n_beads(p) ? 1 : chain_nb(p); }
+
+/* ActiveBrownianChain::Interact, shared/particle.h:964-1012, for bodies of
+ * which at least one is a chain: every bead pair at s_i = v_i separation
+ * ((1 - nb_i)/2 + a), s_j likewise, within r_chain exchanges the R12 force
+ * (sigma_chain, r_chain) on dr = dr0 + s_i - s_j, with the lever-arm
+ * torques s_i x F on i and -s_j x F on j. */
+static void chain_pair(void* ctx, int i, int j) {
+  ostate* s = (ostate*)ctx;
+  const SppParams* p = s->p;
+  int nbi = body_nb(p, i), nbj = body_nb(p, j);
+  if (nbi == 1 && nbj == 1) { bead_pair(ctx, i, j); return; }
+  if (p->force_law == SPP_FORCE_NONE) return;
+  double dx0 = pt(s->x[i] - s->x[j], p->L), dy0 = pt(s->y[i] - s->y[j], p->L);
+  for (int a = 0; a < nbi; ++a)
+    for (int b = 0; b < nbj; ++b) {
+      double oa = p->bead_separation * ((1 - nbi) / 2.0 + a);
+      double ob = p->bead_separation * ((1 - nbj) / 2.0 + b);
+      double six = s->vx[i] * oa, siy = s->vy[i] * oa;
+      double sjx = s->vx[j] * ob, sjy = s->vy[j] * ob;
+      double dx = dx0 + six - sjx, dy = dy0 + siy - sjy;
+      double d = sqrt(dx * dx + dy * dy);
+      if (d < p->r_chain && d > 0) {
+        double Fx, Fy;
+        r12_trunc(dx, dy, d, p->r_chain, p->sigma_chain, p->k_rep, &Fx, &Fy);
+        s->fx[i] += Fx; s->fy[i] += Fy;
+        s->fx[j] -= Fx; s->fy[j] -= Fy;
+        s->tq[i] += six * Fy - siy * Fx;
+        s->tq[j] += -sjx * Fy + sjy * Fx;
+      }
+    }
+}
+
+/* Mobilities of body i: the configured mu / k_perp for single beads, the
+ * Set_nb values for chains. */
+static void body_mobility(const SppParams* p, int i, double* mpar, double* mperp, double* kperp) {
+  if (body_nb(p, i) > 1) {
+    chain_mobility(body_nb(p, i), p->bead_separation, p->sigma_chain, mpar, mperp, kperp);
+  } else {
+    *mpar = p->mu; *mperp = p->mu; *kperp = p->k_perp;
+  }
+}
+
 /* ActiveBrownianChain::Reset, particle.h:878-883: torque = torque0, f = F0 v
- * with F0 = v0 / mu for swimmers (speed v0 = mu F0) and 0 for membrane beads. */
+ * with F0 = v0 / m_parallel for swimmers (speed v0 = m_parallel F0) and 0
+ * for membrane beads. */
 static void bead_reset(ostate* s) {
   const SppParams* p = s->p;
   int nm = n_beads(p);
   for (int i = 0; i < s->n; ++i) {
-    double F0 = i < nm ? 0.0 : p->v0 / p->mu;
+    double mpar, mperp, kperp;
+    body_mobility(p, i, &mpar, &mperp, &kperp);
+    double F0 = i < nm ? 0.0 : p->v0 / mpar;
     s->tq[i] = p->torque0;
     s->fx[i] = F0 * s->vx[i];
     s->fy[i] = F0 * s->vy[i];
@@ -468,7 +539,7 @@ static void ring_forces(ostate* s) {
 static void bead_stage_forces(ostate* s) {
   bead_reset(s);
   ring_forces(s);
-  interact_all(s, bead_pair);
+  interact_all(s, chain_nb(s->p) > 1 ? chain_pair : bead_pair);
 }
 
 /* Moves of ActiveBrownianChain (particle.h:898-962) with m_parallel =
@@ -496,7 +567,9 @@ static double tumble_noise(ostate* s, int i, int64_t step) {
       s->tflag[i] = 0;
     }
   }
-  return p->k_perp * p->dt * s->tflag[i] * p->tumble_torque;
+  double mpar, mperp, kperp;
+  body_mobility(p, i, &mpar, &mperp, &kperp);
+  return kperp * p->dt * s->tflag[i] * p->tumble_torque;
 }
 
 static void bead_step(ostate* s, int64_t step) {
@@ -509,14 +582,26 @@ static void bead_step(ostate* s, int64_t step) {
     bead_stage_forces(s);
     for (int i = 0; i < n; ++i) {
       int swim = i >= nm;
-      double vx = p->mu * s->fx[i], vy = p->mu * s->fy[i];
-      double om = swim ? p->k_perp * s->tq[i] : 0.0;
+      double mpar, mperp, kperp;
+      body_mobility(p, i, &mpar, &mperp, &kperp);
+      double om = swim ? kperp * s->tq[i] : 0.0;
       if (stage == 0) {
         if (!swim) s->dth[i] = 0.0;
         else if (p->rot_noise == SPP_NOISE_TUMBLE) s->dth[i] = tumble_noise(s, i, step);
         else s->dth[i] = sigma * orc_normal(p, i, step);
         s->tho[i] = s->th[i]; s->xo[i] = s->xu[i]; s->yo[i] = s->yu[i];
       }
+      /* m_perp f + (m_par - m_perp) (f . w) w, w the heading the forces
+       * were evaluated at; Move() (Euler) turns first and projects on the
+       * new heading (particle.h:898-915) */
+      double wx = s->vx[i], wy = s->vy[i];
+      if (nst == 1 && swim) {
+        double tn = s->tho[i] + dt * om + s->dth[i];
+        wx = cos(tn); wy = sin(tn);
+      }
+      double fw = s->fx[i] * wx + s->fy[i] * wy;
+      double vx = mperp * s->fx[i] + (mpar - mperp) * fw * wx;
+      double vy = mperp * s->fy[i] + (mpar - mperp) * fw * wy;
       double h, frac;
       if (nst == 1) { h = dt; frac = 1; }
       else if (nst == 2) { h = stage == 0 ? half_dt : dt; frac = stage == 0 ? 0.5 : 1.0; }

@@ -37,7 +37,9 @@ class SppParams(C.Structure):
         ("skin", C.c_double), ("beta_push", C.c_double), ("r_push", C.c_double),
         ("mu", C.c_double), ("k_perp", C.c_double), ("torque0", C.c_double),
         ("k_bond", C.c_double), ("bond_rest", C.c_double), ("kappa_bend", C.c_double), ("rot_noise", C.c_int32), ("reserved", C.c_int32),
-                ("tumble_rate", C.c_double), ("tumble_time", C.c_double), ("tumble_torque", C.c_double),
+        ("tumble_rate", C.c_double), ("tumble_time", C.c_double), ("tumble_torque", C.c_double),
+        ("chain_beads", C.c_int32), ("reserved2", C.c_int32),
+        ("bead_separation", C.c_double), ("sigma_chain", C.c_double), ("r_chain", C.c_double),
     ]
 
     def copy(self):
@@ -110,6 +112,7 @@ PROTOTYPES = {
     "spp_status_string": (C.c_char_p, [C.c_int]),
     "spp_last_error": (C.c_char_p, []),
     "spp_params_init": (C.c_int, [C.POINTER(SppParams), C.c_int]),
+    "spp_chain_mobility": (C.c_int, [C.c_int, C.c_double, C.c_double, _D]),
     "spp_create": (C.c_int, [C.POINTER(SppParams), C.POINTER(_P)]),
     "spp_destroy": (C.c_int, [_P]),
     "spp_set_stream": (C.c_int, [_P, _P]),

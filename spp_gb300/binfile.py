@@ -61,7 +61,10 @@ def state_frame(p, t, x, y, theta, img_x, img_y):
     xu = (np.asarray(x, np.float64) + 2.0 * L * np.asarray(img_x, np.float64)).astype(np.float32)
     yu = (np.asarray(y, np.float64) + 2.0 * L * np.asarray(img_y, np.float64)).astype(np.float32)
     nm = p.n_rings * p.ring_size if p.model == abi.MODEL_BEADS else 0
-    return encode_frame(t, L, xu[nm:], yu[nm:], np.asarray(theta, np.float32)[nm:], xu[:nm], yu[:nm])
+    # the header's nb is the first swimmer's (particle[Nm].nb, parallel/box.h:485)
+    nb = p.chain_beads if p.model == abi.MODEL_BEADS and p.chain_beads > 1 else 1
+    return encode_frame(t, L, xu[nm:], yu[nm:], np.asarray(theta, np.float32)[nm:], xu[:nm], yu[:nm],
+                        nb=nb)
 
 
 def write_system_frame(f, system, t=None):

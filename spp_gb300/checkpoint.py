@@ -36,9 +36,15 @@ def load(path):
         if int(z["format"]) != FORMAT:
             raise ValueError(f"unknown checkpoint format {int(z['format'])}")
         raw = z["params"].tobytes()
-        if len(raw) != C.sizeof(abi.SppParams):
+        n = C.sizeof(abi.SppParams)
+        # SppParams only grows at its end and starts with its own size: a
+        # shorter record of an earlier layout reads with the later fields 0
+        # (chain_beads 0 = single beads, rot_noise 0 = Gaussian noise)
+        if len(raw) < 4 or len(raw) > n or int.from_bytes(raw[:4], "little") != len(raw):
             raise ValueError("checkpoint was written with a different SppParams layout")
-        p = abi.SppParams.from_buffer_copy(raw)
+        p = abi.SppParams()
+        C.memmove(C.addressof(p), raw, len(raw))
+        p.struct_size = n
         snap = Snapshot(z["x"].copy(), z["y"].copy(), z["theta"].copy(), z["img_x"].copy(), z["img_y"].copy(),
                         int(z["step"]))
     return p, snap

@@ -194,6 +194,39 @@ def vesicle_state(p, swimmers_per_ring=None, seed=None):
     return x, y, th.astype(np.float32)
 
 
+def chain_config(n=4096, chain_beads=3, separation=0.5, sigma=0.5, r_chain=0.55, spacing=2.0,
+                 seed=4, integrator=abi.INT_RK2) -> abi.SppParams:
+    """Free multi-bead swimmers, no membranes: n chains of chain_beads beads
+    (ActiveBrownianChain with nb > 1, shared/particle.h:856-1012), beads
+    separation apart, R12 between beads (sigma, cutoff r_chain, A = 1), on a
+    square lattice of the given spacing (L = spacing sqrt(n) / 2); v0 = 1,
+    D_r = 0.1, no intrinsic torque."""
+    G = int(math.ceil(math.sqrt(n)))
+    p = reference_defaults(abi.MODEL_BEADS)
+    p.n_rings, p.ring_size = 0, 0
+    p.n, p.seed, p.integrator = n, seed, integrator
+    p.L = 0.5 * spacing * G
+    p.force_law = abi.FORCE_R12_TRUNC
+    p.k_rep = 1.0
+    p.chain_beads, p.bead_separation, p.sigma_chain, p.r_chain = chain_beads, separation, sigma, r_chain
+    p.v0, p.Dr, p.dt, p.skin, p.torque0 = 1.0, 0.1, 0.002, 0.3, 0.0
+    return p
+
+
+def chain_state(p, seed=None):
+    """Chains of a chain_config on their square lattice, random headings:
+    with spacing > (nb - 1) separation + r_chain no two chains touch."""
+    seed = p.seed if seed is None else seed
+    G = int(math.ceil(math.sqrt(p.n)))
+    spacing = 2 * p.L / G
+    ids = np.arange(p.n, dtype=np.uint32)
+    r = draw(seed, 0, ids, 0, RNG_INIT_ANGLE)
+    x = (-p.L + (ids % G + 0.5) * spacing).astype(np.float32)
+    y = (-p.L + (ids // G + 0.5) * spacing).astype(np.float32)
+    th = ((2 * u01_f32(r[0]).astype(np.float64) - 1) * math.pi).astype(np.float32)
+    return x, y, th
+
+
 def lyapunov_config(n=16384, rho=1.0, seed=3, integrator=abi.INT_RK4) -> abi.SppParams:
     """Continuous-time Vicsek for the Lyapunov spectrum: N = 16,384 at
     rho = 1 (L = 64), v0 = 0.5, g = 1, alpha = 0, D_r = 0, r = 1, RK4 with

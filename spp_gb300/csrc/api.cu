@@ -128,12 +128,7 @@ void free_dev(SppSystem* s) {
   s->stage_img = nullptr;
 }
 
-double interaction_radius(const SppParams& p) {
-  double r = p.model == SPP_MODEL_BEADS ? 0.0 : p.r_align;
-  if (p.force_law != SPP_FORCE_NONE && p.r_rep > r) r = p.r_rep;
-  if (p.model == SPP_MODEL_VICSEK_REF_VECTOR && p.r_push > r) r = p.r_push;
-  return r;
-}
+double interaction_radius(const SppParams& p) { return spp_interaction_range(&p); }
 
 int validate(const SppParams* p) {
   if (!p) return fail(SPP_ERR_INVALID, "params is NULL");
@@ -152,6 +147,17 @@ int validate(const SppParams* p) {
         !std::isfinite(p->tumble_torque) || p->tumble_time / p->dt > 2.0e9)
       return fail(SPP_ERR_INVALID, "tumble_rate >= 0, finite tumble_time / tumble_torque, "
                                    "tumble_time / dt < 2e9");
+  }
+  if (p->chain_beads < 0 || p->chain_beads > SPP_MAX_CHAIN_BEADS)
+    return fail(SPP_ERR_INVALID, "chain_beads must be 0 .. SPP_MAX_CHAIN_BEADS (0 and 1: single beads)");
+  if (p->chain_beads > 1) {
+    if (p->model != SPP_MODEL_BEADS)
+      return fail(SPP_ERR_UNSUPPORTED, "multi-bead swimmers are built for SPP_MODEL_BEADS (ActiveBrownianChain)");
+    if (p->force_law != SPP_FORCE_R12_TRUNC && p->force_law != SPP_FORCE_NONE)
+      return fail(SPP_ERR_INVALID, "chains interact by R12_Repulsive_Truncated (SPP_FORCE_R12_TRUNC) or not at all");
+    if (!(p->bead_separation > 0) || !(p->sigma_chain > 0) || !(p->r_chain > 0) ||
+        !std::isfinite(p->bead_separation) || !std::isfinite(p->sigma_chain) || !std::isfinite(p->r_chain))
+      return fail(SPP_ERR_INVALID, "bead_separation, sigma_chain and r_chain must be finite and > 0");
   }
   switch (p->model) {
     case SPP_MODEL_VICSEK:
@@ -542,6 +548,11 @@ int spp_params_init(SppParams* p, int model) {
   p->tumble_rate = 0.1;
   p->tumble_time = 10 * 0.1;
   p->tumble_torque = 1.0;
+  /* ActiveBrownianChain statics, particle.h:1049-1054 (used with chain_beads > 1) */
+  p->chain_beads = 1;
+  p->bead_separation = 1.0;
+  p->sigma_chain = 1.0;
+  p->r_chain = 1.1;
   switch (model) {
     case SPP_MODEL_ABP:           /* RepulsiveParticle statics, particle.h:774-786 */
       p->integrator = SPP_INT_RK2;
@@ -564,6 +575,15 @@ int spp_params_init(SppParams* p, int model) {
     default:
       return fail(SPP_ERR_UNSUPPORTED, "unknown model");
   }
+  return SPP_OK;
+}
+
+int spp_chain_mobility(int nb, double separation, double sigma, double* out3) {
+  if (!out3) return fail(SPP_ERR_INVALID, "out is NULL");
+  if (nb < 1 || nb > SPP_MAX_CHAIN_BEADS) return fail(SPP_ERR_INVALID, "nb must be 1 .. SPP_MAX_CHAIN_BEADS");
+  if (nb > 1 && (!(separation > 0) || !(sigma > 0)))
+    return fail(SPP_ERR_INVALID, "separation and sigma must be > 0");
+  spp_chain_mobility_d(nb, separation, sigma, out3);
   return SPP_OK;
 }
 

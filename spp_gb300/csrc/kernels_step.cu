@@ -91,13 +91,29 @@ __device__ __forceinline__ void finish_step(const SppConsts& k, const DevState& 
 #define SPP_STAGE_GROUP 3        /* neighbours whose loads are issued together (1: one-ahead prefetch) */
 #endif
 
+/* One neighbour's contribution; the chain kind also needs the neighbour's
+ * bead count (1 for membrane beads). */
+template <int LAW, int KIND>
+__device__ __forceinline__ void stage_pair(const SppConsts& k, const DevState& d, int wrap, SppAccF* a,
+                                           int nbi, int j, float4 pi, float4 pj) {
+  if (KIND == SPP_KIND_CHAIN) {
+    const int nbj = __ldg(d.id + j) < (uint32_t)k.n_beads ? 1 : k.chain_nb;
+    spp_pair_chain(&k, LAW, wrap, a, nbi, nbj, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
+  } else {
+    spp_pair_abp_lkw(&k, LAW, KIND, wrap, a, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
+  }
+}
+
 #ifndef SPP_STAGE_MIN_BLOCKS
 #define SPP_STAGE_MIN_BLOCKS 8   /* 8 x 256 threads per SM: 32 registers */
 #endif
+/* the chain pair loop (bead offsets, lever-arm torques) needs more than
+ * 32 registers: 4 x 256 threads per SM there */
 template <int LAW, int KIND>
-__global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(SppConsts k, DevState d, StageBufs b,
+__global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_STAGE_MIN_BLOCKS) k_abp_stage(SppConsts k, DevState d, StageBufs b,
                                                          cudaGraphConditionalHandle cond,
                                                          int use_cond) {
+  constexpr bool BEADLIKE = (KIND == SPP_KIND_BEADS || KIND == SPP_KIND_CHAIN);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int last = (b.stage == b.nstages - 1);
   const int frozen = d.ctl->frozen;
@@ -106,6 +122,8 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(S
     const float4 pi = b.cur[i];
     SppAccF a;
     spp_accf_zero(&a);
+    const uint32_t pid = BEADLIKE ? d.id[i] : 0u;
+    const int nbi = (KIND == SPP_KIND_CHAIN && pid >= (uint32_t)k.n_beads) ? k.chain_nb : 1;
     const int cnt = d.nn[i];
     const int32_t* __restrict__ nb = d.nbr + i;
     const size_t stride = (size_t)d.n;
@@ -127,9 +145,9 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(S
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
         if (q0 + u < cnt) {
           if (all_inner)
-            spp_pair_abp_lkw(&k, LAW, KIND, 0, &a, pi.x, pi.y, pi.z, pi.w, pg[u].x, pg[u].y, pg[u].z, pg[u].w);
+            stage_pair<LAW, KIND>(k, d, 0, &a, nbi, jg[u], pi, pg[u]);
           else
-            spp_pair_abp_lkw(&k, LAW, KIND, 1, &a, pi.x, pi.y, pi.z, pi.w, pg[u].x, pg[u].y, pg[u].z, pg[u].w);
+            stage_pair<LAW, KIND>(k, d, 1, &a, nbi, jg[u], pi, pg[u]);
         }
       }
     }
@@ -141,31 +159,32 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(S
     if (all_inner) {
       for (int q = 0; q < cnt; ++q) {
         const float4 pj = pn;
+        const int j = jn;
         if (q + 1 < cnt) {
           jn = __ldg(nb + (size_t)(q + 1) * stride);
           pn = __ldg(b.cur + jn);
         }
-        spp_pair_abp_lkw(&k, LAW, KIND, 0, &a, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
+        stage_pair<LAW, KIND>(k, d, 0, &a, nbi, j, pi, pj);
       }
     } else {
       for (int q = 0; q < cnt; ++q) {
         const float4 pj = pn;
+        const int j = jn;
         if (q + 1 < cnt) {
           jn = __ldg(nb + (size_t)(q + 1) * stride);
           pn = __ldg(b.cur + jn);
         }
-        spp_pair_abp_lkw(&k, LAW, KIND, 1, &a, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
+        stage_pair<LAW, KIND>(k, d, 1, &a, nbi, j, pi, pj);
       }
     }
 #endif
     if (LAW == SPP_FORCE_R12_TRUNC && a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
     float fx, fy, tau;
     int turns = 1;
-    uint32_t pid = 0;
-    if (KIND == SPP_KIND_BEADS) {
+    int chain_swimmer = 0;
+    if (BEADLIKE) {
       /* membrane beads add their ring forces; positions of the ring
        * neighbours come from the same stage state, found through id -> slot */
-      pid = d.id[i];
       float rfx = 0.0f, rfy = 0.0f;
       const int bead = pid < (uint32_t)k.n_beads;
       if (bead) {
@@ -179,7 +198,12 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(S
         }
         spp_ring_forces(&k, px, py, &rfx, &rfy);
       }
-      spp_bead_velocity(&k, !bead, &a, rfx, rfy, pi.z, pi.w, &fx, &fy, &tau);
+      if (KIND == SPP_KIND_CHAIN && !bead) {
+        chain_swimmer = 1;
+        spp_chain_velocity(&k, &a, pi.z, pi.w, pi.z, pi.w, &fx, &fy, &tau);
+      } else {
+        spp_bead_velocity(&k, !bead, &a, rfx, rfy, pi.z, pi.w, &fx, &fy, &tau);
+      }
       turns = !bead;
     } else {
       spp_abp_forces(&k, &a, pi.z, pi.w, &fx, &fy, &tau);
@@ -188,10 +212,10 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(S
     if (b.stage == 0) {
       if (!turns) {
         dth = 0.0f;
-      } else if (KIND == SPP_KIND_BEADS && k.tumble) {
+      } else if (BEADLIKE && k.tumble) {
         dth = spp_tumble_noise(&k, pid, d.ctl->step, d.tumble + pid);
       } else {
-        dth = spp_rot_noise(&k, KIND == SPP_KIND_BEADS ? pid : d.id[i], d.ctl->step);
+        dth = spp_rot_noise(&k, BEADLIKE ? pid : d.id[i], d.ctl->step);
       }
       if (b.nstages > 1) d.dth[i] = dth;
     } else {
@@ -199,6 +223,12 @@ __global__ void __launch_bounds__(SPP_BLOCK, SPP_STAGE_MIN_BLOCKS) k_abp_stage(S
     }
     const float4 p0 = (b.stage == 0) ? pi : d.pos[i];
     const float th0 = d.theta[i];
+    if (KIND == SPP_KIND_CHAIN && chain_swimmer && b.nstages == 1) {
+      /* Move() turns first and projects the force on the new heading */
+      float wc, ws;
+      spp_sincosf(spp_euler_theta(&k, th0, tau, dth), &ws, &wc);
+      spp_chain_velocity(&k, &a, pi.z, pi.w, wc, ws, &fx, &fy, &tau);
+    }
     float nx, ny, nt, nc, ns;
     int gx = 0, gy = 0;
     if (b.nstages == 1) {
@@ -355,6 +385,8 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
   SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_BEADS)
   SPP_STAGE_CASE(SPP_FORCE_HARMONIC, SPP_KIND_BEADS)
   SPP_STAGE_CASE(SPP_FORCE_NONE, SPP_KIND_BEADS)
+  SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_CHAIN)
+  SPP_STAGE_CASE(SPP_FORCE_NONE, SPP_KIND_CHAIN)
   {}
 #undef SPP_STAGE_CASE
   if (launches) *launches += 1;

@@ -53,7 +53,49 @@ typedef struct SppConsts {
   uint32_t tumble_u24;
   int32_t tumble_steps;
   float tumble_dth;
+  /* multi-bead swimmers (chain_nb > 1): bead a of a swimmer with heading v
+   * sits at v chain_off[a] from its centre; bead pairs involving a chain
+   * use R12 with chain_sigma / chain_rc2 / chain_c13 (the membrane constants
+   * above stay for bead-bead pairs); chain_reach2 bounds the centre distance
+   * of two bodies that have any bead pair within the cutoff */
+  int32_t chain_nb;
+  float chain_off[SPP_MAX_CHAIN_BEADS];
+  float chain_sigma, chain_rc2, chain_c13, chain_reach2;
+  float chain_f0;              /* F0 = v0 / m_parallel */
+  float chain_mperp, chain_dm; /* m_perpendicular, m_parallel - m_perpendicular */
+  float chain_k;               /* k_perpendicular */
+  float chain_torque0;
 } SppConsts;
+
+/* ActiveBrownianChain::Set_nb (shared/particle.h:856-876): {m_parallel,
+ * m_perpendicular, k_perpendicular} of a swimmer of nb beads. */
+static inline void spp_chain_mobility_d(int nb, double sep, double sigma, double* m) {
+  if (nb <= 1) {
+    m[0] = 0.5; m[1] = 0.5; m[2] = 1.0;
+    return;
+  }
+  const double ar = 1.0 / ((sep * (nb - 1) / sigma) + 1.0);
+  const double e2 = 1.0 - ar * ar;
+  const double e = sqrt(e2);
+  const double lg = log((1.0 + e) / (1.0 - e));
+  m[0] = 1.0;
+  m[1] = 0.5 * (2.0 * e + (3.0 * e2 - 1.0) * lg) / ((1.0 + e2) * lg - 2.0 * e);
+  m[2] = 6.0 / (1.0 + ar * ar) / sigma / sigma;
+}
+
+/* Largest centre distance at which two bodies still interact: the pair
+ * cutoff, alignment and push radii, and for chains the bead cutoff plus the
+ * two half-lengths (nb - 1) separation / 2. */
+static inline double spp_interaction_range(const SppParams* p) {
+  double rc = p->model == SPP_MODEL_BEADS ? 0.0 : p->r_align;
+  if (p->force_law != SPP_FORCE_NONE && p->r_rep > rc) rc = p->r_rep;
+  if (p->model == SPP_MODEL_VICSEK_REF_VECTOR && p->r_push > rc) rc = p->r_push;
+  if (p->model == SPP_MODEL_BEADS && p->chain_beads > 1 && p->force_law != SPP_FORCE_NONE) {
+    const double reach = (p->chain_beads - 1) * p->bead_separation + p->r_chain;
+    if (reach > rc) rc = reach;
+  }
+  return rc;
+}
 
 /* Host-side: round the double parameters to the kernels' floats. */
 static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
@@ -91,9 +133,7 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
   k->r_push = (float)p->r_push;
   k->rpush2 = (float)(p->r_push * p->r_push);
   {
-    double rc = p->model == SPP_MODEL_BEADS ? 0.0 : p->r_align;
-    if (p->force_law != SPP_FORCE_NONE && p->r_rep > rc) rc = p->r_rep;
-    if (p->model == SPP_MODEL_VICSEK_REF_VECTOR && p->r_push > rc) rc = p->r_push;
+    double rc = spp_interaction_range(p);
     double rl = rc + (p->skin > 0 ? p->skin : 0.0);
     k->rlist = (float)rl;
     k->rlist2 = (float)(rl * rl);
@@ -121,7 +161,34 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
       ++c;
     }
     k->tumble_steps = c;
-    k->tumble_dth = (float)((p->k_perp * p->dt) * p->tumble_torque);
+  }
+  k->chain_nb = (p->model == SPP_MODEL_BEADS && p->chain_beads > 1) ? p->chain_beads : 1;
+  for (int a = 0; a < SPP_MAX_CHAIN_BEADS; ++a)
+    k->chain_off[a] = a < k->chain_nb ? (float)(p->bead_separation * ((1 - k->chain_nb) / 2.0 + a)) : 0.0f;
+  {
+    double m[3];
+    spp_chain_mobility_d(k->chain_nb, p->bead_separation, p->sigma_chain, m);
+    const int chain = k->chain_nb > 1;
+    k->chain_sigma = chain ? (float)p->sigma_chain : 0.0f;
+    k->chain_rc2 = chain && p->force_law != SPP_FORCE_NONE ? (float)(p->r_chain * p->r_chain) : 0.0f;
+    {
+      float q = chain && p->r_chain > 0 ? k->chain_sigma / (float)p->r_chain : 0.0f;
+      float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
+      k->chain_c13 = (q8 * q4) * q;
+    }
+    /* 1e-3 above the exact bound: a pure pre-test, never tighter than the
+     * FP32 bead separations it guards */
+    const double reach = ((k->chain_nb - 1) * p->bead_separation + p->r_chain) * 1.001;
+    k->chain_reach2 = chain ? (float)(reach * reach) : 0.0f;
+    k->chain_f0 = chain ? (float)(p->v0 / m[0]) : 0.0f;
+    k->chain_mperp = chain ? (float)m[1] : 0.0f;
+    k->chain_dm = chain ? (float)(m[0] - m[1]) : 0.0f;
+    k->chain_k = chain ? (float)m[2] : 0.0f;
+    k->chain_torque0 = chain ? (float)p->torque0 : 0.0f;
+    /* RTPChain::Noise_Gen turns by k_perpendicular dt torque_tumble: the
+     * swimmers' own k_perpendicular */
+    if (k->tumble)
+      k->tumble_dth = (float)(((chain ? m[2] : p->k_perp) * p->dt) * p->tumble_torque);
   }
 }
 
@@ -169,9 +236,10 @@ SPP_HD void spp_accf_zero(SppAccF* a) { a->fx = 0.0f; a->fy = 0.0f; a->tq = 0.0f
 #define SPP_KIND_CONT 1         /* (1 - alpha)/pi sin(...)                  */
 #define SPP_KIND_CONT_ALPHA 2   /* ... - alpha (dr x v_i) / (pi d)          */
 #define SPP_KIND_BEADS 3        /* repulsion only (ActiveBrownianChain nb = 1) */
+#define SPP_KIND_CHAIN 4        /* beads with multi-bead swimmers (nb > 1) */
 
 SPP_HD int spp_pair_kind(const SppConsts* k) {
-  if (k->model == SPP_MODEL_BEADS) return SPP_KIND_BEADS;
+  if (k->model == SPP_MODEL_BEADS) return k->chain_nb > 1 ? SPP_KIND_CHAIN : SPP_KIND_BEADS;
   if (k->model != SPP_MODEL_CONTINUOUS) return SPP_KIND_ABP;
   return k->alpha_over_pi != 0.0f ? SPP_KIND_CONT_ALPHA : SPP_KIND_CONT;
 }
@@ -196,7 +264,7 @@ SPP_HD void spp_pair_abp_lkw(const SppConsts* k, int law, int kind, int wrap, Sp
     d2 = fmaf(dx, dx, dy * dy);
   }
   const int in_rep = (law != SPP_FORCE_NONE) && (d2 < k->rrep2) && (d2 > 0.0f);
-  const int in_al = (kind != SPP_KIND_BEADS) && d2 < k->ral2;
+  const int in_al = (kind != SPP_KIND_BEADS && kind != SPP_KIND_CHAIN) && d2 < k->ral2;
   if (!(in_rep || in_al)) return;
   float r = 0.0f;
   if (in_rep || (kind == SPP_KIND_CONT_ALPHA && in_al && d2 > 0.0f)) r = spp_rsqrtf(d2);
@@ -229,6 +297,81 @@ SPP_HD void spp_pair_abp_lkw(const SppConsts* k, int law, int kind, int wrap, Sp
 SPP_HD void spp_pair_abp(const SppConsts* k, SppAccF* a, float xi, float yi, float ci, float si,
                          float xj, float yj, float cj, float sj) {
   spp_pair_abp_lkw(k, k->force_law, spp_pair_kind(k), 1, a, xi, yi, ci, si, xj, yj, cj, sj);
+}
+
+/* ActiveBrownianChain::Interact (shared/particle.h:964-1012) as received by
+ * body i from body j; nbi, nbj are their bead counts (1 for membrane beads
+ * and single-bead swimmers).  Two single beads interact by the membrane law
+ * (sigma_m, repulsion_radius_m: the bead kind of spp_pair_abp_lkw).
+ * Otherwise each bead pair (a, b), a outer, at s_i = v_i off[a] and
+ * s_j = v_j off[b] from the centres, whose separation dr = (dr0 + s_i) - s_j
+ * is inside the chain cutoff adds the R12 force F (sigma_p,
+ * repulsion_radius) to i and the lever-arm torque s_i x F = s_i.x F.y -
+ * s_i.y F.x.  A single bead sits at its centre (s = 0): it neither shifts
+ * the separation nor receives torque. */
+SPP_HD void spp_pair_chain(const SppConsts* k, int law, int wrap, SppAccF* a, int nbi, int nbj,
+                           float xi, float yi, float ci, float si, float xj, float yj, float cj,
+                           float sj) {
+  if (nbi == 1 && nbj == 1) {
+    spp_pair_abp_lkw(k, law, SPP_KIND_BEADS, wrap, a, xi, yi, ci, si, xj, yj, cj, sj);
+    return;
+  }
+  if (law == SPP_FORCE_NONE) return;
+  float dx0, dy0, d02;
+  if (wrap) {
+    d02 = spp_sep(k, xi, yi, xj, yj, &dx0, &dy0);
+  } else {
+    dx0 = xi - xj;
+    dy0 = yi - yj;
+    d02 = fmaf(dx0, dx0, dy0 * dy0);
+  }
+  if (!(d02 < k->chain_reach2)) return;
+  for (int p = 0; p < nbi; ++p) {
+    float stx = 0.0f, sty = 0.0f, ex = dx0, ey = dy0;
+    if (nbi > 1) {
+      stx = ci * k->chain_off[p];
+      sty = si * k->chain_off[p];
+      ex = dx0 + stx;
+      ey = dy0 + sty;
+    }
+    for (int q = 0; q < nbj; ++q) {
+      float dx = ex, dy = ey;
+      if (nbj > 1) {
+        dx = ex - cj * k->chain_off[q];
+        dy = ey - sj * k->chain_off[q];
+      }
+      const float d2 = fmaf(dx, dx, dy * dy);
+      if (!(d2 < k->chain_rc2 && d2 > 0.0f)) continue;
+      const float r = spp_rsqrtf(d2);
+      const float u = k->chain_sigma * r;
+      const float u2 = u * u, u4 = u2 * u2, u8 = u4 * u4;
+      const float u13 = (u8 * u4) * u;
+      float t = (k->k_rep * (u13 - k->chain_c13)) * r;
+      if (!(fabsf(t * dx) < SPP_FX_RANGE && fabsf(t * dy) < SPP_FX_RANGE)) { a->ovf = 1; t = 0.0f; }
+      const float Fx = t * dx, Fy = t * dy;
+      a->fx = a->fx + Fx;
+      a->fy = a->fy + Fy;
+      if (nbi > 1) a->tq = a->tq + (stx * Fy - sty * Fx);
+    }
+  }
+}
+
+/* Velocity and angular velocity of a chain swimmer (ActiveBrownianChain::
+ * Reset / Move*, shared/particle.h:878-962): the force f = F0 v + F, with v
+ * = (ci, si) the heading the forces were evaluated at, moves it at
+ *   m_perp f + (m_par - m_perp) (f . w) w
+ * where w is the heading of the position update (v itself in the
+ * Runge-Kutta stages; Move() turns first and projects on the new heading),
+ * and it turns at k_perp (torque0 + lever-arm torques). */
+SPP_HD void spp_chain_velocity(const SppConsts* k, const SppAccF* a, float ci, float si, float wc,
+                               float ws, float* vx, float* vy, float* om) {
+  const float ftx = k->chain_f0 * ci + a->fx;
+  const float fty = k->chain_f0 * si + a->fy;
+  const float fw = ftx * wc + fty * ws;
+  const float g = k->chain_dm * fw;
+  *vx = k->chain_mperp * ftx + g * wc;
+  *vy = k->chain_mperp * fty + g * ws;
+  *om = k->chain_k * (k->chain_torque0 + a->tq);
 }
 
 /* Self-propulsion plus received force, and the torque (RepulsiveParticle::
@@ -288,10 +431,13 @@ SPP_HD void spp_stage_update(float h, float frac_noise, float x0, float y0, floa
 
 /* Euler move (RepulsiveParticle::Move, shared/particle.h:571-587): theta is
  * not wrapped there. */
+SPP_HD float spp_euler_theta(const SppConsts* k, float th0, float tau, float dth) {
+  return fmaf(k->dt, tau, th0) + dth;
+}
 SPP_HD void spp_euler_update(float x0, float y0, float th0, float fx, float fy, float tau, float dth,
                              const SppConsts* k, float* x, float* y, float* th, float* c, float* s,
                              int* imgx, int* imgy) {
-  float t = fmaf(k->dt, tau, th0) + dth;
+  float t = spp_euler_theta(k, th0, tau, dth);
   spp_sincosf(t, s, c);
   *th = t;
   *x = spp_wrap_coord_f(fmaf(fx, k->dt, x0), k->L, k->L2, imgx);

@@ -41,6 +41,27 @@ def rtp_case(integ):
     return p, x.astype(np.float64), y.astype(np.float64), th.astype(np.float64)
 
 
+def chain_case(integ):
+    """Free chiral trimers (ActiveBrownianChain, nb = 3) packed closely
+    enough to collide."""
+    p = configs.chain_config(n=144, chain_beads=3, integrator=integ, seed=5, spacing=1.7)
+    p.torque0 = 0.3
+    x, y, th = configs.chain_state(p)
+    return p, x.astype(np.float64), y.astype(np.float64), th.astype(np.float64)
+
+
+def dimer_case(integ):
+    """Dimer swimmers (nb = 2) inside ring membranes."""
+    p = configs.vesicle_config(n_rings=4, ring_size=40, swimmers_per_ring=8, L=20.0,
+                               integrator=integ, seed=9)
+    x, y, th = configs.vesicle_state(p)
+    p.sigma_rep, p.r_rep, p.k_rep = 0.5, 0.55, 1.0
+    p.bond_rest, p.k_bond, p.kappa_bend = 0.55, 30.0, 0.0
+    p.Dr, p.dt = 0.2, 0.002
+    p.chain_beads, p.bead_separation, p.sigma_chain, p.r_chain = 2, 0.5, 0.5, 0.55
+    return p, x.astype(np.float64), y.astype(np.float64), th.astype(np.float64)
+
+
 def cases():
     out = []
     for integ, name in ((abi.INT_EULER, "euler"), (abi.INT_RK2, "rk2"), (abi.INT_RK4, "rk4")):
@@ -66,6 +87,9 @@ def cases():
         out.append((name, p, x.astype(np.float64), y.astype(np.float64), th.astype(np.float64), 60))
     for integ, name in ((abi.INT_EULER, "rtp_euler"), (abi.INT_RK2, "rtp_rk2")):
         out.append((name, *rtp_case(integ), 80))
+    for integ, name in ((abi.INT_EULER, "chains_euler"), (abi.INT_RK2, "chains_rk2")):
+        out.append((name, *chain_case(integ), 150))
+    out.append(("dimers_rk2", *dimer_case(abi.INT_RK2), 100))
     p = configs.reference_defaults(abi.MODEL_CONTINUOUS)
     p.n, p.L, p.Dr, p.dt, p.v0, p.seed = 1024, 16.0, 0.05, 0.01, 0.5, 11
     x, y, th = configs.random_state(p.n, p.L, seed=3)

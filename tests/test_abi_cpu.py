@@ -5,6 +5,7 @@ import ctypes as C
 import re
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 from spp_gb300 import abi, build
@@ -71,3 +72,40 @@ def test_create_without_gpu_reports_status(lib):
     rc = lib.spp_create(C.byref(p.replace(n=100, L=16.0)), C.byref(h))
     assert rc in (2, 3)  # SPP_ERR_ALLOC / SPP_ERR_CUDA
     assert not h.value
+
+
+def test_chain_mobility_entry_point(lib):
+    """spp_chain_mobility against Set_nb (shared/particle.h:856-876),
+    written out here from its formulas."""
+    m = np.zeros(3)
+    ptr = m.ctypes.data_as(C.POINTER(C.c_double))
+    assert lib.spp_chain_mobility(1, 1.0, 1.0, ptr) == 0
+    assert list(m) == [0.5, 0.5, 1.0]
+    for nb, sep, sig in ((2, 1.0, 1.0), (3, 0.5, 0.5), (8, 0.3, 1.2)):
+        assert lib.spp_chain_mobility(nb, sep, sig, ptr) == 0
+        ar = 1 / ((sep * (nb - 1) / sig) + 1)
+        e2 = 1 - ar * ar
+        e = np.sqrt(e2)
+        Lg = np.log((1 + e) / (1 - e))
+        assert m[0] == 1.0
+        assert abs(m[1] - 0.5 * (2 * e + (3 * e2 - 1) * Lg) / ((1 + e2) * Lg - 2 * e)) < 1e-15
+        assert abs(m[2] - 6 / (1 + ar * ar) / sig / sig) < 1e-15
+        assert 0.5 * m[0] < m[1] < m[0]   # a rod moves more easily along its axis
+    assert lib.spp_chain_mobility(9, 1.0, 1.0, ptr) != 0
+    assert lib.spp_chain_mobility(2, 0.0, 1.0, ptr) != 0
+
+
+def test_create_rejects_bad_chains_without_touching_gpu(lib):
+    p = abi.SppParams()
+    lib.spp_params_init(C.byref(p), abi.MODEL_BEADS)
+    assert (p.chain_beads, p.bead_separation, p.sigma_chain, p.r_chain) == (1, 1.0, 1.0, 1.1)
+    p.n = 64
+    h = C.c_void_p()
+    assert lib.spp_create(C.byref(p.replace(chain_beads=9)), C.byref(h)) == 1
+    assert lib.spp_create(C.byref(p.replace(chain_beads=-1)), C.byref(h)) == 1
+    assert lib.spp_create(C.byref(p.replace(chain_beads=2, bead_separation=0.0)), C.byref(h)) == 1
+    assert lib.spp_create(C.byref(p.replace(chain_beads=2, force_law=abi.FORCE_HARMONIC)), C.byref(h)) == 1
+    q = abi.SppParams()
+    lib.spp_params_init(C.byref(q), abi.MODEL_ABP)
+    assert lib.spp_create(C.byref(q.replace(n=64, chain_beads=2)), C.byref(h)) == 6
+    assert b"SPP_MODEL_BEADS" in lib.spp_last_error()

@@ -77,6 +77,31 @@ def test_checkpoint_file_format(tmp_path):
              img_x=np.ones(8, np.int32), img_y=np.zeros(8, np.int32), step=np.int64(77))
     q, snap = checkpoint.load(path)
     assert bytes(q) == raw and snap.step == 77 and np.array_equal(snap.y, -x)
+    # a record of the layout before the chain fields (struct_size 240)
+    old = bytearray(raw[:240])
+    old[:4] = (240).to_bytes(4, "little")
+    np.savez(path, format=checkpoint.FORMAT, params=np.frombuffer(bytes(old), np.uint8), x=x, y=-x,
+             theta=x / 8, img_x=np.ones(8, np.int32), img_y=np.zeros(8, np.int32), step=np.int64(5))
+    q, _ = checkpoint.load(path)
+    assert q.struct_size == C.sizeof(abi.SppParams) and q.chain_beads == 0 and q.L == p.L
+    old[:4] = (200).to_bytes(4, "little")
+    np.savez(path, format=checkpoint.FORMAT, params=np.frombuffer(bytes(old), np.uint8), x=x, y=-x,
+             theta=x / 8, img_x=np.ones(8, np.int32), img_y=np.zeros(8, np.int32), step=np.int64(5))
+    with pytest.raises(ValueError):
+        checkpoint.load(path)
     np.savez(path, format=99, params=np.frombuffer(raw, np.uint8))
     with pytest.raises(ValueError):
         checkpoint.load(path)
+
+
+def test_chain_frames_carry_chain_length():
+    """The header's nb is the first swimmer's chain length (parallel/box.h:485)."""
+    p = configs.chain_config(n=9, chain_beads=3)
+    x, y, th = configs.chain_state(p)
+    z = np.zeros(9, np.int32)
+    f = binfile.read_frames(binfile.state_frame(p, 0.5, x, y, th, z, z))[0]
+    assert f.nb == 3 and len(f.x) == 9 and len(f.mx) == 0
+    q = configs.vesicle_config(n_rings=2, ring_size=40, swimmers_per_ring=1, L=20.0)
+    xv, yv, tv = configs.vesicle_state(q)
+    z = np.zeros(q.n, np.int32)
+    assert binfile.read_frames(binfile.state_frame(q, 0.0, xv, yv, tv, z, z))[0].nb == 1

@@ -265,3 +265,34 @@ def test_run_and_tumble_fraction_of_time_tumbling(gpu_lib):
     # turns for K steps (start step included) and resets on the next
     expect = K / (K + 1 + 1 / rate_dt - 1)
     assert abs(turning.mean() - expect) < 0.02, (turning.mean(), expect)
+
+
+@pytest.mark.parametrize("integ", [abi.INT_EULER, abi.INT_RK2, abi.INT_RK4])
+def test_chains_bitexact_vs_mirror(gpu_lib, integ):
+    """Free chiral trimers (ActiveBrownianChain with nb = 3): the bead-pair
+    R12 forces and lever-arm torques summed in list order, the anisotropic
+    mobility of Set_nb, and Move()'s projection on the turned heading."""
+    p = configs.chain_config(n=4096, chain_beads=3, integrator=integ, seed=6, spacing=1.7)
+    p.torque0 = 0.3
+    x, y, th = configs.chain_state(p)
+    gpu, obs = run_gpu(p, x, y, th, 300)
+    ref = O.run32(p, O.State32(x, y, th), 300)
+    assert_bitexact(gpu, ref)
+    assert obs.n_rebuilds >= 1
+
+
+@pytest.mark.parametrize("tumble", [False, True])
+def test_dimers_in_vesicles_bitexact_vs_mirror(gpu_lib, tumble):
+    """Dimer swimmers (nb = 2, the default chain length of the reference's
+    membrane driver) inside ring membranes: membrane-membrane pairs by the
+    membrane law, every pair with a dimer by the chain law; optionally run
+    and tumble with the dimers' own k_perpendicular."""
+    p = configs.vesicle_config(n_rings=16, ring_size=64, swimmers_per_ring=16, L=48.0, seed=9)
+    x, y, th = configs.vesicle_state(p)
+    p.chain_beads, p.bead_separation, p.sigma_chain, p.r_chain = 2, 0.5, 0.5, 0.55
+    if tumble:
+        p.rot_noise = abi.NOISE_TUMBLE
+        p.tumble_rate, p.tumble_time, p.tumble_torque = 20.0, 0.03, 3.0
+    gpu, _ = run_gpu(p, x, y, th, 200)
+    ref = O.run32(p, O.State32(x, y, th), 200)
+    assert_bitexact(gpu, ref)

@@ -127,3 +127,53 @@ def test_tumble_schedule_constants():
         q = p.copy()
         q.tumble_time, q.dt = t_tumble, dt
         assert O.tumble_steps(q) == c
+
+
+def _chains(integ, n=144):
+    p = configs.chain_config(n=n, chain_beads=3, integrator=integ, seed=5, spacing=1.7)
+    p.torque0 = 0.3
+    x, y, th = configs.chain_state(p)
+    return p, x, y, th
+
+
+@pytest.mark.parametrize("integ", [abi.INT_EULER, abi.INT_RK2, abi.INT_RK4])
+def test_mirror_tracks_fp64_chains(integ):
+    """Interacting chiral trimers: the FP32 kernel arithmetic stays within
+    FP32 rounding of the FP64 restatement of ActiveBrownianChain."""
+    p, x, y, th = _chains(integ)
+    s32 = O.State32(x, y, th)
+    O.run32(p, s32, 200)
+    a = O.State64(x.astype(np.float64), y.astype(np.float64), th.astype(np.float64))
+    O.run64(p, a, 200)
+    xu = s32.x.astype(np.float64) + 2 * p.L * s32.ix
+    yu = s32.y.astype(np.float64) + 2 * p.L * s32.iy
+    assert np.abs(xu - a.xu).max() < 1e-4 and np.abs(yu - a.yu).max() < 1e-4
+    d = np.abs(((s32.th.astype(np.float64) - a.th) + np.pi) % (2 * np.pi) - np.pi)
+    assert d.max() < 1e-3
+    # the chains did interact: without forces the paths differ
+    q = p.copy()
+    q.force_law = abi.FORCE_NONE
+    b = O.State64(x.astype(np.float64), y.astype(np.float64), th.astype(np.float64))
+    O.run64(q, b, 200)
+    assert np.hypot(a.xu - b.xu, a.yu - b.yu).max() > 1e-2
+
+
+def test_free_chain_speed_and_turn_rate():
+    """Without noise or neighbours a chain swims at v0 = m_parallel F0 along
+    its heading and turns at k_perpendicular torque0 (Set_R0: the circle of
+    radius R0 = v0 / (k torque0))."""
+    p, x, y, th = _chains(abi.INT_RK4, n=16)
+    p.force_law, p.Dr, p.torque0 = abi.FORCE_NONE, 0.0, 0.25
+    ar = 1 / ((p.bead_separation * 2 / p.sigma_chain) + 1)
+    k_perp = 6 / (1 + ar * ar) / p.sigma_chain ** 2   # Set_nb, particle.h:874
+    s = O.State64(x.astype(np.float64), y.astype(np.float64), th.astype(np.float64))
+    th0, x0, y0 = s.th.copy(), s.xu.copy(), s.yu.copy()
+    steps = 500
+    O.run64(p, s, steps)
+    T = steps * p.dt
+    w = k_perp * p.torque0
+    off = ((s.th - th0 - w * T) + np.pi) % (2 * np.pi) - np.pi
+    assert np.abs(off).max() < 1e-9
+    # chord of the circle of radius v0 / w
+    chord = np.hypot(s.xu - x0, s.yu - y0)
+    assert np.abs(chord - 2 * p.v0 / w * np.sin(w * T / 2)).max() < 1e-9

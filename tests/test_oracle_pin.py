@@ -34,7 +34,8 @@ def max_diff(a, b):
 
 @pytest.mark.parametrize("name", ["repulsive_euler", "repulsive_rk2", "repulsive_rk4",
                                   "vicsek_angle", "vicsek_vector", "continuous_euler",
-                                  "beads_euler", "beads_rk2", "rtp_euler", "rtp_rk2"])
+                                  "beads_euler", "beads_rk2", "rtp_euler", "rtp_rk2",
+                                  "chains_euler", "chains_rk2", "dimers_rk2"])
 def test_oracle_matches_golden(name):
     z, meta = load_golden()
     p = params_from(meta[name]["params"])
@@ -44,7 +45,7 @@ def test_oracle_matches_golden(name):
     out = z[f"{name}/out"]
     # FP64 sums in a different pair order; chaotic Vicsek amplifies last bits
     tol = 1e-9
-    nb = p.n_rings * p.ring_size if name.startswith(("beads", "rtp")) else 0
+    nb = p.n_rings * p.ring_size if name.startswith(("beads", "rtp", "dimers")) else 0
     for k, arr in enumerate([s.x, s.y, s.th, s.xu, s.yu]):
         if k == 2:  # membrane beads: the reference diffuses their irrelevant heading
             assert max_diff(arr[nb:], out[k][nb:]) < tol, (name, k)
@@ -141,6 +142,26 @@ def test_oracle_matches_reference_rtp(integ):
     assert max_diff(a.th[nb:], b.th[nb:]) < 1e-11
     # tumbles happened: headings moved by whole tumble turns
     assert max_diff(a.th[nb:], th0[nb:]) > 0.1
+
+
+@pytest.mark.parametrize("integ", [abi.INT_EULER, abi.INT_RK2])
+@pytest.mark.parametrize("case", ["chains", "dimers"])
+def test_oracle_matches_reference_chains(integ, case):
+    """ActiveBrownianChain with nb > 1 (shared/particle.h:856-1012): bead-pair
+    forces with lever-arm torques, Set_nb mobilities, Move()'s projection on
+    the turned heading; free chiral trimers and dimers inside membranes."""
+    _ref_or_skip()
+    import sys
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    from make_golden import chain_case, dimer_case
+    p, x, y, th = (chain_case if case == "chains" else dimer_case)(integ)
+    a = O.State64(x, y, th)
+    b = a.copy()
+    O.run64(p, a, 300)
+    O.run64(p, b, 300, fn="ref")
+    nb = p.n_rings * p.ring_size
+    assert max_diff(a.xu, b.xu) < 1e-11 and max_diff(a.yu, b.yu) < 1e-11
+    assert max_diff(a.th[nb:], b.th[nb:]) < 1e-11
 
 
 def test_force_laws_match_reference():
