@@ -63,13 +63,43 @@ def dist_env():
 # ---------------------------------------------------------------------------
 # CPU baseline: the FP64 restatement (oracle/spp_oracle64.c) on host cores.
 # ---------------------------------------------------------------------------
-def _cpu_worker(conn, n, L, seed):
-    sys.path.insert(0, str(ROOT))
+def _cpu_workload(workload, seed):
+    """(params, FP64 state, advance(k, step)) of one full-size CPU replica."""
+    import numpy as np
     from oracle import oracle as O
     from spp_gb300 import configs
-    p = configs.abp_config(n=n, L=L, seed=seed)
-    x, y, th = configs.random_state(n, L, seed=seed)
+    if workload == "abp":
+        p = configs.abp_config(n=N_FULL, L=L_FULL, seed=seed)
+        x, y, th = configs.random_state(p.n, p.L, seed=seed)
+    elif workload == "vicsek":
+        p = configs.vicsek_config(seed=seed)
+        x, y, th = configs.random_state(p.n, p.L, seed=seed)
+    elif workload == "vesicles":
+        p = configs.vesicle_config(seed=seed)
+        x, y, th = configs.vesicle_state(p)
+    elif workload == "lyapunov":
+        p = configs.lyapunov_config(seed=seed)
+        x, y, th = configs.random_state(p.n, p.L, seed=seed)
+    else:
+        raise ValueError(workload)
     s = O.State64(x, y, th)
+    if workload == "lyapunov":
+        # the Benettin clone method of the reference (parallel/lyapunovbox.h:
+        # 128-194): the base system and k = 8 perturbed clones, renormalised
+        # every 10 steps
+        V = np.random.default_rng(seed).standard_normal(3 * p.n * 8)
+
+        def advance(k, step):
+            O.lyap_clone64(p, s, V, max(1, k // 10), 10)
+    else:
+        def advance(k, step):
+            O.run64(p, s, k, step0=step)
+    return p, advance
+
+
+def _cpu_worker(conn, workload, seed):
+    sys.path.insert(0, str(ROOT))
+    _, advance = _cpu_workload(workload, seed)
     step = 0
     conn.send("ready")
     while True:
@@ -78,7 +108,7 @@ def _cpu_worker(conn, n, L, seed):
             break
         k = int(msg)
         t0 = time.perf_counter()
-        O.run64(p, s, k, step0=step)
+        advance(k, step)
         step += k
         conn.send(time.perf_counter() - t0)
 
@@ -86,18 +116,17 @@ def _cpu_worker(conn, n, L, seed):
 class CpuPool:
     """One process per host core, each holding a full-size replica."""
 
-    def __init__(self, cores, n=N_FULL, L=L_FULL):
+    def __init__(self, cores, workload="abp"):
         ctx = mp.get_context("spawn")
         self.procs, self.conns = [], []
         for r in range(cores):
             a, b = ctx.Pipe()
-            pr = ctx.Process(target=_cpu_worker, args=(b, n, L, 1000 + r), daemon=True)
+            pr = ctx.Process(target=_cpu_worker, args=(b, workload, 1000 + r), daemon=True)
             pr.start()
             self.procs.append(pr)
             self.conns.append(a)
         for c in self.conns:
             assert c.recv() == "ready"
-        self.n = n
 
     def step(self, k):
         t0 = time.perf_counter()
@@ -137,6 +166,31 @@ def cpu_baseline(sim_steps=2, cores=None):
             "sample": f"FP64 restatement of the reference step (oracle/spp_oracle64.c), "
                       f"{cores} concurrent single-thread replicas x N=1,048,576 x {sim_steps} RK2 steps, "
                       f"{wall:.1f} s wall"}
+
+
+# bounded CPU samples of the other configurations (steps per replica)
+CPU_SAMPLE_STEPS = {"vicsek": 1000, "vesicles": 10, "lyapunov": 20}
+
+
+def cpu_baseline_workload(workload, unit, cores=None):
+    """The FP64 restatement of a configuration on every host core (one
+    full-size replica per core), over CPU_SAMPLE_STEPS steps."""
+    cores = cores or cpu_cores()
+    k = CPU_SAMPLE_STEPS[workload]
+    p, _ = _cpu_workload(workload, 0)
+    pool = CpuPool(cores, workload)
+    try:
+        pool.step(min(k, 10))  # warm-up
+        wall = pool.step(k)
+    finally:
+        pool.close()
+    what = {"vicsek": "plain Vicsek steps", "vesicles": "RK4 steps of the vesicle system",
+            "lyapunov": "RK4 steps of the base system and 8 clones (Benettin clone method, "
+                        "oracle/spp_oracle64.c orc64_lyap_clone) from the disordered initial state "
+                        "(shorter neighbour lists than the GPU's flocked window)"}[workload]
+    return {"value": cores * p.n * k / wall, "unit": unit, "cores": cores, "kind": "port",
+            "sample": f"FP64 restatement (oracle/spp_oracle64.c), {cores} concurrent single-thread "
+                      f"replicas x N={p.n:,} x {k} {what}, {wall:.1f} s wall"}
 
 
 # ---------------------------------------------------------------------------
@@ -296,6 +350,14 @@ def run_ours(args):
         for _ in range(args.warmup):
             s.step(S)
         s.sync()
+        # the state entering the timed region: the end-to-end leg replays the
+        # same trajectory through host buffers
+        def pinned_state():
+            return tuple(torch.empty(n, dtype=dt).pin_memory().numpy()
+                         for dt in (torch.float32, torch.float32, torch.float32, torch.int32, torch.int32))
+        buf_in, buf_out = pinned_state(), pinned_state()
+        s.download(out=buf_in)
+        step_at = s.step0 + int(s.observables().step)
         launches0 = s.kernel_launches()
         if dist:
             dist.barrier()
@@ -324,17 +386,14 @@ def run_ours(args):
         rebuild_avg_ms = prof.rebuild_ms / max(1, prof.rebuilds)
 
         # end to end through the C ABI with host buffers (pinned), copies inside:
-        # the host holds the trajectory between chunks of S steps, each chunk
-        # uploads the state the previous one downloaded (starting from the
-        # state the timed region reached, so the work per step is the same)
-        def pinned_state():
-            return tuple(torch.empty(n, dtype=dt).pin_memory().numpy()
-                         for dt in (torch.float32, torch.float32, torch.float32, torch.int32, torch.int32))
-        buf_in, buf_out = pinned_state(), pinned_state()
-        s.download(out=buf_in)
-        step_at = s.step0 + int(s.observables().step)
+        # the host holds the trajectory between chunks of S steps and each
+        # chunk uploads the state the previous one downloaded, starting from
+        # the state that entered the timed region; the steps are bit-exact, so
+        # this is the timed region's own trajectory, chunk for chunk
         e2e_times = []
-        for k in range(0 if args.no_e2e else max(3, min(args.steps, 10))):
+        for k in range(0 if args.no_e2e else args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
             t0 = time.perf_counter()
             s.upload(buf_in[0], buf_in[1], buf_in[2], step0=step_at, img_x=buf_in[3], img_y=buf_in[4])
             s.step(S)
@@ -342,7 +401,7 @@ def run_ours(args):
             e2e_times.append(time.perf_counter() - t0)
             buf_in, buf_out = buf_out, buf_in
             step_at += S
-        e2e_value = n * S / statistics.median(e2e_times) if e2e_times else None
+        e2e_value = n * S * len(e2e_times) / sum(e2e_times) if e2e_times else None
     value = ws * n * S * args.steps / (elapsed_ms / 1e3)
     peak, peak_kind = measured_hbm_peak()
     achieved = ALG_BYTES_PER_PARTICLE_STEP / 2 * n / (stage_avg_ms / 1e3) / 1e9
@@ -371,8 +430,8 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 20 * n,
                 "d2h_bytes_per_step": 20 * n,
                 "path": "spp_upload_state (pinned host: x, y, theta, image counters) + spp_step(200) + "
-                        "spp_download_state (pinned host); each chunk continues from the state the "
-                        "previous one downloaded"},
+                        "spp_download_state (pinned host) per bench step, host wall clock; the timed "
+                        "region's trajectory replayed chunk by chunk from its entry state"},
         "observables": {"polarization": obs.polarization, "rebuilds": obs.n_rebuilds,
                         "max_neighbors": obs.max_neighbors, "list_capacity": obs.list_capacity},
     }
@@ -528,6 +587,8 @@ def other_workload(args):
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                          "note": "effective bandwidth of the whole step; working set L2-resident"}}
     line.update(extra)
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_workload(w, unit)
     print(json.dumps(line), flush=True)
 
 
