@@ -66,6 +66,7 @@ struct SppSystem {
   int64_t step0 = 0;
   bool uploaded = false;
   bool use_graphs = true;
+  bool small_vicsek = false;     /* whole steps in one block (k_vicsek_small) */
   float* stage_x = nullptr;      /* staging for uploads/downloads */
   float* stage_y = nullptr;
   float* stage_t = nullptr;
@@ -201,6 +202,12 @@ int enqueue_rebuild(SppSystem* s, cudaStream_t st, int64_t* launches) {
 
 /* One step of the model, enqueued on st (stream or capture). */
 int enqueue_step(SppSystem* s, cudaStream_t st, bool capture, int64_t* launches) {
+  if (!s->uses_list && s->small_vicsek) {
+    if (launch_vicsek_small(s->k, s->d, 1, st, launches) != 0)
+      return fail(SPP_ERR_CUDA, "k_vicsek_small: shared memory attribute refused");
+    CUDA_TRY(cudaGetLastError());
+    return SPP_OK;
+  }
   if (!s->uses_list) {
     CUDA_TRY(cudaMemsetAsync(s->d.cell_count, 0, sizeof(uint32_t) * s->d.n_keys, st));
     launch_bin_count(s->k, s->d, st, launches);
@@ -270,6 +277,17 @@ int get_graph(SppSystem* s, int nsteps, cudaGraphExec_t* out) {
 }
 
 int run_steps(SppSystem* s, int64_t nsteps) {
+  if (s->small_vicsek) {
+    /* one launch per call runs every step */
+    while (nsteps > 0) {
+      const int chunk = nsteps > (1 << 20) ? (1 << 20) : (int)nsteps;
+      if (launch_vicsek_small(s->k, s->d, chunk, s->stream, &s->host_launches) != 0)
+        return fail(SPP_ERR_CUDA, "k_vicsek_small: shared memory attribute refused");
+      CUDA_TRY(cudaGetLastError());
+      nsteps -= chunk;
+    }
+    return SPP_OK;
+  }
   if (!s->use_graphs) {
     for (int64_t i = 0; i < nsteps; ++i) {
       int rc = enqueue_step(s, s->stream, false, &s->host_launches);
@@ -619,6 +637,10 @@ int spp_create(const SppParams* p, SppSystem** out) {
   d.D = D;
   d.morton_bits = bits;
   d.n_keys = 1u << (2 * bits);
+  {
+    const char* sv = getenv("SPP_VICSEK_SMALL");
+    s->small_vicsek = !s->uses_list && !(sv && sv[0] == '0') && vicsek_small_fits(s->k, d);
+  }
   int cap = p->list_capacity > 0 ? p->list_capacity : list_capacity_for(*p, rcell);
   if (!s->uses_list) cap = 0;
   size_t n = (size_t)p->n;

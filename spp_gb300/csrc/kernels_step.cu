@@ -23,6 +23,7 @@
  * rebuilt every step at dt = 1).
  */
 #include "spp_internal.cuh"
+#include <cooperative_groups.h>
 
 namespace {
 
@@ -312,6 +313,209 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_vicsek_step(SppConsts k, DevState
   finish_step(k, d, 0.0f, 0.0f, 0, 0);
 }
 
+/* Small Vicsek systems in one thread-block cluster: k_vicsek_small runs
+ * nsteps whole steps in a single launch.  Per step every CTA of the cluster
+ * bins all particles into its own shared-memory cell table (count, scan,
+ * cell-ordered copy of the states; cheap next to the pair sums), then
+ * updates its own slice of the particles from that copy.  The state is
+ * double-buffered in global memory (pos/theta <-> pos_alt/theta_alt, read
+ * through L2): step t reads one buffer and writes the other, so a single
+ * cluster barrier per step orders every write before the next step's
+ * reads.  The heading sums are exact fixed point and the noise is keyed by
+ * particle id and step, so the result is bit-identical to the multi-kernel
+ * step (k_bin_count / scan / k_scatter / k_vicsek_step), which at these
+ * sizes is bound by launch latency. */
+#ifndef SPP_SMALL_THREADS
+#define SPP_SMALL_THREADS 1024
+#endif
+#ifndef SPP_SMALL_LANES
+#define SPP_SMALL_LANES 4          /* lanes per particle in the pair sums (1, 2, 4 or 8) */
+#endif
+#define SPP_SMALL_BATCH 4
+#ifndef SPP_SMALL_CLUSTER_MAX
+#define SPP_SMALL_CLUSTER_MAX 16   /* CTAs per cluster, tried downwards in powers of 2 */
+#endif
+
+__global__ void __launch_bounds__(SPP_SMALL_THREADS, 1) k_vicsek_small(SppConsts k, DevState d, int nsteps) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ float4 small_mem[];
+  const int n = d.n, D = d.D, C = D * D;
+  const int need_theta = (k.model == SPP_MODEL_VICSEK_REF_ANGLE);
+  float4* sp = small_mem;                                        /* n cell-ordered states */
+  float* sth = reinterpret_cast<float*>(sp + n);                 /* n headings (REF_ANGLE) */
+  int* cnt = reinterpret_cast<int*>(sth + (need_theta ? n : 0)); /* C counts */
+  int* start = cnt + C;                                          /* C exclusive starts */
+  int* packed = start + C;                                       /* n: cell | rank << 16 */
+  __shared__ int warp_tot[SPP_SMALL_THREADS / 32];
+  __shared__ unsigned ovf;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int R = (int)cluster.num_blocks(), rk = (int)cluster.block_rank();
+  const int per_cta = (n + R - 1) / R;
+  const int i0 = rk * per_cta, i1 = min(n, i0 + per_cta);
+  if (d.ctl->frozen) return;   /* the same word for every CTA: all return or none */
+  uint32_t step = d.ctl->step;
+  if (tid == 0) ovf = 0u;
+  const int per_c = (C + SPP_SMALL_THREADS - 1) / SPP_SMALL_THREADS;
+  for (int t = 0; t < nsteps; ++t, ++step) {
+    const float4* __restrict__ src_pos = (t & 1) ? d.pos_alt : d.pos;
+    const float* __restrict__ src_th = (t & 1) ? d.theta_alt : d.theta;
+    float4* dst_pos = (t & 1) ? d.pos : d.pos_alt;
+    float* dst_th = (t & 1) ? d.theta : d.theta_alt;
+    for (int c = tid; c < C; c += SPP_SMALL_THREADS) cnt[c] = 0;
+    __syncthreads();
+    /* loads from L2 issued SPP_SMALL_BATCH at a time */
+    for (int ib = tid; ib < n; ib += SPP_SMALL_BATCH * SPP_SMALL_THREADS) {
+      float4 pv[SPP_SMALL_BATCH];
+#pragma unroll
+      for (int u = 0; u < SPP_SMALL_BATCH; ++u) {
+        const int i = ib + u * SPP_SMALL_THREADS;
+        pv[u] = i < n ? __ldcg(src_pos + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+#pragma unroll
+      for (int u = 0; u < SPP_SMALL_BATCH; ++u) {
+        const int i = ib + u * SPP_SMALL_THREADS;
+        if (i < n) {
+          const int cx = spp_cell_coord(pv[u].x, k.L, k.L2, D, SPP_BIN_GEOMETRIC);
+          const int cy = spp_cell_coord(pv[u].y, k.L, k.L2, D, SPP_BIN_GEOMETRIC);
+          const int cell = cy * D + cx;
+          packed[i] = cell | (atomicAdd(&cnt[cell], 1) << 16);
+        }
+      }
+    }
+    __syncthreads();
+    /* exclusive scan of the counts: per_c consecutive cells per thread */
+    {
+      const int c0 = tid * per_c;
+      int local = 0;
+      for (int c = c0; c < c0 + per_c && c < C; ++c) local += cnt[c];
+      int incl = local;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      if (lane == 31) warp_tot[wid] = incl;
+      __syncthreads();
+      if (wid == 0) {
+        int w = lane < SPP_SMALL_THREADS / 32 ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, w, o);
+          if (lane >= o) w += v;
+        }
+        if (lane < SPP_SMALL_THREADS / 32) warp_tot[lane] = w;
+      }
+      __syncthreads();
+      int run = incl - local + (wid > 0 ? warp_tot[wid - 1] : 0);
+      for (int c = c0; c < c0 + per_c && c < C; ++c) {
+        start[c] = run;
+        run += cnt[c];
+      }
+    }
+    __syncthreads();
+    for (int ib = tid; ib < n; ib += SPP_SMALL_BATCH * SPP_SMALL_THREADS) {
+      float4 pv[SPP_SMALL_BATCH];
+      float tv[SPP_SMALL_BATCH];
+#pragma unroll
+      for (int u = 0; u < SPP_SMALL_BATCH; ++u) {
+        const int i = ib + u * SPP_SMALL_THREADS;
+        pv[u] = i < n ? __ldcg(src_pos + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        tv[u] = (need_theta && i < n) ? __ldcg(src_th + i) : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < SPP_SMALL_BATCH; ++u) {
+        const int i = ib + u * SPP_SMALL_THREADS;
+        if (i < n) {
+          const int pk = packed[i];
+          const int slot = start[pk & 0xffff] + (pk >> 16);
+          sp[slot] = pv[u];
+          if (need_theta) sth[slot] = tv[u];
+        }
+      }
+    }
+    __syncthreads();
+    /* SPP_SMALL_LANES consecutive lanes per particle: lane q walks cells
+     * q, q + LANES, ... of the 3x3 block; the exact fixed-point partial sums
+     * add up to the same integers in any grouping, and lane 0 of the group
+     * draws the noise and writes the particle */
+    {
+      const int q = tid % SPP_SMALL_LANES;
+      const int grp = tid / SPP_SMALL_LANES;
+      constexpr int GROUPS = SPP_SMALL_THREADS / SPP_SMALL_LANES;
+      for (int base = i0; base < i1; base += GROUPS) {
+        const int i = base + grp;
+        const bool valid = i < i1;
+        SppAcc a;
+        spp_acc_zero(&a);
+        int me = 0;
+        float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (valid) {
+          const int pk = packed[i];
+          const int cell = pk & 0xffff;
+          me = start[cell] + (pk >> 16);
+          p = sp[me];
+          const int cx = cell % D, cy = cell / D;
+          for (int c9 = q; c9 < 9; c9 += SPP_SMALL_LANES) {
+            int ny = cy + c9 / 3 - 1;
+            ny = ny < 0 ? ny + D : (ny >= D ? ny - D : ny);
+            int nx = cx + c9 % 3 - 1;
+            nx = nx < 0 ? nx + D : (nx >= D ? nx - D : nx);
+            const int kk = ny * D + nx;
+            const int s0 = start[kk], s1 = s0 + cnt[kk];
+            for (int j = s0; j < s1; ++j) {
+              const float4 qq = sp[j];
+              spp_pair_vicsek(&k, &a, p.x, p.y, qq.x, qq.y, qq.z, qq.w, need_theta ? sth[j] : 0.0f, j == me);
+            }
+          }
+        }
+#pragma unroll
+        for (int o = 1; o < SPP_SMALL_LANES; o <<= 1) {
+          a.ax.hi += __shfl_xor_sync(0xffffffffu, a.ax.hi, o);
+          a.ax.lo += __shfl_xor_sync(0xffffffffu, a.ax.lo, o);
+          a.ay.hi += __shfl_xor_sync(0xffffffffu, a.ay.hi, o);
+          a.ay.lo += __shfl_xor_sync(0xffffffffu, a.ay.lo, o);
+          a.at.hi += __shfl_xor_sync(0xffffffffu, a.at.hi, o);
+          a.at.lo += __shfl_xor_sync(0xffffffffu, a.at.lo, o);
+          a.cnt += __shfl_xor_sync(0xffffffffu, a.cnt, o);
+          a.ovf |= __shfl_xor_sync(0xffffffffu, a.ovf, o);
+        }
+        if (valid && q == 0) {
+          if (a.ovf) ovf = 1u;
+          const spp_u32x4 r = spp_draw(k.seed, k.system, d.id[i], step, SPP_RNG_VICSEK);
+          float x, y, th, c, sn;
+          int gx = 0, gy = 0;
+          spp_vicsek_update(&k, &a, p.x, p.y, __ldcg(src_th + i), p.z, p.w, r.v[0], &x, &y, &th, &c, &sn,
+                            &gx, &gy);
+          dst_pos[i] = make_float4(x, y, c, sn);
+          dst_th[i] = th;
+          if (gx | gy) {   /* only this thread touches particle i's counters */
+            const int2 g = d.img[i];
+            d.img[i] = make_int2(g.x + gx, g.y + gy);
+          }
+        }
+      }
+    }
+    /* every write of this step before any read of the next */
+    cluster.sync();
+  }
+  if (nsteps & 1) {
+    /* the last step wrote the alternate buffers: move this CTA's slice back */
+    for (int i = i0 + tid; i < i1; i += SPP_SMALL_THREADS) {
+      d.pos[i] = d.pos_alt[i];
+      d.theta[i] = d.theta_alt[i];
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    if (ovf) atomicOr(&d.ctl->fx_overflow, 1u);
+    if (rk == 0) {
+      d.ctl->step = step;
+      d.ctl->need_rebuild = 0u;
+    }
+  }
+}
+
 /* Euler writes its new state to the half buffer (neighbours read pos during
  * the stage); this commits it. */
 __global__ void __launch_bounds__(SPP_BLOCK) k_commit(DevState d) {
@@ -401,6 +605,71 @@ void launch_vicsek_step(const SppConsts& k, const DevState& d, cudaStream_t s, i
   if (nb == 0) nb = 1;
   k_vicsek_step<<<nb, SPP_BLOCK, 0, s>>>(k, d);
   if (launches) *launches += 1;
+}
+
+size_t vicsek_small_smem(const SppConsts& k, const DevState& d) {
+  const size_t n = (size_t)d.n, C = (size_t)d.D * d.D;
+  return n * sizeof(float4) + (k.model == SPP_MODEL_VICSEK_REF_ANGLE ? n * sizeof(float) : 0) +
+         2 * C * sizeof(int) + n * sizeof(int);
+}
+
+bool vicsek_small_fits(const SppConsts& k, const DevState& d) {
+  return d.n <= SPP_SMALL_MAX_N && (int64_t)d.D * d.D < 65536 &&
+         vicsek_small_smem(k, d) <= SPP_SMALL_MAX_SMEM;
+}
+
+/* The largest cluster (16, 8, 4, 2 or 1 CTAs) that fits on the device with
+ * this shared memory. */
+static int small_cluster_size(size_t smem) {
+  static int cached = 0;
+  static size_t cached_smem = 0;
+  if (cached && cached_smem == smem) return cached;
+  cudaFuncSetAttribute(k_vicsek_small, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  int best = 0;
+  for (int cs = SPP_SMALL_CLUSTER_MAX; cs >= 1 && !best; cs >>= 1) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(SPP_SMALL_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_vicsek_small, &cfg) == cudaSuccess && nclusters > 0)
+      best = cs;
+    else
+      cudaGetLastError();
+  }
+  cached = best;
+  cached_smem = smem;
+  return best;
+}
+
+int launch_vicsek_small(const SppConsts& k, const DevState& d, int nsteps, cudaStream_t s, int64_t* launches) {
+  const size_t smem = vicsek_small_smem(k, d);
+  if (cudaFuncSetAttribute(k_vicsek_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return -1;
+  const int cs = small_cluster_size(smem);
+  if (cs < 1) return -1;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(cs);
+  cfg.blockDim = dim3(SPP_SMALL_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, k_vicsek_small, k, d, nsteps) != cudaSuccess) return -1;
+  if (launches) *launches += 1;
+  return 0;
 }
 
 void launch_polarization(const DevState& d, cudaStream_t s) {

@@ -110,6 +110,14 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
                       cudaGraphConditionalHandle cond, int use_cond, cudaStream_t s,
                       int64_t* launches);
 void launch_vicsek_step(const SppConsts& k, const DevState& d, cudaStream_t s, int64_t* launches);
+/* Whole Vicsek steps of a small system in one thread-block cluster
+ * (k_vicsek_small): at most SPP_SMALL_MAX_N particles, fewer than 65536
+ * cells, and SPP_SMALL_MAX_SMEM bytes of cell-ordered copy plus cell table
+ * per CTA. */
+#define SPP_SMALL_MAX_N 16384
+#define SPP_SMALL_MAX_SMEM (224 * 1024)
+bool vicsek_small_fits(const SppConsts& k, const DevState& d);
+int launch_vicsek_small(const SppConsts& k, const DevState& d, int nsteps, cudaStream_t s, int64_t* launches);
 void launch_polarization(const DevState& d, cudaStream_t s);
 /* the two fixed-point heading sums added into sums[0..1] (zeroed by the caller) */
 void launch_polarization_into(const DevState& d, unsigned long long* sums, cudaStream_t s);

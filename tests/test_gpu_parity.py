@@ -86,6 +86,33 @@ def test_vicsek_bitexact_vs_mirror(gpu_lib, model):
     assert abs(obs.polarization - P) < 1e-6
 
 
+@pytest.mark.parametrize("model", [abi.MODEL_VICSEK, abi.MODEL_VICSEK_REF_ANGLE,
+                                   abi.MODEL_VICSEK_REF_VECTOR])
+def test_vicsek_single_block_path_matches_multi_kernel_path(gpu_lib, model, monkeypatch):
+    """Small systems run whole steps in one block (k_vicsek_small); the
+    multi-kernel step (SPP_VICSEK_SMALL=0) and the mirror give the same
+    bits, including the box-crossing counters, for several calls of
+    different lengths and a system at the size limit."""
+    for n, L in ((4096, 32.0), (8192, 40.0)):
+        p = configs.vicsek_config(model=model)
+        p.n, p.L = n, L
+        x, y, th = configs.random_state(p.n, p.L, seed=5)
+        outs = []
+        for small in ("1", "0"):
+            monkeypatch.setenv("SPP_VICSEK_SMALL", small)
+            with System(p) as s:
+                s.upload(x, y, th, step0=17)
+                s.step(1)
+                s.step(40)
+                s.step(159)
+                outs.append(s.download())
+        for a, b in zip(*outs):
+            assert np.array_equal(a, b)
+        ref = O.run32(p, O.State32(x, y, th), 200, step0=17)
+        assert_bitexact(outs[0], ref)
+        assert np.abs(outs[0][3]).max() > 0  # particles crossed the boundary
+
+
 @pytest.mark.parametrize("integ", [abi.INT_EULER, abi.INT_RK4])
 def test_continuous_bitexact_vs_mirror(gpu_lib, integ):
     p = configs.reference_defaults(abi.MODEL_CONTINUOUS)
