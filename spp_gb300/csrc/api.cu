@@ -120,7 +120,7 @@ void free_dev(SppSystem* s) {
   DevState& d = s->d;
   void* ptrs[] = {d.pos, d.half, d.half2, d.theta, d.img, d.id, d.inv, d.kacc, d.dth, d.ref, d.pos_alt,
                   d.theta_alt, d.img_alt, d.id_alt, d.key, d.rank, d.cell_count, d.cell_start,
-                  d.scan_tmp, d.nbr, d.nn, d.tumble, d.ctl, d.red, s->stage_x, s->stage_y, s->stage_t,
+                  d.scan_tmp, d.nbr, d.nn, d.long_q, d.tumble, d.ctl, d.red, s->stage_x, s->stage_y, s->stage_t,
                   s->stage_img};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -671,6 +671,7 @@ int spp_create(const SppParams* p, SppSystem** out) {
   rc = rc ? rc : dalloc(&d.cell_start, d.n_keys);
   rc = rc ? rc : dalloc(&d.scan_tmp, nscan);
   rc = rc ? rc : dalloc(&d.nn, n);
+  rc = rc ? rc : dalloc(&d.long_q, n);
   rc = rc ? rc : dalloc(&d.ctl, 1);
   rc = rc ? rc : dalloc(&d.red, 4);
   rc = rc ? rc : dalloc(&s->stage_x, n);
@@ -692,7 +693,7 @@ int spp_create(const SppParams* p, SppSystem** out) {
     return fail(SPP_ERR_CUDA, std::string("stream/ctl setup: ") + cudaGetErrorString(e));
   }
   s->own_stream = true;
-  s->per_rebuild_kernels = 6;   /* bin_count, scan x3, scatter, build_list */
+  s->per_rebuild_kernels = 7;   /* bin_count, scan x3, scatter, build_list, sort_long */
   s->per_step_kernels = s->uses_list ? (s->nstages == 1 ? 2 : s->nstages) : 6;
   *out = s;
   return SPP_OK;

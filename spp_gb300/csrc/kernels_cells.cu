@@ -35,6 +35,7 @@ __device__ __forceinline__ uint32_t cell_key(const SppConsts& k, const DevState&
 
 __global__ void __launch_bounds__(SPP_BLOCK) k_bin_count(SppConsts k, DevState d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) d.ctl->long_n = 0u;   /* the long-list queue of this rebuild (k_build_list) */
   if (i >= d.n) return;
   float4 p = d.pos[i];
   int cx, cy;
@@ -159,8 +160,8 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_scatter(DevState d) {
 #define SPP_LIST_LOCAL 16
 #endif
 /* keys kept in shared memory per thread (column threadIdx.x of a
- * [LIST_LOCAL][SPP_BLOCK] array: conflict-free), the rest of a longer list
- * sorted in place in global memory */
+ * [LIST_LOCAL][SPP_BLOCK] array: conflict-free); a longer list is finished
+ * by k_sort_long */
 constexpr int LIST_LOCAL = SPP_LIST_LOCAL;
 
 __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState d, int with_list) {
@@ -199,28 +200,10 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
                 }
                 keys(pos) = key;
               } else if (cnt < cap) {
-                /* long list: the first LIST_LOCAL keys are still local; keep the
-                 * tail sorted in place in global memory */
-                int pos = (int)cnt;
-                while (pos > LIST_LOCAL) {
-                  const int32_t prev = d.nbr[(size_t)(pos - 1) * d.n + i];
-                  if (d.id_alt[prev] < (uint32_t)(key >> 32)) break;
-                  d.nbr[(size_t)pos * d.n + i] = prev;
-                  --pos;
-                }
-                if (pos == LIST_LOCAL && keys(LIST_LOCAL - 1) > key) {
-                  /* belongs among the local keys: swap with the local maximum */
-                  unsigned long long moved = keys(LIST_LOCAL - 1);
-                  int lp = LIST_LOCAL - 1;
-                  while (lp > 0 && keys(lp - 1) > key) {
-                    keys(lp) = keys(lp - 1);
-                    --lp;
-                  }
-                  keys(lp) = key;
-                  d.nbr[(size_t)pos * d.n + i] = (int32_t)(uint32_t)moved;
-                } else {
-                  d.nbr[(size_t)pos * d.n + i] = (int32_t)j;
-                }
+                /* a longer list: the first LIST_LOCAL keys stay sorted in
+                 * shared memory, the rest is appended unsorted and
+                 * k_sort_long orders the whole list */
+                d.nbr[(size_t)cnt * d.n + i] = (int32_t)j;
               }
               ++cnt;
             }
@@ -231,6 +214,8 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
       const uint32_t nw = nloc < cap ? nloc : cap;
       for (uint32_t q = 0; q < nw; ++q) d.nbr[(size_t)q * d.n + i] = (int32_t)(uint32_t)keys(q);
       d.nn[i] = (int32_t)(cnt < cap ? cnt : cap);
+      if (cnt > (uint32_t)LIST_LOCAL && cap > (uint32_t)LIST_LOCAL)
+        d.long_q[atomicAdd(&d.ctl->long_n, 1u)] = i;
       d.ref[i] = make_float2(p.x, p.y);
 #undef keys
     }
@@ -251,6 +236,95 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
     }
   }
   if (i == 0) atomicAdd(&d.ctl->n_rebuilds, 1u);
+}
+
+/* Sorts the list of particle i (m entries, m <= 32 R) by (id, slot): one
+ * warp, R keys per lane, element e = r * 32 + lane, a bitonic network
+ * (partners across lanes by shuffle, across r in registers).  Ids are
+ * unique, so the order is the one the insertion sort of short lists gives. */
+template <int R>
+__device__ __forceinline__ void warp_sort_list(const DevState& d, int i, int m) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long key[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int q = r * 32 + lane;
+    if (q < m) {
+      const int32_t j = d.nbr[(size_t)q * d.n + i];
+      key[r] = ((unsigned long long)d.id_alt[j] << 32) | (unsigned long long)(uint32_t)j;
+    } else {
+      key[r] = ~0ull;
+    }
+  }
+#pragma unroll
+  for (int size = 2; size <= 32 * R; size <<= 1) {
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      if (stride >= 32) {
+        const int rs = stride >> 5;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int rp = r ^ rs;
+          if (rp > r) {
+            const bool up = ((r * 32 + lane) & size) == 0;
+            const unsigned long long a = key[r], b = key[rp];
+            if (up ? (a > b) : (a < b)) {
+              key[r] = b;
+              key[rp] = a;
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const unsigned long long other = __shfl_xor_sync(0xffffffffu, key[r], stride);
+          const bool up = ((r * 32 + lane) & size) == 0;
+          const bool lower = (lane & stride) == 0;
+          const bool keep_min = (up == lower);
+          const unsigned long long lo = key[r] < other ? key[r] : other;
+          const unsigned long long hi = key[r] < other ? other : key[r];
+          key[r] = keep_min ? lo : hi;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int q = r * 32 + lane;
+    if (q < m) d.nbr[(size_t)q * d.n + i] = (int32_t)(uint32_t)key[r];
+  }
+}
+
+/* Lists longer than LIST_LOCAL, queued by k_build_list: one warp per list
+ * (grid-stride over the queue).  Lists beyond 512 entries, which only
+ * extreme densities produce, are insertion-sorted by one lane. */
+__global__ void __launch_bounds__(SPP_BLOCK) k_sort_long(DevState d) {
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+  const uint32_t total = d.ctl->long_n;
+  for (uint32_t w = (uint32_t)warp; w < total; w += (uint32_t)nwarps) {
+    const int i = d.long_q[w];
+    const int m = d.nn[i];
+    if (m <= 32) warp_sort_list<1>(d, i, m);
+    else if (m <= 64) warp_sort_list<2>(d, i, m);
+    else if (m <= 128) warp_sort_list<4>(d, i, m);
+    else if (m <= 256) warp_sort_list<8>(d, i, m);
+    else if (m <= 512) warp_sort_list<16>(d, i, m);
+    else if ((threadIdx.x & 31) == 0) {
+      for (int q = 1; q < m; ++q) {
+        const int32_t j = d.nbr[(size_t)q * d.n + i];
+        const uint32_t idj = d.id_alt[j];
+        int pos = q;
+        while (pos > 0) {
+          const int32_t prev = d.nbr[(size_t)(pos - 1) * d.n + i];
+          if (d.id_alt[prev] < idj) break;
+          d.nbr[(size_t)pos * d.n + i] = prev;
+          --pos;
+        }
+        d.nbr[(size_t)pos * d.n + i] = j;
+      }
+    }
+  }
 }
 
 /* Unique pairs (by particle id) within r, through the cell list. */
@@ -365,6 +439,13 @@ void launch_build_list(const SppConsts& k, const DevState& d, int with_list, cud
   if (d.n == 0) return;
   k_build_list<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(k, d, with_list);
   if (launches) *launches += 1;
+  if (with_list) {
+    /* 8 warps per block, at most 8 blocks per SM of a 152-SM part */
+    int nb = (d.n + 7) / 8;
+    if (nb > 1216) nb = 1216;
+    k_sort_long<<<nb, SPP_BLOCK, 0, s>>>(d);
+    if (launches) *launches += 1;
+  }
 }
 
 void launch_pairs_count(const SppConsts& k, const DevState& d, float r2, unsigned long long* counter,

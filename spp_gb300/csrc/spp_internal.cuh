@@ -39,7 +39,8 @@ struct Ctl {
   uint32_t late_rebuilds; /* rebuilds decided after some particle had already moved > skin/2 */
   uint32_t bad_nonfinite; /* smallest index of an uploaded particle with a non-finite value (or ~0) */
   uint32_t bad_range;     /* smallest index of an uploaded position outside [-L, L) (or ~0) */
-  uint32_t pad[3];
+  uint32_t long_n;        /* lists longer than the in-block sort queued by the last build */
+  uint32_t pad[2];
 };
 
 struct DevState {
@@ -69,6 +70,7 @@ struct DevState {
   uint32_t* scan_tmp;     /* block sums of the scan */
   int32_t* nbr;
   int32_t* nn;
+  int32_t* long_q;        /* particles whose list k_sort_long orders (n entries) */
   int32_t* tumble;        /* run-and-tumble state by particle id (SPP_NOISE_TUMBLE), else NULL */
   Ctl* ctl;
   double* red;            /* reduction scratch (polarization) */
