@@ -86,6 +86,24 @@ static int abp_accumulate(const SppConsts* k, int n, const float* x, const float
       }
     });
     qsort(cand, (size_t)m, sizeof(int), cmp_int);
+    if (k->lanes > 1) {
+      /* the kernels' lane split: lane r sums the neighbours with id % 4 == r
+       * in id order, then (p0 + p1) + (p2 + p3) */
+      SppAccF part[SPP_GATHER_LANES];
+      for (int r = 0; r < SPP_GATHER_LANES; ++r) spp_accf_zero(&part[r]);
+      for (int q = 0; q < m; ++q) {
+        int j = cand[q];
+        spp_pair_abp(k, &part[j & 3], x[i], y[i], c[i], s[i], x[j], y[j], c[j], s[j]);
+      }
+      a.fx = spp_lane_sum4(part[0].fx, part[1].fx, part[2].fx, part[3].fx);
+      a.fy = spp_lane_sum4(part[0].fy, part[1].fy, part[2].fy, part[3].fy);
+      a.tq = spp_lane_sum4(part[0].tq, part[1].tq, part[2].tq, part[3].tq);
+      a.cnt = part[0].cnt + part[1].cnt + part[2].cnt + part[3].cnt;
+      a.ovf = part[0].ovf | part[1].ovf | part[2].ovf | part[3].ovf;
+      ovf |= a.ovf;
+      acc[i] = a;
+      continue;
+    }
     const int chain = spp_pair_kind(k) == SPP_KIND_CHAIN;
     const int nbi = chain && i >= k->n_beads ? k->chain_nb : 1;
     for (int q = 0; q < m; ++q) {
@@ -470,20 +488,37 @@ int orc32_lyap_run(const SppParams* p, int nsteps, int64_t step0, int renorm_eve
           }
         });
         qsort(cand, (size_t)m, sizeof(int), cmp_int);
-        SppAccF a;
-        spp_accf_zero(&a);
-        float tacc[SPP_LYAP_MAX];
-        for (int v = 0; v < K; ++v) tacc[v] = 0.0f;
+        /* one lane (k.lanes == 1) or the kernels' four: neighbours with
+         * id % 4 == r in lane r, lane sums combined as (p0 + p1) + (p2 + p3) */
+        const int L = k.lanes;
+        SppAccF part[SPP_GATHER_LANES];
+        float tpart[SPP_GATHER_LANES][SPP_LYAP_MAX];
+        for (int r = 0; r < L; ++r) {
+          spp_accf_zero(&part[r]);
+          for (int v = 0; v < K; ++v) tpart[r][v] = 0.0f;
+        }
         for (int q = 0; q < m; ++q) {
           int j = cand[q];
-          spp_pair_abp(&k, &a, cx[i], cy[i], cc[i], cs[i], cx[j], cy[j], cc[j], cs[j]);
+          const int r = L > 1 ? (j & 3) : 0;
+          spp_pair_abp(&k, &part[r], cx[i], cy[i], cc[i], cs[i], cx[j], cy[j], cc[j], cs[j]);
           float dx, dy;
           float d2 = spp_sep(&k, cx[i], cy[i], cx[j], cy[j], &dx, &dy);
           if (d2 < k.ral2) {
             float cij = spp_tangent_coupling(cc[i], cs[i], cc[j], cs[j]);
             for (int v = 0; v < K; ++v)
-              tacc[v] = tacc[v] + cij * (uin[(size_t)(v * 3 + 2) * n + j] - uin[(size_t)(v * 3 + 2) * n + i]);
+              tpart[r][v] = tpart[r][v] + cij * (uin[(size_t)(v * 3 + 2) * n + j] - uin[(size_t)(v * 3 + 2) * n + i]);
           }
+        }
+        SppAccF a = part[0];
+        float tacc[SPP_LYAP_MAX];
+        for (int v = 0; v < K; ++v) tacc[v] = tpart[0][v];
+        if (L > 1) {
+          a.fx = spp_lane_sum4(part[0].fx, part[1].fx, part[2].fx, part[3].fx);
+          a.fy = spp_lane_sum4(part[0].fy, part[1].fy, part[2].fy, part[3].fy);
+          a.tq = spp_lane_sum4(part[0].tq, part[1].tq, part[2].tq, part[3].tq);
+          a.cnt = part[0].cnt + part[1].cnt + part[2].cnt + part[3].cnt;
+          a.ovf = part[0].ovf | part[1].ovf | part[2].ovf | part[3].ovf;
+          for (int v = 0; v < K; ++v) tacc[v] = spp_lane_sum4(tpart[0][v], tpart[1][v], tpart[2][v], tpart[3][v]);
         }
         A[i] = a;
         const float gp = k.g * k.one_minus_alpha_over_pi;

@@ -120,7 +120,7 @@ void free_dev(SppSystem* s) {
   DevState& d = s->d;
   void* ptrs[] = {d.pos, d.half, d.half2, d.theta, d.img, d.id, d.inv, d.kacc, d.dth, d.ref, d.pos_alt,
                   d.theta_alt, d.img_alt, d.id_alt, d.key, d.rank, d.cell_count, d.cell_start,
-                  d.scan_tmp, d.nbr, d.nn, d.long_q, d.tumble, d.ctl, d.red, s->stage_x, s->stage_y, s->stage_t,
+                  d.scan_tmp, d.nbr, d.nn, d.long_q, d.nn_lanes, d.tumble, d.ctl, d.red, s->stage_x, s->stage_y, s->stage_t,
                   s->stage_img};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -672,6 +672,7 @@ int spp_create(const SppParams* p, SppSystem** out) {
   rc = rc ? rc : dalloc(&d.scan_tmp, nscan);
   rc = rc ? rc : dalloc(&d.nn, n);
   rc = rc ? rc : dalloc(&d.long_q, n);
+  if (s->k.lanes > 1) rc = rc ? rc : dalloc(&d.nn_lanes, n);
   rc = rc ? rc : dalloc(&d.ctl, 1);
   rc = rc ? rc : dalloc(&d.red, 4);
   rc = rc ? rc : dalloc(&s->stage_x, n);
@@ -1020,6 +1021,10 @@ int spp_lyap_step(SppSystem* s, int nsteps, int renorm_every) {
   s->target_step += nsteps;
   s->lyap_renorm_every = renorm_every;
   s->lyap_steps += nsteps;
+  if (!s->use_graphs) {
+    int rc = run_lyap_direct(s, nsteps);
+    return rc != SPP_OK ? rc : recover(s);
+  }
   return launch_lyap_chunks(s, nsteps);
 }
 

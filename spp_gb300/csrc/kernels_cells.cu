@@ -160,14 +160,27 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_scatter(DevState d) {
 #define SPP_LIST_LOCAL 16
 #endif
 /* keys kept in shared memory per thread (column threadIdx.x of a
- * [LIST_LOCAL][SPP_BLOCK] array: conflict-free); a longer list is finished
- * by k_sort_long */
+ * [LIST_LOCAL][SPP_BLOCK] array: conflict-free); entries up to LIST_TAIL
+ * are inserted in order in global memory, a list longer than that is
+ * finished by k_sort_long */
 constexpr int LIST_LOCAL = SPP_LIST_LOCAL;
+#ifndef SPP_LIST_TAIL
+#define SPP_LIST_TAIL 24
+#endif
+constexpr int LIST_TAIL = SPP_LIST_TAIL;
 
+/* spp_list_order with the lane count known at compile time */
+template <int LANES>
+__device__ __forceinline__ uint32_t list_order(uint32_t id) {
+  return LANES == 1 ? id : ((id & 3u) << 30) | (id >> 2);
+}
+
+template <int LANES>
 __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState d, int with_list) {
   __shared__ unsigned long long skeys[LIST_LOCAL][SPP_BLOCK];
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t cnt = 0;
+  unsigned long long lane_cnt = 0;   /* neighbours per id % 4, 16 bits each */
   if (i < d.n) {
     float4 p = d.pos_alt[i];
     if (with_list) {
@@ -190,8 +203,10 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
             float dx, dy;
             float d2 = spp_sep(&k, p.x, p.y, q.x, q.y, &dx, &dy);
             if (d2 < k.rlist2) {
+              const uint32_t idj = d.id_alt[j];
               const unsigned long long key =
-                  ((unsigned long long)d.id_alt[j] << 32) | (unsigned long long)j;
+                  ((unsigned long long)list_order<LANES>(idj) << 32) | (unsigned long long)j;
+              if (LANES > 1) lane_cnt += 1ull << (16 * (idj & 3u));
               if (cnt < (uint32_t)LIST_LOCAL) {
                 int pos = (int)cnt;
                 while (pos > 0 && keys(pos - 1) > key) {
@@ -199,10 +214,32 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
                   --pos;
                 }
                 keys(pos) = key;
+              } else if (cnt < cap && cnt < (uint32_t)LIST_TAIL) {
+                /* a longer list: the first LIST_LOCAL keys are still local;
+                 * keep the next ones sorted in place in global memory */
+                int pos = (int)cnt;
+                while (pos > LIST_LOCAL) {
+                  const int32_t prev = d.nbr[(size_t)(pos - 1) * d.n + i];
+                  if (list_order<LANES>(d.id_alt[prev]) < (uint32_t)(key >> 32)) break;
+                  d.nbr[(size_t)pos * d.n + i] = prev;
+                  --pos;
+                }
+                if (pos == LIST_LOCAL && keys(LIST_LOCAL - 1) > key) {
+                  /* belongs among the local keys: swap with the local maximum */
+                  unsigned long long moved = keys(LIST_LOCAL - 1);
+                  int lp = LIST_LOCAL - 1;
+                  while (lp > 0 && keys(lp - 1) > key) {
+                    keys(lp) = keys(lp - 1);
+                    --lp;
+                  }
+                  keys(lp) = key;
+                  d.nbr[(size_t)pos * d.n + i] = (int32_t)(uint32_t)moved;
+                } else {
+                  d.nbr[(size_t)pos * d.n + i] = (int32_t)j;
+                }
               } else if (cnt < cap) {
-                /* a longer list: the first LIST_LOCAL keys stay sorted in
-                 * shared memory, the rest is appended unsorted and
-                 * k_sort_long orders the whole list */
+                /* a long list: the rest is appended unsorted and k_sort_long
+                 * orders the whole list */
                 d.nbr[(size_t)cnt * d.n + i] = (int32_t)j;
               }
               ++cnt;
@@ -214,7 +251,8 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
       const uint32_t nw = nloc < cap ? nloc : cap;
       for (uint32_t q = 0; q < nw; ++q) d.nbr[(size_t)q * d.n + i] = (int32_t)(uint32_t)keys(q);
       d.nn[i] = (int32_t)(cnt < cap ? cnt : cap);
-      if (cnt > (uint32_t)LIST_LOCAL && cap > (uint32_t)LIST_LOCAL)
+      if (LANES > 1) d.nn_lanes[i] = lane_cnt;   /* meaningful when the list fits */
+      if (cnt > (uint32_t)LIST_TAIL && cap > (uint32_t)LIST_TAIL)
         d.long_q[atomicAdd(&d.ctl->long_n, 1u)] = i;
       d.ref[i] = make_float2(p.x, p.y);
 #undef keys
@@ -243,7 +281,7 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
  * (partners across lanes by shuffle, across r in registers).  Ids are
  * unique, so the order is the one the insertion sort of short lists gives. */
 template <int R>
-__device__ __forceinline__ void warp_sort_list(const DevState& d, int i, int m) {
+__device__ __forceinline__ void warp_sort_list(const SppConsts& k, const DevState& d, int i, int m) {
   const int lane = threadIdx.x & 31;
   unsigned long long key[R];
 #pragma unroll
@@ -251,7 +289,7 @@ __device__ __forceinline__ void warp_sort_list(const DevState& d, int i, int m) 
     const int q = r * 32 + lane;
     if (q < m) {
       const int32_t j = d.nbr[(size_t)q * d.n + i];
-      key[r] = ((unsigned long long)d.id_alt[j] << 32) | (unsigned long long)(uint32_t)j;
+      key[r] = ((unsigned long long)spp_list_order(&k, d.id_alt[j]) << 32) | (unsigned long long)(uint32_t)j;
     } else {
       key[r] = ~0ull;
     }
@@ -298,26 +336,26 @@ __device__ __forceinline__ void warp_sort_list(const DevState& d, int i, int m) 
 /* Lists longer than LIST_LOCAL, queued by k_build_list: one warp per list
  * (grid-stride over the queue).  Lists beyond 512 entries, which only
  * extreme densities produce, are insertion-sorted by one lane. */
-__global__ void __launch_bounds__(SPP_BLOCK) k_sort_long(DevState d) {
+__global__ void __launch_bounds__(SPP_BLOCK) k_sort_long(SppConsts k, DevState d) {
   const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
   const uint32_t total = d.ctl->long_n;
   for (uint32_t w = (uint32_t)warp; w < total; w += (uint32_t)nwarps) {
     const int i = d.long_q[w];
     const int m = d.nn[i];
-    if (m <= 32) warp_sort_list<1>(d, i, m);
-    else if (m <= 64) warp_sort_list<2>(d, i, m);
-    else if (m <= 128) warp_sort_list<4>(d, i, m);
-    else if (m <= 256) warp_sort_list<8>(d, i, m);
-    else if (m <= 512) warp_sort_list<16>(d, i, m);
+    if (m <= 32) warp_sort_list<1>(k, d, i, m);
+    else if (m <= 64) warp_sort_list<2>(k, d, i, m);
+    else if (m <= 128) warp_sort_list<4>(k, d, i, m);
+    else if (m <= 256) warp_sort_list<8>(k, d, i, m);
+    else if (m <= 512) warp_sort_list<16>(k, d, i, m);
     else if ((threadIdx.x & 31) == 0) {
       for (int q = 1; q < m; ++q) {
         const int32_t j = d.nbr[(size_t)q * d.n + i];
-        const uint32_t idj = d.id_alt[j];
+        const uint32_t oj = spp_list_order(&k, d.id_alt[j]);
         int pos = q;
         while (pos > 0) {
           const int32_t prev = d.nbr[(size_t)(pos - 1) * d.n + i];
-          if (d.id_alt[prev] < idj) break;
+          if (spp_list_order(&k, d.id_alt[prev]) < oj) break;
           d.nbr[(size_t)pos * d.n + i] = prev;
           --pos;
         }
@@ -437,13 +475,17 @@ void launch_scatter(const DevState& d, cudaStream_t s, int64_t* launches) {
 void launch_build_list(const SppConsts& k, const DevState& d, int with_list, cudaStream_t s,
                        int64_t* launches) {
   if (d.n == 0) return;
-  k_build_list<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(k, d, with_list);
+  if (with_list && k.lanes == SPP_GATHER_LANES)
+    k_build_list<SPP_GATHER_LANES><<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(k, d, with_list);
+  else
+    k_build_list<1><<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(k, d, with_list);
   if (launches) *launches += 1;
   if (with_list) {
-    /* 8 warps per block, at most 8 blocks per SM of a 152-SM part */
+    /* 8 warps per block, 8 blocks per SM of a 152-SM part, looping over
+     * the queue */
     int nb = (d.n + 7) / 8;
     if (nb > 1216) nb = 1216;
-    k_sort_long<<<nb, SPP_BLOCK, 0, s>>>(d);
+    k_sort_long<<<nb, SPP_BLOCK, 0, s>>>(k, d);
     if (launches) *launches += 1;
   }
 }

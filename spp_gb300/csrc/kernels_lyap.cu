@@ -48,9 +48,15 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_tangent_gather(DevState d, int K,
  * group: a small system (N = 16,384) still spreads over the GPU, a
  * neighbour's components for the group are one float4 load, and the sum over
  * neighbours for each vector is the same FP32 expression in the same
- * (id-sorted list) order as with one vector per thread. */
+ * (id-sorted list) order as with one vector per thread.  With LANES = 4
+ * (k.lanes) four threads share a particle as in k_abp_stage: lane r sums
+ * the neighbours with id % 4 == r and the lane sums combine as
+ * (p0 + p1) + (p2 + p3). */
+template <int LANES>
 __global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevState d, LyapState L, TanStage t) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tg = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = tg / LANES;
+  const int lane_r = tg % LANES;
   const int v0 = blockIdx.y * TAN_GROUP;
   if (i >= d.n || d.ctl->frozen) return;
   const int n = d.n;
@@ -59,17 +65,22 @@ __global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevSta
   const float4 pi = t.cur[i];
   const float4 ui = *reinterpret_cast<const float4*>(L.uslot + (size_t)i * KP + v0);
   float acc[TAN_GROUP] = {0.0f, 0.0f, 0.0f, 0.0f};
-  const int cnt = d.nn[i];
+  int q_begin = 0, q_end = d.nn[i];
+  if (LANES > 1) {
+    const unsigned long long lc = d.nn_lanes[i];
+    for (int r = 0; r < lane_r; ++r) q_begin += (int)((lc >> (16 * r)) & 0xffffull);
+    q_end = q_begin + (int)((lc >> (16 * lane_r)) & 0xffffull);
+  }
   const int32_t* __restrict__ nb = d.nbr + i;
   /* the next neighbour's index, state and components are loaded before the
    * current one is used */
-  int jn = cnt > 0 ? __ldg(nb) : i;
+  int jn = q_begin < q_end ? __ldg(nb + (size_t)q_begin * n) : i;
   float4 pn = __ldg(t.cur + jn);
   float4 un = __ldg(reinterpret_cast<const float4*>(L.uslot + (size_t)jn * KP + v0));
-  for (int q = 0; q < cnt; ++q) {
+  for (int q = q_begin; q < q_end; ++q) {
     const float4 pj = pn;
     const float4 uj = un;
-    if (q + 1 < cnt) {
+    if (q + 1 < q_end) {
       jn = __ldg(nb + (size_t)(q + 1) * n);
       pn = __ldg(t.cur + jn);
       un = __ldg(reinterpret_cast<const float4*>(L.uslot + (size_t)jn * KP + v0));
@@ -83,6 +94,14 @@ __global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevSta
       acc[2] = acc[2] + cij * (uj.z - ui.z);
       acc[3] = acc[3] + cij * (uj.w - ui.w);
     }
+  }
+  if (LANES > 1) {
+    const unsigned gmask = ((1u << LANES) - 1u) << ((threadIdx.x & 31) & ~(LANES - 1));
+#pragma unroll
+    for (int o = 1; o < LANES; o <<= 1)
+#pragma unroll
+      for (int u = 0; u < TAN_GROUP; ++u) acc[u] = acc[u] + __shfl_xor_sync(gmask, acc[u], o);
+    if (lane_r != 0) return;
   }
   const float gp = k.g * k.one_minus_alpha_over_pi;
   const float uiv[TAN_GROUP] = {ui.x, ui.y, ui.z, ui.w};
@@ -224,8 +243,13 @@ void launch_tangent_stage(const SppConsts& k, const DevState& d, const LyapState
   t.uout = (stage & 1) ? ub : ua;
   const dim3 ggrid((unsigned)((d.n + SPP_BLOCK - 1) / SPP_BLOCK), (unsigned)L.K);
   k_tangent_gather<<<ggrid, SPP_BLOCK, 0, s>>>(d, L.K, t.uin, L.uslot);
-  const dim3 tgrid((unsigned)((d.n + TAN_BLOCK - 1) / TAN_BLOCK), (unsigned)(tan_padded(L.K) / TAN_GROUP));
-  k_tangent_stage<<<tgrid, TAN_BLOCK, 0, s>>>(k, d, L, t);
+  const int lanes = k.lanes;
+  const dim3 tgrid((unsigned)(((size_t)d.n * lanes + TAN_BLOCK - 1) / TAN_BLOCK),
+                   (unsigned)(tan_padded(L.K) / TAN_GROUP));
+  if (lanes == SPP_GATHER_LANES)
+    k_tangent_stage<SPP_GATHER_LANES><<<tgrid, TAN_BLOCK, 0, s>>>(k, d, L, t);
+  else
+    k_tangent_stage<1><<<tgrid, TAN_BLOCK, 0, s>>>(k, d, L, t);
   if (launches) *launches += 2;
 }
 

@@ -109,13 +109,20 @@ __device__ __forceinline__ void stage_pair(const SppConsts& k, const DevState& d
 #define SPP_STAGE_MIN_BLOCKS 8   /* 8 x 256 threads per SM: 32 registers */
 #endif
 /* the chain pair loop (bead offsets, lever-arm torques) needs more than
- * 32 registers: 4 x 256 threads per SM there */
-template <int LAW, int KIND>
+ * 32 registers: 4 x 256 threads per SM there.
+ * LANES threads per particle (LANES = k.lanes: 1, or 4 for small ABP /
+ * continuous systems): lane r sums the neighbours with id % 4 == r, one
+ * id-ordered segment of the list (spp_list_order), and the lane sums
+ * combine through xor shuffles as (p0 + p1) + (p2 + p3); lane 0 then
+ * finishes the particle. */
+template <int LAW, int KIND, int LANES>
 __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_STAGE_MIN_BLOCKS) k_abp_stage(SppConsts k, DevState d, StageBufs b,
                                                          cudaGraphConditionalHandle cond,
                                                          int use_cond) {
   constexpr bool BEADLIKE = (KIND == SPP_KIND_BEADS || KIND == SPP_KIND_CHAIN);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tg = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = tg / LANES;
+  const int lane_r = tg % LANES;
   const int last = (b.stage == b.nstages - 1);
   const int frozen = d.ctl->frozen;
   float disp2 = 0.0f, step2 = 0.0f;
@@ -125,26 +132,30 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
     spp_accf_zero(&a);
     const uint32_t pid = BEADLIKE ? d.id[i] : 0u;
     const int nbi = (KIND == SPP_KIND_CHAIN && pid >= (uint32_t)k.n_beads) ? k.chain_nb : 1;
-    const int cnt = d.nn[i];
+    int q_begin = 0, q_end = d.nn[i];
+    if (LANES > 1) {
+      const unsigned long long lc = d.nn_lanes[i];
+      for (int r = 0; r < lane_r; ++r) q_begin += (int)((lc >> (16 * r)) & 0xffffull);
+      q_end = q_begin + (int)((lc >> (16 * lane_r)) & 0xffffull);
+    }
     const int32_t* __restrict__ nb = d.nbr + i;
     const size_t stride = (size_t)d.n;
     /* Warps whose particles are all far from the box edges skip the
      * minimum-image corrections (they would not change any separation). */
     const int inner = fabsf(pi.x) < k.interior && fabsf(pi.y) < k.interior;
     const int all_inner = __all_sync(__activemask(), inner);
-#if SPP_STAGE_GROUP > 1
     /* list entries and neighbour states are loaded SPP_STAGE_GROUP at a time
      * (independent loads in flight), the pairs evaluated in list order */
-    for (int q0 = 0; q0 < cnt; q0 += SPP_STAGE_GROUP) {
+    for (int q0 = q_begin; q0 < q_end; q0 += SPP_STAGE_GROUP) {
       int jg[SPP_STAGE_GROUP];
       float4 pg[SPP_STAGE_GROUP];
 #pragma unroll
-      for (int u = 0; u < SPP_STAGE_GROUP; ++u) jg[u] = q0 + u < cnt ? __ldg(nb + (size_t)(q0 + u) * stride) : i;
+      for (int u = 0; u < SPP_STAGE_GROUP; ++u) jg[u] = q0 + u < q_end ? __ldg(nb + (size_t)(q0 + u) * stride) : i;
 #pragma unroll
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) pg[u] = __ldg(b.cur + jg[u]);
 #pragma unroll
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
-        if (q0 + u < cnt) {
+        if (q0 + u < q_end) {
           if (all_inner)
             stage_pair<LAW, KIND>(k, d, 0, &a, nbi, jg[u], pi, pg[u]);
           else
@@ -152,33 +163,19 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
         }
       }
     }
-#else
-    /* the next neighbour's index and state are loaded before the current
-     * pair is evaluated, so the dependent loads overlap the arithmetic */
-    int jn = cnt > 0 ? __ldg(nb) : i;
-    float4 pn = __ldg(b.cur + jn);
-    if (all_inner) {
-      for (int q = 0; q < cnt; ++q) {
-        const float4 pj = pn;
-        const int j = jn;
-        if (q + 1 < cnt) {
-          jn = __ldg(nb + (size_t)(q + 1) * stride);
-          pn = __ldg(b.cur + jn);
-        }
-        stage_pair<LAW, KIND>(k, d, 0, &a, nbi, j, pi, pj);
-      }
-    } else {
-      for (int q = 0; q < cnt; ++q) {
-        const float4 pj = pn;
-        const int j = jn;
-        if (q + 1 < cnt) {
-          jn = __ldg(nb + (size_t)(q + 1) * stride);
-          pn = __ldg(b.cur + jn);
-        }
-        stage_pair<LAW, KIND>(k, d, 1, &a, nbi, j, pi, pj);
+    if (LANES > 1) {
+      /* the lanes of one particle are consecutive and all present */
+      const unsigned gmask = ((1u << LANES) - 1u) << ((threadIdx.x & 31) & ~(LANES - 1));
+#pragma unroll
+      for (int o = 1; o < LANES; o <<= 1) {
+        a.fx = a.fx + __shfl_xor_sync(gmask, a.fx, o);
+        a.fy = a.fy + __shfl_xor_sync(gmask, a.fy, o);
+        a.tq = a.tq + __shfl_xor_sync(gmask, a.tq, o);
+        a.cnt += __shfl_xor_sync(gmask, a.cnt, o);
+        a.ovf |= __shfl_xor_sync(gmask, a.ovf, o);
       }
     }
-#endif
+  if (LANES == 1 || lane_r == 0) {
     if (LAW == SPP_FORCE_R12_TRUNC && a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
     float fx, fy, tau;
     int turns = 1;
@@ -267,6 +264,7 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
       disp2 = spp_sep(&k, nx, ny, r.x, r.y, &ddx, &ddy);
       step2 = spp_sep(&k, nx, ny, p0.x, p0.y, &ddx, &ddy);
     }
+  }
   }
   if (last) finish_step(k, d, disp2, step2, cond, use_cond);
 }
@@ -570,12 +568,16 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
     b.cur = bufs[cur_sel[stage]];
     b.out = bufs[out_sel[stage]];
   }
-  int nb = blocks_for(d.n);
-  if (nb == 0) nb = 1;
   const int kind = spp_pair_kind(&k);
-#define SPP_STAGE_CASE(L, K)                                                   \
-  if (k.force_law == L && kind == K) {                                        \
-    k_abp_stage<L, K><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond);     \
+  const int lanes = (kind == SPP_KIND_BEADS || kind == SPP_KIND_CHAIN) ? 1 : k.lanes;
+  int nb = blocks_for(d.n * lanes);
+  if (nb == 0) nb = 1;
+#define SPP_STAGE_CASE(L, K)                                                             \
+  if (k.force_law == L && kind == K) {                                                  \
+    if (lanes == SPP_GATHER_LANES)                                                      \
+      k_abp_stage<L, K, SPP_GATHER_LANES><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond); \
+    else                                                                                \
+      k_abp_stage<L, K, 1><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond);         \
   } else
   SPP_STAGE_CASE(SPP_FORCE_HARMONIC, SPP_KIND_ABP)
   SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_ABP)

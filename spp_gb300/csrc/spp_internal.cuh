@@ -71,6 +71,7 @@ struct DevState {
   int32_t* nbr;
   int32_t* nn;
   int32_t* long_q;        /* particles whose list k_sort_long orders (n entries) */
+  unsigned long long* nn_lanes; /* list entries per id % 4, 16 bits each (lanes > 1), else NULL */
   int32_t* tumble;        /* run-and-tumble state by particle id (SPP_NOISE_TUMBLE), else NULL */
   Ctl* ctl;
   double* red;            /* reduction scratch (polarization) */

@@ -65,7 +65,17 @@ typedef struct SppConsts {
   float chain_mperp, chain_dm; /* m_perpendicular, m_parallel - m_perpendicular */
   float chain_k;               /* k_perpendicular */
   float chain_torque0;
+  /* lanes per particle in the neighbour sums of the Verlet-list kernels
+   * (1, or SPP_GATHER_LANES for the ABP / continuous models up to
+   * SPP_LANES_MAX_N particles, where one thread per particle leaves the GPU
+   * idle): a neighbour belongs to lane id % lanes; each lane sums its
+   * neighbours in id order and the lane sums combine as
+   * (p0 + p1) + (p2 + p3) */
+  int32_t lanes;
 } SppConsts;
+
+#define SPP_GATHER_LANES 4
+#define SPP_LANES_MAX_N 131072
 
 /* ActiveBrownianChain::Set_nb (shared/particle.h:856-876): {m_parallel,
  * m_perpendicular, k_perpendicular} of a swimmer of nb beads. */
@@ -162,6 +172,8 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
     }
     k->tumble_steps = c;
   }
+  k->lanes = ((p->model == SPP_MODEL_ABP || p->model == SPP_MODEL_CONTINUOUS) && p->n <= SPP_LANES_MAX_N)
+                 ? SPP_GATHER_LANES : 1;
   k->chain_nb = (p->model == SPP_MODEL_BEADS && p->chain_beads > 1) ? p->chain_beads : 1;
   for (int a = 0; a < SPP_MAX_CHAIN_BEADS; ++a)
     k->chain_off[a] = a < k->chain_nb ? (float)(p->bead_separation * ((1 - k->chain_nb) / 2.0 + a)) : 0.0f;
@@ -191,6 +203,17 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
       k->tumble_dth = (float)(((chain ? m[2] : p->k_perp) * p->dt) * p->tumble_torque);
   }
 }
+
+/* Sort key of neighbour id in the Verlet lists: the id itself with one
+ * lane, else (id % 4, id / 4), which groups each lane's neighbours into one
+ * id-ordered segment (ids < 2^30 with 4 lanes). */
+SPP_HD uint32_t spp_list_order(const SppConsts* k, uint32_t id) {
+  return k->lanes == 1 ? id : ((id & 3u) << 30) | (id >> 2);
+}
+
+/* The fixed combination of the four lane sums (the butterfly of xor
+ * shuffles 1 then 2 computes exactly this on every lane). */
+SPP_HD float spp_lane_sum4(float p0, float p1, float p2, float p3) { return (p0 + p1) + (p2 + p3); }
 
 /* Accumulator for the sums particle i receives. */
 typedef struct SppAcc {
