@@ -32,6 +32,7 @@ namespace {
  * components for one group are one float4 load. */
 constexpr int TAN_GROUP = 4;
 constexpr int TAN_BLOCK = 128;
+constexpr int TAN_LOADS = 3;
 
 __host__ __device__ inline int tan_padded(int K) { return (K + TAN_GROUP - 1) / TAN_GROUP * TAN_GROUP; }
 
@@ -65,6 +66,19 @@ __global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevSta
   const float4 pi = t.cur[i];
   const float4 ui = *reinterpret_cast<const float4*>(L.uslot + (size_t)i * KP + v0);
   float acc[TAN_GROUP] = {0.0f, 0.0f, 0.0f, 0.0f};
+  /* with one vector per lane, that vector's stage inputs (stored by particle
+   * id, so scattered) are loaded first: their latency overlaps the
+   * neighbour walk.  Only this thread touches these elements. */
+  const int vmine = v0 + lane_r;
+  float pre_t0[3] = {0.0f, 0.0f, 0.0f}, pre_a[3] = {0.0f, 0.0f, 0.0f};
+  if (LANES == TAN_GROUP && vmine < L.K) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t e = (size_t)(vmine * 3 + c) * n + idi;
+      pre_t0[c] = L.t0[e];
+      if (t.stage != 0) pre_a[c] = L.acc[e];
+    }
+  }
   int q_begin = 0, q_end = d.nn[i];
   if (LANES > 1) {
     const unsigned long long lc = d.nn_lanes[i];
@@ -72,27 +86,32 @@ __global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevSta
     q_end = q_begin + (int)((lc >> (16 * lane_r)) & 0xffffull);
   }
   const int32_t* __restrict__ nb = d.nbr + i;
-  /* the next neighbour's index, state and components are loaded before the
-   * current one is used */
-  int jn = q_begin < q_end ? __ldg(nb + (size_t)q_begin * n) : i;
-  float4 pn = __ldg(t.cur + jn);
-  float4 un = __ldg(reinterpret_cast<const float4*>(L.uslot + (size_t)jn * KP + v0));
-  for (int q = q_begin; q < q_end; ++q) {
-    const float4 pj = pn;
-    const float4 uj = un;
-    if (q + 1 < q_end) {
-      jn = __ldg(nb + (size_t)(q + 1) * n);
-      pn = __ldg(t.cur + jn);
-      un = __ldg(reinterpret_cast<const float4*>(L.uslot + (size_t)jn * KP + v0));
+  /* list entries, then the neighbours' states and components, are loaded
+   * TAN_LOADS at a time (independent loads in flight); the terms are added
+   * in list order */
+  for (int q0 = q_begin; q0 < q_end; q0 += TAN_LOADS) {
+    int jg[TAN_LOADS];
+#pragma unroll
+    for (int w = 0; w < TAN_LOADS; ++w) jg[w] = q0 + w < q_end ? __ldg(nb + (size_t)(q0 + w) * n) : i;
+    float4 pg[TAN_LOADS], ug[TAN_LOADS];
+#pragma unroll
+    for (int w = 0; w < TAN_LOADS; ++w) {
+      pg[w] = __ldg(t.cur + jg[w]);
+      ug[w] = __ldg(reinterpret_cast<const float4*>(L.uslot + (size_t)jg[w] * KP + v0));
     }
-    float dx, dy;
-    const float d2 = spp_sep(&k, pi.x, pi.y, pj.x, pj.y, &dx, &dy);
-    if (d2 < k.ral2) {
-      const float cij = spp_tangent_coupling(pi.z, pi.w, pj.z, pj.w);
-      acc[0] = acc[0] + cij * (uj.x - ui.x);
-      acc[1] = acc[1] + cij * (uj.y - ui.y);
-      acc[2] = acc[2] + cij * (uj.z - ui.z);
-      acc[3] = acc[3] + cij * (uj.w - ui.w);
+#pragma unroll
+    for (int w = 0; w < TAN_LOADS; ++w) {
+      if (q0 + w < q_end) {
+        float dx, dy;
+        const float d2 = spp_sep(&k, pi.x, pi.y, pg[w].x, pg[w].y, &dx, &dy);
+        if (d2 < k.ral2) {
+          const float cij = spp_tangent_coupling(pi.z, pi.w, pg[w].z, pg[w].w);
+          acc[0] = acc[0] + cij * (ug[w].x - ui.x);
+          acc[1] = acc[1] + cij * (ug[w].y - ui.y);
+          acc[2] = acc[2] + cij * (ug[w].z - ui.z);
+          acc[3] = acc[3] + cij * (ug[w].w - ui.w);
+        }
+      }
     }
   }
   if (LANES > 1) {
@@ -101,20 +120,29 @@ __global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevSta
     for (int o = 1; o < LANES; o <<= 1)
 #pragma unroll
       for (int u = 0; u < TAN_GROUP; ++u) acc[u] = acc[u] + __shfl_xor_sync(gmask, acc[u], o);
-    if (lane_r != 0) return;
   }
+  /* every lane now holds the four sums: with four lanes, lane r advances
+   * vector v0 + r; with one, the thread advances all four */
   const float gp = k.g * k.one_minus_alpha_over_pi;
   const float uiv[TAN_GROUP] = {ui.x, ui.y, ui.z, ui.w};
 #pragma unroll
   for (int u = 0; u < TAN_GROUP; ++u) {
+    if (LANES == TAN_GROUP && u != lane_r) continue;
     const int v = v0 + u;
     if (v >= L.K) break;
     const float slope[3] = {-k.v0 * pi.w * uiv[u], k.v0 * pi.z * uiv[u], gp * acc[u]};
+    float t0v[3], av[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const size_t e = (size_t)(v * 3 + c) * n + idi;
-      float t0 = L.t0[e];
-      float a = t.stage == 0 ? 0.0f : L.acc[e];
+      t0v[c] = LANES == TAN_GROUP ? pre_t0[c] : L.t0[e];
+      av[c] = LANES == TAN_GROUP ? pre_a[c] : (t.stage == 0 ? 0.0f : L.acc[e]);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const size_t e = (size_t)(v * 3 + c) * n + idi;
+      float t0 = t0v[c];
+      float a = av[c];
       float uo = 0.0f;
       spp_tangent_stage_update(&k, t.stage, t.nstages, slope[c], &t0, &a, &uo);
       if (t.stage == t.nstages - 1) L.t0[e] = t0;
