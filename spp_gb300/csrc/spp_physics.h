@@ -75,7 +75,9 @@ typedef struct SppConsts {
 } SppConsts;
 
 #define SPP_GATHER_LANES 4
-#define SPP_LANES_MAX_N 131072
+#ifndef SPP_LANES_MAX_N
+#define SPP_LANES_MAX_N 16384
+#endif
 
 /* ActiveBrownianChain::Set_nb (shared/particle.h:856-876): {m_parallel,
  * m_perpendicular, k_perpendicular} of a swimmer of nb beads. */
