@@ -323,3 +323,39 @@ def test_dimers_in_vesicles_bitexact_vs_mirror(gpu_lib, tumble):
     gpu, _ = run_gpu(p, x, y, th, 200)
     ref = O.run32(p, O.State32(x, y, th), 200)
     assert_bitexact(gpu, ref)
+
+
+def clustered_state(n, L, clusters, seed):
+    """Uniform background plus tight clusters (sizes, radius 0.35): lists of
+    every length class, from a few entries to beyond 512."""
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-L, L, n)
+    y = rng.uniform(-L, L, n)
+    th = rng.uniform(-np.pi, np.pi, n)
+    start = 0
+    centres = [(-0.5 * L, -0.5 * L), (0.5 * L, -0.5 * L), (-0.5 * L, 0.5 * L), (0.5 * L, 0.5 * L),
+               (0.0, 0.0), (0.0, 0.5 * L)]
+    for size, (cx, cy) in zip(clusters, centres):
+        r = 0.35 * np.sqrt(rng.uniform(0, 1, size))
+        a = rng.uniform(0, 2 * np.pi, size)
+        x[start:start + size] = cx + r * np.cos(a)
+        y[start:start + size] = cy + r * np.sin(a)
+        start += size
+    return x.astype(np.float32), y.astype(np.float32), th.astype(np.float32)
+
+
+@pytest.mark.parametrize("n", [4096, 20000])
+def test_long_lists_bitexact_vs_mirror(gpu_lib, n):
+    """Clusters of 700, 300, 150, 100, 60 and 28 particles in a sparse background:
+    lists longer than the 16 shared-memory keys are finished in place up to
+    24 entries, then by the warp bitonic sort (32 to 512 keys) and beyond 512
+    by the one-lane fallback; the list overflows and regrows on the way.
+    4096 particles use four lanes per particle, 20,000 one."""
+    p = configs.reference_defaults(abi.MODEL_CONTINUOUS)
+    p.n, p.L, p.dt, p.v0, p.seed, p.skin, p.integrator = n, 40.0, 0.01, 0.2, 3, 0.3, abi.INT_RK2
+    p.Dr = 0.05
+    x, y, th = clustered_state(p.n, p.L, (700, 300, 150, 100, 60, 28), seed=8)
+    gpu, obs = run_gpu(p, x, y, th, 30)
+    ref = O.run32(p, O.State32(x, y, th), 30)
+    assert_bitexact(gpu, ref)
+    assert obs.max_neighbors > 600
