@@ -204,7 +204,7 @@ int enqueue_rebuild(SppSystem* s, cudaStream_t st, int64_t* launches) {
 int enqueue_step(SppSystem* s, cudaStream_t st, bool capture, int64_t* launches) {
   if (!s->uses_list && s->small_vicsek) {
     if (launch_vicsek_small(s->k, s->d, 1, st, launches) != 0)
-      return fail(SPP_ERR_CUDA, "k_vicsek_small: shared memory attribute refused");
+      return fail(SPP_ERR_CUDA, "k_vicsek_small: cluster launch refused (shared memory or cluster shape)");
     CUDA_TRY(cudaGetLastError());
     return SPP_OK;
   }
@@ -282,7 +282,7 @@ int run_steps(SppSystem* s, int64_t nsteps) {
     while (nsteps > 0) {
       const int chunk = nsteps > (1 << 20) ? (1 << 20) : (int)nsteps;
       if (launch_vicsek_small(s->k, s->d, chunk, s->stream, &s->host_launches) != 0)
-        return fail(SPP_ERR_CUDA, "k_vicsek_small: shared memory attribute refused");
+        return fail(SPP_ERR_CUDA, "k_vicsek_small: cluster launch refused (shared memory or cluster shape)");
       CUDA_TRY(cudaGetLastError());
       nsteps -= chunk;
     }
@@ -499,7 +499,7 @@ int launch_lyap_chunks(SppSystem* s, int64_t nsteps) {
     int rc = get_lyap_graph(s, chunk, &exec);
     if (rc != SPP_OK) return rc;
     CUDA_TRY(cudaGraphLaunch(exec, s->stream));
-    s->graph_kernels += (int64_t)chunk * 3 * s->nstages + 6;
+    s->graph_kernels += (int64_t)chunk * (2 * s->nstages + 1) + 6;  /* stages x (base, tangent) + gather; renormalisation */
     left -= chunk;
   }
   return SPP_OK;
@@ -983,7 +983,7 @@ int spp_lyap_init(SppSystem* s, int K, uint64_t seed) {
   rc = rc ? rc : dalloc(&L.ua, len);
   rc = rc ? rc : dalloc(&L.ub, len);
   rc = rc ? rc : dalloc(&L.acc, len);
-  rc = rc ? rc : dalloc(&L.uslot, tangent_slot_floats(K, s->p.n));
+  rc = rc ? rc : dalloc(&L.uslot, 2 * tangent_slot_floats(K, s->p.n));
   rc = rc ? rc : dalloc(&L.partial, (size_t)SPP_GRAM_BLOCKS * SPP_GRAM_ENTRIES);
   rc = rc ? rc : dalloc(&L.rinv, (size_t)SPP_LYAP_MAX * SPP_LYAP_MAX);
   rc = rc ? rc : dalloc(&L.log_stretch, SPP_LYAP_MAX);
@@ -991,7 +991,7 @@ int spp_lyap_init(SppSystem* s, int K, uint64_t seed) {
   if (rc != SPP_OK) { free_lyap(s); return rc; }
   CUDA_TRY(cudaMemsetAsync(L.log_stretch, 0, sizeof(double) * SPP_LYAP_MAX, s->stream));
   CUDA_TRY(cudaMemsetAsync(L.error, 0, sizeof(uint32_t), s->stream));
-  CUDA_TRY(cudaMemsetAsync(L.uslot, 0, sizeof(float) * tangent_slot_floats(K, s->p.n), s->stream));
+  CUDA_TRY(cudaMemsetAsync(L.uslot, 0, 2 * sizeof(float) * tangent_slot_floats(K, s->p.n), s->stream));
   launch_tangent_init(L, seed, s->p.system_id, s->stream);
   launch_renormalize(L, 0, s->stream, &s->host_launches);
   s->host_launches += 1;

@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevSta
   const int KP = tan_padded(L.K);
   const uint32_t idi = d.id[i];
   const float4 pi = t.cur[i];
-  const float4 ui = *reinterpret_cast<const float4*>(L.uslot + (size_t)i * KP + v0);
+  const float4 ui = *reinterpret_cast<const float4*>(t.us_in + (size_t)i * KP + v0);
   float acc[TAN_GROUP] = {0.0f, 0.0f, 0.0f, 0.0f};
   /* with one vector per lane, that vector's stage inputs (stored by particle
    * id, so scattered) are loaded first: their latency overlaps the
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevSta
 #pragma unroll
     for (int w = 0; w < TAN_LOADS; ++w) {
       pg[w] = __ldg(t.cur + jg[w]);
-      ug[w] = __ldg(reinterpret_cast<const float4*>(L.uslot + (size_t)jg[w] * KP + v0));
+      ug[w] = __ldg(reinterpret_cast<const float4*>(t.us_in + (size_t)jg[w] * KP + v0));
     }
 #pragma unroll
     for (int w = 0; w < TAN_LOADS; ++w) {
@@ -145,8 +145,13 @@ __global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevSta
       float a = av[c];
       float uo = 0.0f;
       spp_tangent_stage_update(&k, t.stage, t.nstages, slope[c], &t0, &a, &uo);
-      if (t.stage == t.nstages - 1) L.t0[e] = t0;
-      else t.uout[e] = uo;
+      if (t.stage == t.nstages - 1) {
+        L.t0[e] = t0;
+      } else {
+        t.uout[e] = uo;
+        /* the next stage's heading component, straight into slot order */
+        if (c == 2) t.us_out[(size_t)i * KP + v] = uo;
+      }
       if (t.nstages == 4 && t.stage < 3) L.acc[e] = a;
     }
   }
@@ -269,8 +274,16 @@ void launch_tangent_stage(const SppConsts& k, const DevState& d, const LyapState
   float* ub = L.ub;
   t.uin = stage == 0 ? L.t0 : ((stage & 1) ? ua : ub);
   t.uout = (stage & 1) ? ub : ua;
-  const dim3 ggrid((unsigned)((d.n + SPP_BLOCK - 1) / SPP_BLOCK), (unsigned)L.K);
-  k_tangent_gather<<<ggrid, SPP_BLOCK, 0, s>>>(d, L.K, t.uin, L.uslot);
+  const size_t sf = tangent_slot_floats(L.K, d.n);
+  t.us_in = L.uslot + (size_t)(stage & 1) * sf;
+  t.us_out = stage < nstages - 1 ? L.uslot + (size_t)((stage + 1) & 1) * sf : nullptr;
+  if (stage == 0) {
+    /* the step's start vectors (by particle id) into slot order; later
+     * stages get theirs from the stage before */
+    const dim3 ggrid((unsigned)((d.n + SPP_BLOCK - 1) / SPP_BLOCK), (unsigned)L.K);
+    k_tangent_gather<<<ggrid, SPP_BLOCK, 0, s>>>(d, L.K, t.uin, L.uslot);
+    if (launches) *launches += 1;
+  }
   const int lanes = k.lanes;
   const dim3 tgrid((unsigned)(((size_t)d.n * lanes + TAN_BLOCK - 1) / TAN_BLOCK),
                    (unsigned)(tan_padded(L.K) / TAN_GROUP));
@@ -278,7 +291,7 @@ void launch_tangent_stage(const SppConsts& k, const DevState& d, const LyapState
     k_tangent_stage<SPP_GATHER_LANES><<<tgrid, TAN_BLOCK, 0, s>>>(k, d, L, t);
   else
     k_tangent_stage<1><<<tgrid, TAN_BLOCK, 0, s>>>(k, d, L, t);
-  if (launches) *launches += 2;
+  if (launches) *launches += 1;
 }
 
 void launch_renormalize(const LyapState& L, int accumulate, cudaStream_t s, int64_t* launches) {

@@ -24,6 +24,7 @@
  */
 #include "spp_internal.cuh"
 #include <cooperative_groups.h>
+#include <mutex>
 
 namespace {
 
@@ -620,42 +621,45 @@ bool vicsek_small_fits(const SppConsts& k, const DevState& d) {
          vicsek_small_smem(k, d) <= SPP_SMALL_MAX_SMEM;
 }
 
-/* The largest cluster (16, 8, 4, 2 or 1 CTAs) that fits on the device with
- * this shared memory. */
-static int small_cluster_size(size_t smem) {
-  static int cached = 0;
-  static size_t cached_smem = 0;
-  if (cached && cached_smem == smem) return cached;
-  cudaFuncSetAttribute(k_vicsek_small, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  int best = 0;
-  for (int cs = SPP_SMALL_CLUSTER_MAX; cs >= 1 && !best; cs >>= 1) {
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = cs;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(cs);
-    cfg.blockDim = dim3(SPP_SMALL_THREADS);
-    cfg.dynamicSmemBytes = smem;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, k_vicsek_small, &cfg) == cudaSuccess && nclusters > 0)
-      best = cs;
-    else
+/* Once per process: the dynamic shared-memory limit of k_vicsek_small set
+ * to its maximum (every launch needs at most that, so systems of any size
+ * and host threads share the setting), and the largest cluster (16, 8, 4, 2
+ * or 1 CTAs) that fits on the device at that shared memory.  0 on failure. */
+static int small_cluster_size() {
+  static std::once_flag once;
+  static int best = 0;
+  std::call_once(once, [] {
+    if (cudaFuncSetAttribute(k_vicsek_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             SPP_SMALL_MAX_SMEM) != cudaSuccess ||
+        cudaFuncSetAttribute(k_vicsek_small, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+            cudaSuccess) {
       cudaGetLastError();
-  }
-  cached = best;
-  cached_smem = smem;
+      return;
+    }
+    for (int cs = SPP_SMALL_CLUSTER_MAX; cs >= 1 && !best; cs >>= 1) {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = cs;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3(cs);
+      cfg.blockDim = dim3(SPP_SMALL_THREADS);
+      cfg.dynamicSmemBytes = SPP_SMALL_MAX_SMEM;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, k_vicsek_small, &cfg) == cudaSuccess && nclusters > 0)
+        best = cs;
+      else
+        cudaGetLastError();
+    }
+  });
   return best;
 }
 
 int launch_vicsek_small(const SppConsts& k, const DevState& d, int nsteps, cudaStream_t s, int64_t* launches) {
-  const size_t smem = vicsek_small_smem(k, d);
-  if (cudaFuncSetAttribute(k_vicsek_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return -1;
-  const int cs = small_cluster_size(smem);
+  const int cs = small_cluster_size();
   if (cs < 1) return -1;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
@@ -665,7 +669,7 @@ int launch_vicsek_small(const SppConsts& k, const DevState& d, int nsteps, cudaS
   attr[0].val.clusterDim.z = 1;
   cfg.gridDim = dim3(cs);
   cfg.blockDim = dim3(SPP_SMALL_THREADS);
-  cfg.dynamicSmemBytes = smem;
+  cfg.dynamicSmemBytes = vicsek_small_smem(k, d);
   cfg.stream = s;
   cfg.attrs = attr;
   cfg.numAttrs = 1;

@@ -10,7 +10,8 @@ struct LyapState {
   float* ua;              /* stage inputs (RK2/RK4) */
   float* ub;
   float* acc;             /* RK4 slope sums */
-  float* uslot;           /* the stage input's heading components in slot order, [n][K padded to 4] */
+  float* uslot;           /* two buffers of the stage inputs' heading components in slot order,
+                             [2][n][K padded to 4]: stage s reads buffer s % 2, writes the other */
   double* partial;        /* Gram partials [SPP_GRAM_BLOCKS][SPP_GRAM_ENTRIES] */
   double* rinv;           /* R^{-1}, [SPP_LYAP_MAX][SPP_LYAP_MAX] */
   double* log_stretch;    /* running sums of log R_aa, FP64 */
@@ -21,6 +22,8 @@ struct TanStage {
   const float4* cur;      /* base state of this stage (slot order) */
   const float* uin;       /* tangent stage input */
   float* uout;            /* next stage input */
+  const float* us_in;     /* this stage's heading components in slot order */
+  float* us_out;          /* the next stage's, written here (NULL in the last stage) */
   int stage, nstages;
 };
 
