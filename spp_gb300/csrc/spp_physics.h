@@ -582,7 +582,9 @@ SPP_HD void spp_tangent_stage_update(const SppConsts* k, int stage, int nst, flo
 /* Gram-matrix layout of the FP64 renormalisation: entries (a, b), b <= a,
  * packed row by row. */
 #define SPP_GRAM_ENTRIES (SPP_LYAP_MAX * (SPP_LYAP_MAX + 1) / 2)
+#ifndef SPP_GRAM_BLOCKS
 #define SPP_GRAM_BLOCKS 64
+#endif
 #define SPP_GRAM_THREADS 256
 SPP_HD int spp_gram_index(int a, int b) { return a * (a + 1) / 2 + b; }
 
@@ -595,16 +597,20 @@ SPP_HD int spp_cholesky_inverse(int K, const double* G, double* Rinv, double* lo
   double R[SPP_LYAP_MAX][SPP_LYAP_MAX];
   for (int a = 0; a < K; ++a)
     for (int b = 0; b < K; ++b) R[a][b] = 0.0;
+  /* one FP64 division per diagonal entry (FP64 division is a long
+   * dependent sequence on this GPU): the rest multiply by the reciprocal */
+  double inv[SPP_LYAP_MAX];
   for (int j = 0; j < K; ++j) {
     double d = G[spp_gram_index(j, j)];
     for (int q = 0; q < j; ++q) d -= R[q][j] * R[q][j];
     if (!(d > 0.0)) return 1;
     const double rjj = sqrt(d);
     R[j][j] = rjj;
+    inv[j] = 1.0 / rjj;
     for (int c = j + 1; c < K; ++c) {
       double v = G[spp_gram_index(c, j)];
       for (int q = 0; q < j; ++q) v -= R[q][j] * R[q][c];
-      R[j][c] = v / rjj;
+      R[j][c] = v * inv[j];
     }
     log_r[j] = log(rjj);
   }
@@ -612,11 +618,11 @@ SPP_HD int spp_cholesky_inverse(int K, const double* G, double* Rinv, double* lo
   for (int a = 0; a < K; ++a)
     for (int b = 0; b < K; ++b) Rinv[a * SPP_LYAP_MAX + b] = 0.0;
   for (int c = 0; c < K; ++c) {
-    Rinv[c * SPP_LYAP_MAX + c] = 1.0 / R[c][c];
+    Rinv[c * SPP_LYAP_MAX + c] = inv[c];
     for (int r = c - 1; r >= 0; --r) {
       double v = 0.0;
       for (int q = r + 1; q <= c; ++q) v += R[r][q] * Rinv[q * SPP_LYAP_MAX + c];
-      Rinv[r * SPP_LYAP_MAX + c] = -v / R[r][r];
+      Rinv[r * SPP_LYAP_MAX + c] = -v * inv[r];
     }
   }
   return 0;
