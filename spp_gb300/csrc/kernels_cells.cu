@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_scatter(DevState d) {
  * array, insertion-sorted there (lists hold ~5 entries at unit density) and
  * written once; lists longer than the array fall back to sorting in place. */
 #ifndef SPP_LIST_LOCAL
-#define SPP_LIST_LOCAL 16
+#define SPP_LIST_LOCAL 12
 #endif
 /* keys kept in shared memory per thread (column threadIdx.x of a
  * [LIST_LOCAL][SPP_BLOCK] array: conflict-free); entries up to LIST_TAIL
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_scatter(DevState d) {
  * finished by k_sort_long */
 constexpr int LIST_LOCAL = SPP_LIST_LOCAL;
 #ifndef SPP_LIST_TAIL
-#define SPP_LIST_TAIL 24
+#define SPP_LIST_TAIL 16
 #endif
 constexpr int LIST_TAIL = SPP_LIST_TAIL;
 

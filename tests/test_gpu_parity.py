@@ -347,8 +347,8 @@ def clustered_state(n, L, clusters, seed):
 @pytest.mark.parametrize("n", [4096, 20000])
 def test_long_lists_bitexact_vs_mirror(gpu_lib, n):
     """Clusters of 700, 300, 150, 100, 60 and 28 particles in a sparse background:
-    lists longer than the 16 shared-memory keys are finished in place up to
-    24 entries, then by the warp bitonic sort (32 to 512 keys) and beyond 512
+    lists longer than the 12 shared-memory keys are finished in place up to
+    16 entries, then by the warp bitonic sort (32 to 512 keys) and beyond 512
     by the one-lane fallback; the list overflows and regrows on the way.
     4096 particles use four lanes per particle, 20,000 one."""
     p = configs.reference_defaults(abi.MODEL_CONTINUOUS)
