@@ -125,7 +125,31 @@ typedef struct SppParams {
   double bead_separation; /* ActiveBrownianChain::separation: distance between a swimmer's beads */
   double sigma_chain;     /* ActiveBrownianChain::sigma_p: R12 sigma of bead pairs that involve a chain */
   double r_chain;         /* ActiveBrownianChain::repulsion_radius: their cutoff */
+  /* Closed box with walls (the reference built without
+   * PERIODIC_BOUNDARY_CONDITION, shared/parameters.h:6): no wrap and no
+   * minimum image; the four box walls of Box::Init_Topology
+   * (parallel/box.h:92-101) plus n_walls extra segments (Geometry::Add_Wall,
+   * shared/geometry.h:34-47) act on every particle each stage
+   * (parallel/box.h:296-302).  Built for SPP_MODEL_ABP (Wall::Interact
+   * (RepulsiveParticle*), shared/wall.h:215-265) and SPP_MODEL_CONTINUOUS
+   * (Wall::Interact(ContinuousParticle*), :192-213). */
+  int32_t boundary;       /* enum SppBoundary */
+  int32_t n_walls;        /* extra wall segments, 0 .. SPP_MAX_WALLS - 4 */
+  double walls[4][4];     /* x1, y1, x2, y2 of the extra segments (point_1 -> point_2) */
+  double A_w;             /* RepulsiveParticle::A_w: wall repulsion amplitude */
+  double sigma_w;         /* RepulsiveParticle::sigma_w: its screening length */
+  double r_c_w;           /* RepulsiveParticle::r_c_w: its cutoff */
+  double r_f_w;           /* RepulsiveParticle::r_f_w: range of the wall alignment torque */
+  double g_w;             /* RepulsiveParticle::g_w: wall alignment strength */
+  double g_w_cont;        /* ContinuousParticle::gw: wall torque strength of the continuous model */
 } SppParams;
+
+/* Boundary of the box. */
+enum SppBoundary {
+  SPP_BOUNDARY_PERIODIC = 0,  /* periodic box [-L, L)^2 */
+  SPP_BOUNDARY_WALLS = 1      /* closed box: the box walls plus SppParams.walls */
+};
+#define SPP_MAX_WALLS 8
 
 /* Largest chain_beads. */
 #define SPP_MAX_CHAIN_BEADS 8

@@ -49,6 +49,10 @@ def orc():
         L.orc64_lyap_clone.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D,
                                        _D, _D, _D]
         L.orc32_rsqrt.argtypes = [C.c_float]
+        L.orc32_wall_terms.argtypes = [_P, C.c_float, C.c_float, C.c_float, _F]
+        L.orc32_wall_terms.restype = None
+        L.orc64_wall_terms.argtypes = [_P, C.c_double, C.c_double, C.c_double, _D]
+        L.orc64_wall_terms.restype = None
         L.orc32_tumble_steps.argtypes = [_P]
         L.orc32_tumble_steps.restype = C.c_int32
         L.orc32_radial.argtypes = [_F, _F, C.c_int, C.c_double, C.c_double, C.c_int, _U64]
@@ -69,6 +73,8 @@ def ref():
         L = C.CDLL(str(path))
         L.ref_run.argtypes = [_P, C.c_int, C.c_int64, _D, _D, _D, _D, _D]
         L.ref_run.restype = C.c_int
+        L.ref_wall_terms.argtypes = [_P, C.c_double, C.c_double, C.c_double, _D]
+        L.ref_wall_terms.restype = None
         L.ref_r12_truncated.argtypes = [C.c_double] * 5 + [_D, _D]
         L.ref_spring.argtypes = [C.c_double] * 4 + [_D, _D]
         _ref = L
@@ -293,3 +299,19 @@ def math32(fn, a, b=None):
     out = np.empty_like(a)
     orc().orc32_math(MATH_FNS[fn], len(a), _f(a), _f(b), _f(out))
     return out
+
+
+def wall_terms(p, x, y, th, fn="orc64"):
+    """Walls of p's closed box on one particle: {fx, fy, RepulsiveParticle
+    torque, ContinuousParticle torque} from the FP64 restatement
+    (fn='orc64'), the reference's own Wall::Interact (fn='ref'), or the
+    kernels' FP32 arithmetic (fn='orc32': {fx, fy, torque})."""
+    if fn == "orc32":
+        out = np.zeros(3, np.float32)
+        orc().orc32_wall_terms(C.byref(p), float(x), float(y), float(th), _f(out))
+        return out
+    out = np.zeros(4, np.float64)
+    lib = orc().orc64_wall_terms if fn == "orc64" else ref().ref_wall_terms
+    lib(C.byref(p), float(x), float(y), float(th), _d(out))
+    return out
+

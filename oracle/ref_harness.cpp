@@ -19,6 +19,7 @@
  * which changes FP64 sums only in the last bits.
  */
 #include "particle.h"   /* shared/particle.h of the reference */
+#include "wall.h"       /* shared/wall.h of the reference */
 #include "../include/spp.h"
 #include <vector>
 #include <cmath>
@@ -286,4 +287,45 @@ extern "C" void ref_spring(double dx, double dy, double sigma, double A, double*
   Real d = std::sqrt(dr.Square());
   C2DVector f = Spring(dr, d, sigma, A);
   *fx = f.x; *fy = f.y;
+}
+
+/* The reference's walls (Wall::Init, Wall::Interact, shared/wall.h) on one
+ * particle, for the segments p->walls[0 .. p->n_walls) alone.  out4 =
+ * {f.x, f.y, torque} of a RepulsiveParticle, or {0, 0, 0, torque} of a
+ * ContinuousParticle.  The harness is built with the reference's
+ * PERIODIC_BOUNDARY_CONDITION, so the box is set 1e9 wide here: then the
+ * Periodic_Transform calls of Wall change nothing, as in the reference's
+ * closed-box build. */
+extern "C" void ref_wall_terms(const SppParams* p, double x, double y, double th, double* out4) {
+  set_box(1e9);
+  out4[0] = out4[1] = out4[2] = out4[3] = 0.0;
+  if (p->model == SPP_MODEL_CONTINUOUS) {
+    ContinuousParticle::gw = p->g_w_cont;
+    ContinuousParticle q;
+    q.r.x = x; q.r.y = y; q.theta = th;
+    q.v.x = std::cos(th); q.v.y = std::sin(th);
+    q.torque = 0;
+    for (int e = 0; e < p->n_walls; ++e) {
+      Wall w;
+      w.Init(p->walls[e][0], p->walls[e][1], p->walls[e][2], p->walls[e][3]);
+      w.Interact(&q);
+    }
+    out4[3] = q.torque;
+  } else {
+    RepulsiveParticle::r_c_w = p->r_c_w;
+    RepulsiveParticle::r_f_w = p->r_f_w;
+    RepulsiveParticle::sigma_w = p->sigma_w;
+    RepulsiveParticle::A_w = p->A_w;
+    RepulsiveParticle::g_w = p->g_w;
+    RepulsiveParticle q;
+    q.r.x = x; q.r.y = y; q.theta = th;
+    q.v.x = std::cos(th); q.v.y = std::sin(th);
+    q.f.x = 0; q.f.y = 0; q.torque = 0;
+    for (int e = 0; e < p->n_walls; ++e) {
+      Wall w;
+      w.Init(p->walls[e][0], p->walls[e][1], p->walls[e][2], p->walls[e][3]);
+      w.Interact(&q);
+    }
+    out4[0] = q.f.x; out4[1] = q.f.y; out4[2] = q.torque;
+  }
 }

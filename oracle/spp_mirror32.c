@@ -152,7 +152,7 @@ static void body_rates(const SppConsts* k, int i, const SppAccF* a, const float*
       spp_bead_velocity(k, !bead, a, rfx, rfy, ci, si, fx, fy, tau);
     }
   } else {
-    spp_abp_forces(k, a, ci, si, fx, fy, tau);
+    spp_abp_forces(k, k->n_walls > 0, a, cx[i], cy[i], ci, si, fx, fy, tau);
     *dth = spp_rot_noise(k, (uint32_t)i, step);
   }
 }
@@ -189,7 +189,7 @@ static int abp_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t
         int gx = ix[i], gy = iy[i];
         float nt, ncs, nsn;
         spp_euler_update(x[i], y[i], th[i], fx, fy, tau, dth, k, &hx[i], &hy[i], &nt, &ncs, &nsn,
-                         &gx, &gy);
+                         &gx, &gy, k->closed);
         kx[i] = nt; hc[i] = ncs; hs[i] = nsn;
         ix[i] = gx; iy[i] = gy;
       }
@@ -224,7 +224,7 @@ static int abp_run32(const SppParams* p, const SppConsts* k, int nsteps, int64_t
         float tnew;
         int gx = ix[i], gy = iy[i];
         spp_stage_update(h, frac, x[i], y[i], th[i], fx, fy, tau, dth, k, &nx[i], &ny[i], &tnew,
-                         &nc[i], &ns[i], &gx, &gy);
+                         &nc[i], &ns[i], &gx, &gy, k->closed);
         if (last) { th[i] = tnew; ix[i] = gx; iy[i] = gy; }
       }
       if (last) {
@@ -533,7 +533,7 @@ int orc32_lyap_run(const SppParams* p, int nsteps, int64_t step0, int renorm_eve
       /* base stage update */
       for (int i = 0; i < n; ++i) {
         float fx, fy, tau;
-        spp_abp_forces(&k, &A[i], cc[i], cs[i], &fx, &fy, &tau);
+        spp_abp_forces(&k, k.n_walls > 0, &A[i], cx[i], cy[i], cc[i], cs[i], &fx, &fy, &tau);
         float dth = spp_rot_noise(&k, (uint32_t)i, step);
         float h, frac;
         if (nst == 2) {
@@ -549,7 +549,7 @@ int orc32_lyap_run(const SppParams* p, int nsteps, int64_t step0, int renorm_eve
         float tnew;
         int gx = ix[i], gy = iy[i];
         spp_stage_update(h, frac, x[i], y[i], th[i], fx, fy, tau, dth, &k, &nx[i], &ny[i], &tnew,
-                         &nc[i], &ns[i], &gx, &gy);
+                         &nc[i], &ns[i], &gx, &gy, k.closed);
         if (last) { th[i] = tnew; ix[i] = gx; iy[i] = gy; }
       }
       /* tangent stage update */
@@ -628,4 +628,22 @@ int32_t orc32_tumble_steps(const SppParams* p) {
   SppConsts k;
   spp_consts_from_params(&k, p);
   return k.tumble_steps;
+}
+
+/* The kernels' FP32 wall terms (spp_wall_terms) for one particle at (x, y)
+ * with heading (cos th, sin th) from spp_sincosf, for the segments
+ * p->walls[0 .. n_walls) alone: out3 = {fx, fy, torque}. */
+void orc32_wall_terms(const SppParams* p, float x, float y, float th, float* out3) {
+  SppConsts k;
+  spp_consts_from_params(&k, p);
+  for (int e = 0; e < p->n_walls; ++e) {   /* drop the 4 box walls */
+    k.wall_x1[e] = k.wall_x1[e + 4]; k.wall_y1[e] = k.wall_y1[e + 4];
+    k.wall_x2[e] = k.wall_x2[e + 4]; k.wall_y2[e] = k.wall_y2[e + 4];
+    k.wall_ex[e] = k.wall_ex[e + 4]; k.wall_ey[e] = k.wall_ey[e + 4];
+    k.wall_len[e] = k.wall_len[e + 4];
+  }
+  k.n_walls = p->n_walls;
+  float s, c;
+  spp_sincosf(th, &s, &c);
+  spp_wall_terms(&k, x, y, c, s, &out3[0], &out3[1], &out3[2]);
 }

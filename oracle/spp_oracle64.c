@@ -50,8 +50,14 @@ static double orc_uniform_pm_pi(const SppParams* p, int pid, int64_t step) {
   return -M_PI * (1.0 - u) + M_PI * u; /* gsl_ran_flat(r, -pi, pi): a (1-u) + b u */
 }
 
+/* Set for a closed box (SPP_BOUNDARY_WALLS) for the duration of a run: the
+ * reference built without PERIODIC_BOUNDARY_CONDITION skips every
+ * Periodic_Transform. */
+static int g_closed = 0;
+
 /* Periodic_Transform, shared/c2dvector.h:67-73 */
 static inline double pt(double x, double L) {
+  if (g_closed) return x;
   double L2 = 2.0 * L;
   return x - L2 * (double)(int)floor(x / L2 + 0.5);
 }
@@ -126,6 +132,7 @@ typedef struct {
   double *avx, *avy, *ath;        /* Vicsek averages */
   double *tho, *xo, *yo, *dth;    /* theta_old, r_old, dtheta */
   double *k1f_x, *k1f_y, *k1t, *k2f_x, *k2f_y, *k2t, *k3f_x, *k3f_y, *k3t;
+  double* wtq;                    /* wall torque of RepulsiveParticle (added after the alignment normalisation) */
   int* tflag;                     /* RTPChain::tumble_flag */
   double* telapsed;               /* RTPChain::tumble_elapesed_time */
 } ostate;
@@ -144,11 +151,13 @@ static void state_alloc(ostate* s, const SppParams* p) {
   s->k1f_x = dalloc(n); s->k1f_y = dalloc(n); s->k1t = dalloc(n);
   s->k2f_x = dalloc(n); s->k2f_y = dalloc(n); s->k2t = dalloc(n);
   s->k3f_x = dalloc(n); s->k3f_y = dalloc(n); s->k3t = dalloc(n);
+  s->wtq = dalloc(n);
   s->tflag = (int*)calloc((size_t)(n > 0 ? n : 1), sizeof(int));
   s->telapsed = dalloc(n);
 }
 static void state_free(ostate* s) {
   free(s->tflag);
+  free(s->wtq);
   free(s->telapsed);
   double* arr[] = {s->x, s->y, s->xu, s->yu, s->th, s->vx, s->vy, s->fx, s->fy, s->tq,
                    s->avx, s->avy, s->ath, s->tho, s->xo, s->yo, s->dth,
@@ -315,14 +324,114 @@ static void abp_reset(ostate* s) {
 static double abp_torque(const ostate* s, int i) {
   const SppParams* p = s->p;
   if (p->model == SPP_MODEL_CONTINUOUS) return p->g * s->tq[i];
-  if (p->align_mode == SPP_ALIGN_MEAN) return p->g * s->tq[i] / s->nb[i];
-  return s->tq[i];
+  if (p->align_mode == SPP_ALIGN_MEAN) return p->g * s->tq[i] / s->nb[i] + s->wtq[i];
+  return s->tq[i] + s->wtq[i];
 }
 static void set_v(ostate* s, int i) { s->vx[i] = cos(s->th[i]); s->vy[i] = sin(s->th[i]); }
+
+/* Walls of a closed box: Box::Init_Topology (parallel/box.h:97-101) plus
+ * the extra segments, each through Wall::Init (shared/wall.h:27-41). */
+typedef struct { double x1, y1, x2, y2, dx, dy, len, theta; } owall;
+
+static int box_walls(const SppParams* p, owall* w) {
+  double seg[SPP_MAX_WALLS][4] = {{-p->L, -p->L, -p->L, p->L}, {-p->L, p->L, p->L, p->L},
+                                  {p->L, p->L, p->L, -p->L}, {p->L, -p->L, -p->L, -p->L}};
+  int nw = 4;
+  for (int e = 0; e < p->n_walls && nw < SPP_MAX_WALLS; ++e, ++nw)
+    for (int c = 0; c < 4; ++c) seg[nw][c] = p->walls[e][c];
+  for (int e = 0; e < nw; ++e) {
+    w[e].x1 = seg[e][0]; w[e].y1 = seg[e][1]; w[e].x2 = seg[e][2]; w[e].y2 = seg[e][3];
+    double dx = w[e].x2 - w[e].x1, dy = w[e].y2 - w[e].y1;
+    w[e].len = sqrt(dx * dx + dy * dy);
+    w[e].dx = dx / w[e].len; w[e].dy = dy / w[e].len;
+    double th = atan(w[e].dy / w[e].dx);
+    if (w[e].dx < 0.) th += M_PI;
+    th -= 2 * M_PI * (int)(th / M_PI);
+    w[e].theta = th;
+  }
+  return nw;
+}
+
+/* Wall::Interact (shared/wall.h:192-265) of the walls w[0..nw) on one
+ * particle at (x, y) with heading theta (v = (vx, vy)): RepulsiveParticle
+ * force and torque into *fx, *fy, *wtq; ContinuousParticle torque into
+ * *ctq (before the factor g of Move). */
+static void wall_terms64(const SppParams* p, const owall* w, int nw, double x, double y, double th,
+                         double vx, double vy, double* fx, double* fy, double* wtq, double* ctq) {
+  for (int e = 0; e < nw; ++e) {
+    double r1x = pt(x - w[e].x1, p->L), r1y = pt(y - w[e].y1, p->L);
+    double proj = r1x * w[e].dx + r1y * w[e].dy;
+    if (p->model == SPP_MODEL_CONTINUOUS) {
+      double drx = r1x - w[e].dx * proj, dry = r1y - w[e].dy * proj;
+      double d2 = drx * drx + dry * dry;
+      if (d2 < 1) *ctq += p->g_w_cont * ((vx * dry - vy * drx) / (2 * M_PI * d2));
+      continue;
+    }
+    /* Distance_Vector, wall.h:127-148 */
+    double drx, dry;
+    if (proj < w[e].len && proj > 0) {
+      drx = r1x - w[e].dx * proj; dry = r1y - w[e].dy * proj;
+    } else {
+      double r2x = pt(x - w[e].x2, p->L), r2y = pt(y - w[e].y2, p->L);
+      double d21 = r1x * r1x + r1y * r1y, d22 = r2x * r2x + r2y * r2y;
+      if (d22 < d21) { drx = r2x; dry = r2y; } else { drx = r1x; dry = r1y; }
+    }
+    double d2 = drx * drx + dry * dry;
+    double d = sqrt(d2);
+    if (d < p->r_c_w) {
+      drx /= d; dry /= d;
+      double rc2 = p->r_c_w * p->r_c_w;
+      double mag = p->A_w * (exp(-d / p->sigma_w) * (1. / d2 + 1. / (p->sigma_w * d)) -
+                             exp(-p->r_c_w / p->sigma_w) * (1. / rc2 + 1. / (p->sigma_w * p->r_c_w)));
+      *fx += drx * mag; *fy += dry * mag;
+    }
+    if (d < p->r_f_w && proj < w[e].len && proj > 0.) {
+      double sx = cos(th), sy = sin(th);
+      if (drx * sx + dry * sy < 0.) {
+        double dtheta = th - w[e].theta;
+        double t = p->g_w * sin(dtheta) / M_PI;
+        dtheta -= 2 * M_PI * ((int)(dtheta / (2 * M_PI)));
+        if (dtheta < 0.) dtheta += 2 * M_PI;
+        if (dtheta > M_PI / 2 && dtheta < 3 * M_PI / 2) t *= -1.;
+        *wtq -= t;
+      }
+    }
+  }
+}
+
+/* The walls of a closed box on every particle after the pair sums
+ * (parallel/box.h:296-302). */
+static void walls_interact(ostate* s) {
+  const SppParams* p = s->p;
+  owall w[SPP_MAX_WALLS];
+  const int nw = box_walls(p, w);
+  for (int i = 0; i < s->n; ++i) {
+    s->wtq[i] = 0.0;
+    wall_terms64(p, w, nw, s->x[i], s->y[i], s->th[i], s->vx[i], s->vy[i], &s->fx[i], &s->fy[i],
+                 &s->wtq[i], &s->tq[i]);
+  }
+}
+
+/* One particle against the segments p->walls[0 .. n_walls) alone (the
+ * box walls are segments like these), for the pin against the reference's
+ * Wall::Interact. */
+void orc64_wall_terms(const SppParams* p, double x, double y, double th, double* out4) {
+  owall w[SPP_MAX_WALLS];
+  SppParams q = *p;
+  q.L = 1e9;                /* box_walls puts its 4 box walls far away: skip them */
+  box_walls(&q, w);
+  const int nw = p->n_walls;
+  for (int e = 0; e < nw; ++e) w[e] = w[e + 4];
+  out4[0] = out4[1] = out4[2] = out4[3] = 0.0;
+  g_closed = 1;
+  wall_terms64(p, w, nw, x, y, th, cos(th), sin(th), &out4[0], &out4[1], &out4[2], &out4[3]);
+  g_closed = 0;
+}
 
 static void abp_stage_forces(ostate* s) {
   abp_reset(s);
   interact_all(s, s->p->model == SPP_MODEL_CONTINUOUS ? cont_pair : abp_pair);
+  if (s->p->boundary == SPP_BOUNDARY_WALLS) walls_interact(s);
 }
 
 static void abp_step(ostate* s, int64_t step) {
@@ -636,6 +745,7 @@ static void cont_euler_step(ostate* s, int64_t step) {
   double dt = p->dt, sigma = sqrt(2 * p->Dr * dt);
   for (int i = 0; i < s->n; ++i) { s->nb[i] = 1; s->tq[i] = 0; }
   interact_all(s, cont_pair);
+  if (p->boundary == SPP_BOUNDARY_WALLS) walls_interact(s);
   for (int i = 0; i < s->n; ++i) {
     double torque = p->g * s->tq[i] + sigma * orc_normal(p, i, step);
     s->th[i] += torque * dt;
@@ -703,6 +813,7 @@ int orc64_run(const SppParams* p, int nsteps, int64_t step0, double* x, double* 
   memcpy(s.th, th, sizeof(double) * n);
   for (int i = 0; i < n; ++i) set_v(&s, i);
   int rc = 0;
+  g_closed = p->boundary == SPP_BOUNDARY_WALLS;
   for (int k = 0; k < nsteps; ++k) {
     int64_t step = step0 + k;
     switch (p->model) {
@@ -721,6 +832,7 @@ int orc64_run(const SppParams* p, int nsteps, int64_t step0, double* x, double* 
   memcpy(x, s.x, sizeof(double) * n); memcpy(y, s.y, sizeof(double) * n);
   memcpy(xu, s.xu, sizeof(double) * n); memcpy(yu, s.yu, sizeof(double) * n);
   memcpy(th, s.th, sizeof(double) * n);
+  g_closed = 0;
   state_free(&s);
   return rc;
 }

@@ -19,6 +19,7 @@ STATUS_NAMES = {0: "SPP_OK", 1: "SPP_ERR_INVALID", 2: "SPP_ERR_ALLOC", 3: "SPP_E
 MODEL_VICSEK, MODEL_VICSEK_REF_ANGLE, MODEL_VICSEK_REF_VECTOR = 0, 1, 2
 MODEL_CONTINUOUS, MODEL_ABP, MODEL_BEADS = 3, 4, 5
 NOISE_GAUSSIAN, NOISE_TUMBLE = 0, 1
+BOUNDARY_PERIODIC, BOUNDARY_WALLS = 0, 1
 INT_EULER, INT_RK2, INT_RK4 = 1, 2, 4
 FORCE_NONE, FORCE_HARMONIC, FORCE_R12_TRUNC = 0, 1, 2
 ALIGN_REFERENCE, ALIGN_MEAN = 0, 1
@@ -40,6 +41,9 @@ class SppParams(C.Structure):
         ("tumble_rate", C.c_double), ("tumble_time", C.c_double), ("tumble_torque", C.c_double),
         ("chain_beads", C.c_int32), ("reserved2", C.c_int32),
         ("bead_separation", C.c_double), ("sigma_chain", C.c_double), ("r_chain", C.c_double),
+        ("boundary", C.c_int32), ("n_walls", C.c_int32), ("walls", (C.c_double * 4) * 4),
+        ("A_w", C.c_double), ("sigma_w", C.c_double), ("r_c_w", C.c_double), ("r_f_w", C.c_double),
+        ("g_w", C.c_double), ("g_w_cont", C.c_double),
     ]
 
     def copy(self):
@@ -50,11 +54,13 @@ class SppParams(C.Structure):
     def replace(self, **kw):
         q = self.copy()
         for k, v in kw.items():
-            setattr(q, k, v)
+            set_field(q, k, v)
         return q
 
     def as_dict(self):
-        return {name: getattr(self, name) for name, _ in self._fields_}
+        def plain(v):
+            return [plain(e) for e in v] if isinstance(v, C.Array) else v
+        return {name: plain(getattr(self, name)) for name, _ in self._fields_}
 
 
 class SppObservables(C.Structure):
@@ -92,11 +98,22 @@ class SppOrderStats(C.Structure):
                 ("p4_mean", C.c_double), ("binder", C.c_double), ("binder_reference", C.c_double)]
 
 
+def set_field(p, name, value):
+    """Sets a field, array fields (walls) from nested sequences."""
+    cur = getattr(p, name)
+    if isinstance(cur, C.Array):
+        for a, row in enumerate(value):
+            for b, v in enumerate(row):
+                cur[a][b] = v
+    else:
+        setattr(p, name, value)
+
+
 def new_params(**kw) -> SppParams:
     p = SppParams()
     p.struct_size = C.sizeof(SppParams)
     for k, v in kw.items():
-        setattr(p, k, v)
+        set_field(p, k, v)
     return p
 
 

@@ -227,6 +227,48 @@ def chain_state(p, seed=None):
     return x, y, th
 
 
+def walls_config(n=4096, L=40.0, model=abi.MODEL_ABP, integrator=abi.INT_RK2, seed=6,
+                 extra_walls=((-10.0, -4.0, 8.0, 12.0), (6.0, -14.0, -12.0, 2.0))):
+    """A closed box (the reference built without PERIODIC_BOUNDARY_CONDITION):
+    the four box walls plus extra segments, with the wall interactions of
+    RepulsiveParticle (screened repulsion A_w = 3, sigma_w = 0.4, cutoff 1.5;
+    alignment g_w = 2 within 1.2) or ContinuousParticle (gw = 20).  ABP: the
+    reference's R12 pair law and alignment; continuous: g = 1, alpha = 0."""
+    p = reference_defaults(model)
+    p.n, p.L, p.seed, p.integrator = n, L, seed, integrator
+    p.boundary = abi.BOUNDARY_WALLS
+    p.n_walls = len(extra_walls)
+    abi.set_field(p, "walls", [list(w) for w in extra_walls])
+    p.A_w, p.sigma_w, p.r_c_w, p.r_f_w, p.g_w, p.g_w_cont = 3.0, 0.4, 1.5, 1.2, 2.0, 20.0
+    p.Dr, p.dt, p.skin = 0.1, 0.005, 0.3
+    if model == abi.MODEL_CONTINUOUS:
+        p.g, p.alpha, p.v0, p.dt = 1.0, 0.0, 0.5, 0.01
+    return p
+
+
+def walls_state(p, seed=None):
+    """Particles on a square lattice of spacing 1.05 inside the box, at
+    least 2 from the box walls and 1.6 from the extra segments; random
+    headings."""
+    seed = p.seed if seed is None else seed
+    g = np.arange(-p.L + 2.0, p.L - 2.0, 1.05)
+    X, Y = np.meshgrid(g, g)
+    x, y = X.ravel(), Y.ravel()
+    keep = np.ones(x.size, bool)
+    for w in range(p.n_walls):
+        x1, y1, x2, y2 = list(p.walls[w])
+        ex, ey = x2 - x1, y2 - y1
+        t = np.clip(((x - x1) * ex + (y - y1) * ey) / (ex * ex + ey * ey), 0.0, 1.0)
+        keep &= np.hypot(x - (x1 + t * ex), y - (y1 + t * ey)) > 1.6
+    x, y = x[keep][:p.n], y[keep][:p.n]
+    if x.size < p.n:
+        raise ValueError("box too small for n particles")
+    ids = np.arange(p.n, dtype=np.uint32)
+    r = draw(seed, 0, ids, 0, RNG_INIT_ANGLE)
+    th = ((2 * u01_f32(r[0]).astype(np.float64) - 1) * math.pi).astype(np.float32)
+    return x.astype(np.float32), y.astype(np.float32), th
+
+
 def lyapunov_config(n=16384, rho=1.0, seed=3, integrator=abi.INT_RK4) -> abi.SppParams:
     """Continuous-time Vicsek for the Lyapunov spectrum: N = 16,384 at
     rho = 1 (L = 64), v0 = 0.5, g = 1, alpha = 0, D_r = 0, r = 1, RK4 with

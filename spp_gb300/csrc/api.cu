@@ -160,6 +160,26 @@ int validate(const SppParams* p) {
         !std::isfinite(p->bead_separation) || !std::isfinite(p->sigma_chain) || !std::isfinite(p->r_chain))
       return fail(SPP_ERR_INVALID, "bead_separation, sigma_chain and r_chain must be finite and > 0");
   }
+  if (p->boundary != SPP_BOUNDARY_PERIODIC && p->boundary != SPP_BOUNDARY_WALLS)
+    return fail(SPP_ERR_INVALID, "boundary must be SPP_BOUNDARY_PERIODIC or SPP_BOUNDARY_WALLS");
+  if (p->boundary == SPP_BOUNDARY_WALLS) {
+    if (p->model != SPP_MODEL_ABP && p->model != SPP_MODEL_CONTINUOUS)
+      return fail(SPP_ERR_UNSUPPORTED, "walls are built for SPP_MODEL_ABP and SPP_MODEL_CONTINUOUS "
+                                       "(Wall::Interact of RepulsiveParticle and ContinuousParticle)");
+    if (p->n_walls < 0 || p->n_walls > SPP_MAX_WALLS - 4)
+      return fail(SPP_ERR_INVALID, "n_walls must be 0 .. SPP_MAX_WALLS - 4 (the box has 4 walls)");
+    for (int w = 0; w < p->n_walls; ++w) {
+      const double* q = p->walls[w];
+      if (!std::isfinite(q[0]) || !std::isfinite(q[1]) || !std::isfinite(q[2]) || !std::isfinite(q[3]) ||
+          (q[0] == q[2] && q[1] == q[3]))
+        return fail(SPP_ERR_INVALID, "wall " + std::to_string(w) + ": finite end points, nonzero length");
+    }
+    const double wp[6] = {p->A_w, p->sigma_w, p->r_c_w, p->r_f_w, p->g_w, p->g_w_cont};
+    for (double v : wp)
+      if (!std::isfinite(v)) return fail(SPP_ERR_INVALID, "wall parameters must be finite");
+    if (p->r_c_w > 0 && !(p->sigma_w > 0))
+      return fail(SPP_ERR_INVALID, "wall repulsion (r_c_w > 0) needs sigma_w > 0");
+  }
   switch (p->model) {
     case SPP_MODEL_VICSEK:
     case SPP_MODEL_VICSEK_REF_ANGLE:
@@ -566,6 +586,11 @@ int spp_params_init(SppParams* p, int model) {
   p->tumble_rate = 0.1;
   p->tumble_time = 10 * 0.1;
   p->tumble_torque = 1.0;
+  /* walls: RepulsiveParticle's wall statics are never assigned in the
+   * reference (particle.h:781-785: zero), ContinuousParticle::gw = 20
+   * (particle.h:378) */
+  p->boundary = SPP_BOUNDARY_PERIODIC;
+  p->g_w_cont = 20.0;
   /* ActiveBrownianChain statics, particle.h:1049-1054 (used with chain_beads > 1) */
   p->chain_beads = 1;
   p->bead_separation = 1.0;
@@ -968,9 +993,10 @@ int spp_lyap_init(SppSystem* s, int K, uint64_t seed) {
   if (!s) return fail(SPP_ERR_INVALID, "system is NULL");
   if (!s->uploaded) return fail(SPP_ERR_INVALID, "no state uploaded");
   if (K < 1 || K > SPP_LYAP_MAX) return fail(SPP_ERR_INVALID, "need 1 <= K <= 8 tangent vectors");
-  if (s->p.model != SPP_MODEL_CONTINUOUS || s->p.alpha != 0.0 || s->p.force_law != SPP_FORCE_NONE)
+  if (s->p.model != SPP_MODEL_CONTINUOUS || s->p.alpha != 0.0 || s->p.force_law != SPP_FORCE_NONE ||
+      s->p.boundary != SPP_BOUNDARY_PERIODIC)
     return fail(SPP_ERR_UNSUPPORTED,
-                "the tangent dynamics is built for the continuous model with alpha = 0 and no repulsion");
+                "the tangent dynamics is built for the periodic continuous model with alpha = 0 and no repulsion");
   if (s->nstages < 2) return fail(SPP_ERR_UNSUPPORTED, "tangent dynamics needs RK2 or RK4");
   int rc = spp_sync(s);
   if (rc != SPP_OK) return rc;

@@ -548,10 +548,10 @@ int spp_batch_create(const SppParams* systems, int n_systems, SppBatch** out) {
     const SppParams& p = systems[s];
     if (p.struct_size != sizeof(SppParams) || p.n < 1 || !(p.L > 0) || !(p.r_align > 0) ||
         (p.model != SPP_MODEL_VICSEK && p.model != SPP_MODEL_VICSEK_REF_ANGLE &&
-         p.model != SPP_MODEL_VICSEK_REF_VECTOR)) {
+         p.model != SPP_MODEL_VICSEK_REF_VECTOR) || p.boundary != SPP_BOUNDARY_PERIODIC) {
       delete b;
       return bfail(SPP_ERR_INVALID, "system " + std::to_string(s) +
-                                        ": batches hold Vicsek-family systems with n >= 1, L > 0");
+                                        ": batches hold periodic Vicsek-family systems with n >= 1, L > 0");
     }
     double rc = p.r_align;
     if (p.model == SPP_MODEL_VICSEK_REF_VECTOR && p.r_push > rc) rc = p.r_push;

@@ -419,7 +419,8 @@ __global__ void k_init_state(SppConsts k, DevState d, const float* __restrict__ 
   if (i >= d.n) return;
   const float xi = x[i], yi = y[i], ti = th[i];
   if (!isfinite(xi) || !isfinite(yi) || !isfinite(ti)) atomicMin(&d.ctl->bad_nonfinite, (uint32_t)i);
-  else if (!(xi >= -k.L && xi < k.L && yi >= -k.L && yi < k.L)) atomicMin(&d.ctl->bad_range, (uint32_t)i);
+  else if (!k.closed && !(xi >= -k.L && xi < k.L && yi >= -k.L && yi < k.L))
+    atomicMin(&d.ctl->bad_range, (uint32_t)i);  /* a closed box has no wrap to undo: any finite position */
   float s, c;
   spp_sincosf(ti, &s, &c);
   d.pos[i] = make_float4(xi, yi, c, s);

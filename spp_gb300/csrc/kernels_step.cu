@@ -116,7 +116,7 @@ __device__ __forceinline__ void stage_pair(const SppConsts& k, const DevState& d
  * id-ordered segment of the list (spp_list_order), and the lane sums
  * combine through xor shuffles as (p0 + p1) + (p2 + p3); lane 0 then
  * finishes the particle. */
-template <int LAW, int KIND, int LANES>
+template <int LAW, int KIND, int LANES, int CLOSED>
 __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_STAGE_MIN_BLOCKS) k_abp_stage(SppConsts k, DevState d, StageBufs b,
                                                          cudaGraphConditionalHandle cond,
                                                          int use_cond) {
@@ -157,7 +157,8 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
 #pragma unroll
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
         if (q0 + u < q_end) {
-          if (all_inner)
+          /* the minimum image only off the interior of a periodic box */
+          if (all_inner || CLOSED)
             stage_pair<LAW, KIND>(k, d, 0, &a, nbi, jg[u], pi, pg[u]);
           else
             stage_pair<LAW, KIND>(k, d, 1, &a, nbi, jg[u], pi, pg[u]);
@@ -205,7 +206,7 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
       }
       turns = !bead;
     } else {
-      spp_abp_forces(&k, &a, pi.z, pi.w, &fx, &fy, &tau);
+      spp_abp_forces(&k, CLOSED, &a, pi.x, pi.y, pi.z, pi.w, &fx, &fy, &tau);
     }
     float dth;
     if (b.stage == 0) {
@@ -231,7 +232,7 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
     float nx, ny, nt, nc, ns;
     int gx = 0, gy = 0;
     if (b.nstages == 1) {
-      spp_euler_update(p0.x, p0.y, th0, fx, fy, tau, dth, &k, &nx, &ny, &nt, &nc, &ns, &gx, &gy);
+      spp_euler_update(p0.x, p0.y, th0, fx, fy, tau, dth, &k, &nx, &ny, &nt, &nc, &ns, &gx, &gy, CLOSED);
     } else {
       float h, frac;
       if (b.nstages == 2) {
@@ -251,7 +252,7 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
         frac = b.stage < 2 ? 0.5f : 1.0f;
       }
       spp_stage_update(h, frac, p0.x, p0.y, th0, fx, fy, tau, dth, &k, &nx, &ny, &nt, &nc, &ns,
-                       &gx, &gy);
+                       &gx, &gy, CLOSED);
     }
     b.out[i] = make_float4(nx, ny, nc, ns);
     if (last) {
@@ -262,8 +263,8 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
       }
       const float2 r = d.ref[i];
       float ddx, ddy;
-      disp2 = spp_sep(&k, nx, ny, r.x, r.y, &ddx, &ddy);
-      step2 = spp_sep(&k, nx, ny, p0.x, p0.y, &ddx, &ddy);
+      disp2 = spp_sep_cl(&k, CLOSED, nx, ny, r.x, r.y, &ddx, &ddy);
+      step2 = spp_sep_cl(&k, CLOSED, nx, ny, p0.x, p0.y, &ddx, &ddy);
     }
   }
   }
@@ -573,22 +574,34 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
   const int lanes = (kind == SPP_KIND_BEADS || kind == SPP_KIND_CHAIN) ? 1 : k.lanes;
   int nb = blocks_for(d.n * lanes);
   if (nb == 0) nb = 1;
-#define SPP_STAGE_CASE(L, K)                                                             \
-  if (k.force_law == L && kind == K) {                                                  \
-    if (lanes == SPP_GATHER_LANES)                                                      \
-      k_abp_stage<L, K, SPP_GATHER_LANES><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond); \
-    else                                                                                \
-      k_abp_stage<L, K, 1><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond);         \
+  /* closed boxes (walls) exist for the ABP and continuous kinds only */
+#define SPP_STAGE_CASE(L, K)                                                                   \
+  if (k.force_law == L && kind == K) {                                                        \
+    if (lanes == SPP_GATHER_LANES)                                                            \
+      k_abp_stage<L, K, SPP_GATHER_LANES, 0><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond); \
+    else                                                                                      \
+      k_abp_stage<L, K, 1, 0><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond);             \
   } else
-  SPP_STAGE_CASE(SPP_FORCE_HARMONIC, SPP_KIND_ABP)
-  SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_ABP)
-  SPP_STAGE_CASE(SPP_FORCE_NONE, SPP_KIND_ABP)
-  SPP_STAGE_CASE(SPP_FORCE_NONE, SPP_KIND_CONT)
-  SPP_STAGE_CASE(SPP_FORCE_NONE, SPP_KIND_CONT_ALPHA)
-  SPP_STAGE_CASE(SPP_FORCE_HARMONIC, SPP_KIND_CONT)
-  SPP_STAGE_CASE(SPP_FORCE_HARMONIC, SPP_KIND_CONT_ALPHA)
-  SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_CONT)
-  SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_CONT_ALPHA)
+#define SPP_STAGE_CASE_W(L, K)                                                                 \
+  if (k.force_law == L && kind == K) {                                                        \
+    if (lanes == SPP_GATHER_LANES && k.closed)                                                \
+      k_abp_stage<L, K, SPP_GATHER_LANES, 1><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond); \
+    else if (lanes == SPP_GATHER_LANES)                                                       \
+      k_abp_stage<L, K, SPP_GATHER_LANES, 0><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond); \
+    else if (k.closed)                                                                        \
+      k_abp_stage<L, K, 1, 1><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond);             \
+    else                                                                                      \
+      k_abp_stage<L, K, 1, 0><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond);             \
+  } else
+  SPP_STAGE_CASE_W(SPP_FORCE_HARMONIC, SPP_KIND_ABP)
+  SPP_STAGE_CASE_W(SPP_FORCE_R12_TRUNC, SPP_KIND_ABP)
+  SPP_STAGE_CASE_W(SPP_FORCE_NONE, SPP_KIND_ABP)
+  SPP_STAGE_CASE_W(SPP_FORCE_NONE, SPP_KIND_CONT)
+  SPP_STAGE_CASE_W(SPP_FORCE_NONE, SPP_KIND_CONT_ALPHA)
+  SPP_STAGE_CASE_W(SPP_FORCE_HARMONIC, SPP_KIND_CONT)
+  SPP_STAGE_CASE_W(SPP_FORCE_HARMONIC, SPP_KIND_CONT_ALPHA)
+  SPP_STAGE_CASE_W(SPP_FORCE_R12_TRUNC, SPP_KIND_CONT)
+  SPP_STAGE_CASE_W(SPP_FORCE_R12_TRUNC, SPP_KIND_CONT_ALPHA)
   SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_BEADS)
   SPP_STAGE_CASE(SPP_FORCE_HARMONIC, SPP_KIND_BEADS)
   SPP_STAGE_CASE(SPP_FORCE_NONE, SPP_KIND_BEADS)
@@ -596,6 +609,7 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
   SPP_STAGE_CASE(SPP_FORCE_NONE, SPP_KIND_CHAIN)
   {}
 #undef SPP_STAGE_CASE
+#undef SPP_STAGE_CASE_W
   if (launches) *launches += 1;
   if (nstages == 1) {
     k_commit<<<nb, SPP_BLOCK, 0, s>>>(d);

@@ -72,6 +72,17 @@ typedef struct SppConsts {
    * neighbours in id order and the lane sums combine as
    * (p0 + p1) + (p2 + p3) */
   int32_t lanes;
+  /* closed box (SPP_BOUNDARY_WALLS): no wrap, no minimum image, and the
+   * n_walls segments below act on every particle; segment w starts at
+   * (wall_x1, wall_y1), runs along the unit vector (wall_ex, wall_ey) for
+   * wall_len */
+  int32_t closed;
+  int32_t n_walls;
+  float wall_x1[SPP_MAX_WALLS], wall_y1[SPP_MAX_WALLS], wall_x2[SPP_MAX_WALLS], wall_y2[SPP_MAX_WALLS];
+  float wall_ex[SPP_MAX_WALLS], wall_ey[SPP_MAX_WALLS], wall_len[SPP_MAX_WALLS];
+  float wall_A, wall_sigma, wall_rc, wall_rf, wall_g_over_pi;
+  float wall_cut;              /* e^(-r_c/sigma) (1/r_c^2 + 1/(sigma r_c)), the truncation shift */
+  float wall_gcont_over_2pi;   /* ContinuousParticle::gw / (2 pi) */
 } SppConsts;
 
 #define SPP_GATHER_LANES 4
@@ -176,6 +187,47 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
   }
   k->lanes = ((p->model == SPP_MODEL_ABP || p->model == SPP_MODEL_CONTINUOUS) && p->n <= SPP_LANES_MAX_N)
                  ? SPP_GATHER_LANES : 1;
+  k->closed = p->boundary == SPP_BOUNDARY_WALLS ? 1 : 0;
+  k->n_walls = 0;
+  for (int w = 0; w < SPP_MAX_WALLS; ++w) {
+    k->wall_x1[w] = k->wall_y1[w] = k->wall_x2[w] = k->wall_y2[w] = 0.0f;
+    k->wall_ex[w] = k->wall_ey[w] = k->wall_len[w] = 0.0f;
+  }
+  k->wall_A = k->wall_sigma = k->wall_rc = k->wall_rf = k->wall_g_over_pi = 0.0f;
+  k->wall_cut = 0.0f;
+  k->wall_gcont_over_2pi = 0.0f;
+  if (k->closed) {
+    /* Box::Init_Topology (parallel/box.h:97-101), then the extra segments */
+    double seg[SPP_MAX_WALLS][4] = {{-p->L, -p->L, -p->L, p->L},
+                                    {-p->L, p->L, p->L, p->L},
+                                    {p->L, p->L, p->L, -p->L},
+                                    {p->L, -p->L, -p->L, -p->L}};
+    int nw = 4;
+    for (int w = 0; w < p->n_walls && nw < SPP_MAX_WALLS; ++w, ++nw)
+      for (int c = 0; c < 4; ++c) seg[nw][c] = p->walls[w][c];
+    k->n_walls = nw;
+    for (int w = 0; w < nw; ++w) {
+      /* Wall::Init (shared/wall.h:27-41) */
+      const double dx = seg[w][2] - seg[w][0], dy = seg[w][3] - seg[w][1];
+      const double len = sqrt(dx * dx + dy * dy);
+      k->wall_x1[w] = (float)seg[w][0];
+      k->wall_y1[w] = (float)seg[w][1];
+      k->wall_x2[w] = (float)seg[w][2];
+      k->wall_y2[w] = (float)seg[w][3];
+      k->wall_ex[w] = (float)(dx / len);
+      k->wall_ey[w] = (float)(dy / len);
+      k->wall_len[w] = (float)len;
+    }
+    k->wall_A = (float)p->A_w;
+    k->wall_sigma = (float)p->sigma_w;
+    k->wall_rc = (float)p->r_c_w;
+    k->wall_rf = (float)p->r_f_w;
+    k->wall_g_over_pi = (float)(p->g_w / 3.14159265358979323846);
+    if (p->r_c_w > 0 && p->sigma_w > 0)
+      k->wall_cut = (float)(exp(-p->r_c_w / p->sigma_w) *
+                            (1.0 / (p->r_c_w * p->r_c_w) + 1.0 / (p->sigma_w * p->r_c_w)));
+    k->wall_gcont_over_2pi = (float)(p->g_w_cont / (2.0 * 3.14159265358979323846));
+  }
   k->chain_nb = (p->model == SPP_MODEL_BEADS && p->chain_beads > 1) ? p->chain_beads : 1;
   for (int a = 0; a < SPP_MAX_CHAIN_BEADS; ++a)
     k->chain_off[a] = a < k->chain_nb ? (float)(p->bead_separation * ((1 - k->chain_nb) / 2.0 + a)) : 0.0f;
@@ -235,12 +287,29 @@ SPP_HD void spp_fx_add_guarded(spp_fx* acc, float t, int32_t* ovf) {
   spp_fx_add(acc, t);
 }
 
-/* Minimum-image separation r_i - r_j and its squared length. */
+/* Minimum-image separation r_i - r_j and its squared length (the plain
+ * difference in a closed box; `closed` is k->closed, a compile-time
+ * constant in the specialised kernels). */
+SPP_HD float spp_sep_cl(const SppConsts* k, int closed, float xi, float yi, float xj, float yj,
+                        float* dx, float* dy) {
+  if (closed) {
+    *dx = xi - xj;
+    *dy = yi - yj;
+  } else {
+    *dx = spp_min_image_f(xi - xj, k->L, k->L2);
+    *dy = spp_min_image_f(yi - yj, k->L, k->L2);
+  }
+  return fmaf(*dx, *dx, *dy * *dy);
+}
 SPP_HD float spp_sep(const SppConsts* k, float xi, float yi, float xj, float yj, float* dx,
                      float* dy) {
-  *dx = spp_min_image_f(xi - xj, k->L, k->L2);
-  *dy = spp_min_image_f(yi - yj, k->L, k->L2);
-  return fmaf(*dx, *dx, *dy * *dy);
+  return spp_sep_cl(k, k->closed, xi, yi, xj, yj, dx, dy);
+}
+
+/* A coordinate after a move: wrapped into [-L, L) (image counter updated)
+ * in a periodic box, left as it is in a closed one. */
+SPP_HD float spp_move_coord(const SppConsts* k, int closed, float x, int* img) {
+  return closed ? x : spp_wrap_coord_f(x, k->L, k->L2, img);
 }
 
 /* Accumulator of the Verlet-list models.  Their neighbour lists are sorted
@@ -282,8 +351,8 @@ SPP_HD void spp_pair_abp_lkw(const SppConsts* k, int law, int kind, int wrap, Sp
                              float yi, float ci, float si, float xj, float yj, float cj, float sj) {
   float dx, dy, d2;
   if (wrap) {
-    d2 = spp_sep(k, xi, yi, xj, yj, &dx, &dy);
-  } else { /* both particles far from the boundary: the minimum image is the plain difference */
+    d2 = spp_sep_cl(k, 0, xi, yi, xj, yj, &dx, &dy);
+  } else { /* both particles far from the boundary, or a closed box: the plain difference */
     dx = xi - xj;
     dy = yi - yj;
     d2 = fmaf(dx, dx, dy * dy);
@@ -321,7 +390,7 @@ SPP_HD void spp_pair_abp_lkw(const SppConsts* k, int law, int kind, int wrap, Sp
 
 SPP_HD void spp_pair_abp(const SppConsts* k, SppAccF* a, float xi, float yi, float ci, float si,
                          float xj, float yj, float cj, float sj) {
-  spp_pair_abp_lkw(k, k->force_law, spp_pair_kind(k), 1, a, xi, yi, ci, si, xj, yj, cj, sj);
+  spp_pair_abp_lkw(k, k->force_law, spp_pair_kind(k), !k->closed, a, xi, yi, ci, si, xj, yj, cj, sj);
 }
 
 /* ActiveBrownianChain::Interact (shared/particle.h:964-1012) as received by
@@ -344,7 +413,7 @@ SPP_HD void spp_pair_chain(const SppConsts* k, int law, int wrap, SppAccF* a, in
   if (law == SPP_FORCE_NONE) return;
   float dx0, dy0, d02;
   if (wrap) {
-    d02 = spp_sep(k, xi, yi, xj, yj, &dx0, &dy0);
+    d02 = spp_sep_cl(k, 0, xi, yi, xj, yj, &dx0, &dy0);
   } else {
     dx0 = xi - xj;
     dy0 = yi - yj;
@@ -399,16 +468,93 @@ SPP_HD void spp_chain_velocity(const SppConsts* k, const SppAccF* a, float ci, f
   *om = k->chain_k * (k->chain_torque0 + a->tq);
 }
 
+/* The walls of a closed box acting on a particle at (x, y) with heading
+ * (c, s), summed in wall order into force (wfx, wfy) and torque wtq.
+ *   SPP_MODEL_ABP, Wall::Interact(RepulsiveParticle*) (shared/wall.h:
+ *     215-265): dr = Distance_Vector (the perpendicular from the segment, or
+ *     from its nearer end beyond it, :127-148), d = |dr|;
+ *     for d < r_c_w the force along dr/d of strength
+ *       A_w (e^(-d/sigma_w) (1/d^2 + 1/(sigma_w d)) - the same at r_c_w);
+ *     for d < r_f_w beside the segment, heading towards it (dr . v < 0), the
+ *     torque -(g_w/pi) sin(theta - theta_w), negated when cos(theta -
+ *     theta_w) < 0 (i.e. pi/2 < theta - theta_w < 3pi/2 mod 2pi);
+ *   SPP_MODEL_CONTINUOUS, Wall::Interact(ContinuousParticle*) (:192-213):
+ *     dr the perpendicular from the wall's line, for |dr|^2 < 1 the torque
+ *     gw (v x dr) / (2 pi |dr|^2).
+ * (cos theta_w, sin theta_w) is the wall's unit direction (Wall::Init
+ * reduces theta_w to the same angle, :36-40). */
+SPP_HD void spp_wall_terms(const SppConsts* k, float x, float y, float c, float s, float* wfx,
+                           float* wfy, float* wtq) {
+  float fx = 0.0f, fy = 0.0f, tq = 0.0f;
+  for (int w = 0; w < k->n_walls; ++w) {
+    const float ex = k->wall_ex[w], ey = k->wall_ey[w];
+    const float r1x = x - k->wall_x1[w], r1y = y - k->wall_y1[w];
+    const float proj = fmaf(r1x, ex, r1y * ey);
+    if (k->model == SPP_MODEL_CONTINUOUS) {
+      const float dx = r1x - ex * proj, dy = r1y - ey * proj;
+      const float d2 = fmaf(dx, dx, dy * dy);
+      if (d2 < 1.0f && d2 > 0.0f)
+        tq = tq + k->wall_gcont_over_2pi * ((c * dy - s * dx) / d2);
+      continue;
+    }
+    const int beside = proj < k->wall_len[w] && proj > 0.0f;
+    float dx, dy;
+    if (beside) {
+      dx = r1x - ex * proj;
+      dy = r1y - ey * proj;
+    } else {
+      const float r2x = x - k->wall_x2[w], r2y = y - k->wall_y2[w];
+      const float d21 = fmaf(r1x, r1x, r1y * r1y), d22 = fmaf(r2x, r2x, r2y * r2y);
+      dx = d22 < d21 ? r2x : r1x;
+      dy = d22 < d21 ? r2y : r1y;
+    }
+    const float d2 = fmaf(dx, dx, dy * dy);
+    const float d = sqrtf(d2);
+    if (d < k->wall_rc && d2 > 0.0f) {
+      const float u = -d / k->wall_sigma;
+      const float e = u > -80.0f ? spp_expf(u) : 0.0f;   /* spp_expf covers |x| < 80 */
+      const float mag = k->wall_A * (e * (1.0f / d2 + 1.0f / (k->wall_sigma * d)) - k->wall_cut);
+      fx = fx + (dx / d) * mag;
+      fy = fy + (dy / d) * mag;
+    }
+    if (d < k->wall_rf && beside && fmaf(dx, c, dy * s) < 0.0f) {
+      float t = k->wall_g_over_pi * (s * ex - c * ey);   /* (g_w / pi) sin(theta - theta_w) */
+      if (fmaf(c, ex, s * ey) < 0.0f) t = -t;
+      tq = tq - t;
+    }
+  }
+  *wfx = fx;
+  *wfy = fy;
+  *wtq = tq;
+}
+
 /* Self-propulsion plus received force, and the torque (RepulsiveParticle::
- * Reset :559-564 and the alignment normalisations). */
-SPP_HD void spp_abp_forces(const SppConsts* k, const SppAccF* a, float ci, float si, float* fx,
-                           float* fy, float* tau) {
+ * Reset :559-564 and the alignment normalisations), plus, with walls
+ * (k->n_walls > 0, a closed box; a compile-time constant in the specialised
+ * kernels), the walls at the particle's position (x, y), added after the pair sums
+ * as the reference adds them (parallel/box.h:296-302).  The continuous
+ * model's wall torque enters before the factor g, which
+ * ContinuousParticle::Move applies to the whole torque (particle.h:273). */
+SPP_HD void spp_abp_forces(const SppConsts* k, int walls, const SppAccF* a, float xi, float yi,
+                           float ci, float si, float* fx, float* fy, float* tau) {
+  float wfx = 0.0f, wfy = 0.0f, wtq = 0.0f;
+  if (walls) spp_wall_terms(k, xi, yi, ci, si, &wfx, &wfy, &wtq);
   *fx = k->v0 * ci + a->fx;
   *fy = k->v0 * si + a->fy;
   float S = a->tq;
-  if (k->model == SPP_MODEL_CONTINUOUS) *tau = k->g * S;
-  else if (k->align_mode == SPP_ALIGN_MEAN) *tau = (k->g * S) / (float)(a->cnt + 1);
-  else *tau = S * k->g_over_area;
+  if (k->model == SPP_MODEL_CONTINUOUS) {
+    if (walls) S = S + wtq;
+    *tau = k->g * S;
+  } else if (k->align_mode == SPP_ALIGN_MEAN) {
+    *tau = (k->g * S) / (float)(a->cnt + 1);
+  } else {
+    *tau = S * k->g_over_area;
+  }
+  if (walls && k->model != SPP_MODEL_CONTINUOUS) {
+    *fx = *fx + wfx;
+    *fy = *fy + wfy;
+    *tau = *tau + wtq;
+  }
 }
 
 /* RTPChain::Noise_Gen (shared/particle.h:1085-1103) on an integer state: 0
@@ -445,13 +591,13 @@ SPP_HD float spp_rot_noise(const SppConsts* k, uint32_t pid, uint32_t step) {
  * (dt, 1) and finally dt/6 times the weighted sum of the four slopes. */
 SPP_HD void spp_stage_update(float h, float frac_noise, float x0, float y0, float th0, float fx,
                              float fy, float tau, float dth, const SppConsts* k, float* x, float* y,
-                             float* th, float* c, float* s, int* imgx, int* imgy) {
+                             float* th, float* c, float* s, int* imgx, int* imgy, int closed) {
   float t = fmaf(h, tau, th0) + frac_noise * dth;
   t = spp_wrap_angle_f(t);
   spp_sincosf(t, s, c);
   *th = t;
-  *x = spp_wrap_coord_f(fmaf(fx, h, x0), k->L, k->L2, imgx);
-  *y = spp_wrap_coord_f(fmaf(fy, h, y0), k->L, k->L2, imgy);
+  *x = spp_move_coord(k, closed, fmaf(fx, h, x0), imgx);
+  *y = spp_move_coord(k, closed, fmaf(fy, h, y0), imgy);
 }
 
 /* Euler move (RepulsiveParticle::Move, shared/particle.h:571-587): theta is
@@ -461,12 +607,12 @@ SPP_HD float spp_euler_theta(const SppConsts* k, float th0, float tau, float dth
 }
 SPP_HD void spp_euler_update(float x0, float y0, float th0, float fx, float fy, float tau, float dth,
                              const SppConsts* k, float* x, float* y, float* th, float* c, float* s,
-                             int* imgx, int* imgy) {
+                             int* imgx, int* imgy, int closed) {
   float t = spp_euler_theta(k, th0, tau, dth);
   spp_sincosf(t, s, c);
   *th = t;
-  *x = spp_wrap_coord_f(fmaf(fx, k->dt, x0), k->L, k->L2, imgx);
-  *y = spp_wrap_coord_f(fmaf(fy, k->dt, y0), k->L, k->L2, imgy);
+  *x = spp_move_coord(k, closed, fmaf(fx, k->dt, x0), imgx);
+  *y = spp_move_coord(k, closed, fmaf(fy, k->dt, y0), imgy);
 }
 
 /* ------------------------------------------------------------------ */

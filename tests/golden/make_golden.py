@@ -98,6 +98,29 @@ def cases():
     return out
 
 
+WALL_SEGMENTS = [[-5.0, -3.0, 4.0, 6.0], [2.0, -8.0, -6.0, 1.0], [-20.0, -20.0, -20.0, 20.0],
+                 [20.0, 20.0, 20.0, -20.0]]
+
+
+def wall_case(model):
+    """Wall::Interact of the reference on single particles near four
+    segments (two oblique, two box walls): parameters and sample points."""
+    p = configs.reference_defaults(model)
+    p.L, p.n = 20.0, 1
+    p.boundary = abi.BOUNDARY_WALLS
+    p.n_walls = 4
+    abi.set_field(p, "walls", WALL_SEGMENTS)
+    p.A_w, p.sigma_w, p.r_c_w, p.r_f_w, p.g_w, p.g_w_cont = 3.0, 0.4, 1.5, 1.2, 2.0, 20.0
+    rng = np.random.default_rng(11)
+    pts = []
+    for t in range(400):
+        w = WALL_SEGMENTS[t % 4]
+        u = rng.uniform(-0.2, 1.2)
+        pts.append((w[0] + u * (w[2] - w[0]) + rng.uniform(-1.6, 1.6),
+                    w[1] + u * (w[3] - w[1]) + rng.uniform(-1.6, 1.6), rng.uniform(-np.pi, np.pi)))
+    return p, np.array(pts, np.float64)
+
+
 def main():
     if O.ref() is None:
         raise SystemExit("reference checkout not found: cannot regenerate the fixtures")
@@ -109,6 +132,11 @@ def main():
         O.run64(p, s, steps, fn="ref")
         blob[f"{name}/out"] = np.stack([s.x, s.y, s.th, s.xu, s.yu])
         meta[name] = {"params": {k: v for k, v in p.as_dict().items()}, "steps": steps}
+    for model, name in ((abi.MODEL_ABP, "walls_abp"), (abi.MODEL_CONTINUOUS, "walls_continuous")):
+        p, pts = wall_case(model)
+        blob[f"{name}/in"] = pts
+        blob[f"{name}/out"] = np.array([O.wall_terms(p, *q, fn="ref") for q in pts])
+        meta[name] = {"params": {k: v for k, v in p.as_dict().items()}, "steps": 0}
     blob["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
     path = Path(__file__).resolve().parent / "reference_runs.npz"
     np.savez_compressed(path, **blob)

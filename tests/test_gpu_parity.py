@@ -359,3 +359,22 @@ def test_long_lists_bitexact_vs_mirror(gpu_lib, n):
     ref = O.run32(p, O.State32(x, y, th), 30)
     assert_bitexact(gpu, ref)
     assert obs.max_neighbors > 600
+
+
+@pytest.mark.parametrize("model,integ", [(abi.MODEL_ABP, abi.INT_EULER), (abi.MODEL_ABP, abi.INT_RK2),
+                                         (abi.MODEL_ABP, abi.INT_RK4), (abi.MODEL_CONTINUOUS, abi.INT_EULER),
+                                         (abi.MODEL_CONTINUOUS, abi.INT_RK2)])
+@pytest.mark.parametrize("n", [4096, 20000])
+def test_walls_bitexact_vs_mirror(gpu_lib, model, integ, n):
+    """Closed box with two oblique walls (Wall::Interact of
+    RepulsiveParticle / ContinuousParticle): no wrap, no minimum image, the
+    wall terms after the pair sums; four lanes per particle at 4096, one at
+    20,000."""
+    L = 40.0 if n == 4096 else 80.0
+    p = configs.walls_config(n=n, L=L, model=model, integrator=integ)
+    x, y, th = configs.walls_state(p)
+    steps = 150
+    gpu, _ = run_gpu(p, x, y, th, steps)
+    ref = O.run32(p, O.State32(x, y, th), steps)
+    assert_bitexact(gpu, ref)
+    assert not gpu[3].any() and not gpu[4].any()

@@ -1,0 +1,109 @@
+"""Closed boxes with walls on the CPU.
+
+The FP64 restatement of Wall::Interact (shared/wall.h:127-265) is pinned to
+the reference's own code where the checkout is present, and everywhere to the
+golden fixtures made from it.  The kernels' FP32 wall terms are compared with
+the FP64 restatement, a closed box keeps its particles, and the parameters
+are validated before any GPU work."""
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spp_gb300 import abi, build, configs
+
+sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+from make_golden import WALL_SEGMENTS, wall_case  # noqa: E402
+from test_oracle_pin import load_golden, params_from  # noqa: E402
+
+
+@pytest.mark.parametrize("name", ["walls_abp", "walls_continuous"])
+def test_wall_terms_match_golden(name):
+    """RepulsiveParticle force and torque, ContinuousParticle torque, against
+    the reference's outputs on 400 particles near four segments."""
+    z, meta = load_golden()
+    p = params_from(meta[name]["params"])
+    pts, ref = z[f"{name}/in"], z[f"{name}/out"]
+    got = np.array([O.wall_terms(p, *q) for q in pts])
+    assert np.max(np.abs(got - ref) / (1 + np.abs(ref))) < 1e-12
+    assert np.count_nonzero(np.any(ref != 0, axis=1)) > 200
+
+
+@pytest.mark.parametrize("model", [abi.MODEL_ABP, abi.MODEL_CONTINUOUS])
+def test_wall_terms_match_reference(model):
+    if O.ref() is None:
+        pytest.skip("reference checkout absent; the golden fixtures pin the walls instead")
+    p, _ = wall_case(model)
+    rng = np.random.default_rng(5)
+    for _ in range(300):
+        w = WALL_SEGMENTS[rng.integers(4)]
+        u = rng.uniform(-0.3, 1.3)
+        x = w[0] + u * (w[2] - w[0]) + rng.uniform(-1.6, 1.6)
+        y = w[1] + u * (w[3] - w[1]) + rng.uniform(-1.6, 1.6)
+        th = rng.uniform(-np.pi, np.pi)
+        a, b = O.wall_terms(p, x, y, th), O.wall_terms(p, x, y, th, fn="ref")
+        assert np.all(np.abs(a - b) <= 1e-12 * (1 + np.abs(b)))
+
+
+@pytest.mark.parametrize("model", [abi.MODEL_ABP, abi.MODEL_CONTINUOUS])
+def test_fp32_wall_terms_track_fp64(model):
+    """The kernels' FP32 arithmetic (spp_wall_terms, with the FP32 exponential)
+    against the FP64 restatement at the same float inputs; the continuous
+    torque's perpendicular distance is a difference of nearby numbers, hence
+    the looser bound there."""
+    p, pts = wall_case(model)
+    worst = 0.0
+    for x, y, th in pts:
+        x, y, th = float(np.float32(x)), float(np.float32(y)), float(np.float32(th))
+        a = O.wall_terms(p, x, y, th)
+        ref = np.array([a[0], a[1], a[2] if model == abi.MODEL_ABP else a[3]])
+        got = O.wall_terms(p, x, y, th, fn="orc32").astype(np.float64)
+        worst = max(worst, float(np.max(np.abs(got - ref) / (1 + np.abs(ref)))))
+    assert worst < (1e-3 if model == abi.MODEL_ABP else 3e-3)
+
+
+@pytest.mark.parametrize("integ", [abi.INT_EULER, abi.INT_RK2, abi.INT_RK4])
+def test_mirror_tracks_fp64_in_closed_box(integ):
+    """ABP in a closed box with two oblique walls: the FP32 mirror stays
+    within FP32 rounding of the FP64 restatement, the box keeps every
+    particle (no wrap, image counters 0) and the walls did act."""
+    p = configs.walls_config(n=900, L=20.0, integrator=integ)
+    x, y, th = configs.walls_state(p)
+    s32 = O.State32(x, y, th)
+    O.run32(p, s32, 300)
+    a = O.State64(x.astype(np.float64), y.astype(np.float64), th.astype(np.float64))
+    O.run64(p, a, 300)
+    assert np.abs(s32.x - a.x).max() < 2e-3 and np.abs(s32.y - a.y).max() < 2e-3
+    assert not s32.ix.any() and not s32.iy.any()
+    assert np.abs(s32.x).max() < p.L + 0.5 and np.abs(s32.y).max() < p.L + 0.5
+    q = p.copy()
+    q.A_w = q.g_w = 0.0
+    b = O.State64(x.astype(np.float64), y.astype(np.float64), th.astype(np.float64))
+    O.run64(q, b, 300)
+    assert np.hypot(a.x - b.x, a.y - b.y).max() > 0.05
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return abi.lib()
+
+
+def test_create_rejects_bad_walls_without_touching_gpu(lib):
+    p = configs.walls_config(n=64, L=10.0)
+    h = C.c_void_p()
+    assert lib.spp_create(C.byref(p.replace(boundary=7)), C.byref(h)) == 1
+    assert lib.spp_create(C.byref(p.replace(n_walls=5)), C.byref(h)) == 1
+    bad = p.copy()
+    abi.set_field(bad, "walls", [[1.0, 1.0, 1.0, 1.0]])
+    assert lib.spp_create(C.byref(bad), C.byref(h)) == 1
+    assert b"nonzero length" in lib.spp_last_error()
+    assert lib.spp_create(C.byref(p.replace(sigma_w=0.0)), C.byref(h)) == 1
+    v = configs.vicsek_config()
+    assert lib.spp_create(C.byref(v.replace(boundary=abi.BOUNDARY_WALLS)), C.byref(h)) == 6
+    d = abi.SppParams()
+    lib.spp_params_init(C.byref(d), abi.MODEL_CONTINUOUS)
+    assert (d.boundary, d.n_walls, d.A_w, d.g_w_cont) == (abi.BOUNDARY_PERIODIC, 0, 0.0, 20.0)
