@@ -246,6 +246,26 @@ def walls_config(n=4096, L=40.0, model=abi.MODEL_ABP, integrator=abi.INT_RK2, se
     return p
 
 
+def star_trap_walls(n_hands=2, half_delta=0.3, r_big=15.0, r_small=6.0):
+    """Segments of a star-shaped trap (Star_Trap_Initialization,
+    shared/set-up.h:259-290): 3 n_hands end points (the tip at r_big, two
+    inner points at r_small, rotated by 2 pi / n_hands per hand), each hand
+    contributing two walls.  n_hands = 2 gives the 4 segments a closed box
+    takes besides its own walls."""
+    pts = [(r_big, 0.0)]
+    a, b = (0.5 * 2 * math.pi / n_hands) - half_delta, (0.5 * 2 * math.pi / n_hands) + half_delta
+    pts += [(r_small * math.cos(a), r_small * math.sin(a)), (r_small * math.cos(b), r_small * math.sin(b))]
+    for i in range(3, 3 * n_hands):
+        x, y = pts[i - 3]
+        c, s = math.cos(2 * math.pi / n_hands), math.sin(2 * math.pi / n_hands)
+        pts.append((c * x - s * y, s * x + c * y))
+    walls = []
+    for i in range(0, 3 * (n_hands - 1) + 1, 3):
+        walls.append((*pts[i], *pts[i + 1]))
+        walls.append((*pts[i + 2], *pts[(i + 3) % (3 * n_hands)]))
+    return walls
+
+
 def walls_state(p, seed=None):
     """Particles on a square lattice of spacing 1.05 inside the box, at
     least 2 from the box walls and 1.6 from the extra segments; random

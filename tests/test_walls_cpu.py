@@ -107,3 +107,20 @@ def test_create_rejects_bad_walls_without_touching_gpu(lib):
     d = abi.SppParams()
     lib.spp_params_init(C.byref(d), abi.MODEL_CONTINUOUS)
     assert (d.boundary, d.n_walls, d.A_w, d.g_w_cont) == (abi.BOUNDARY_PERIODIC, 0, 0.0, 20.0)
+
+
+def test_star_trap_segments():
+    """Star_Trap_Initialization (shared/set-up.h:259-290) with 2 hands: four
+    segments from the tips at r_big to the inner points at r_small."""
+    w = np.array(configs.star_trap_walls(2, half_delta=0.3))
+    assert w.shape == (4, 4)
+    r1 = np.hypot(w[:, 0], w[:, 1])
+    r2 = np.hypot(w[:, 2], w[:, 3])
+    assert np.allclose(np.sort(np.concatenate([r1, r2])), [6] * 4 + [15] * 4)
+    p = configs.walls_config(n=400, L=20.0, extra_walls=configs.star_trap_walls(2))
+    x, y, th = configs.walls_state(p)
+    s32 = O.State32(x, y, th)
+    O.run32(p, s32, 100)
+    a = O.State64(x.astype(np.float64), y.astype(np.float64), th.astype(np.float64))
+    O.run64(p, a, 100)
+    assert np.abs(s32.x - a.x).max() < 1e-3
