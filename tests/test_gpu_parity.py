@@ -382,7 +382,7 @@ def test_walls_bitexact_vs_mirror(gpu_lib, model, integ, n):
 
 def test_star_trap_bitexact_vs_mirror(gpu_lib):
     """ABP in a closed box holding a two-hand star trap (four segments)."""
-    p = configs.walls_config(n=3000, L=30.0, extra_walls=configs.star_trap_walls(2))
+    p = configs.walls_config(n=2500, L=30.0, extra_walls=configs.star_trap_walls(2))
     x, y, th = configs.walls_state(p)
     gpu, _ = run_gpu(p, x, y, th, 200)
     ref = O.run32(p, O.State32(x, y, th), 200)
