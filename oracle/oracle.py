@@ -55,7 +55,7 @@ def orc():
         L.orc64_wall_terms.restype = None
         L.orc32_tumble_steps.argtypes = [_P]
         L.orc32_tumble_steps.restype = C.c_int32
-        L.orc32_radial.argtypes = [_F, _F, C.c_int, C.c_double, C.c_double, C.c_int, _U64]
+        L.orc32_radial.argtypes = [_F, _F, C.c_int, C.c_double, C.c_double, C.c_int, _U64, C.c_int]
         L.orc32_pair_distribution.argtypes = [_F, _F, _F, _F, C.c_int, C.c_double, C.c_double, C.c_int,
                                               C.c_int, _U64]
         L.orc32_rsqrt.restype = C.c_float
@@ -162,12 +162,13 @@ def tumble_steps(p):
     return int(orc().orc32_tumble_steps(C.byref(q)))
 
 
-def radial32(x, y, L, r_max, nbins):
-    """Ordered-pair radial histogram, FP32 as spp_radial_distribution computes it (O(N^2))."""
+def radial32(x, y, L, r_max, nbins, closed=False):
+    """Ordered-pair radial histogram, FP32 as spp_radial_distribution computes it (O(N^2));
+    closed: a closed box (plain differences)."""
     x = np.ascontiguousarray(x, np.float32)
     y = np.ascontiguousarray(y, np.float32)
     out = np.zeros(nbins, np.uint64)
-    orc().orc32_radial(_f(x), _f(y), len(x), float(L), float(r_max), int(nbins), _u64(out))
+    orc().orc32_radial(_f(x), _f(y), len(x), float(L), float(r_max), int(nbins), _u64(out), int(bool(closed)))
     return out
 
 

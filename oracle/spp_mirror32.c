@@ -584,15 +584,15 @@ int orc32_lyap_run(const SppParams* p, int nsteps, int64_t step0, int renorm_eve
 /* spp_pair_distribution), all ordered pairs, same FP32 expressions  */
 /* ---------------------------------------------------------------- */
 void orc32_radial(const float* x, const float* y, int n, double L, double r_max, int nbins,
-                  uint64_t* counts) {
+                  uint64_t* counts, int closed) {
   const float Lf = (float)L, L2 = (float)(2.0 * L);
   const float rm = (float)r_max, r2max = rm * rm, dr = rm / (float)nbins;
   for (int b = 0; b < nbins; ++b) counts[b] = 0;
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) {
       if (j == i) continue;
-      const float dx = spp_min_image_f(x[i] - x[j], Lf, L2);
-      const float dy = spp_min_image_f(y[i] - y[j], Lf, L2);
+      const float dx = closed ? x[i] - x[j] : spp_min_image_f(x[i] - x[j], Lf, L2);
+      const float dy = closed ? y[i] - y[j] : spp_min_image_f(y[i] - y[j], Lf, L2);
       const float d2 = fmaf(dx, dx, dy * dy);
       if (d2 < r2max) {
         int b = (int)(sqrtf(d2) / dr);

@@ -39,6 +39,7 @@ int ofail(int status, const std::string& msg) {
 /* ---------------------------------------------------------------- */
 struct Grid {
   int n, D;
+  int closed;             /* a closed box: plain differences, no minimum image */
   float L, L2;
   const float4* pos;
   uint32_t *count, *start, *key, *rank, *tmp;
@@ -62,7 +63,8 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_obs_scatter(Grid g) {
   g.sorted[g.start[g.key[i]] + g.rank[i]] = g.pos[i];
 }
 
-/* Radial histogram: ordered pairs within r_max, minimum image. */
+/* Radial histogram: ordered pairs within r_max, minimum image (plain
+ * differences in a closed box). */
 __global__ void __launch_bounds__(SPP_BLOCK) k_obs_radial(Grid g, float r2max, float dr, int nbins,
                                                           unsigned long long* counts) {
   extern __shared__ uint32_t hist[];
@@ -84,8 +86,8 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_obs_radial(Grid g, float r2max, f
         for (uint32_t j = s0; j < s1; ++j) {
           if ((int)j == i) continue;
           const float4 q = g.sorted[j];
-          const float dx = spp_min_image_f(p.x - q.x, g.L, g.L2);
-          const float dy = spp_min_image_f(p.y - q.y, g.L, g.L2);
+          const float dx = g.closed ? p.x - q.x : spp_min_image_f(p.x - q.x, g.L, g.L2);
+          const float dy = g.closed ? p.y - q.y : spp_min_image_f(p.y - q.y, g.L, g.L2);
           const float d2 = fmaf(dx, dx, dy * dy);
           if (d2 < r2max) {
             int b = (int)(sqrtf(d2) / dr);
@@ -204,6 +206,7 @@ int grid_build(SppSystem* s, double range, Grid* g, cudaStream_t* st) {
   g->D = D;
   g->L = k.L;
   g->L2 = k.L2;
+  g->closed = k.closed;
   g->pos = d.pos;
   const size_t nc = (size_t)D * D, n = (size_t)d.n;
   cudaError_t e = cudaMalloc((void**)&g->count, sizeof(uint32_t) * nc);

@@ -154,3 +154,17 @@ def test_ring_shapes_match_fp64(gpu_lib):
             assert shapes["sw_" + key][r] == pytest.approx(v, rel=1e-7, abs=1e-7), key
         # a ring of 64 beads at rest length 1 stays near-circular: R ~ 10.2, Delta small
         assert 9.0 < shapes["mb_Rg"][r] < 11.5 and shapes["mb_Delta"][r] < 0.05
+
+
+def test_radial_distribution_in_a_closed_box(gpu_lib):
+    """In a closed box pairs are plain differences: particles near opposite
+    walls are far apart, not minimum-image neighbours."""
+    p = configs.walls_config(n=900, L=20.0)
+    x, y, th = configs.walls_state(p)
+    with System(p) as s:
+        s.upload(x, y, th)
+        s.step(200)
+        gx, gy, _, _, _ = s.download()
+        rad = s.radial_distribution(5.0, 50)
+    assert np.array_equal(rad, O.radial32(gx, gy, p.L, 5.0, 50, closed=True))
+    assert not np.array_equal(rad, O.radial32(gx, gy, p.L, 5.0, 50))
