@@ -40,7 +40,8 @@ enum SppStatus {
   SPP_ERR_OVERFLOW = 4,    /* neighbour-list or fixed-point range exceeded */
   SPP_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
   SPP_ERR_UNSUPPORTED = 6, /* model/integrator pair not built */
-  SPP_ERR_NUMERIC = 7      /* non-finite value detected */
+  SPP_ERR_NUMERIC = 7,     /* non-finite value detected */
+  SPP_ERR_BOUNDS = 8       /* a kernel met an index out of range (builds with SPP_CHECKED) */
 };
 
 /* Particle models (shared/particle.h). */

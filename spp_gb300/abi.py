@@ -14,7 +14,7 @@ LIB_PATH = PKG / "lib" / "libspp_gb300.so"
 SPP_OK = 0
 STATUS_NAMES = {0: "SPP_OK", 1: "SPP_ERR_INVALID", 2: "SPP_ERR_ALLOC", 3: "SPP_ERR_CUDA",
                 4: "SPP_ERR_OVERFLOW", 5: "SPP_ERR_TIMEOUT", 6: "SPP_ERR_UNSUPPORTED",
-                7: "SPP_ERR_NUMERIC"}
+                7: "SPP_ERR_NUMERIC", 8: "SPP_ERR_BOUNDS"}
 
 MODEL_VICSEK, MODEL_VICSEK_REF_ANGLE, MODEL_VICSEK_REF_VECTOR = 0, 1, 2
 MODEL_CONTINUOUS, MODEL_ABP, MODEL_BEADS = 3, 4, 5

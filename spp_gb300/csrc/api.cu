@@ -395,6 +395,9 @@ int recover(SppSystem* s) {
     Ctl c;
     int rc = read_ctl(s, &c);
     if (rc != SPP_OK) return rc;
+    if (c.bad_index)
+      return fail(SPP_ERR_BOUNDS, "a kernel met an index out of range and skipped the access "
+                                  "(SPP_CHECKED build); the state is not reliable");
     if (c.fx_overflow)
       return fail(SPP_ERR_OVERFLOW, "a pair term exceeded the fixed-point range (overlapping "
                                     "particles under an R12 force?); the state is not reliable");
@@ -555,6 +558,7 @@ const char* spp_status_string(int st) {
     case SPP_ERR_TIMEOUT: return "SPP_ERR_TIMEOUT";
     case SPP_ERR_UNSUPPORTED: return "SPP_ERR_UNSUPPORTED";
     case SPP_ERR_NUMERIC: return "SPP_ERR_NUMERIC";
+    case SPP_ERR_BOUNDS: return "SPP_ERR_BOUNDS";
     default: return "SPP_ERR_UNKNOWN";
   }
 }

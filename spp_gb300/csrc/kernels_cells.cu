@@ -40,6 +40,7 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_bin_count(SppConsts k, DevState d
   float4 p = d.pos[i];
   int cx, cy;
   uint32_t key = cell_key(k, d, p.x, p.y, &cx, &cy);
+  if (!spp_index_ok(d.ctl, key, d.n_keys)) key = 0u;
   unsigned mask = __activemask();
   unsigned peers = __match_any_sync(mask, key);
   int lane = threadIdx.x & 31;
@@ -141,7 +142,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const uint32_t* __r
 __global__ void __launch_bounds__(SPP_BLOCK) k_scatter(DevState d) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n) return;
-  uint32_t dst = d.cell_start[d.key[i]] + d.rank[i];
+  const uint32_t key = d.key[i];
+  if (!spp_index_ok(d.ctl, key, d.n_keys)) return;
+  uint32_t dst = d.cell_start[key] + d.rank[i];
+  if (!spp_index_ok(d.ctl, dst, d.n)) return;
   d.pos_alt[dst] = d.pos[i];
   d.theta_alt[dst] = d.theta[i];
   d.img_alt[dst] = d.img[i];
@@ -196,7 +200,9 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_build_list(SppConsts k, DevState 
           int nx = cx + ox;
           nx = nx < 0 ? nx + D : (nx >= D ? nx - D : nx);
           uint32_t kk = spp_morton((uint32_t)nx, (uint32_t)ny);
+          if (!spp_index_ok(d.ctl, kk, d.n_keys)) continue;
           uint32_t s0 = d.cell_start[kk], c = d.cell_count[kk];
+          if (!spp_index_ok(d.ctl, (long long)s0 + c, (long long)d.n + 1)) continue;
           for (uint32_t j = s0; j < s0 + c; ++j) {
             if ((int)j == i) continue;
             float4 q = d.pos_alt[j];
@@ -288,7 +294,8 @@ __device__ __forceinline__ void warp_sort_list(const SppConsts& k, const DevStat
   for (int r = 0; r < R; ++r) {
     const int q = r * 32 + lane;
     if (q < m) {
-      const int32_t j = d.nbr[(size_t)q * d.n + i];
+      int32_t j = d.nbr[(size_t)q * d.n + i];
+      if (!spp_index_ok(d.ctl, j, d.n)) j = i;
       key[r] = ((unsigned long long)spp_list_order(&k, d.id_alt[j]) << 32) | (unsigned long long)(uint32_t)j;
     } else {
       key[r] = ~0ull;
@@ -342,6 +349,7 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_sort_long(SppConsts k, DevState d
   const uint32_t total = d.ctl->long_n;
   for (uint32_t w = (uint32_t)warp; w < total; w += (uint32_t)nwarps) {
     const int i = d.long_q[w];
+    if (!spp_index_ok(d.ctl, i, d.n)) continue;
     const int m = d.nn[i];
     if (m <= 32) warp_sort_list<1>(k, d, i, m);
     else if (m <= 64) warp_sort_list<2>(k, d, i, m);

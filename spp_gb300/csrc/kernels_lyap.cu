@@ -92,7 +92,10 @@ __global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevSta
   for (int q0 = q_begin; q0 < q_end; q0 += TAN_LOADS) {
     int jg[TAN_LOADS];
 #pragma unroll
-    for (int w = 0; w < TAN_LOADS; ++w) jg[w] = q0 + w < q_end ? __ldg(nb + (size_t)(q0 + w) * n) : i;
+    for (int w = 0; w < TAN_LOADS; ++w) {
+      jg[w] = q0 + w < q_end ? __ldg(nb + (size_t)(q0 + w) * n) : i;
+      if (!spp_index_ok(d.ctl, jg[w], n)) jg[w] = i;
+    }
     float4 pg[TAN_LOADS], ug[TAN_LOADS];
 #pragma unroll
     for (int w = 0; w < TAN_LOADS; ++w) {

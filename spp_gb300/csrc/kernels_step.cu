@@ -151,7 +151,10 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
       int jg[SPP_STAGE_GROUP];
       float4 pg[SPP_STAGE_GROUP];
 #pragma unroll
-      for (int u = 0; u < SPP_STAGE_GROUP; ++u) jg[u] = q0 + u < q_end ? __ldg(nb + (size_t)(q0 + u) * stride) : i;
+      for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
+        jg[u] = q0 + u < q_end ? __ldg(nb + (size_t)(q0 + u) * stride) : i;
+        if (!spp_index_ok(d.ctl, jg[u], d.n)) jg[u] = i;
+      }
 #pragma unroll
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) pg[u] = __ldg(b.cur + jg[u]);
 #pragma unroll
@@ -191,7 +194,8 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
         float px[5], py[5];
 #pragma unroll
         for (int o = -2; o <= 2; ++o) {
-          const uint32_t slot = o == 0 ? (uint32_t)i : d.inv[spp_ring_neighbor(&k, pid, o)];
+          uint32_t slot = o == 0 ? (uint32_t)i : d.inv[spp_ring_neighbor(&k, pid, o)];
+          if (!spp_index_ok(d.ctl, slot, d.n)) slot = (uint32_t)i;
           const float4 q = o == 0 ? pi : __ldg(b.cur + slot);
           px[o + 2] = q.x;
           py[o + 2] = q.y;
@@ -291,7 +295,9 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_vicsek_step(SppConsts k, DevState
         int nx = cx + ox;
         nx = nx < 0 ? nx + D : (nx >= D ? nx - D : nx);
         const uint32_t kk = spp_morton((uint32_t)nx, (uint32_t)ny);
+        if (!spp_index_ok(d.ctl, kk, d.n_keys)) continue;
         const uint32_t s0 = d.cell_start[kk], c = d.cell_count[kk];
+        if (!spp_index_ok(d.ctl, (long long)s0 + c, (long long)d.n + 1)) continue;
         for (uint32_t j = s0; j < s0 + c; ++j) {
           const float4 q = __ldg(d.pos_alt + j);
           const float thj = need_theta ? d.theta_alt[j] : 0.0f;
@@ -429,6 +435,7 @@ __global__ void __launch_bounds__(SPP_SMALL_THREADS, 1) k_vicsek_small(SppConsts
         if (i < n) {
           const int pk = packed[i];
           const int slot = start[pk & 0xffff] + (pk >> 16);
+          if (!spp_index_ok(d.ctl, slot, n)) continue;
           sp[slot] = pv[u];
           if (need_theta) sth[slot] = tv[u];
         }

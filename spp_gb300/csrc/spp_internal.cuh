@@ -40,8 +40,23 @@ struct Ctl {
   uint32_t bad_nonfinite; /* smallest index of an uploaded particle with a non-finite value (or ~0) */
   uint32_t bad_range;     /* smallest index of an uploaded position outside [-L, L) (or ~0) */
   uint32_t long_n;        /* lists longer than the in-block sort queued by the last build */
-  uint32_t pad[2];
+  uint32_t bad_index;     /* SPP_CHECKED builds: a kernel met an index out of range */
+  uint32_t pad[1];
 };
+
+/* SPP_CHECKED builds check every list, cell and slot index a hot kernel
+ * uses; an index out of [0, bound) sets Ctl.bad_index (the next sync
+ * returns SPP_ERR_BOUNDS) and the caller skips the access.  Without
+ * SPP_CHECKED the check is the constant true. */
+#ifdef SPP_CHECKED
+__device__ __forceinline__ bool spp_index_ok(Ctl* ctl, long long idx, long long bound) {
+  if (idx >= 0 && idx < bound) return true;
+  atomicOr(&ctl->bad_index, 1u);
+  return false;
+}
+#else
+__device__ __forceinline__ bool spp_index_ok(Ctl*, long long, long long) { return true; }
+#endif
 
 struct DevState {
   int n;
