@@ -54,10 +54,8 @@ def workload_config(n):
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from spp_gb300.replicas import dist_env as env
+    return env()
 
 
 # ---------------------------------------------------------------------------
@@ -375,9 +373,8 @@ def run_ours(args):
         launches = s.kernel_launches() - launches0
         elapsed_ms = sum(times)
         if dist:
-            t = torch.tensor([elapsed_ms], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            elapsed_ms = float(t.item())
+            from spp_gb300.replicas import max_over_ranks
+            elapsed_ms = max_over_ranks(elapsed_ms, dist)   # the slowest rank sets the wall time
             dist.barrier()
         obs = s.observables()
         # kernel-level timing for the roofline: CUDA events around every stage kernel
@@ -482,6 +479,33 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # the other configurations (one JSON line each; not the headline)
 # ---------------------------------------------------------------------------
+def sweep_sharded(args):
+    """The 512-point sweep with the surrogate over N GPUs (torchrun): points
+    split by cost, each rank runs its shard, surrogate fits use every rank's
+    completed points; points/hour over the slowest rank's wall time."""
+    import numpy as np
+    import torch.distributed as dist
+    from spp_gb300 import configs, replicas
+    ws, rank, local = dist_env()
+    os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist.init_process_group("gloo")   # host-side exchange of small arrays
+    pts = configs.sweep_points(n_points=512)
+    dist.barrier()
+    t0 = time.perf_counter()
+    ans, full, ret, res = replicas.run_sweep_sharded(pts, rank, ws, replicas.Exchange(dist), max_steps=20000,
+                                                     window=500, seed=4)
+    wall = replicas.max_over_ranks(time.perf_counter() - t0, dist)
+    if rank == 0:
+        print(json.dumps({"metric": "sweep points/hour at |dP|<=0.02 vs full runs", "workload": "sweep",
+                          "value": len(pts) / wall * 3600.0, "unit": "points/hour", "n_gpus": ws,
+                          "higher_is_better": True, "scaling": "strong", "data": "synthetic",
+                          "config": {"workload": "512 Vicsek points (N log-uniform [1024, 65536]), 20,000 steps, "
+                                                 "surrogate sweep sharded by cost over the ranks"},
+                          "wall_s": wall, "retired": int(ret.sum()),
+                          "answered": int(np.isfinite(ans).sum())}), flush=True)
+    dist.destroy_process_group()
+
+
 def other_workload(args):
     """Throughput of configurations 1, 3, 4 and 5 on one GPU: plain Vicsek
     N=4096 (32 B/particle-step), vesicles with swimmers (163,840 bodies, RK4,
@@ -518,6 +542,9 @@ def other_workload(args):
                           "config": {"workload": f"64 sweep points ({n:,} particles), 40 steps; "
                                                  "60 training iterations of the 5-member surrogate on 300 samples"},
                           "train_ms_per_iteration": train_ms / 60}), flush=True)
+        return
+    if w == "sweep" and dist_env()[0] > 1:
+        sweep_sharded(args)
         return
     if w == "sweep":
         line = {"metric": "sweep points/hour at |dP|<=0.02 vs full runs", "n_gpus": 1, "data": "synthetic"}

@@ -223,9 +223,15 @@ class SweepResult:
 
 def run_sweep(points, max_steps=20000, window=500, pilot_frac=0.2, holdout_frac=0.1, tol=0.02,
               max_rounds=2, run_frac=0.5, surrogate=None, seed=4, x0=None, use_surrogate=True,
-              chunk=2000):
+              chunk=2000, exchange=None):
     """Runs the sweep and returns a SweepResult.  With use_surrogate=False
     every point runs to the end (the plain batched sweep).
+
+    exchange (spp_gb300.replicas.Exchange) makes this one shard of a sweep
+    over several ranks: every fit uses all ranks' completed points, the
+    conformal multiplier all ranks' fresh residuals, and the rounds end
+    together (their collectives stay matched); without it the sweep is
+    local.
 
     Rounds r = 0 .. max_rounds: fit on every completed non-held-out point;
     the error bound of a remaining point is c x spread, with c the coverage
@@ -235,6 +241,8 @@ def run_sweep(points, max_steps=20000, window=500, pilot_frac=0.2, holdout_frac=
     points whose bound exceeds tol, the run_frac with the largest bounds run
     to the end (all of them in the last round); the points left when no
     bound exceeds tol retire with the mean of a fit on everything run."""
+    from .replicas import Exchange
+    ex = exchange if exchange is not None else Exchange()
     t_start = time.perf_counter()
     timings = {"runs_s": 0.0, "train_s": 0.0}
     n = len(points)
@@ -280,23 +288,27 @@ def run_sweep(points, max_steps=20000, window=500, pilot_frac=0.2, holdout_frac=
             fresh = []
             for r in range(max_rounds + 2):
                 t1 = time.perf_counter()
-                sur.fit(f[np.isfinite(p_full) & ~heldout], p_full[np.isfinite(p_full) & ~heldout])
+                done = np.isfinite(p_full) & ~heldout
+                f_fit, p_fit = ex([f[done], p_full[done]])
+                sur.fit(f_fit, p_fit)
                 mean, spread = sur.predict(f)
                 timings["train_s"] += time.perf_counter() - t1
-                if r == max_rounds + 1 or not remaining.any():
+                if r == max_rounds + 1 or not ex.any(remaining.any()):
                     break
                 rounds += 1
-                scale = float(np.quantile(np.concatenate(fresh), sur.coverage)) if fresh else sur.oof_scale
+                res_all = ex([np.concatenate(fresh) if fresh else np.zeros(0)])[0]
+                scale = float(np.quantile(res_all, sur.coverage)) if res_all.size else sur.oof_scale
                 scales.append(scale)
                 bnd = scale * sur.floor(spread)
                 bound[remaining] = bnd[remaining]
                 unsure = np.flatnonzero(remaining & (bnd > tol))
-                if unsure.size == 0:
+                if not ex.any(unsure.size > 0):
                     break
-                if r < max_rounds:
+                if r < max_rounds and unsure.size:
                     keep = max(1, int(math.ceil(run_frac * unsure.size)))
                     unsure = unsure[np.argsort(-bnd[unsure], kind="stable")][:keep]
-                run(unsure)
+                if unsure.size:
+                    run(unsure)
                 st = b.poll()
                 for s in unsure:
                     p_full[s] = st[s].p_stationary
