@@ -114,7 +114,11 @@ typedef struct SppParams {
   double bond_rest;       /* ring bond rest length */
   double kappa_bend;      /* bending stiffness on consecutive bond angles */
   int32_t rot_noise;      /* enum SppRotNoise (swimmers of SPP_MODEL_BEADS) */
-  int32_t reserved;
+  int32_t gather_lanes;   /* threads per particle in the Verlet-list neighbour sums of the
+                           * ABP and continuous models: 0 = automatic (4 up to 16,384
+                           * particles, else 1), or 1 or 4 (spp_autotune chooses); the
+                           * other models take 0 or 1.  The lane count fixes the order in
+                           * which neighbour terms are added, so it is part of the result */
   double tumble_rate;     /* RTPChain::lambda: a tumble starts with probability rate * dt per step */
   double tumble_time;     /* RTPChain::t_tumble: a tumble lasts while its elapsed time < t_tumble */
   double tumble_torque;   /* RTPChain::torque_tumble: dtheta = k_perp dt (+-1) torque_tumble per step */
@@ -390,6 +394,42 @@ int spp_profile(SppSystem* s, int nsteps, SppProfile* out);
 /* spp_step(nsteps) bracketed by CUDA events on the handle's stream; waits for
  * completion and returns the elapsed device time in *ms. */
 int spp_time_steps(SppSystem* s, int nsteps, double* ms);
+/* ---- autotuner of the launch shape (no counterpart in the reference) ----
+ * The reference fixes its cell and list geometry from compile-time globals
+ * (shared/parameters.h:93-99).  spp_autotune() times the candidate shapes
+ * of a Verlet-list system (SPP_MODEL_ABP, _CONTINUOUS, _BEADS) on the device
+ * and writes the fastest into *p:
+ *   SPP_TUNE_LANES  gather_lanes in {1, 4} (ABP and continuous only): threads
+ *                   per particle in the neighbour sums.  Changes the order of
+ *                   the neighbour additions, hence the low bits of the result.
+ *   SPP_TUNE_SKIN   skin in {0.5, 1, 1.5, 2} x p->skin: list length against
+ *                   rebuild frequency.  Every neighbour list is summed in
+ *                   particle-id order, so the trajectory does not depend on
+ *                   the skin; candidates whose trial missed a rebuild
+ *                   (late_rebuilds > 0) are not chosen.
+ * Each candidate is a fresh system given (x, y, theta) (host arrays of
+ * p->n values in particle-id order), stepped trial_steps steps untimed
+ * (graph capture, list growth), then trial_steps steps timed with CUDA
+ * events (spp_time_steps).  The
+ * report lists every candidate in the order tried.  Takes the device memory
+ * of one system at a time. */
+#define SPP_TUNE_LANES 1
+#define SPP_TUNE_SKIN 2
+#define SPP_TUNE_MAX_CANDIDATES 8
+typedef struct SppTuneCandidate {
+  int32_t gather_lanes;
+  int32_t status;         /* SPP_OK, or the status that ruled the candidate out */
+  double skin;
+  double ms_per_step;     /* timed device time per step (0 if not measured) */
+  int64_t late_rebuilds;  /* rebuilds that came later than the skin allows, in the trial */
+} SppTuneCandidate;
+typedef struct SppTuneReport {
+  int32_t n_candidates;
+  int32_t best;           /* index of the chosen candidate */
+  SppTuneCandidate c[SPP_TUNE_MAX_CANDIDATES];
+} SppTuneReport;
+int spp_autotune(SppParams* p, const float* x, const float* y, const float* theta, int trial_steps,
+                 int what, SppTuneReport* report);
 /* Number of kernels this handle has launched (graph replays count each
  * kernel node they run). */
 int64_t spp_kernel_launches(SppSystem* s);

@@ -50,6 +50,20 @@ struct State {
   int64_t step = 0;
 };
 
+// Chooses p's launch shape (threads per particle, Verlet skin) by timing the
+// candidates on the device from the state (x, y, theta); call before
+// constructing the Box.  The reference fixes both from compile-time globals
+// (shared/parameters.h:80-99).
+inline SppTuneReport Autotune(SppParams& p, const std::vector<float>& x, const std::vector<float>& y,
+                              const std::vector<float>& theta, int trial_steps = 200,
+                              int what = SPP_TUNE_LANES | SPP_TUNE_SKIN) {
+  if ((int64_t)x.size() != p.n || (int64_t)y.size() != p.n || (int64_t)theta.size() != p.n)
+    throw Error(SPP_ERR_INVALID, "Autotune: state arrays must hold n values");
+  SppTuneReport r;
+  check(spp_autotune(&p, x.data(), y.data(), theta.data(), trial_steps, what, &r), "spp_autotune");
+  return r;
+}
+
 class Box {
  public:
   explicit Box(const SppParams& p) : p_(p), t(0.0), polarization(0.0) {

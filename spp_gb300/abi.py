@@ -37,7 +37,7 @@ class SppParams(C.Structure):
         ("r_rep", C.c_double), ("k_rep", C.c_double), ("sigma_rep", C.c_double),
         ("skin", C.c_double), ("beta_push", C.c_double), ("r_push", C.c_double),
         ("mu", C.c_double), ("k_perp", C.c_double), ("torque0", C.c_double),
-        ("k_bond", C.c_double), ("bond_rest", C.c_double), ("kappa_bend", C.c_double), ("rot_noise", C.c_int32), ("reserved", C.c_int32),
+        ("k_bond", C.c_double), ("bond_rest", C.c_double), ("kappa_bend", C.c_double), ("rot_noise", C.c_int32), ("gather_lanes", C.c_int32),
         ("tumble_rate", C.c_double), ("tumble_time", C.c_double), ("tumble_torque", C.c_double),
         ("chain_beads", C.c_int32), ("reserved2", C.c_int32),
         ("bead_separation", C.c_double), ("sigma_chain", C.c_double), ("r_chain", C.c_double),
@@ -98,8 +98,26 @@ class SppOrderStats(C.Structure):
                 ("p4_mean", C.c_double), ("binder", C.c_double), ("binder_reference", C.c_double)]
 
 
+TUNE_LANES, TUNE_SKIN = 1, 2
+TUNE_MAX_CANDIDATES = 8
+
+
+class SppTuneCandidate(C.Structure):
+    _fields_ = [("gather_lanes", C.c_int32), ("status", C.c_int32), ("skin", C.c_double),
+                ("ms_per_step", C.c_double), ("late_rebuilds", C.c_int64)]
+
+
+class SppTuneReport(C.Structure):
+    _fields_ = [("n_candidates", C.c_int32), ("best", C.c_int32),
+                ("c", SppTuneCandidate * TUNE_MAX_CANDIDATES)]
+
+
 def set_field(p, name, value):
-    """Sets a field, array fields (walls) from nested sequences."""
+    """Sets a field, array fields (walls) from nested sequences.  "reserved"
+    is the former name of gather_lanes (0 in parameter records written
+    before it had a meaning, i.e. the automatic lane count)."""
+    if name == "reserved":
+        name = "gather_lanes"
     cur = getattr(p, name)
     if isinstance(cur, C.Array):
         for a, row in enumerate(value):
@@ -175,6 +193,8 @@ PROTOTYPES = {
     "spp_lyap_vectors": (C.c_int, [_P, _F, C.c_int]),
     "spp_pairs_noalloc": (C.c_int, [_P, _P, C.c_int, C.c_double, C.c_double, _P, _P, C.c_int64,
                                     _P, _P]),
+    "spp_autotune": (C.c_int, [C.POINTER(SppParams), _F, _F, _F, C.c_int, C.c_int,
+                               C.POINTER(SppTuneReport)]),
 }
 
 _lib = None

@@ -160,6 +160,10 @@ int validate(const SppParams* p) {
         !std::isfinite(p->bead_separation) || !std::isfinite(p->sigma_chain) || !std::isfinite(p->r_chain))
       return fail(SPP_ERR_INVALID, "bead_separation, sigma_chain and r_chain must be finite and > 0");
   }
+  if (p->gather_lanes != 0 && p->gather_lanes != 1 && p->gather_lanes != SPP_GATHER_LANES)
+    return fail(SPP_ERR_INVALID, "gather_lanes must be 0 (automatic), 1 or 4");
+  if (p->gather_lanes == SPP_GATHER_LANES && p->model != SPP_MODEL_ABP && p->model != SPP_MODEL_CONTINUOUS)
+    return fail(SPP_ERR_UNSUPPORTED, "gather_lanes = 4 is built for SPP_MODEL_ABP and SPP_MODEL_CONTINUOUS");
   if (p->boundary != SPP_BOUNDARY_PERIODIC && p->boundary != SPP_BOUNDARY_WALLS)
     return fail(SPP_ERR_INVALID, "boundary must be SPP_BOUNDARY_PERIODIC or SPP_BOUNDARY_WALLS");
   if (p->boundary == SPP_BOUNDARY_WALLS) {

@@ -66,9 +66,9 @@ typedef struct SppConsts {
   float chain_k;               /* k_perpendicular */
   float chain_torque0;
   /* lanes per particle in the neighbour sums of the Verlet-list kernels
-   * (1, or SPP_GATHER_LANES for the ABP / continuous models up to
-   * SPP_LANES_MAX_N particles, where one thread per particle leaves the GPU
-   * idle): a neighbour belongs to lane id % lanes; each lane sums its
+   * (1, or SPP_GATHER_LANES for the ABP / continuous models: by default up
+   * to SPP_LANES_MAX_N particles, where one thread per particle leaves the
+   * GPU idle; SppParams.gather_lanes overrides): a neighbour belongs to lane id % lanes; each lane sums its
    * neighbours in id order and the lane sums combine as
    * (p0 + p1) + (p2 + p3) */
   int32_t lanes;
@@ -185,8 +185,17 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
     }
     k->tumble_steps = c;
   }
-  k->lanes = ((p->model == SPP_MODEL_ABP || p->model == SPP_MODEL_CONTINUOUS) && p->n <= SPP_LANES_MAX_N)
-                 ? SPP_GATHER_LANES : 1;
+  {
+    /* gather_lanes: 0 = automatic, else 1 or SPP_GATHER_LANES (ABP and
+     * continuous only; spp_create rejects the rest) */
+    const int lane_model = p->model == SPP_MODEL_ABP || p->model == SPP_MODEL_CONTINUOUS;
+    if (!lane_model || p->gather_lanes == 1)
+      k->lanes = 1;
+    else if (p->gather_lanes == SPP_GATHER_LANES)
+      k->lanes = SPP_GATHER_LANES;
+    else
+      k->lanes = p->n <= SPP_LANES_MAX_N ? SPP_GATHER_LANES : 1;
+  }
   k->closed = p->boundary == SPP_BOUNDARY_WALLS ? 1 : 0;
   k->n_walls = 0;
   for (int w = 0; w < SPP_MAX_WALLS; ++w) {

@@ -6,8 +6,8 @@ as one device batch (``Batch``), and an ensemble MLP trained on the sweep's
 own completed runs predicts each point's stationary polarization from its
 parameters and the moments of its polarization over a short start-up
 window.  Points whose predicted error is small retire after the window; the
-others run to the end, and a held-out 10% runs to the end to judge the
-surrogate.
+others run to the end, and a held-out 10% runs to the end to measure the
+surrogate's error.
 
 The ensemble is K-fold bagged: member e is fitted with the completed points
 of fold e left out (weight 0).  A point's error bound is c x (ensemble
@@ -21,7 +21,7 @@ Protocol (``run_sweep``):
   1. every point runs ``window`` steps (device-side moments of P);
   2. a pilot subset and the held-out points run to ``max_steps``; their
      stationary P (mean over the second half) are the training targets and
-     the judge's ground truth;
+     the held-out points' ground truth;
   3. rounds: fit on all completed non-held-out points; of the points whose
      bound exceeds ``tol``, the ``run_frac`` with the largest bounds (all of
      them in the last round) resume and run to the end -- the plain full run
@@ -211,8 +211,8 @@ class SweepResult:
     p_full: np.ndarray            # P of the points run to the end (NaN otherwise)
     bound: np.ndarray             # error bound of the decision that retired a point (NaN otherwise)
     retired: np.ndarray           # bool: answered by the surrogate
-    heldout: np.ndarray           # bool: judge points
-    heldout_err: np.ndarray       # |prediction - full run| on the judge points
+    heldout: np.ndarray           # bool: held-out points (always run in full)
+    heldout_err: np.ndarray       # |prediction - full run| on the held-out points
     particle_steps: int           # work actually done
     particle_steps_plain: int     # work of running every point to the end
     rounds: int
