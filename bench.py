@@ -249,11 +249,11 @@ def measured_hbm_peak():
     return 6800.0, "fallback"
 
 
-def ncu_traffic_per_launch(n):
-    """DRAM bytes per k_abp_stage launch from the committed ncu summary
-    (profiles/k_abp_stage_abp1M_rk2.md, the line 'dram bytes per launch:
-    <bytes> at n=<n>'), scaled to n particles."""
-    f = ROOT / "profiles" / "k_abp_stage_abp1M_rk2.md"
+def ncu_traffic_per_launch(n, summary="k_abp_stage_abp1M_rk2.md"):
+    """DRAM bytes per k_abp_stage launch from a committed ncu summary
+    (profiles/<summary>, the line 'dram bytes per launch: <bytes> at
+    n=<n>'), scaled to n particles."""
+    f = ROOT / "profiles" / summary
     if not f.exists():
         return None
     import re
@@ -613,6 +613,9 @@ def other_workload(args):
                          "frac": achieved / peak, "alg_bytes_per_unit": alg,
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                          "note": "effective bandwidth of the whole step; working set L2-resident"}}
+    if w == "vesicles":
+        line["roofline"]["traffic"] = ncu_traffic_per_launch(p.n, "k_abp_stage_vesicles163k_rk4.md")
+        line["roofline"]["traffic_note"] = "cold-cache DRAM bytes per k_abp_stage launch (ncu, 4 stages per step)"
     line.update(extra)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_workload(w, unit)
