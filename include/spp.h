@@ -406,7 +406,10 @@ int spp_time_steps(SppSystem* s, int nsteps, double* ms);
  *                   rebuild frequency.  Every neighbour list is summed in
  *                   particle-id order, so the trajectory does not depend on
  *                   the skin; candidates whose trial missed a rebuild
- *                   (late_rebuilds > 0) are not chosen.
+ *                   (late_rebuilds > 0) are not chosen.  (Lyapunov runs: the
+ *                   skin moves the list-overflow recoveries, each of which
+ *                   adds a renormalisation point, so the exponents agree
+ *                   across skins to rounding, not bit for bit.)
  * Each candidate is a fresh system given (x, y, theta) (host arrays of
  * p->n values in particle-id order), stepped trial_steps steps untimed
  * (graph capture, list growth), then trial_steps steps timed with CUDA
