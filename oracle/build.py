@@ -56,6 +56,7 @@ def build_ref(force=False):
         return out if out.exists() else None
     deps = [HERE / "ref_harness.cpp", HERE / "refshim" / "gsl" / "gsl_rng.h",
             HERE / "refshim" / "gsl" / "gsl_randist.h", shared / "particle.h",
+            shared / "vector-set.h", shared / "state-hyper-vector.h",
             REPO / "spp_gb300" / "csrc" / "spp_fp32.h"]
     if force or _stale(out, deps):
         out.parent.mkdir(parents=True, exist_ok=True)

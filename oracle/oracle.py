@@ -48,6 +48,7 @@ def orc():
         L.orc64_lyap_tangent.argtypes = [_P, C.c_int, C.c_int, C.c_int, _D, _D, _D, _D, _D, _D, _D]
         L.orc64_lyap_clone.argtypes = [_P, C.c_int, C.c_int, C.c_int, C.c_double, _D, _D, _D, _D,
                                        _D, _D, _D]
+        L.orc64_gram_schmidt.argtypes = [C.c_int, C.c_int, _D, _D, C.c_double]
         L.orc32_rsqrt.argtypes = [C.c_float]
         L.orc32_wall_terms.argtypes = [_P, C.c_float, C.c_float, C.c_float, _F]
         L.orc32_wall_terms.restype = None
@@ -77,6 +78,8 @@ def ref():
         L.ref_wall_terms.restype = None
         L.ref_r12_truncated.argtypes = [C.c_double] * 5 + [_D, _D]
         L.ref_spring.argtypes = [C.c_double] * 4 + [_D, _D]
+        L.ref_vectorset_renormalize.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _D, _D, _D]
+        L.ref_vectorset_renormalize.restype = C.c_int
         _ref = L
     return _ref
 
@@ -289,6 +292,27 @@ def lyap_clone64(p, state: State64, V, n_intervals, tau, eps=1e-7):
     if rc:
         raise RuntimeError(f"oracle lyap clone failed {rc}")
     return ls
+
+
+def gram_schmidt64(V, n, eps, fn="oracle", L=32.0):
+    """Orthonormalises K deviation vectors [K][3][n] (a copy) and returns
+    (U, log growth ratios log(R_aa / eps)): the oracle's modified
+    Gram-Schmidt, or with fn="ref" the reference's own VectorSet::
+    Renormalize(us) and LyapunovBox growth ratio (oracle/ref_harness.cpp)."""
+    V = np.ascontiguousarray(V, np.float64).copy()
+    K = V.size // (3 * n)
+    if fn == "ref":
+        U = np.empty_like(V)
+        ratio = np.empty(K, np.float64)
+        rc = ref().ref_vectorset_renormalize(K, n, float(L), float(eps), _d(V), _d(U), _d(ratio))
+        if rc:
+            raise RuntimeError(f"reference renormalisation failed {rc}")
+        return U, np.log(ratio)
+    ls = np.zeros(K, np.float64)
+    rc = orc().orc64_gram_schmidt(K, n, _d(V), _d(ls), float(eps))
+    if rc:
+        raise RuntimeError(f"oracle Gram-Schmidt failed {rc}")
+    return V, ls
 
 
 MATH_FNS = {"sin": 0, "cos": 1, "atan2": 2, "log": 3, "exp": 4, "wrap": 5}

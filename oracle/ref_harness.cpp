@@ -12,7 +12,8 @@
  * shipped (set-up.h assigns the const globals of parameters.h:81,83;
  * parameters.h:50 fixes Particle to ActiveBrownianChain).  Neither header is
  * included here, so no reference file needs patching: particle.h,
- * c2dvector.h, parameters.h and force-fields.h compile unmodified.
+ * c2dvector.h, parameters.h, force-fields.h, wall.h, vector-set.h and
+ * state-hyper-vector.h compile unmodified.
  *
  * Pair enumeration uses a cell list of width >= the largest cutoff; pairs
  * are visited in a different order than the reference's cell traversal,
@@ -20,6 +21,7 @@
  */
 #include "particle.h"   /* shared/particle.h of the reference */
 #include "wall.h"       /* shared/wall.h of the reference */
+#include "vector-set.h" /* shared/vector-set.h and state-hyper-vector.h of the reference */
 #include "../include/spp.h"
 #include <vector>
 #include <cmath>
@@ -328,4 +330,47 @@ extern "C" void ref_wall_terms(const SppParams* p, double x, double y, double th
     }
     out4[0] = q.f.x; out4[1] = q.f.y; out4[2] = q.torque;
   }
+}
+
+/* The renormalisation of the reference's Benettin clone method on K
+ * deviation vectors of n particles, stored [K][3][n] (x, y, theta blocks):
+ * VectorSet::Renormalize(us) (shared/vector-set.h:118-127) writes the
+ * orthonormal directions to U, and ratio[a] is the growth ratio that
+ * LyapunovBox::Evolution_Reorthonormalize takes from them
+ * (parallel/lyapunovbox.h:177-181: the deviation projected on its
+ * orthonormalised direction, |.| / amplitude; restated here with the
+ * reference's own State_Hyper_Vector operators, since lyapunovbox.h needs
+ * Box and MPI).  The reference keeps its base trajectory in v[0], which
+ * Renormalize skips, so the K deviations sit in v[1..K]. */
+extern "C" int ref_vectorset_renormalize(int K, int n, double L, double amplitude, const double* V,
+                                         double* U, double* ratio) {
+  if (K < 1 || n < 1) return 1;
+  set_box(L);
+  C2DVector::Init_Rand(1);
+  VectorSet::direction_num = K + 1;
+  VectorSet::particle_num = n;
+  VectorSet::amplitude = amplitude;
+  VectorSet vs, us;
+  for (int a = 0; a < K; ++a) {
+    const double* v = V + (size_t)a * 3 * n;
+    BasicParticle0* q = vs.v[a + 1].particle;
+    for (int i = 0; i < n; ++i) {
+      q[i].r.x = v[i];
+      q[i].r.y = v[n + i];
+      q[i].theta = v[2 * n + i];
+    }
+  }
+  vs.Renormalize(us);
+  for (int a = 0; a < K; ++a) {
+    const BasicParticle0* q = us.v[a + 1].particle;
+    double* u = U + (size_t)a * 3 * n;
+    for (int i = 0; i < n; ++i) {
+      u[i] = q[i].r.x;
+      u[n + i] = q[i].r.y;
+      u[2 * n + i] = q[i].theta;
+    }
+    State_Hyper_Vector proj = us.v[a + 1] * (vs.v[a + 1] * us.v[a + 1]);
+    ratio[a] = proj.Magnitude() / VectorSet::amplitude;
+  }
+  return 0;
 }

@@ -914,6 +914,16 @@ static void mgs(int K, size_t len, double* V, double* log_stretch, double scale)
   }
 }
 
+/* The clone method's renormalisation on its own: K deviation vectors
+ * [K][3][n] are orthonormalised in place and log(|R_aa| / scale) is added
+ * to log_stretch[a], where R_aa is what LyapunovBox's growth ratio
+ * (parallel/lyapunovbox.h:177-181) measures times the amplitude. */
+int orc64_gram_schmidt(int K, int n, double* V, double* log_stretch, double scale) {
+  if (K < 1 || n < 1 || !V) return SPP_ERR_INVALID;
+  mgs(K, (size_t)3 * n, V, log_stretch, scale);
+  return SPP_OK;
+}
+
 typedef struct {
   ostate* s;
   const double* U;  /* stage tangent input [K][3][n] */

@@ -6,7 +6,11 @@ with the GSL calls answered by the Philox shim) on small seeded cases and
 stores inputs and outputs.  The fixtures pin the FP64 restatement
 (oracle/spp_oracle64.c) where the reference checkout is absent.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [runs] [gram_schmidt]   (default: both)
+
+reference_gram_schmidt.npz pins the Lyapunov clone method's
+renormalisation (shared/vector-set.h:118-127, parallel/lyapunovbox.h:
+177-181) the same way.
 """
 import json
 import sys
@@ -121,9 +125,41 @@ def wall_case(model):
     return p, np.array(pts, np.float64)
 
 
-def main():
+def gram_schmidt_cases():
+    """Deviation vectors [K][3][n] at the clone method's scale (eps = 1e-7):
+    independent ones, and a set whose later vectors are the earlier ones
+    plus 1e-3 of new noise (nearly dependent, where modified and classical
+    Gram-Schmidt part)."""
+    n, K, eps = 300, 5, 1e-7
+    rng = np.random.default_rng(21)
+    free = rng.standard_normal((K, 3 * n)) * eps
+    close = np.empty((K, 3 * n))
+    close[0] = rng.standard_normal(3 * n) * eps
+    for a in range(1, K):
+        close[a] = close[a - 1] + 1e-3 * rng.standard_normal(3 * n) * eps
+    return n, eps, {"independent": free.ravel(), "nearly_dependent": close.ravel()}
+
+
+def gram_schmidt_fixture():
+    """tests/golden/reference_gram_schmidt.npz: the reference's
+    VectorSet::Renormalize(us) and LyapunovBox growth ratios."""
+    n, eps, cases_ = gram_schmidt_cases()
+    blob = {"n": np.array(n), "eps": np.array(eps)}
+    for name, V in cases_.items():
+        U, logr = O.gram_schmidt64(V, n, eps, fn="ref")
+        blob[f"{name}/in"], blob[f"{name}/U"], blob[f"{name}/log_ratio"] = V, U, logr
+    path = Path(__file__).resolve().parent / "reference_gram_schmidt.npz"
+    np.savez_compressed(path, **blob)
+    print(path, path.stat().st_size, "bytes")
+
+
+def main(parts=("runs", "gram_schmidt")):
     if O.ref() is None:
         raise SystemExit("reference checkout not found: cannot regenerate the fixtures")
+    if "gram_schmidt" in parts:
+        gram_schmidt_fixture()
+    if "runs" not in parts:
+        return
     blob = {}
     meta = {}
     for name, p, x, y, th, steps in cases():
@@ -144,4 +180,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]) or ("runs", "gram_schmidt"))

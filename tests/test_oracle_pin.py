@@ -195,3 +195,42 @@ def test_golden_fixtures_reproduce_from_reference():
         s = O.State64(x, y, th, xu, yu)
         O.run64(p, s, meta[name]["steps"], fn="ref")
         assert max_diff(np.stack([s.x, s.y, s.th, s.xu, s.yu]), z[f"{name}/out"]) < 1e-12, name
+
+
+GRAM_SCHMIDT = Path(__file__).resolve().parent / "golden" / "reference_gram_schmidt.npz"
+# |dU| and |d log ratio| allowed per case.  Independent deviations: FP64
+# summation order only.  Nearly dependent ones (each 1e-3 away from the
+# previous): the reference takes the growth ratio as the raw deviation's
+# dot product with its orthonormalised direction, which cancels ~1e3-fold
+# there, where the restatement takes the norm of the orthogonalised vector;
+# the two agree to ~1e-9 in the log.
+GS_TOL = {"independent": (1e-13, 1e-13), "nearly_dependent": (1e-12, 1e-8)}
+
+
+@pytest.mark.parametrize("case", ["independent", "nearly_dependent"])
+def test_gram_schmidt_matches_golden(case):
+    """The clone method's renormalisation (VectorSet::Renormalize(us),
+    shared/vector-set.h:118-127) and growth ratios (parallel/
+    lyapunovbox.h:177-181), replayed from the reference's fixtures."""
+    z = np.load(GRAM_SCHMIDT)
+    U, logr = O.gram_schmidt64(z[f"{case}/in"], int(z["n"]), float(z["eps"]))
+    tol_u, tol_l = GS_TOL[case]
+    assert max_diff(U, z[f"{case}/U"]) < tol_u
+    assert max_diff(logr, z[f"{case}/log_ratio"]) < tol_l
+
+
+def test_gram_schmidt_matches_reference():
+    """Live against the reference's own VectorSet on fresh vectors, and the
+    committed fixture is what the reference produces today."""
+    _ref_or_skip()
+    rng = np.random.default_rng(5)
+    n, K, eps = 200, 4, 1e-7
+    V = rng.standard_normal(K * 3 * n) * eps
+    U, logr = O.gram_schmidt64(V, n, eps)
+    Ur, logr_r = O.gram_schmidt64(V, n, eps, fn="ref")
+    assert max_diff(U, Ur) < 1e-13 and max_diff(logr, logr_r) < 1e-13
+    assert max_diff(U.reshape(K, -1) @ U.reshape(K, -1).T, np.eye(K)) < 1e-13
+    z = np.load(GRAM_SCHMIDT)
+    for case in GS_TOL:
+        Ur, logr_r = O.gram_schmidt64(z[f"{case}/in"], int(z["n"]), float(z["eps"]), fn="ref")
+        assert np.array_equal(Ur, z[f"{case}/U"]) and np.array_equal(logr_r, z[f"{case}/log_ratio"])
