@@ -57,11 +57,13 @@ def build_ref(force=False):
     deps = [HERE / "ref_harness.cpp", HERE / "refshim" / "gsl" / "gsl_rng.h",
             HERE / "refshim" / "gsl" / "gsl_randist.h", shared / "particle.h",
             shared / "vector-set.h", shared / "state-hyper-vector.h",
+            REFERENCE_DIR / "analyze" / "statistics.h",
+            HERE / "refshim" / "boost" / "algorithm" / "string.hpp",
             REPO / "spp_gb300" / "csrc" / "spp_fp32.h"]
     if force or _stale(out, deps):
         out.parent.mkdir(parents=True, exist_ok=True)
         _run(["g++", "-std=c++14", *CFLAGS, "-w", "-DRUNGE_KUTTA4",
-              "-I", str(HERE / "refshim"), "-I", str(shared),
+              "-I", str(HERE / "refshim"), "-I", str(shared), "-I", str(REFERENCE_DIR / "analyze"),
               "-o", str(out), str(HERE / "ref_harness.cpp"), "-lm"])
     return out
 

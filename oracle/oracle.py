@@ -80,6 +80,8 @@ def ref():
         L.ref_spring.argtypes = [C.c_double] * 4 + [_D, _D]
         L.ref_vectorset_renormalize.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _D, _D, _D]
         L.ref_vectorset_renormalize.restype = C.c_int
+        L.ref_order_parameters.argtypes = [_D, C.c_int, C.c_double, _D]
+        L.ref_order_parameters.restype = C.c_int
         _ref = L
     return _ref
 

@@ -22,6 +22,9 @@
 #include "particle.h"   /* shared/particle.h of the reference */
 #include "wall.h"       /* shared/wall.h of the reference */
 #include "vector-set.h" /* shared/vector-set.h and state-hyper-vector.h of the reference */
+#include <fstream>
+#include <sstream>
+#include "statistics.h" /* analyze/statistics.h of the reference (Boost: oracle/refshim) */
 #include "../include/spp.h"
 #include <vector>
 #include <cmath>
@@ -372,5 +375,29 @@ extern "C" int ref_vectorset_renormalize(int K, int n, double L, double amplitud
     State_Hyper_Vector proj = us.v[a + 1] * (vs.v[a + 1] * us.v[a + 1]);
     ratio[a] = proj.Magnitude() / VectorSet::amplitude;
   }
+  return 0;
+}
+
+/* The order-parameter judges of the reference's analysis on a polarization
+ * series p[0..T): Stat<double>::Compute with Find_Correlation_Length
+ * (analyze/statistics.h:35-82) on P and on P^4, then the combination of
+ * Compute_Order_Parameters (analyze/analyze.h:121-146): <P>, its error,
+ * sigma2 = variance * area and G = 1 - <P^4> / (3 <P^2>), the reference's
+ * form.  The reference forms P^4 as |v|^2 |v|^2 from the mean heading
+ * vector v; from a series of P it is (P P)(P P).  out: mean, mean_square,
+ * variance, std, min, max, corr_len, error, sigma2, p4_mean, G. */
+extern "C" int ref_order_parameters(const double* series, int T, double area, double* out) {
+  if (T < 2) return 1;
+  Stat<double> p, p4;
+  for (int i = 0; i < T; ++i) {
+    const double s2 = series[i] * series[i];
+    p.Add_Data(series[i]);
+    p4.Add_Data(s2 * s2);
+  }
+  p.Compute();
+  p4.Compute();
+  const double v[11] = {p.mean, p.mean_square, p.variance, p.std, p.min, p.max, p.corr_len,
+                        p.error, p.variance * area, p4.mean, 1 - (p4.mean / (3 * p.mean_square))};
+  for (int q = 0; q < 11; ++q) out[q] = v[q];
   return 0;
 }

@@ -6,11 +6,13 @@ with the GSL calls answered by the Philox shim) on small seeded cases and
 stores inputs and outputs.  The fixtures pin the FP64 restatement
 (oracle/spp_oracle64.c) where the reference checkout is absent.
 
-    python tests/golden/make_golden.py [runs] [gram_schmidt]   (default: both)
+    python tests/golden/make_golden.py [runs] [gram_schmidt] [order_parameters]
+    (default: all three)
 
 reference_gram_schmidt.npz pins the Lyapunov clone method's
 renormalisation (shared/vector-set.h:118-127, parallel/lyapunovbox.h:
-177-181) the same way.
+177-181) the same way, and reference_order_parameters.npz the analysis
+statistics (analyze/statistics.h:35-82, analyze/analyze.h:121-146).
 """
 import json
 import sys
@@ -153,11 +155,49 @@ def gram_schmidt_fixture():
     print(path, path.stat().st_size, "bytes")
 
 
-def main(parts=("runs", "gram_schmidt")):
+ORDER_KEYS = ["mean", "mean_square", "variance", "std", "min", "max", "corr_len", "error", "sigma2",
+              "p4_mean", "binder_reference"]
+
+
+def ar1_series(T, phi, seed, mean=0.6, sd=0.05):
+    """A polarization-like AR(1) series: correlation time ~ 1 / (1 - phi)."""
+    rng = np.random.default_rng(seed)
+    x = np.empty(T)
+    x[0] = mean
+    for t in range(1, T):
+        x[t] = mean + phi * (x[t - 1] - mean) + sd * rng.standard_normal()
+    return x
+
+
+ORDER_CASES = [(600, 0.9, 1), (1000, 0.0, 2), (257, 0.98, 3), (2, 0.5, 4), (5000, 0.995, 5)]
+
+
+def order_parameters_fixture():
+    """tests/golden/reference_order_parameters.npz: the reference's own
+    Stat::Compute / Find_Correlation_Length and the combination of
+    Compute_Order_Parameters on AR(1) series (area 4096)."""
+    import ctypes as C
+    blob = {"keys": np.frombuffer(json.dumps(ORDER_KEYS).encode(), dtype=np.uint8)}
+    for T, phi, seed in ORDER_CASES:
+        x = ar1_series(T, phi, seed)
+        out = np.zeros(len(ORDER_KEYS))
+        rc = O.ref().ref_order_parameters(x.ctypes.data_as(C.POINTER(C.c_double)), T, 4096.0,
+                                          out.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc:
+            raise SystemExit(f"reference statistics failed on case {T}")
+        blob[f"T{T}_seed{seed}/in"], blob[f"T{T}_seed{seed}/out"] = x, out
+    path = Path(__file__).resolve().parent / "reference_order_parameters.npz"
+    np.savez_compressed(path, **blob)
+    print(path, path.stat().st_size, "bytes")
+
+
+def main(parts=("runs", "gram_schmidt", "order_parameters")):
     if O.ref() is None:
         raise SystemExit("reference checkout not found: cannot regenerate the fixtures")
     if "gram_schmidt" in parts:
         gram_schmidt_fixture()
+    if "order_parameters" in parts:
+        order_parameters_fixture()
     if "runs" not in parts:
         return
     blob = {}
@@ -180,4 +220,4 @@ def main(parts=("runs", "gram_schmidt")):
 
 
 if __name__ == "__main__":
-    main(tuple(sys.argv[1:]) or ("runs", "gram_schmidt"))
+    main(tuple(sys.argv[1:]) or ("runs", "gram_schmidt", "order_parameters"))
