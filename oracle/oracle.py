@@ -82,6 +82,8 @@ def ref():
         L.ref_vectorset_renormalize.restype = C.c_int
         L.ref_order_parameters.argtypes = [_D, C.c_int, C.c_double, _D]
         L.ref_order_parameters.restype = C.c_int
+        L.ref_write_records.argtypes = [C.c_int, C.c_int, _D, _D, _D, C.c_char_p, C.c_long]
+        L.ref_write_records.restype = C.c_long
         _ref = L
     return _ref
 

@@ -401,3 +401,34 @@ extern "C" int ref_order_parameters(const double* series, int T, double area, do
   for (int q = 0; q < 11; ++q) out[q] = v[q];
   return 0;
 }
+
+/* The record bytes that the reference's frame writer emits per particle
+ * (operator<<(ostream&, Box*), parallel/box.h:476-502, calls Write on each):
+ * kind 0 through RepulsiveParticle::Write (shared/particle.h:759-764:
+ * r_original, then theta), kind 1 through ActiveBrownianChain::Write with
+ * F0 = 0 (a membrane bead, :1038-1039: r_original only), kind 2 with F0 = 1
+ * (a swimmer, :1040-1045).  Returns the byte count, or -1 if cap is short. */
+extern "C" long ref_write_records(int kind, int n, const double* xu, const double* yu,
+                                  const double* th, unsigned char* out, long cap) {
+  std::ostringstream os(std::ios::binary);
+  for (int i = 0; i < n; ++i) {
+    if (kind == 0) {
+      RepulsiveParticle q;
+      q.r_original.x = xu[i];
+      q.r_original.y = yu[i];
+      q.theta = th[i];
+      q.Write(os);
+    } else {
+      ActiveBrownianChain q;
+      q.Set_F0(kind == 1 ? 0.0 : 1.0);
+      q.r_original.x = xu[i];
+      q.r_original.y = yu[i];
+      q.theta = th[i];
+      q.Write(os);
+    }
+  }
+  const std::string b = os.str();
+  if ((long)b.size() > cap) return -1;
+  for (size_t k = 0; k < b.size(); ++k) out[k] = (unsigned char)b[k];
+  return (long)b.size();
+}

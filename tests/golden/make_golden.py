@@ -6,13 +6,15 @@ with the GSL calls answered by the Philox shim) on small seeded cases and
 stores inputs and outputs.  The fixtures pin the FP64 restatement
 (oracle/spp_oracle64.c) where the reference checkout is absent.
 
-    python tests/golden/make_golden.py [runs] [gram_schmidt] [order_parameters]
-    (default: all three)
+    python tests/golden/make_golden.py [runs] [gram_schmidt] [order_parameters] [records]
+    (default: all four)
 
 reference_gram_schmidt.npz pins the Lyapunov clone method's
 renormalisation (shared/vector-set.h:118-127, parallel/lyapunovbox.h:
 177-181) the same way, and reference_order_parameters.npz the analysis
-statistics (analyze/statistics.h:35-82, analyze/analyze.h:121-146).
+statistics (analyze/statistics.h:35-82, analyze/analyze.h:121-146), and
+reference_records.npz the particle records of the .bin frame writer
+(shared/particle.h:759-764, 1022-1045).
 """
 import json
 import sys
@@ -191,9 +193,31 @@ def order_parameters_fixture():
     print(path, path.stat().st_size, "bytes")
 
 
-def main(parts=("runs", "gram_schmidt", "order_parameters")):
+def records_fixture():
+    """tests/golden/reference_records.npz: the bytes of the reference's own
+    particle Write methods (RepulsiveParticle, ActiveBrownianChain membrane
+    bead and swimmer) for seeded unwrapped positions and headings."""
+    import ctypes as C
+    rng = np.random.default_rng(31)
+    n = 200
+    xu = rng.uniform(-5e4, 5e4, n)
+    yu = rng.uniform(-5e4, 5e4, n)
+    th = rng.uniform(-np.pi, np.pi, n)
+    blob = {"xu": xu, "yu": yu, "theta": th}
+    for kind in (0, 1, 2):
+        buf = C.create_string_buffer(16 * n)
+        m = O.ref().ref_write_records(kind, n, O._d(xu), O._d(yu), O._d(th), buf, 16 * n)
+        blob[f"kind{kind}"] = np.frombuffer(buf.raw[:m], dtype=np.uint8)
+    path = Path(__file__).resolve().parent / "reference_records.npz"
+    np.savez_compressed(path, **blob)
+    print(path, path.stat().st_size, "bytes")
+
+
+def main(parts=("runs", "gram_schmidt", "order_parameters", "records")):
     if O.ref() is None:
         raise SystemExit("reference checkout not found: cannot regenerate the fixtures")
+    if "records" in parts:
+        records_fixture()
     if "gram_schmidt" in parts:
         gram_schmidt_fixture()
     if "order_parameters" in parts:
@@ -220,4 +244,4 @@ def main(parts=("runs", "gram_schmidt", "order_parameters")):
 
 
 if __name__ == "__main__":
-    main(tuple(sys.argv[1:]) or ("runs", "gram_schmidt", "order_parameters"))
+    main(tuple(sys.argv[1:]) or ("runs", "gram_schmidt", "order_parameters", "records"))

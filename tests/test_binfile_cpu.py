@@ -4,6 +4,7 @@ reader's health rules."""
 import struct
 
 import numpy as np
+import pytest
 
 from spp_gb300 import abi, binfile, configs
 
@@ -105,3 +106,42 @@ def test_chain_frames_carry_chain_length():
     xv, yv, tv = configs.vesicle_state(q)
     z = np.zeros(q.n, np.int32)
     assert binfile.read_frames(binfile.state_frame(q, 0.0, xv, yv, tv, z, z))[0].nb == 1
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
+def test_records_match_the_reference_writer(kind):
+    """Where the reference checkout is present, the frame's particle records
+    are byte for byte what the reference's own Write methods emit
+    (shared/particle.h compiled in the oracle harness): kind 0
+    RepulsiveParticle::Write (:759-764, x, y, theta), kind 1 a membrane bead
+    of ActiveBrownianChain::Write (F0 = 0, :1038-1039, x, y), kind 2 one of
+    its swimmers (:1040-1045).  Values include large unwrapped positions and
+    the float32 rounding edge."""
+    import ctypes as C
+    from oracle import oracle as O
+    r = O.ref()
+    if r is None:
+        pytest.skip("reference checkout absent")
+    rng = np.random.default_rng(kind)
+    n = 300
+    xu = np.concatenate([rng.uniform(-5e4, 5e4, n - 4), [0.0, -0.0, 1.0 + 2.0 ** -24, 16777217.0]])
+    yu = rng.uniform(-5e4, 5e4, n)
+    th = rng.uniform(-np.pi, np.pi, n)
+    buf = C.create_string_buffer(16 * n)
+    m = r.ref_write_records(kind, n, O._d(xu), O._d(yu), O._d(th), buf, 16 * n)
+    assert m == (8 if kind == 1 else 12) * n
+    frame = binfile.encode_frame(1.5, 64.0, xu, yu, th) if kind != 1 else \
+        binfile.encode_frame(1.5, 64.0, [], [], [], mx=xu, my=yu)
+    assert frame[binfile.HEADER.size:] == buf.raw[:m]
+
+
+def test_records_match_the_reference_fixture():
+    """The same pin replayed from tests/golden/reference_records.npz (made by
+    tests/golden/make_golden.py from the reference's Write methods)."""
+    from pathlib import Path
+    z = np.load(Path(__file__).resolve().parent / "golden" / "reference_records.npz")
+    xu, yu, th = z["xu"], z["yu"], z["theta"]
+    head = binfile.HEADER.size
+    assert binfile.encode_frame(0.0, 8.0, xu, yu, th)[head:] == z["kind0"].tobytes()
+    assert binfile.encode_frame(0.0, 8.0, xu, yu, th)[head:] == z["kind2"].tobytes()
+    assert binfile.encode_frame(0.0, 8.0, [], [], [], mx=xu, my=yu)[head:] == z["kind1"].tobytes()
