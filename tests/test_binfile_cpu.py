@@ -71,6 +71,7 @@ def test_checkpoint_file_format(tmp_path):
     from spp_gb300 import checkpoint
     p = configs.abp_config(n=8, L=4.0, seed=3)
     p.struct_size = C.sizeof(abi.SppParams)
+    p.gather_lanes = 4   # a tuned lane count is part of the result and travels with the state
     raw = bytes(C.string_at(C.addressof(p), C.sizeof(p)))
     x = np.arange(8, dtype=np.float32)
     path = tmp_path / "ck.npz"
@@ -78,6 +79,7 @@ def test_checkpoint_file_format(tmp_path):
              img_x=np.ones(8, np.int32), img_y=np.zeros(8, np.int32), step=np.int64(77))
     q, snap = checkpoint.load(path)
     assert bytes(q) == raw and snap.step == 77 and np.array_equal(snap.y, -x)
+    assert q.gather_lanes == 4
     # a record of the layout before the chain fields (struct_size 240)
     old = bytearray(raw[:240])
     old[:4] = (240).to_bytes(4, "little")
