@@ -357,6 +357,7 @@ def run_ours(args):
         s.download(out=buf_in)
         step_at = s.step0 + int(s.observables().step)
         launches0 = s.kernel_launches()
+        regrow0 = int(s.observables().list_regrowths)
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
@@ -371,6 +372,8 @@ def run_ours(args):
         clocks = sampler.stop()
         torch.cuda.synchronize()
         launches = s.kernel_launches() - launches0
+        # spp_time_steps times list-overflow recoveries too; count them
+        overflows = int(s.observables().list_regrowths) - regrow0
         elapsed_ms = sum(times)
         if dist:
             from spp_gb300.replicas import max_over_ranks
@@ -411,6 +414,7 @@ def run_ours(args):
         "config": workload_config(n),
         "ms_per_sim_step": elapsed_ms / args.steps / S,
         "gpu_launches": int(launches),
+        "overflows_in_timed_region": overflows,
         "clocks": clocks,
         "wall_s_timed_region": wall,
         "roofline": {
@@ -461,8 +465,9 @@ def run_reference(args):
     value = cores * N_FULL * args.steps / total
     sample = (f"each bench step: {cores} concurrent single-thread replicas (one per host core) x "
               f"N=1,048,576 x 1 RK2 step of the FP64 restatement (oracle/spp_oracle64.c); the "
-              f"reference's own code cannot run on this host (needs GSL/MPI, and its compiled "
-              f"harness is x86-only here)")
+              f"reference's own code cannot run here: it is header-only C++ that needs GSL and "
+              f"MPI, and its source checkout, from which the harness is compiled, is not on "
+              f"this machine")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,

@@ -172,6 +172,8 @@ typedef struct SppObservables {
   int64_t late_rebuilds;  /* list rebuilds decided only after some particle had moved more than
                              skin/2 since the previous build: pairs may have been missed (the
                              time step is too large for the skin) */
+  int64_t list_regrowths; /* neighbour-list overflows met so far: each one grew the list and re-ran
+                             the frozen steps */
 } SppObservables;
 
 typedef struct SppSystem SppSystem;
@@ -392,7 +394,10 @@ typedef struct SppProfile {
  * stream.  The state advances exactly as under spp_step. */
 int spp_profile(SppSystem* s, int nsteps, SppProfile* out);
 /* spp_step(nsteps) bracketed by CUDA events on the handle's stream; waits for
- * completion and returns the elapsed device time in *ms. */
+ * completion and returns the elapsed device time in *ms.  The end event is
+ * recorded after any list-overflow recovery has finished the requested
+ * steps, so recovered steps are timed as well (the host round trip of a
+ * recovery included). */
 int spp_time_steps(SppSystem* s, int nsteps, double* ms);
 /* ---- autotuner of the launch shape (no counterpart in the reference) ----
  * The reference fixes its cell and list geometry from compile-time globals
@@ -453,11 +458,15 @@ void* spp_stream(SppSystem* s);
  * Scratch is one static device array of about 1.8 MB that every GPU loading
  * this library holds until the process exits; n <= SPP_NOALLOC_MAX_N and at
  * most SPP_NOALLOC_MAX_CELLS_PER_SIDE^2 cells, larger n is rejected with
- * SPP_ERR_INVALID.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress, with that device current); make that first
- * call before any stream capture.  Calls share the array: calls that overlap
- * on the GPU race and must be ordered by the caller.  Allocates nothing:
- * no cudaMalloc, cudaFree or allocating library routine is called. */
+ * SPP_ERR_INVALID.  The first call in a CUDA context (each device's primary
+ * context, a context the caller made current, or a new primary context after
+ * cudaDeviceReset) looks up the array's device address in that context
+ * (cudaGetSymbolAddress) and remembers it by the context's id; make that
+ * first call before any stream capture (a first call inside a capture is
+ * refused with SPP_ERR_INVALID).  Calls share the array: calls that overlap
+ * on the GPU race and must be ordered by the caller; the host-side set-up
+ * is safe from several threads.  Allocates nothing: no cudaMalloc, cudaFree
+ * or allocating library routine is called. */
 #define SPP_NOALLOC_MAX_N 65536
 #define SPP_NOALLOC_MAX_CELLS_PER_SIDE 256
 int spp_pairs_noalloc(const float* x, const float* y, int n, double L, double r, int32_t* pi,

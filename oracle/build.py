@@ -4,8 +4,8 @@
   the FP32 kernel-arithmetic mirror (spp_mirror32.c), plain C.
 - ``oracle/_ref/libspp_ref.so``: the reference's own shared/particle.h driven
   by ref_harness.cpp, compiled from the reference checkout in place (never
-  copied).  Built only where that checkout exists (``SPP_REFERENCE_DIR``,
-  default /root/reference).
+  copied).  Built only where that checkout exists: ``SPP_REFERENCE_DIR``, else
+  a directory named ``reference`` beside this repository.
 
 Both use -ffp-contract=off so that only explicit fmaf() calls fuse, exactly as
 the kernels (built with -fmad=false) do.
@@ -17,7 +17,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
-REFERENCE_DIR = Path(os.environ.get("SPP_REFERENCE_DIR", "/root/reference"))
+REFERENCE_DIR = Path(os.environ.get("SPP_REFERENCE_DIR", str(REPO.parent / "reference")))
 
 CFLAGS = ["-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-Wall",
           "-Wno-unused-function", "-Wno-misleading-indentation"]

@@ -62,6 +62,7 @@ struct SppSystem {
   int64_t host_launches = 0;
   int64_t graph_kernels = 0;
   int64_t direct_rebuilds = 0;
+  int64_t regrowths = 0;         /* neighbour-list regrowths after an overflow */
   int64_t target_step = 0;       /* step the caller has asked to reach */
   int64_t step0 = 0;
   bool uploaded = false;
@@ -430,6 +431,7 @@ int recover(SppSystem* s) {
     s->lyap_graphs.clear();
     rc = alloc_list(s, cap);
     if (rc != SPP_OK) return rc;
+    s->regrowths++;
     CUDA_TRY(cudaMemsetAsync(&s->d.ctl->frozen, 0, sizeof(uint32_t), s->stream));
     CUDA_TRY(cudaMemsetAsync(&s->d.ctl->list_need, 0, sizeof(uint32_t), s->stream));
     rc = enqueue_rebuild(s, s->stream, &s->host_launches);
@@ -867,6 +869,7 @@ int spp_observables(SppSystem* s, SppObservables* o) {
   o->max_neighbors = (int32_t)c.max_nn;
   o->cells_per_side = s->d.D;
   o->late_rebuilds = c.late_rebuilds;
+  o->list_regrowths = s->regrowths;
   return SPP_OK;
 }
 
@@ -1098,6 +1101,10 @@ int spp_time_steps(SppSystem* s, int nsteps, double* ms) {
   CUDA_TRY(cudaEventCreate(&b));
   cudaEventRecord(a, s->stream);
   int rc = spp_step(s, nsteps);
+  /* A list overflow freezes the stage kernels; recover() then regrows the
+   * list and runs the skipped steps.  The end event follows that recovery,
+   * so every requested step lies inside the timed interval. */
+  if (rc == SPP_OK) rc = spp_sync(s);
   cudaEventRecord(b, s->stream);
   cudaError_t e = cudaEventSynchronize(b);
   float t = 0;
@@ -1107,7 +1114,7 @@ int spp_time_steps(SppSystem* s, int nsteps, double* ms) {
   if (rc != SPP_OK) return rc;
   if (e != cudaSuccess) return fail(SPP_ERR_CUDA, cudaGetErrorString(e));
   *ms = t;
-  return spp_sync(s);
+  return SPP_OK;
 }
 
 int64_t spp_kernel_launches(SppSystem* s) {

@@ -6,8 +6,9 @@
  * (serial/box.h:380-424 -> RepulsiveParticle::Move_Runge_Kutta{2,4}_k,
  * shared/particle.h:589-726), in one pass: one thread per particle (cell
  * order) gathers its Verlet neighbours' float4 (x, y, cos, sin) state,
- * accumulates force, torque and neighbour count in int64 fixed point, and
- * writes its stage state.  The last stage also
+ * sums force and torque in FP32 in ascending neighbour id (the lists are
+ * sorted by id at every build, so the sums are reproducible), counts the
+ * neighbours, and writes its stage state.  The last stage also
  *   - advances theta / image counters in place,
  *   - reduces the largest squared displacement since the last list build,
  *   - and, in the block that finishes last, decides whether the list must be

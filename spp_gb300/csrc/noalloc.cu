@@ -17,7 +17,10 @@
  * overlap on the GPU (different streams, or different host threads without
  * ordering) race on it and must be serialised by the caller.
  */
+#include <cuda.h>   /* CUcontext and CUresult types only: the two driver entry points below
+                       come from the runtime (cudaGetDriverEntryPointByVersion) */
 #include <cmath>
+#include <mutex>
 #include <string>
 #include "spp_internal.cuh"
 
@@ -42,9 +45,68 @@ struct NaScratch {
 
 static __device__ __align__(256) NaScratch g_na_scratch;
 
-/* Host-side device address of g_na_scratch, per device (set up once). */
-constexpr int NA_MAX_DEVICES = 64;
-NaScratch* g_na_ptr[NA_MAX_DEVICES] = {nullptr};
+/* Host-side device addresses of g_na_scratch, one per CUDA context.  Each
+ * context that loads this library holds its own copy of the array, and a
+ * context created after cudaDeviceReset may place it elsewhere, so the
+ * address is keyed by the context's unique id (cuCtxGetId: ids are never
+ * reused within a process), not by the device ordinal.  The table is read
+ * and written under g_na_mu. */
+constexpr int NA_MAX_CONTEXTS = 64;
+struct NaEntry {
+  unsigned long long ctx_id;
+  NaScratch* ptr;
+};
+std::mutex g_na_mu;
+NaEntry g_na_cache[NA_MAX_CONTEXTS];
+int g_na_used = 0;
+int g_na_next = 0;   /* slot replaced next once the table is full */
+
+typedef CUresult(CUDAAPI* NaCtxGetCurrent)(CUcontext*);
+typedef CUresult(CUDAAPI* NaCtxGetId)(CUcontext, unsigned long long*);
+
+/* Unique id of the calling thread's current context; false if there is none
+ * (the runtime has not made one current on this thread yet) or the driver
+ * does not offer the entry points. */
+bool na_current_context(unsigned long long* id) {
+  static std::once_flag once;
+  static NaCtxGetCurrent get_current = nullptr;
+  static NaCtxGetId get_id = nullptr;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<NaCtxGetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<NaCtxGetId>(f);
+    cudaGetLastError();
+  });
+  if (!get_current || !get_id) return false;
+  CUcontext c = nullptr;
+  if (get_current(&c) != CUDA_SUCCESS || !c) return false;
+  return get_id(c, id) == CUDA_SUCCESS;
+}
+
+NaScratch* na_lookup(unsigned long long id) {
+  std::lock_guard<std::mutex> g(g_na_mu);
+  for (int i = 0; i < g_na_used; ++i)
+    if (g_na_cache[i].ctx_id == id) return g_na_cache[i].ptr;
+  return nullptr;
+}
+
+void na_remember(unsigned long long id, NaScratch* ptr) {
+  std::lock_guard<std::mutex> g(g_na_mu);
+  for (int i = 0; i < g_na_used; ++i)
+    if (g_na_cache[i].ctx_id == id) { g_na_cache[i].ptr = ptr; return; }
+  if (g_na_used < NA_MAX_CONTEXTS) {
+    g_na_cache[g_na_used++] = {id, ptr};
+  } else {
+    g_na_cache[g_na_next] = {id, ptr};
+    g_na_next = (g_na_next + 1) % NA_MAX_CONTEXTS;
+  }
+}
 
 __global__ void k_na_clear(NaScratch* s, int n_keys) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -173,22 +235,34 @@ extern "C" int spp_pairs_noalloc(const float* x, const float* y, int n, double L
   if (D > NA_MAX_SIDE) D = NA_MAX_SIDE;  /* wider cells only add candidates */
   if (D < 3)
     return na_fail(SPP_ERR_INVALID, "spp_pairs_noalloc: box too small for the cell grid (2L/r < 3)");
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return na_fail(SPP_ERR_CUDA, cudaGetErrorString(e));
-  if (dev < 0 || dev >= NA_MAX_DEVICES)
-    return na_fail(SPP_ERR_INVALID, "spp_pairs_noalloc: device index out of range");
-  if (!g_na_ptr[dev]) {
-    /* first call on this device: resolve the device address of the scratch
-     * array with the device current (no allocation is involved) */
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  /* The scratch array's device address in the current context: known from an
+   * earlier call in this context, else looked up now with cudaGetSymbolAddress
+   * (which makes the device's primary context current if the thread has none;
+   * no allocation is involved).  The lookup may load this library's device
+   * code, which a stream capture must not see: inside a capture only an
+   * address found earlier in the same context is used. */
+  unsigned long long ctx = 0;
+  bool have_ctx = na_current_context(&ctx);
+  NaScratch* s = have_ctx ? na_lookup(ctx) : nullptr;
+  cudaError_t e;
+  if (!s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+      cudaGetLastError();
+      cs = cudaStreamCaptureStatusActive;   /* cannot tell: treat as capturing */
+    }
+    if (cs != cudaStreamCaptureStatusNone)
+      return na_fail(SPP_ERR_INVALID, "spp_pairs_noalloc: the first call in a CUDA context sets up the "
+                                      "scratch address and must come before any stream capture");
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_na_scratch);
     if (e != cudaSuccess)
       return na_fail(SPP_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_na_ptr[dev] = reinterpret_cast<NaScratch*>(p);
+    s = reinterpret_cast<NaScratch*>(p);
+    if (!have_ctx) have_ctx = na_current_context(&ctx);
+    if (have_ctx) na_remember(ctx, s);
   }
-  NaScratch* s = g_na_ptr[dev];
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   int bits = 0;
   while ((1 << bits) < D) ++bits;
   const int n_keys = 1 << (2 * bits);

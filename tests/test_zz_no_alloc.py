@@ -27,7 +27,7 @@ def pairs_via_system(x, y, n, L, r):
         return s.pairs(r)
 
 
-def pairs_noalloc(lib, x, y, L, r, cap):
+def pairs_noalloc(lib, x, y, L, r, cap, stream=None):
     import torch
     n = len(x)
     dx = torch.from_numpy(np.ascontiguousarray(x, np.float32)).cuda()
@@ -36,10 +36,13 @@ def pairs_noalloc(lib, x, y, L, r, cap):
     pj = torch.empty(cap, dtype=torch.int32, device="cuda")
     cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
     torch.cuda.synchronize()
+    handle = C.c_void_p(stream.cuda_stream) if stream is not None else None
     rc = lib.spp_pairs_noalloc(C.c_void_p(dx.data_ptr()), C.c_void_p(dy.data_ptr()), n, float(L),
                                float(r), C.c_void_p(pi.data_ptr()), C.c_void_p(pj.data_ptr()),
-                               cap, C.c_void_p(cnt.data_ptr()), None)
+                               cap, C.c_void_p(cnt.data_ptr()), handle)
     assert rc == abi.SPP_OK, lib.spp_last_error()
+    if stream is not None:
+        stream.synchronize()
     torch.cuda.synchronize()
     total = int(cnt.item())
     m = min(total, cap)
@@ -80,3 +83,65 @@ def test_noalloc_rejects_sizes_beyond_the_limit(gpu_lib):
     small_box = gpu_lib.spp_pairs_noalloc(C.c_void_p(1), C.c_void_p(1), 10, 1.0, 1.0, None, None, 0,
                                           C.c_void_p(1), None)
     assert small_box == 1
+
+
+def test_noalloc_clamped_grid_smallest_grid_and_a_stream(gpu_lib):
+    """Grid edge cases against the existing pair search: a sparse box whose
+    2L/r (1024) is clamped to 256 cells per side (wider cells, more
+    candidates, the same pairs), the smallest grid of 3 x 3 cells, where every
+    wrapped neighbour cell is distinct (checked against the oracle's FP32
+    pair predicate, since a system handle needs cells wider than its list
+    radius), and a call enqueued on a non-default stream."""
+    import torch
+    from oracle import oracle as O
+    n, L, r = 4096, 512.0, 1.0
+    x, y, _ = configs.random_state(n, L, seed=21)
+    # a cluster as well, so that the sparse box has pairs to find
+    x[:512] = (x[:512] / L * 4.0).astype(np.float32)
+    y[:512] = (y[:512] / L * 4.0).astype(np.float32)
+    ref = pairs_via_system(x, y, n, L, r)
+    assert ref.size > 100
+    total, got = pairs_noalloc(gpu_lib, x, y, L, r, 8 * n)
+    assert total == ref.size and np.array_equal(got, ref)
+    side = torch.cuda.Stream()
+    total, got = pairs_noalloc(gpu_lib, x, y, L, r, 8 * n, stream=side)
+    assert total == ref.size and np.array_equal(got, ref)
+
+    n3, L3 = 60, 1.6      # floor(2L / (1.001 r)) = 3 cells per side
+    x3, y3, _ = configs.random_state(n3, L3, seed=22)
+    ref3 = O.pairs32(configs.abp_config(n=n3, L=L3, seed=1), x3, y3, r)
+    assert ref3.size > 0
+    total, got = pairs_noalloc(gpu_lib, x3, y3, L3, r, 8 * n3 * n3)
+    assert total == ref3.size and np.array_equal(got, ref3)
+
+
+def test_noalloc_calls_take_no_device_memory(gpu_lib):
+    """The promise itself: after one warm call (the context, the library's
+    device code and the caller's buffers exist), further calls leave the
+    device's free memory unchanged."""
+    import torch
+    n, L, r = 8192, 64.0, 1.0
+    x, y, _ = configs.random_state(n, L, seed=23)
+    dx = torch.from_numpy(x).cuda()
+    dy = torch.from_numpy(y).cuda()
+    cap = 8 * n
+    pi = torch.empty(cap, dtype=torch.int32, device="cuda")
+    pj = torch.empty(cap, dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+
+    def call():
+        rc = gpu_lib.spp_pairs_noalloc(C.c_void_p(dx.data_ptr()), C.c_void_p(dy.data_ptr()), n,
+                                       float(L), float(r), C.c_void_p(pi.data_ptr()),
+                                       C.c_void_p(pj.data_ptr()), cap, C.c_void_p(cnt.data_ptr()),
+                                       None)
+        assert rc == abi.SPP_OK, gpu_lib.spp_last_error()
+
+    call()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        call()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert int(cnt.item()) > 0
