@@ -43,7 +43,7 @@ def build_oracle(force=False) -> Path:
                    REPO / "spp_gb300" / "csrc" / "spp_physics.h"]
     if force or _stale(out, deps):
         out.parent.mkdir(parents=True, exist_ok=True)
-        _run(["gcc", "-std=gnu11", *CFLAGS, "-o", str(out), *map(str, srcs), "-lm"])
+        _run(["gcc", "-std=gnu11", *CFLAGS, "-pthread", "-o", str(out), *map(str, srcs), "-lm"])
     return out
 
 

@@ -60,6 +60,13 @@ def orc():
         L.orc32_pair_distribution.argtypes = [_F, _F, _F, _F, C.c_int, C.c_double, C.c_double, C.c_int,
                                               C.c_int, _U64]
         L.orc32_rsqrt.restype = C.c_float
+        _I8 = C.POINTER(C.c_int8)
+        for nm in ("orc64_watch", "orc32_watch"):
+            f = getattr(L, nm)
+            f.argtypes = [_I, _I, _I, _I8, _D, C.c_int64, C.c_double, C.c_double]
+            f.restype = None
+        for nm in ("orc64_watch_count", "orc32_watch_count"):
+            getattr(L, nm).restype = C.c_int64
         _orc = L
     return _orc
 
@@ -146,6 +153,112 @@ def run32(p, state: State32, nsteps, step0=0):
     if rc != 0:
         raise RuntimeError(f"mirror run failed with status {rc}")
     return s
+
+
+def cutoff_events(p, state, nsteps, window, step0=0, cap=1 << 20):
+    """Advance `state` (State64: the FP64 restatement, State32: the FP32
+    mirror) by nsteps and return the pair evaluations that came within
+    `window` of the alignment radius: a structured array of (stage, i, j,
+    inside, d), stage counting the force evaluations of this call, i < j,
+    inside the run's own predicate and d the run's own distance."""
+    fp64 = isinstance(state, State64)
+    L = orc()
+    start = state.copy() if fp64 else State32(state.x, state.y, state.th, state.ix, state.iy)
+    while True:
+        st = np.empty(cap, np.int32)
+        pi = np.empty(cap, np.int32)
+        pj = np.empty(cap, np.int32)
+        ins = np.empty(cap, np.int8)
+        dist = np.empty(cap, np.float64)
+        watch = L.orc64_watch if fp64 else L.orc32_watch
+        watch(_i(st), _i(pi), _i(pj), ins.ctypes.data_as(C.POINTER(C.c_int8)), _d(dist), cap,
+              float(p.r_align), float(window))
+        try:
+            (run64 if fp64 else run32)(p, state, nsteps, step0=step0)
+            cnt = (L.orc64_watch_count if fp64 else L.orc32_watch_count)()
+        finally:
+            watch(None, None, None, None, None, 0, 0.0, 0.0)
+        if cnt <= cap:
+            break
+        cap = int(cnt)
+        for a in ("x", "y", "th") + (("xu", "yu") if fp64 else ("ix", "iy")):
+            setattr(state, a, getattr(start, a).copy())
+    ev = np.zeros(cnt, dtype=[("stage", np.int32), ("i", np.int32), ("j", np.int32), ("inside", np.int8),
+                              ("d", np.float64)])
+    ev["stage"], ev["i"], ev["j"], ev["inside"], ev["d"] = st[:cnt], pi[:cnt], pj[:cnt], ins[:cnt], dist[:cnt]
+    return ev
+
+
+def predicate_mismatches(ev32, ev64, r, window):
+    """Pairs (stage, i, j) on which the FP32 and FP64 runs took different sides
+    of the alignment cutoff r.  Both runs record every evaluation within
+    `window` of r.  A pair recorded by one run only lay within the window
+    there and outside it in the other run; it is counted as a mismatch when
+    its recorded distance is within window/2 of r (the two runs then differ
+    there by more than window/2, and the other run's side is unknown).
+    Returns a structured array like cutoff_events'."""
+    def key(e):
+        return ((e["stage"].astype(np.int64) << 42) | (e["i"].astype(np.int64) << 21)
+                | e["j"].astype(np.int64))
+    k32, k64 = key(ev32), key(ev64)
+    _, a, b = np.intersect1d(k32, k64, return_indices=True)
+    out = [ev32[a][ev32[a]["inside"] != ev64[b]["inside"]]]
+    for e, k, other in ((ev32, k32, k64), (ev64, k64, k32)):
+        lone = e[~np.isin(k, other)]
+        out.append(lone[np.abs(lone["d"] - r) < 0.5 * window])
+    return np.concatenate(out)
+
+
+def stages_per_step(p):
+    return {1: 1, 2: 2, 4: 4}[int(p.integrator)] if p.model in (3, 4, 5) else 1
+
+
+def cutoff_divergence(p, x, y, th, nsteps, window=1e-3, step0=0, hops=1, close=0.0):
+    """The FP64 restatement and the FP32 mirror (the kernels' arithmetic) run
+    side by side from the same state for nsteps, step by step, recording the
+    pair evaluations near the hard alignment cutoff.  Where the two
+    precisions put a pair on different sides of the cutoff, the torques of
+    its two particles jump (by ~ dt g / n_i) and their headings part by far
+    more than rounding; their neighbours then feel the changed headings
+    through their own alignment sums.  Returns (final State64, final
+    State32, the mismatched pair evaluations, level): level 0 for members of
+    a mismatched pair (from that step on), level h <= hops for particles
+    within the alignment radius of a level h-1 particle at any later step,
+    99 for the rest.  With close > 0, particles closer than `close` to
+    another at the start of a step are level 0 as well: the continuous
+    model's alpha torque alpha (dr x v)/(pi d) takes its direction from dr/d,
+    whose FP32 rounding error grows as 1/d where two particles (which do not
+    repel) pass through each other."""
+    s64, s32 = State64(x, y, th), State32(x, y, th)
+    nst = stages_per_step(p)
+    level = np.full(p.n, 99, np.int32)
+    found = []
+
+    def hop():
+        if not (level < hops).any():
+            return
+        pr = pairs64(s64.x, s64.y, p.L, p.r_align)
+        a = (pr >> 32).astype(np.int64)
+        b = (pr & 0xFFFFFFFF).astype(np.int64)
+        la, lb = level[a].copy(), level[b].copy()
+        np.minimum.at(level, b, np.where(la < hops, la + 1, 99))
+        np.minimum.at(level, a, np.where(lb < hops, lb + 1, 99))
+
+    for t in range(nsteps):
+        if close > 0:
+            pr = pairs64(s64.x, s64.y, p.L, close)
+            level[(pr >> 32).astype(np.int64)] = 0
+            level[(pr & 0xFFFFFFFF).astype(np.int64)] = 0
+        hop()
+        e64 = cutoff_events(p, s64, 1, window, step0=step0 + t)
+        e32 = cutoff_events(p, s32, 1, window, step0=step0 + t)
+        mm = predicate_mismatches(e32, e64, p.r_align, window)
+        mm["stage"] += t * nst
+        level[mm["i"]] = 0
+        level[mm["j"]] = 0
+        found.append(mm)
+    hop()
+    return s64, s32, np.concatenate(found), level
 
 
 def pairs64(x, y, L, r, cap=None):

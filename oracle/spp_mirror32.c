@@ -59,6 +59,44 @@ static void mcells_free(mcells* c) { free(c->head); free(c->next); }
     }                                                                                \
   } while (0)
 
+/* Cutoff-event recorder, the FP32 counterpart of orc64_watch: pair
+ * evaluations whose separation lies within `window` of the alignment radius
+ * are recorded as (stage, i, j, inside, d) with the kernels' own predicate
+ * (d2 < ral2 in FP32, d2 from spp_sep); stage counts the force evaluations
+ * since orc32_watch(). */
+static struct {
+  int32_t *stage, *pi, *pj;
+  int8_t* inside;
+  double* dist;
+  int64_t cap, cnt;
+  double r, window;
+  int32_t cur;
+  int on;
+} g_w32;
+
+void orc32_watch(int32_t* stage, int32_t* pi, int32_t* pj, int8_t* inside, double* dist, int64_t cap,
+                 double r, double window) {
+  g_w32.stage = stage; g_w32.pi = pi; g_w32.pj = pj; g_w32.inside = inside; g_w32.dist = dist;
+  g_w32.cap = cap; g_w32.cnt = 0; g_w32.r = r; g_w32.window = window; g_w32.cur = 0;
+  g_w32.on = stage != NULL;
+}
+int64_t orc32_watch_count(void) { return g_w32.cnt; }
+
+static void watch32(const SppConsts* k, int i, int j, float xi, float yi, float xj, float yj) {
+  float dx, dy;
+  const float d2 = spp_sep(k, xi, yi, xj, yj, &dx, &dy);
+  const double d = sqrt((double)d2);
+  if (fabs(d - g_w32.r) >= g_w32.window) return;
+  if (g_w32.cnt < g_w32.cap) {
+    g_w32.stage[g_w32.cnt] = g_w32.cur;
+    g_w32.pi[g_w32.cnt] = i;
+    g_w32.pj[g_w32.cnt] = j;
+    g_w32.inside[g_w32.cnt] = (int8_t)(d2 < k->ral2);
+    g_w32.dist[g_w32.cnt] = d;
+  }
+  g_w32.cnt++;
+}
+
 static double mirror_rcut(const SppParams* p) { return spp_interaction_range(p); }
 
 static int cmp_int(const void* a, const void* b) {
@@ -86,6 +124,9 @@ static int abp_accumulate(const SppConsts* k, int n, const float* x, const float
       }
     });
     qsort(cand, (size_t)m, sizeof(int), cmp_int);
+    if (g_w32.on)
+      for (int q = 0; q < m; ++q)
+        if (cand[q] > i) watch32(k, i, cand[q], x[i], y[i], x[cand[q]], y[cand[q]]);
     if (k->lanes > 1) {
       /* the kernels' lane split: lane r sums the neighbours with id % 4 == r
        * in id order, then (p0 + p1) + (p2 + p3) */
@@ -98,6 +139,8 @@ static int abp_accumulate(const SppConsts* k, int n, const float* x, const float
       a.fx = spp_lane_sum4(part[0].fx, part[1].fx, part[2].fx, part[3].fx);
       a.fy = spp_lane_sum4(part[0].fy, part[1].fy, part[2].fy, part[3].fy);
       a.tq = spp_lane_sum4(part[0].tq, part[1].tq, part[2].tq, part[3].tq);
+      a.ss = spp_lane_sum4(part[0].ss, part[1].ss, part[2].ss, part[3].ss);
+      a.sc = spp_lane_sum4(part[0].sc, part[1].sc, part[2].sc, part[3].sc);
       a.cnt = part[0].cnt + part[1].cnt + part[2].cnt + part[3].cnt;
       a.ovf = part[0].ovf | part[1].ovf | part[2].ovf | part[3].ovf;
       ovf |= a.ovf;
@@ -120,6 +163,7 @@ static int abp_accumulate(const SppConsts* k, int n, const float* x, const float
   }
   free(cand);
   mcells_free(&cl);
+  g_w32.cur++;
   return ovf;
 }
 
@@ -516,6 +560,8 @@ int orc32_lyap_run(const SppParams* p, int nsteps, int64_t step0, int renorm_eve
           a.fx = spp_lane_sum4(part[0].fx, part[1].fx, part[2].fx, part[3].fx);
           a.fy = spp_lane_sum4(part[0].fy, part[1].fy, part[2].fy, part[3].fy);
           a.tq = spp_lane_sum4(part[0].tq, part[1].tq, part[2].tq, part[3].tq);
+          a.ss = spp_lane_sum4(part[0].ss, part[1].ss, part[2].ss, part[3].ss);
+          a.sc = spp_lane_sum4(part[0].sc, part[1].sc, part[2].sc, part[3].sc);
           a.cnt = part[0].cnt + part[1].cnt + part[2].cnt + part[3].cnt;
           a.ovf = part[0].ovf | part[1].ovf | part[2].ovf | part[3].ovf;
           for (int v = 0; v < K; ++v) tacc[v] = spp_lane_sum4(tpart[0][v], tpart[1][v], tpart[2][v], tpart[3][v]);

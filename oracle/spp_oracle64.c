@@ -30,6 +30,7 @@
  * this file against it.
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 #include "../include/spp.h"
@@ -53,7 +54,45 @@ static double orc_uniform_pm_pi(const SppParams* p, int pid, int64_t step) {
 /* Set for a closed box (SPP_BOUNDARY_WALLS) for the duration of a run: the
  * reference built without PERIODIC_BOUNDARY_CONDITION skips every
  * Periodic_Transform. */
-static int g_closed = 0;
+static __thread int g_closed = 0;
+
+/* Cutoff-event recorder (parity tests): while on, every pair evaluation of
+ * the alignment predicate whose distance lies within `window` of the
+ * alignment radius is recorded as (stage, i, j, inside, d), with i < j and
+ * `stage` counting the force evaluations since orc64_watch() (one per
+ * Euler step, two per RK2 step, four per RK4 step).  The FP32 mirror
+ * records the same events from its own arithmetic (orc32_watch), so a test
+ * can find the pairs on which the two precisions took different sides of
+ * the hard cutoff. */
+static __thread struct {
+  int32_t *stage, *pi, *pj;
+  int8_t* inside;
+  double* dist;
+  int64_t cap, cnt;
+  double r, window;
+  int32_t cur;
+  int on;
+} g_w;
+
+void orc64_watch(int32_t* stage, int32_t* pi, int32_t* pj, int8_t* inside, double* dist, int64_t cap,
+                 double r, double window) {
+  g_w.stage = stage; g_w.pi = pi; g_w.pj = pj; g_w.inside = inside; g_w.dist = dist;
+  g_w.cap = cap; g_w.cnt = 0; g_w.r = r; g_w.window = window; g_w.cur = 0;
+  g_w.on = stage != NULL;
+}
+int64_t orc64_watch_count(void) { return g_w.cnt; }
+
+static inline void watch_pair(int i, int j, double d, int inside) {
+  if (!g_w.on || fabs(d - g_w.r) >= g_w.window) return;
+  if (g_w.cnt < g_w.cap) {
+    g_w.stage[g_w.cnt] = g_w.cur;
+    g_w.pi[g_w.cnt] = i < j ? i : j;
+    g_w.pj[g_w.cnt] = i < j ? j : i;
+    g_w.inside[g_w.cnt] = (int8_t)inside;
+    g_w.dist[g_w.cnt] = d;
+  }
+  g_w.cnt++;
+}
 
 /* Periodic_Transform, shared/c2dvector.h:67-73 */
 static inline double pt(double x, double L) {
@@ -230,6 +269,7 @@ static void abp_pair(void* ctx, int i, int j) {
     s->fx[i] += Fx; s->fy[i] += Fy;
     s->fx[j] -= Fx; s->fy[j] -= Fy;
   }
+  watch_pair(i, j, d, d < p->r_align);
   if (d < p->r_align) {
     s->nb[i]++; s->nb[j]++;
     double t = sin(s->th[j] - s->th[i]);
@@ -245,6 +285,7 @@ static void cont_pair(void* ctx, int i, int j) {
   const SppParams* p = s->p;
   double dx = pt(s->x[i] - s->x[j], p->L), dy = pt(s->y[i] - s->y[j], p->L);
   double d2 = dx * dx + dy * dy;
+  watch_pair(i, j, sqrt(d2), d2 < p->r_align * p->r_align);
   if (d2 < p->r_align * p->r_align) {
     s->nb[i]++; s->nb[j]++;
     double d = sqrt(d2);
@@ -432,6 +473,7 @@ static void abp_stage_forces(ostate* s) {
   abp_reset(s);
   interact_all(s, s->p->model == SPP_MODEL_CONTINUOUS ? cont_pair : abp_pair);
   if (s->p->boundary == SPP_BOUNDARY_WALLS) walls_interact(s);
+  g_w.cur++;
 }
 
 static void abp_step(ostate* s, int64_t step) {
@@ -746,6 +788,7 @@ static void cont_euler_step(ostate* s, int64_t step) {
   for (int i = 0; i < s->n; ++i) { s->nb[i] = 1; s->tq[i] = 0; }
   interact_all(s, cont_pair);
   if (p->boundary == SPP_BOUNDARY_WALLS) walls_interact(s);
+  g_w.cur++;
   for (int i = 0; i < s->n; ++i) {
     double torque = p->g * s->tq[i] + sigma * orc_normal(p, i, step);
     s->th[i] += torque * dt;
@@ -1045,48 +1088,79 @@ int orc64_lyap_tangent(const SppParams* p, int nsteps, int renorm_every, int K, 
  * dynamics; the differences (State_Hyper_Vector::operator-, min image and
  * wrapped angle) are Gram-Schmidt'ed into the next directions, and
  * log(|projection| / eps) (the ratio of :177-183) is summed per direction. */
+/* One system of an interval of the clone method: the base (a < 0) or
+ * clone a, evolved tau steps on its own thread (orc64_run keeps its state
+ * in thread-local storage). */
+#define ORC_CLONE_MAX 16
+typedef struct {
+  const SppParams* p;
+  int tau;
+  int64_t step;
+  double *x, *y, *th, *xu, *yu;
+  int rc;
+} clone_job;
+
+static void* clone_thread(void* arg) {
+  clone_job* j = (clone_job*)arg;
+  j->rc = orc64_run(j->p, j->tau, j->step, j->x, j->y, j->th, j->xu, j->yu);
+  return NULL;
+}
+
 int orc64_lyap_clone(const SppParams* p, int n_intervals, int tau, int K, double eps, double* x,
                      double* y, double* th, double* xu, double* yu, double* V, double* log_stretch) {
   int n = p->n;
   size_t len = (size_t)3 * n;
-  double *bx = malloc(sizeof(double) * n), *by = malloc(sizeof(double) * n),
-         *bt = malloc(sizeof(double) * n), *bxu = malloc(sizeof(double) * n),
-         *byu = malloc(sizeof(double) * n);
-  double *cx = malloc(sizeof(double) * n), *cy = malloc(sizeof(double) * n),
-         *ct = malloc(sizeof(double) * n), *cxu = malloc(sizeof(double) * n),
-         *cyu = malloc(sizeof(double) * n);
+  /* system 0 is the base trajectory, 1..K the clones base + eps u_a */
+  double* buf = malloc(sizeof(double) * (size_t)5 * n * (size_t)(K + 1));
+  clone_job job[ORC_CLONE_MAX + 1];
+  pthread_t tid[ORC_CLONE_MAX + 1];
+  int started[ORC_CLONE_MAX + 1];
   int64_t step = 0;
   int rc = SPP_OK;
+  if (K > ORC_CLONE_MAX) rc = SPP_ERR_INVALID;
   for (int it = 0; it < n_intervals && rc == SPP_OK; ++it) {
-    memcpy(bx, x, sizeof(double) * n); memcpy(by, y, sizeof(double) * n);
-    memcpy(bt, th, sizeof(double) * n); memcpy(bxu, xu, sizeof(double) * n);
-    memcpy(byu, yu, sizeof(double) * n);
-    rc = orc64_run(p, tau, step, bx, by, bt, bxu, byu);
-    for (int a = 0; a < K && rc == SPP_OK; ++a) {
-      const double* u = V + (size_t)a * len;
+    for (int a = 0; a <= K; ++a) {
+      double* q = buf + (size_t)5 * n * a;
+      clone_job* j = &job[a];
+      j->p = p; j->tau = tau; j->step = step;
+      j->x = q; j->y = q + n; j->th = q + 2 * n; j->xu = q + 3 * n; j->yu = q + 4 * n;
+      const double* u = a == 0 ? NULL : V + (size_t)(a - 1) * len;
       for (int i = 0; i < n; ++i) {
-        cx[i] = pt(x[i] + eps * u[i], p->L);
-        cy[i] = pt(y[i] + eps * u[n + i], p->L);
-        ct[i] = th[i] + eps * u[2 * n + i];
-        cxu[i] = xu[i] + eps * u[i];
-        cyu[i] = yu[i] + eps * u[n + i];
+        const double ux = u ? eps * u[i] : 0.0, uy = u ? eps * u[n + i] : 0.0;
+        const double ut = u ? eps * u[2 * n + i] : 0.0;
+        j->x[i] = u ? pt(x[i] + ux, p->L) : x[i];
+        j->y[i] = u ? pt(y[i] + uy, p->L) : y[i];
+        j->th[i] = th[i] + ut;
+        j->xu[i] = xu[i] + ux;
+        j->yu[i] = yu[i] + uy;
       }
-      rc = orc64_run(p, tau, step, cx, cy, ct, cxu, cyu);
+    }
+    for (int a = 0; a <= K; ++a) {
+      started[a] = pthread_create(&tid[a], NULL, clone_thread, &job[a]) == 0;
+      if (!started[a]) clone_thread(&job[a]);   /* no thread: run it here */
+    }
+    for (int a = 0; a <= K; ++a)
+      if (started[a]) pthread_join(tid[a], NULL);
+    for (int a = 0; a <= K; ++a)
+      if (job[a].rc != SPP_OK) rc = job[a].rc;
+    if (rc != SPP_OK) break;
+    const clone_job* b = &job[0];
+    for (int a = 0; a < K; ++a) {
+      const clone_job* c = &job[a + 1];
       double* w = V + (size_t)a * len;
       for (int i = 0; i < n; ++i) {
-        double dth = ct[i] - bt[i];
-        w[i] = pt(cx[i] - bx[i], p->L);
-        w[n + i] = pt(cy[i] - by[i], p->L);
+        double dth = c->th[i] - b->th[i];
+        w[i] = pt(c->x[i] - b->x[i], p->L);
+        w[n + i] = pt(c->y[i] - b->y[i], p->L);
         w[2 * n + i] = dth - 2 * M_PI * ceil((dth - M_PI) / (2 * M_PI));
       }
     }
     mgs(K, len, V, log_stretch, eps);
-    memcpy(x, bx, sizeof(double) * n); memcpy(y, by, sizeof(double) * n);
-    memcpy(th, bt, sizeof(double) * n); memcpy(xu, bxu, sizeof(double) * n);
-    memcpy(yu, byu, sizeof(double) * n);
+    memcpy(x, b->x, sizeof(double) * n); memcpy(y, b->y, sizeof(double) * n);
+    memcpy(th, b->th, sizeof(double) * n); memcpy(xu, b->xu, sizeof(double) * n);
+    memcpy(yu, b->yu, sizeof(double) * n);
     step += tau;
   }
-  free(bx); free(by); free(bt); free(bxu); free(byu);
-  free(cx); free(cy); free(ct); free(cxu); free(cyu);
+  free(buf);
   return rc;
 }

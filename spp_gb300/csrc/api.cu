@@ -201,6 +201,9 @@ int validate(const SppParams* p) {
           p->integrator != SPP_INT_RK4)
         return fail(SPP_ERR_INVALID, "integrator must be SPP_INT_EULER, _RK2 or _RK4");
       if (!(p->skin > 0)) return fail(SPP_ERR_INVALID, "the Verlet-list models need skin > 0");
+      if (p->model == SPP_MODEL_CONTINUOUS && p->force_law != SPP_FORCE_NONE)
+        return fail(SPP_ERR_UNSUPPORTED, "ContinuousParticle has no pair repulsion (shared/particle.h:296-338): "
+                                         "force_law must be SPP_FORCE_NONE");
       if (p->model != SPP_MODEL_CONTINUOUS && p->force_law != SPP_FORCE_NONE &&
           p->force_law != SPP_FORCE_HARMONIC && p->force_law != SPP_FORCE_R12_TRUNC)
         return fail(SPP_ERR_INVALID, "unknown force law");

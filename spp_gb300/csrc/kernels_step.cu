@@ -176,6 +176,8 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
       for (int o = 1; o < LANES; o <<= 1) {
         a.fx = a.fx + __shfl_xor_sync(gmask, a.fx, o);
         a.fy = a.fy + __shfl_xor_sync(gmask, a.fy, o);
+        a.ss = a.ss + __shfl_xor_sync(gmask, a.ss, o);
+        a.sc = a.sc + __shfl_xor_sync(gmask, a.sc, o);
         a.tq = a.tq + __shfl_xor_sync(gmask, a.tq, o);
         a.cnt += __shfl_xor_sync(gmask, a.cnt, o);
         a.ovf |= __shfl_xor_sync(gmask, a.ovf, o);
@@ -606,10 +608,6 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
   SPP_STAGE_CASE_W(SPP_FORCE_NONE, SPP_KIND_ABP)
   SPP_STAGE_CASE_W(SPP_FORCE_NONE, SPP_KIND_CONT)
   SPP_STAGE_CASE_W(SPP_FORCE_NONE, SPP_KIND_CONT_ALPHA)
-  SPP_STAGE_CASE_W(SPP_FORCE_HARMONIC, SPP_KIND_CONT)
-  SPP_STAGE_CASE_W(SPP_FORCE_HARMONIC, SPP_KIND_CONT_ALPHA)
-  SPP_STAGE_CASE_W(SPP_FORCE_R12_TRUNC, SPP_KIND_CONT)
-  SPP_STAGE_CASE_W(SPP_FORCE_R12_TRUNC, SPP_KIND_CONT_ALPHA)
   SPP_STAGE_CASE(SPP_FORCE_R12_TRUNC, SPP_KIND_BEADS)
   SPP_STAGE_CASE(SPP_FORCE_HARMONIC, SPP_KIND_BEADS)
   SPP_STAGE_CASE(SPP_FORCE_NONE, SPP_KIND_BEADS)

@@ -33,6 +33,7 @@ typedef struct SppConsts {
   float g, g_over_area;        /* g / (pi R_a^2) */
   float ral2;                  /* alignment radius squared */
   float rrep2, inv_rrep, k_rep, sigma_rep, c13;
+  float k_over_rrep;           /* k_rep / r_rep (harmonic law: t = k_rep r - k_rep / r_rep) */
   float one_minus_alpha_over_pi, alpha_over_pi;
   float beta_push, r_push, rpush2;
   float rlist, rlist2;         /* Verlet list radius */
@@ -144,6 +145,7 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
     k->inv_rrep = (float)(1.0 / p->r_rep);
   }
   k->k_rep = (float)p->k_rep;
+  k->k_over_rrep = (p->force_law == SPP_FORCE_NONE || p->r_rep <= 0) ? 0.0f : (float)(p->k_rep / p->r_rep);
   k->sigma_rep = (float)p->sigma_rep;
   {
     float q = (p->r_rep > 0) ? k->sigma_rep / (float)p->r_rep : 0.0f;
@@ -327,12 +329,17 @@ SPP_HD float spp_move_coord(const SppConsts* k, int closed, float x, int* img) {
  * contributors in the same order). */
 typedef struct SppAccF {
   float fx, fy;     /* received force */
-  float tq;         /* received torque sum */
+  float ss, sc;     /* sums of sin theta_j and cos theta_j over the aligning neighbours:
+                       sum_j sin(theta_j - theta_i) = cos theta_i ss - sin theta_i sc */
+  float tq;         /* torque terms that do not factor that way (the alpha term of the
+                       continuous model, lever-arm torques of chains) */
   int32_t cnt;      /* neighbours within the alignment radius (self excluded) */
   int32_t ovf;      /* an R12 term left the checked range */
 } SppAccF;
 
-SPP_HD void spp_accf_zero(SppAccF* a) { a->fx = 0.0f; a->fy = 0.0f; a->tq = 0.0f; a->cnt = 0; a->ovf = 0; }
+SPP_HD void spp_accf_zero(SppAccF* a) {
+  a->fx = 0.0f; a->fy = 0.0f; a->ss = 0.0f; a->sc = 0.0f; a->tq = 0.0f; a->cnt = 0; a->ovf = 0;
+}
 
 /* Alignment-term kinds of the gather loop. */
 #define SPP_KIND_ABP 0          /* sin(theta_j - theta_i), neighbour count */
@@ -353,9 +360,14 @@ SPP_HD int spp_pair_kind(const SppConsts* k) {
  * arguments), so the branches on them vanish there; the CPU mirror passes
  * k->force_law and spp_pair_kind(k) and evaluates the same arithmetic.
  * Callers present the neighbours j in ascending particle id.
+ * Every term is evaluated and then masked (no data-dependent branches, so a
+ * warp's lanes stay converged); a masked term adds exactly nothing: t = 0
+ * gives fmaf(0, dx, f) = f, and the alignment sums are predicated adds.
  * With r = 1/d from spp_rsqrtf:
- *   harmonic  k (1 - d / r_rep) dr / d  ->  t = k (r - 1/r_rep),  F = t dr
- *   R12       A ((sigma/d)^13 - (sigma/r_c)^13) dr / d  ->  t = A (q^13 - c^13) r, q = sigma r */
+ *   harmonic  k (1 - d / r_rep) dr / d  ->  t = k r - k / r_rep,  F = t dr
+ *   R12       A ((sigma/d)^13 - (sigma/r_c)^13) dr / d  ->  t = A (q^13 - c^13) r, q = sigma r
+ * The alignment term sin(theta_j - theta_i) = s_j c_i - c_j s_i factors:
+ * the loop sums s_j and c_j and spp_align_sum combines them once. */
 SPP_HD void spp_pair_abp_lkw(const SppConsts* k, int law, int kind, int wrap, SppAccF* a, float xi,
                              float yi, float ci, float si, float xj, float yj, float cj, float sj) {
   float dx, dy, d2;
@@ -366,35 +378,44 @@ SPP_HD void spp_pair_abp_lkw(const SppConsts* k, int law, int kind, int wrap, Sp
     dy = yi - yj;
     d2 = fmaf(dx, dx, dy * dy);
   }
+  const int aligns = (kind != SPP_KIND_BEADS && kind != SPP_KIND_CHAIN);
   const int in_rep = (law != SPP_FORCE_NONE) && (d2 < k->rrep2) && (d2 > 0.0f);
-  const int in_al = (kind != SPP_KIND_BEADS && kind != SPP_KIND_CHAIN) && d2 < k->ral2;
-  if (!(in_rep || in_al)) return;
+  const int in_al = aligns && d2 < k->ral2;
   float r = 0.0f;
-  if (in_rep || (kind == SPP_KIND_CONT_ALPHA && in_al && d2 > 0.0f)) r = spp_rsqrtf(d2);
-  if (in_rep) {
+  if (law != SPP_FORCE_NONE || kind == SPP_KIND_CONT_ALPHA) r = spp_rsqrtf(d2);
+  if (law != SPP_FORCE_NONE) {
     float t;
     if (law == SPP_FORCE_HARMONIC) {
-      t = k->k_rep * (r - k->inv_rrep);
+      t = fmaf(k->k_rep, r, -k->k_over_rrep);
+      t = in_rep ? t : 0.0f;
     } else {
       const float q = k->sigma_rep * r;
       const float q2 = q * q, q4 = q2 * q2, q8 = q4 * q4;
       const float q13 = (q8 * q4) * q;
-      t = (k->k_rep * (q13 - k->c13)) * r;
+      t = in_rep ? (k->k_rep * (q13 - k->c13)) * r : 0.0f;
       if (!(fabsf(t * dx) < SPP_FX_RANGE && fabsf(t * dy) < SPP_FX_RANGE)) { a->ovf = 1; t = 0.0f; }
     }
-    a->fx = a->fx + t * dx;
-    a->fy = a->fy + t * dy;
+    a->fx = fmaf(t, dx, a->fx);
+    a->fy = fmaf(t, dy, a->fy);
   }
-  if (in_al) {
-    a->cnt += 1;
-    float term = sj * ci - cj * si; /* sin(theta_j - theta_i) */
-    if (kind != SPP_KIND_ABP) {
-      term = k->one_minus_alpha_over_pi * term;
-      if (kind == SPP_KIND_CONT_ALPHA && d2 > 0.0f)
-        term = term - (k->alpha_over_pi * (dx * si - dy * ci)) * r;
+  if (aligns) {
+    a->cnt += in_al;
+    if (in_al) {
+      a->ss = a->ss + sj;
+      a->sc = a->sc + cj;
     }
-    a->tq = a->tq + term;
+    if (kind == SPP_KIND_CONT_ALPHA && in_al && d2 > 0.0f)
+      a->tq = a->tq - (k->alpha_over_pi * (dx * si - dy * ci)) * r;
   }
+}
+
+/* The alignment torque sum of the ABP and continuous kinds from the
+ * accumulated sums: sum_j sin(theta_j - theta_i), times (1 - alpha)/pi for
+ * the continuous model, plus the terms kept in tq (alpha term). */
+SPP_HD float spp_align_sum(const SppConsts* k, const SppAccF* a, float ci, float si) {
+  float S = fmaf(ci, a->ss, -(si * a->sc));
+  if (k->model == SPP_MODEL_CONTINUOUS) S = fmaf(k->one_minus_alpha_over_pi, S, a->tq);
+  return S;
 }
 
 SPP_HD void spp_pair_abp(const SppConsts* k, SppAccF* a, float xi, float yi, float ci, float si,
@@ -548,9 +569,9 @@ SPP_HD void spp_abp_forces(const SppConsts* k, int walls, const SppAccF* a, floa
                            float ci, float si, float* fx, float* fy, float* tau) {
   float wfx = 0.0f, wfy = 0.0f, wtq = 0.0f;
   if (walls) spp_wall_terms(k, xi, yi, ci, si, &wfx, &wfy, &wtq);
-  *fx = k->v0 * ci + a->fx;
-  *fy = k->v0 * si + a->fy;
-  float S = a->tq;
+  *fx = fmaf(k->v0, ci, a->fx);
+  *fy = fmaf(k->v0, si, a->fy);
+  float S = spp_align_sum(k, a, ci, si);
   if (k->model == SPP_MODEL_CONTINUOUS) {
     if (walls) S = S + wtq;
     *tau = k->g * S;
@@ -609,8 +630,9 @@ SPP_HD void spp_stage_update(float h, float frac_noise, float x0, float y0, floa
   *y = spp_move_coord(k, closed, fmaf(fy, h, y0), imgy);
 }
 
-/* Euler move (RepulsiveParticle::Move, shared/particle.h:571-587): theta is
- * not wrapped there. */
+/* Euler move (RepulsiveParticle::Move, shared/particle.h:571-587: the step
+ * along the force of the old heading; ContinuousParticle::Move, :268-280:
+ * along the new heading): theta is not wrapped there. */
 SPP_HD float spp_euler_theta(const SppConsts* k, float th0, float tau, float dth) {
   return fmaf(k->dt, tau, th0) + dth;
 }
@@ -620,6 +642,13 @@ SPP_HD void spp_euler_update(float x0, float y0, float th0, float fx, float fy, 
   float t = spp_euler_theta(k, th0, tau, dth);
   spp_sincosf(t, s, c);
   *th = t;
+  if (k->model == SPP_MODEL_CONTINUOUS) {
+    /* ContinuousParticle::Move (shared/particle.h:268-280) turns first and
+     * then steps along the new heading: r += v (speed dt) */
+    *x = spp_move_coord(k, closed, fmaf(*c, k->v0dt, x0), imgx);
+    *y = spp_move_coord(k, closed, fmaf(*s, k->v0dt, y0), imgy);
+    return;
+  }
   *x = spp_move_coord(k, closed, fmaf(fx, k->dt, x0), imgx);
   *y = spp_move_coord(k, closed, fmaf(fy, k->dt, y0), imgy);
 }

@@ -127,25 +127,139 @@ def test_continuous_bitexact_vs_mirror(gpu_lib, integ):
     assert_bitexact(gpu, ref)
 
 
-def test_abp_vs_fp64_within_spec(gpu_lib):
-    """Config-2 physics at N=4096: 100 RK2 steps against the FP64 oracle."""
-    p = configs.abp_config(n=4096, L=32.0, seed=1)
+def reference_lattice_abp(integrator):
+    """RepulsiveParticle as shipped (R12 force, g sin / (pi R_a^2)) on a
+    lattice start: the R12 law does not admit the overlaps of a uniform
+    random start."""
+    p = configs.reference_defaults(abi.MODEL_ABP)
+    p.n, p.L, p.Dr, p.dt, p.seed, p.integrator, p.skin = 4096, 32.0, 0.1, 0.005, 5, integrator, 0.3
+    x, y = lattice(64, p.L)
+    _, _, th = configs.random_state(p.n, p.L, seed=7)
+    return p, x, y, th
+
+
+def continuous_alpha0(integrator):
+    """ContinuousParticle with alpha = 0, g = 1 (the Lyapunov workload's
+    model) and rotational noise D_r = 0.05."""
+    p = configs.lyapunov_config(n=4096)
+    p.integrator, p.Dr = integrator, 0.05
+    x, y, th = configs.random_state(p.n, p.L, seed=2)
+    return p, x, y, th
+
+
+def continuous_reference(integrator):
+    """ContinuousParticle with the reference's defaults (g = 4, alpha = 0.5,
+    dt = 2^-10, shared/particle.h:373-378) and D_r = 0.05."""
+    p = configs.reference_defaults(abi.MODEL_CONTINUOUS)
+    p.n, p.L, p.seed, p.skin, p.integrator, p.Dr = 4096, 32.0, 3, 0.3, integrator, 0.05
+    x, y, th = configs.random_state(p.n, p.L, seed=2)
+    return p, x, y, th
+
+
+def harmonic_abp(integrator):
+    """The configured repulsive ABP/Vicsek physics (harmonic k(1 - r/2a),
+    (g/n_i) sum sin alignment) at N = 4096."""
+    p = configs.abp_config(n=4096, L=32.0, seed=1, integrator=integrator)
     x, y, th = configs.random_state(p.n, p.L, seed=1)
-    (gx, gy, gth, gix, giy), _ = run_gpu(p, x, y, th, 100)
-    a = O.run64(p, O.State64(x, y, th), 100)
+    return p, x, y, th
+
+
+TWO_PI = 2.0 * np.pi
+# case: (state maker, integrator, alignment hops exempted, close-approach radius, heading tolerance)
+FP64_CASES = {
+    "abp_harmonic_rk2": (harmonic_abp, abi.INT_RK2, 1, 0.0, 1e-5),
+    "abp_harmonic_rk4": (harmonic_abp, abi.INT_RK4, 1, 0.0, 1e-5),
+    "abp_r12_reference_euler": (reference_lattice_abp, abi.INT_EULER, 1, 0.0, 1e-5),
+    "abp_r12_reference_rk2": (reference_lattice_abp, abi.INT_RK2, 1, 0.0, 1e-5),
+    "abp_r12_reference_rk4": (reference_lattice_abp, abi.INT_RK4, 1, 0.0, 1e-5),
+    "continuous_alpha0_euler": (continuous_alpha0, abi.INT_EULER, 2, 0.0, 1e-5),
+    "continuous_alpha0_rk2": (continuous_alpha0, abi.INT_RK2, 2, 0.0, 1e-5),
+    "continuous_alpha0_rk4": (continuous_alpha0, abi.INT_RK4, 2, 0.0, 1e-5),
+    "continuous_reference_euler": (continuous_reference, abi.INT_EULER, 2, 0.02, 1e-5 * TWO_PI),
+    "continuous_reference_rk2": (continuous_reference, abi.INT_RK2, 2, 0.02, 1e-5 * TWO_PI),
+    "continuous_reference_rk4": (continuous_reference, abi.INT_RK4, 2, 0.02, 1e-5 * TWO_PI),
+}
+
+
+@pytest.mark.parametrize("case", sorted(FP64_CASES))
+def test_vs_fp64_100_steps(gpu_lib, case):
+    """The kernels against the FP64 restatement of the reference (itself
+    pinned bit for bit, or to 1e-11, to the reference's own particle.h) over
+    100 steps at N = 4096: every particle within 1e-5 of the box side in
+    position and within the case's tolerance in heading, except those a hard
+    cutoff legitimately separates.
+
+    Where FP32 and FP64 put a pair on different sides of the alignment
+    radius (found by recording, in both precisions, every evaluation within
+    1e-3 of the cutoff: oracle.cutoff_divergence), the two particles' torques
+    jump by ~ dt g / n_i and their headings part by far more than rounding;
+    their neighbours feel that through their own alignment sums.  Exempt
+    are the members of such pairs and the particles within `hops` alignment
+    radii of them afterwards (hops = 2 for the continuous model, whose
+    torque g sum sin / pi is not normalised by the neighbour count).  The
+    continuous model's alpha torque alpha (dr x v) / (pi d) takes its
+    direction from dr / d; with no repulsion, pairs pass through each other,
+    and FP32's position resolution near |x| ~ L (2e-6) then moves headings
+    by ~ 1e-5 over 100 steps at distances ~ 0.1: pairs closer than 0.02 are
+    exempt, and headings are held to 1e-5 of a full turn there.  The GPU is
+    first shown bit-identical to the FP32 mirror whose cutoff decisions are
+    recorded, so those decisions are the kernels' own."""
+    make, integ, hops, close, th_tol = FP64_CASES[case]
+    p, x, y, th = make(integ)
+    steps = 100
+    gpu, _ = run_gpu(p, x, y, th, steps)
+    s64, s32, mism, level = O.cutoff_divergence(p, x, y, th, steps, hops=hops, close=close)
+    assert_bitexact(gpu, s32)
+    gx, gy, gth, gix, giy = gpu
     xu = gx.astype(np.float64) + 2 * p.L * gix
     yu = gy.astype(np.float64) + 2 * p.L * giy
-    rel_pos = np.maximum(np.abs(xu - a.xu), np.abs(yu - a.yu)) / (2 * p.L)
-    dth = np.abs((gth.astype(np.float64) - a.th + np.pi) % (2 * np.pi) - np.pi)
-    print(f"max rel pos err {rel_pos.max():.3g}, median theta err {np.median(dth):.3g}, "
-          f"theta err > 1e-5 at {np.sum(dth > 1e-5)} particles")
-    assert rel_pos.max() < 1e-5
-    assert np.median(dth) < 1e-6
-    # FP32 and FP64 disagree, now and then, on whether a pair lies inside the
-    # hard alignment cutoff; the torque jump then moves that particle's
-    # heading by ~dt * g / n_i ~ 1e-3 and nudges its neighbours.  About half a
-    # percent of the particles carry such an event after 100 steps.
-    assert np.mean(dth > 1e-5) < 0.02
+    rel_pos = np.maximum(np.abs(xu - s64.xu), np.abs(yu - s64.yu)) / (2 * p.L)
+    dth = np.abs((gth.astype(np.float64) - s64.th + np.pi) % TWO_PI - np.pi)
+    ok = level > hops
+    print(f"{case}: {mism.size} FP32/FP64 cutoff mismatches, {np.sum(~ok)} of {p.n} particles exempt; "
+          f"others: max |dr|/2L {rel_pos[ok].max():.3g}, max |dtheta| {dth[ok].max():.3g}, "
+          f"median |dtheta| {np.median(dth[ok]):.3g}; all: max |dr|/2L {rel_pos.max():.3g}, "
+          f"max |dtheta| {dth.max():.3g}")
+    assert rel_pos[ok].max() <= 1e-5
+    assert dth[ok].max() <= th_tol
+    assert np.mean(~ok) < 0.1
+
+
+def werr(a, b, period):
+    d = np.asarray(a, np.float64) - np.asarray(b, np.float64)
+    return np.abs((d + period / 2) % period - period / 2)
+
+
+@pytest.mark.parametrize("model,steps", [(abi.MODEL_VICSEK, 10), (abi.MODEL_VICSEK_REF_ANGLE, 10),
+                                         (abi.MODEL_VICSEK_REF_VECTOR, 5)])
+def test_vicsek_vs_fp64_short_horizon(gpu_lib, model, steps):
+    """The discrete Vicsek models (config-1 rule, VicsekParticle's angle
+    average, VicsekParticle2's vector sum with push, shared/particle.h:
+    145-250) against the FP64 restatement.  At dt = 1 they are chaotic: a
+    heading sum that nearly cancels (the vector rules) turns rounding
+    differences into large heading differences, and a pair crossing the
+    cutoff differently moves a particle by a whole step.  So the horizon is
+    short and the bounds are quantiles: the angle average (well conditioned)
+    keeps every particle within 1e-5 over 10 steps."""
+    p = configs.vicsek_config(model=model)
+    x, y, th = configs.random_state(p.n, p.L, seed=0)
+    (gx, gy, gth, gix, giy), _ = run_gpu(p, x, y, th, steps)
+    a = O.run64(p, O.State64(x, y, th), steps)
+    e = werr(gth, a.th, TWO_PI)
+    xu = gx.astype(np.float64) + 2 * p.L * gix
+    yu = gy.astype(np.float64) + 2 * p.L * giy
+    ep = np.maximum(np.abs(xu - a.xu), np.abs(yu - a.yu)) / (2 * p.L)
+    print(f"model {model}, {steps} steps: |dtheta| median {np.median(e):.3g}, q90 {np.quantile(e, 0.9):.3g}, "
+          f"q99 {np.quantile(e, 0.99):.3g}, max {e.max():.3g}, > 1e-5 at {np.mean(e > 1e-5):.2%}; "
+          f"|dr|/2L q99 {np.quantile(ep, 0.99):.3g}, max {ep.max():.3g}")
+    if model == abi.MODEL_VICSEK_REF_ANGLE:
+        assert e.max() <= 1e-5 and ep.max() <= 1e-5
+    elif model == abi.MODEL_VICSEK:
+        assert np.median(e) < 1e-6 and np.quantile(e, 0.99) < 1e-5 and e.max() < 1e-3
+        assert np.mean(e > 1e-5) < 0.02 and np.quantile(ep, 0.99) < 1e-5
+    else:
+        assert np.median(e) < 1e-6 and np.quantile(e, 0.9) < 1e-5 and e.max() < 1e-2
+        assert np.mean(e > 1e-5) < 0.05 and np.quantile(ep, 0.99) < 1e-5
 
 
 def test_pairs_bitexact_vs_mirror(gpu_lib):
