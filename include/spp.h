@@ -152,7 +152,12 @@ typedef struct SppParams {
 /* Boundary of the box. */
 enum SppBoundary {
   SPP_BOUNDARY_PERIODIC = 0,  /* periodic box [-L, L)^2 */
-  SPP_BOUNDARY_WALLS = 1      /* closed box: the box walls plus SppParams.walls */
+  SPP_BOUNDARY_WALLS = 1,     /* closed box: the box walls plus SppParams.walls */
+  SPP_BOUNDARY_CIRCLE = 2     /* circular box of radius L (the reference built with CIRCULAR_BOX,
+                                 parallel/box.h:285-294): no wrap, no walls; a particle beyond
+                                 r = L - 1 turns away from the circle by the torque
+                                 40 g (v x r)_z / (2 pi r (L - r)).  SPP_MODEL_ABP and
+                                 SPP_MODEL_CONTINUOUS, n_walls = 0 */
 };
 #define SPP_MAX_WALLS 8
 
@@ -216,6 +221,15 @@ int spp_upload_state(SppSystem* s, const float* x, const float* y, const float* 
  * box crossings: r_original = r + 2L * img. */
 int spp_download_state(SppSystem* s, float* x, float* y, float* theta, int32_t* img_x,
                        int32_t* img_y, int n);
+/* Run-and-tumble state (SPP_NOISE_TUMBLE) per particle id: RTPChain::
+ * tumble_flag and tumble_elapesed_time (shared/particle.h:1063-1064) as one
+ * integer, 0 while running and +-c during the c-th step of a tumble turning
+ * by +-tumble_torque.  spp_upload_state starts every swimmer running;
+ * spp_upload_tumble (after it) restores a saved state, so that a snapshot
+ * of state + tumble + step counter resumes bit for bit.  SPP_ERR_INVALID
+ * for systems without run and tumble and for out-of-range values. */
+int spp_download_tumble(SppSystem* s, int32_t* state, int n);
+int spp_upload_tumble(SppSystem* s, const int32_t* state, int n);
 /* Multi_Step(nsteps) (parallel/box.h:394-439): nsteps full integrator steps.
  * The neighbour list is rebuilt on device when a particle has moved more
  * than skin/2 since the last build.  Asynchronous on the handle's stream;

@@ -60,6 +60,8 @@ def orc():
         L.orc32_pair_distribution.argtypes = [_F, _F, _F, _F, C.c_int, C.c_double, C.c_double, C.c_int,
                                               C.c_int, _U64]
         L.orc32_rsqrt.restype = C.c_float
+        L.orc32_circle_torque.argtypes = [_P, C.c_float, C.c_float, C.c_float]
+        L.orc32_circle_torque.restype = C.c_float
         _I8 = C.POINTER(C.c_int8)
         for nm in ("orc64_watch", "orc32_watch"):
             f = getattr(L, nm)
@@ -441,6 +443,11 @@ def math32(fn, a, b=None):
     out = np.empty_like(a)
     orc().orc32_math(MATH_FNS[fn], len(a), _f(a), _f(b), _f(out))
     return out
+
+
+def circle_torque32(p, x, y, th):
+    """The kernels' FP32 circle torque (spp_circle_torque) of one particle."""
+    return float(orc().orc32_circle_torque(C.byref(p), float(x), float(y), float(th)))
 
 
 def wall_terms(p, x, y, th, fn="orc64"):

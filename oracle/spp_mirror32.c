@@ -196,7 +196,7 @@ static void body_rates(const SppConsts* k, int i, const SppAccF* a, const float*
       spp_bead_velocity(k, !bead, a, rfx, rfy, ci, si, fx, fy, tau);
     }
   } else {
-    spp_abp_forces(k, k->n_walls > 0, a, cx[i], cy[i], ci, si, fx, fy, tau);
+    spp_abp_forces(k, k->closed, a, cx[i], cy[i], ci, si, fx, fy, tau);
     *dth = spp_rot_noise(k, (uint32_t)i, step);
   }
 }
@@ -579,7 +579,7 @@ int orc32_lyap_run(const SppParams* p, int nsteps, int64_t step0, int renorm_eve
       /* base stage update */
       for (int i = 0; i < n; ++i) {
         float fx, fy, tau;
-        spp_abp_forces(&k, k.n_walls > 0, &A[i], cx[i], cy[i], cc[i], cs[i], &fx, &fy, &tau);
+        spp_abp_forces(&k, k.closed, &A[i], cx[i], cy[i], cc[i], cs[i], &fx, &fy, &tau);
         float dth = spp_rot_noise(&k, (uint32_t)i, step);
         float h, frac;
         if (nst == 2) {
@@ -692,4 +692,13 @@ void orc32_wall_terms(const SppParams* p, float x, float y, float th, float* out
   float s, c;
   spp_sincosf(th, &s, &c);
   spp_wall_terms(&k, x, y, c, s, &out3[0], &out3[1], &out3[2]);
+}
+
+/* The circle torque of one particle (FP32, the kernels' spp_circle_torque). */
+float orc32_circle_torque(const SppParams* p, float x, float y, float th) {
+  SppConsts k;
+  spp_consts_from_params(&k, p);
+  float s, c;
+  spp_sincosf(th, &s, &c);
+  return spp_circle_torque(&k, x, y, c, s);
 }

@@ -453,6 +453,25 @@ static void walls_interact(ostate* s) {
   }
 }
 
+/* The circular box: Box::Interact, parallel/box.h:285-294 (CIRCULAR_BOX
+ * without PERIODIC_BOUNDARY_CONDITION): beyond r = L - 1 the torque
+ * 40 g (v_y x - v_x y) / (2 pi r (L - r)) is added with the pair terms --
+ * to the continuous model's torque sum, which Move multiplies by g, and
+ * after the alignment normalisation of the repulsive model, where the
+ * walls' torques go as well. */
+static void circle_interact(ostate* s) {
+  const SppParams* p = s->p;
+  for (int i = 0; i < s->n; ++i) {
+    s->wtq[i] = 0.0;
+    const double r = sqrt(s->x[i] * s->x[i] + s->y[i] * s->y[i]);
+    if (r > p->L - 1) {
+      const double t = 40 * p->g * (s->vy[i] * s->x[i] - s->vx[i] * s->y[i]) / (2 * M_PI * r * (p->L - r));
+      if (p->model == SPP_MODEL_CONTINUOUS) s->tq[i] += t;
+      else s->wtq[i] += t;
+    }
+  }
+}
+
 /* One particle against the segments p->walls[0 .. n_walls) alone (the
  * box walls are segments like these), for the pin against the reference's
  * Wall::Interact. */
@@ -473,6 +492,7 @@ static void abp_stage_forces(ostate* s) {
   abp_reset(s);
   interact_all(s, s->p->model == SPP_MODEL_CONTINUOUS ? cont_pair : abp_pair);
   if (s->p->boundary == SPP_BOUNDARY_WALLS) walls_interact(s);
+  if (s->p->boundary == SPP_BOUNDARY_CIRCLE) circle_interact(s);
   g_w.cur++;
 }
 
@@ -788,6 +808,7 @@ static void cont_euler_step(ostate* s, int64_t step) {
   for (int i = 0; i < s->n; ++i) { s->nb[i] = 1; s->tq[i] = 0; }
   interact_all(s, cont_pair);
   if (p->boundary == SPP_BOUNDARY_WALLS) walls_interact(s);
+  if (p->boundary == SPP_BOUNDARY_CIRCLE) circle_interact(s);
   g_w.cur++;
   for (int i = 0; i < s->n; ++i) {
     double torque = p->g * s->tq[i] + sigma * orc_normal(p, i, step);
@@ -856,7 +877,7 @@ int orc64_run(const SppParams* p, int nsteps, int64_t step0, double* x, double* 
   memcpy(s.th, th, sizeof(double) * n);
   for (int i = 0; i < n; ++i) set_v(&s, i);
   int rc = 0;
-  g_closed = p->boundary == SPP_BOUNDARY_WALLS;
+  g_closed = p->boundary == SPP_BOUNDARY_WALLS || p->boundary == SPP_BOUNDARY_CIRCLE;
   for (int k = 0; k < nsteps; ++k) {
     int64_t step = step0 + k;
     switch (p->model) {

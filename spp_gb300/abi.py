@@ -19,7 +19,7 @@ STATUS_NAMES = {0: "SPP_OK", 1: "SPP_ERR_INVALID", 2: "SPP_ERR_ALLOC", 3: "SPP_E
 MODEL_VICSEK, MODEL_VICSEK_REF_ANGLE, MODEL_VICSEK_REF_VECTOR = 0, 1, 2
 MODEL_CONTINUOUS, MODEL_ABP, MODEL_BEADS = 3, 4, 5
 NOISE_GAUSSIAN, NOISE_TUMBLE = 0, 1
-BOUNDARY_PERIODIC, BOUNDARY_WALLS = 0, 1
+BOUNDARY_PERIODIC, BOUNDARY_WALLS, BOUNDARY_CIRCLE = 0, 1, 2
 INT_EULER, INT_RK2, INT_RK4 = 1, 2, 4
 FORCE_NONE, FORCE_HARMONIC, FORCE_R12_TRUNC = 0, 1, 2
 ALIGN_REFERENCE, ALIGN_MEAN = 0, 1
@@ -153,6 +153,8 @@ PROTOTYPES = {
     "spp_set_stream": (C.c_int, [_P, _P]),
     "spp_upload_state": (C.c_int, [_P, _F, _F, _F, _I32, _I32, C.c_int, C.c_int64]),
     "spp_download_state": (C.c_int, [_P, _F, _F, _F, _I32, _I32, C.c_int]),
+    "spp_download_tumble": (C.c_int, [_P, C.POINTER(C.c_int32), C.c_int]),
+    "spp_upload_tumble": (C.c_int, [_P, C.POINTER(C.c_int32), C.c_int]),
     "spp_step": (C.c_int, [_P, C.c_int]),
     "spp_sync": (C.c_int, [_P]),
     "spp_observables": (C.c_int, [_P, C.POINTER(SppObservables)]),

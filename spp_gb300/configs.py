@@ -266,6 +266,37 @@ def star_trap_walls(n_hands=2, half_delta=0.3, r_big=15.0, r_small=6.0):
     return walls
 
 
+def circle_config(n=4096, L=40.0, model=abi.MODEL_ABP, integrator=abi.INT_RK2, seed=6):
+    """A circular box of radius L (the reference built with CIRCULAR_BOX and
+    without PERIODIC_BOUNDARY_CONDITION, parallel/box.h:285-294): particles
+    beyond r = L - 1 turn away from the circle.  ABP: the reference's R12 pair
+    law and alignment; continuous: g = 1, alpha = 0."""
+    p = reference_defaults(model)
+    p.n, p.L, p.seed, p.integrator = n, L, seed, integrator
+    p.boundary = abi.BOUNDARY_CIRCLE
+    p.Dr, p.dt, p.skin = 0.1, 0.005, 0.3
+    if model == abi.MODEL_CONTINUOUS:
+        p.g, p.alpha, p.v0, p.dt = 1.0, 0.0, 0.5, 0.01
+    return p
+
+
+def circle_state(p, seed=None):
+    """Particles on a square lattice of spacing 1.05 inside radius L - 1.2;
+    random headings."""
+    seed = p.seed if seed is None else seed
+    g = np.arange(-p.L + 2.0, p.L - 2.0, 1.05)
+    X, Y = np.meshgrid(g, g)
+    x, y = X.ravel(), Y.ravel()
+    keep = np.hypot(x, y) < p.L - 1.2
+    x, y = x[keep][:p.n], y[keep][:p.n]
+    if x.size < p.n:
+        raise ValueError("circle too small for n particles")
+    ids = np.arange(p.n, dtype=np.uint32)
+    r = draw(seed, 0, ids, 0, RNG_INIT_ANGLE)
+    th = ((2 * u01_f32(r[0]).astype(np.float64) - 1) * math.pi).astype(np.float32)
+    return x.astype(np.float32), y.astype(np.float32), th
+
+
 def walls_state(p, seed=None):
     """Particles on a square lattice of spacing 1.05 inside the box, at
     least 2 from the box walls and 1.6 from the extra segments; random

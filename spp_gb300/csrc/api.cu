@@ -165,8 +165,15 @@ int validate(const SppParams* p) {
     return fail(SPP_ERR_INVALID, "gather_lanes must be 0 (automatic), 1 or 4");
   if (p->gather_lanes == SPP_GATHER_LANES && p->model != SPP_MODEL_ABP && p->model != SPP_MODEL_CONTINUOUS)
     return fail(SPP_ERR_UNSUPPORTED, "gather_lanes = 4 is built for SPP_MODEL_ABP and SPP_MODEL_CONTINUOUS");
-  if (p->boundary != SPP_BOUNDARY_PERIODIC && p->boundary != SPP_BOUNDARY_WALLS)
-    return fail(SPP_ERR_INVALID, "boundary must be SPP_BOUNDARY_PERIODIC or SPP_BOUNDARY_WALLS");
+  if (p->boundary != SPP_BOUNDARY_PERIODIC && p->boundary != SPP_BOUNDARY_WALLS &&
+      p->boundary != SPP_BOUNDARY_CIRCLE)
+    return fail(SPP_ERR_INVALID, "boundary must be SPP_BOUNDARY_PERIODIC, _WALLS or _CIRCLE");
+  if (p->boundary == SPP_BOUNDARY_CIRCLE) {
+    if (p->model != SPP_MODEL_ABP && p->model != SPP_MODEL_CONTINUOUS)
+      return fail(SPP_ERR_UNSUPPORTED, "the circular box is built for SPP_MODEL_ABP and SPP_MODEL_CONTINUOUS "
+                                       "(the particles with a torque, parallel/box.h:285-294)");
+    if (p->n_walls != 0) return fail(SPP_ERR_INVALID, "the circular box has no wall segments (n_walls = 0)");
+  }
   if (p->boundary == SPP_BOUNDARY_WALLS) {
     if (p->model != SPP_MODEL_ABP && p->model != SPP_MODEL_CONTINUOUS)
       return fail(SPP_ERR_UNSUPPORTED, "walls are built for SPP_MODEL_ABP and SPP_MODEL_CONTINUOUS "
@@ -827,6 +834,42 @@ int spp_download_state(SppSystem* s, float* x, float* y, float* theta, int32_t* 
   CUDA_TRY(cudaMemcpyAsync(theta, s->stage_t, bytes, cudaMemcpyDeviceToHost, s->stream));
   if (img_x) CUDA_TRY(cudaMemcpyAsync(img_x, img_dev, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s->stream));
   if (img_y) CUDA_TRY(cudaMemcpyAsync(img_y, img_dev + n, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return SPP_OK;
+}
+
+int spp_download_tumble(SppSystem* s, int32_t* state, int n) {
+  if (!s || !state) return fail(SPP_ERR_INVALID, "NULL argument");
+  if (n != s->p.n) return fail(SPP_ERR_INVALID, "n differs from the system's particle count");
+  if (!s->uploaded) return fail(SPP_ERR_INVALID, "no state uploaded");
+  if (!s->d.tumble) return fail(SPP_ERR_INVALID, "the system has no run-and-tumble state "
+                                                 "(rot_noise is not SPP_NOISE_TUMBLE)");
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  CUDA_TRY(cudaMemcpyAsync(state, s->d.tumble, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost,
+                           s->stream));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return SPP_OK;
+}
+
+int spp_upload_tumble(SppSystem* s, const int32_t* state, int n) {
+  if (!s || !state) return fail(SPP_ERR_INVALID, "NULL argument");
+  if (n != s->p.n) return fail(SPP_ERR_INVALID, "n differs from the system's particle count");
+  if (!s->uploaded) return fail(SPP_ERR_INVALID, "upload the state (spp_upload_state) first");
+  if (!s->d.tumble) return fail(SPP_ERR_INVALID, "the system has no run-and-tumble state "
+                                                 "(rot_noise is not SPP_NOISE_TUMBLE)");
+  /* 0 (running) or +-c with 1 <= c <= the tumble length in steps; membrane
+   * beads never tumble */
+  const int32_t cmax = s->k.tumble_steps;
+  for (int i = 0; i < n; ++i) {
+    const int32_t v = state[i];
+    if (v < -cmax || v > cmax || (v != 0 && i < s->k.n_beads))
+      return fail(SPP_ERR_INVALID, "tumble state of particle " + std::to_string(i) + " out of range");
+  }
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  CUDA_TRY(cudaMemcpyAsync(s->d.tumble, state, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice,
+                           s->stream));
   CUDA_TRY(cudaStreamSynchronize(s->stream));
   return SPP_OK;
 }

@@ -95,15 +95,18 @@ __device__ __forceinline__ void finish_step(const SppConsts& k, const DevState& 
 #endif
 
 /* One neighbour's contribution; the chain kind also needs the neighbour's
- * bead count (1 for membrane beads). */
+ * bead count (1 for membrane beads).  valid = 0 marks a padding entry of a
+ * load group: the ABP, continuous and bead kinds mask it (no branch), the
+ * chain kind skips it. */
 template <int LAW, int KIND>
 __device__ __forceinline__ void stage_pair(const SppConsts& k, const DevState& d, int wrap, SppAccF* a,
-                                           int nbi, int j, float4 pi, float4 pj) {
+                                           int nbi, int j, float4 pi, float4 pj, int valid) {
   if (KIND == SPP_KIND_CHAIN) {
+    if (!valid) return;
     const int nbj = __ldg(d.id + j) < (uint32_t)k.n_beads ? 1 : k.chain_nb;
     spp_pair_chain(&k, LAW, wrap, a, nbi, nbj, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
   } else {
-    spp_pair_abp_lkw(&k, LAW, KIND, wrap, a, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w);
+    spp_pair_abp_lkwv(&k, LAW, KIND, wrap, a, pi.x, pi.y, pi.z, pi.w, pj.x, pj.y, pj.z, pj.w, valid);
   }
 }
 
@@ -116,7 +119,11 @@ __device__ __forceinline__ void stage_pair(const SppConsts& k, const DevState& d
  * continuous systems): lane r sums the neighbours with id % 4 == r, one
  * id-ordered segment of the list (spp_list_order), and the lane sums
  * combine through xor shuffles as (p0 + p1) + (p2 + p3); lane 0 then
- * finishes the particle. */
+ * finishes the particle.
+ * Latency: every per-particle input of the stage (state, list length,
+ * heading, the step's noise and start-of-step position, the list-build
+ * position) is loaded before the neighbour walk, so those loads overlap it,
+ * and the frozen flag is read alongside rather than ahead of them. */
 template <int LAW, int KIND, int LANES, int CLOSED>
 __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_STAGE_MIN_BLOCKS) k_abp_stage(SppConsts k, DevState d, StageBufs b,
                                                          cudaGraphConditionalHandle cond,
@@ -126,20 +133,37 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
   const int i = tg / LANES;
   const int lane_r = tg % LANES;
   const int last = (b.stage == b.nstages - 1);
-  const int frozen = d.ctl->frozen;
+  const bool inb = i < d.n;
+  const bool head = LANES == 1 || lane_r == 0;   /* the lane that finishes the particle */
   float disp2 = 0.0f, step2 = 0.0f;
-  if (i < d.n && !frozen) {
-    const float4 pi = b.cur[i];
-    SppAccF a;
-    spp_accf_zero(&a);
-    const uint32_t pid = BEADLIKE ? d.id[i] : 0u;
-    const int nbi = (KIND == SPP_KIND_CHAIN && pid >= (uint32_t)k.n_beads) ? k.chain_nb : 1;
-    int q_begin = 0, q_end = d.nn[i];
+  float4 pi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  int q_begin = 0, q_end = 0;
+  uint32_t pid = 0u;
+  float th0 = 0.0f, dth_in = 0.0f;
+  float2 p0 = make_float2(0.0f, 0.0f), rf = make_float2(0.0f, 0.0f);
+  if (inb) {
+    pi = b.cur[i];
+    q_end = d.nn[i];
     if (LANES > 1) {
       const unsigned long long lc = d.nn_lanes[i];
       for (int r = 0; r < lane_r; ++r) q_begin += (int)((lc >> (16 * r)) & 0xffffull);
       q_end = q_begin + (int)((lc >> (16 * lane_r)) & 0xffffull);
     }
+    if (head) {
+      if (BEADLIKE || b.stage == 0) pid = d.id[i];
+      th0 = d.theta[i];
+      if (b.stage > 0) {
+        dth_in = d.dth[i];
+        p0 = reinterpret_cast<const float2*>(d.pos)[2 * (size_t)i];
+      }
+      if (last) rf = d.ref[i];
+    }
+  }
+  const int frozen = d.ctl->frozen;
+  if (inb && !frozen) {
+    SppAccF a;
+    spp_accf_zero(&a);
+    const int nbi = (KIND == SPP_KIND_CHAIN && pid >= (uint32_t)k.n_beads) ? k.chain_nb : 1;
     const int32_t* __restrict__ nb = d.nbr + i;
     const size_t stride = (size_t)d.n;
     /* Warps whose particles are all far from the box edges skip the
@@ -160,13 +184,11 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) pg[u] = __ldg(b.cur + jg[u]);
 #pragma unroll
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
-        if (q0 + u < q_end) {
-          /* the minimum image only off the interior of a periodic box */
-          if (all_inner || CLOSED)
-            stage_pair<LAW, KIND>(k, d, 0, &a, nbi, jg[u], pi, pg[u]);
-          else
-            stage_pair<LAW, KIND>(k, d, 1, &a, nbi, jg[u], pi, pg[u]);
-        }
+        /* the minimum image only off the interior of a periodic box */
+        if (all_inner || CLOSED)
+          stage_pair<LAW, KIND>(k, d, 0, &a, nbi, jg[u], pi, pg[u], q0 + u < q_end);
+        else
+          stage_pair<LAW, KIND>(k, d, 1, &a, nbi, jg[u], pi, pg[u], q0 + u < q_end);
       }
     }
     if (LANES > 1) {
@@ -183,7 +205,7 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
         a.ovf |= __shfl_xor_sync(gmask, a.ovf, o);
       }
     }
-  if (LANES == 1 || lane_r == 0) {
+  if (head) {
     if (LAW == SPP_FORCE_R12_TRUNC && a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
     float fx, fy, tau;
     int turns = 1;
@@ -222,14 +244,13 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
       } else if (BEADLIKE && k.tumble) {
         dth = spp_tumble_noise(&k, pid, d.ctl->step, d.tumble + pid);
       } else {
-        dth = spp_rot_noise(&k, BEADLIKE ? pid : d.id[i], d.ctl->step);
+        dth = spp_rot_noise(&k, pid, d.ctl->step);
       }
       if (b.nstages > 1) d.dth[i] = dth;
+      p0 = make_float2(pi.x, pi.y);
     } else {
-      dth = d.dth[i];
+      dth = dth_in;
     }
-    const float4 p0 = (b.stage == 0) ? pi : d.pos[i];
-    const float th0 = d.theta[i];
     if (KIND == SPP_KIND_CHAIN && chain_swimmer && b.nstages == 1) {
       /* Move() turns first and projects the force on the new heading */
       float wc, ws;
@@ -268,9 +289,8 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
         const int2 g = d.img[i];
         d.img[i] = make_int2(g.x + gx, g.y + gy);
       }
-      const float2 r = d.ref[i];
       float ddx, ddy;
-      disp2 = spp_sep_cl(&k, CLOSED, nx, ny, r.x, r.y, &ddx, &ddy);
+      disp2 = spp_sep_cl(&k, CLOSED, nx, ny, rf.x, rf.y, &ddx, &ddy);
       step2 = spp_sep_cl(&k, CLOSED, nx, ny, p0.x, p0.y, &ddx, &ddy);
     }
   }

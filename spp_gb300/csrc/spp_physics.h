@@ -79,6 +79,8 @@ typedef struct SppConsts {
    * wall_len */
   int32_t closed;
   int32_t n_walls;
+  int32_t circle;              /* circular box (SPP_BOUNDARY_CIRCLE): closed, no walls */
+  float circ_k;                /* 40 g / (2 pi): the circle's torque prefactor */
   float wall_x1[SPP_MAX_WALLS], wall_y1[SPP_MAX_WALLS], wall_x2[SPP_MAX_WALLS], wall_y2[SPP_MAX_WALLS];
   float wall_ex[SPP_MAX_WALLS], wall_ey[SPP_MAX_WALLS], wall_len[SPP_MAX_WALLS];
   float wall_A, wall_sigma, wall_rc, wall_rf, wall_g_over_pi;
@@ -198,8 +200,10 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
     else
       k->lanes = p->n <= SPP_LANES_MAX_N ? SPP_GATHER_LANES : 1;
   }
-  k->closed = p->boundary == SPP_BOUNDARY_WALLS ? 1 : 0;
+  k->closed = p->boundary == SPP_BOUNDARY_WALLS || p->boundary == SPP_BOUNDARY_CIRCLE ? 1 : 0;
   k->n_walls = 0;
+  k->circle = p->boundary == SPP_BOUNDARY_CIRCLE ? 1 : 0;
+  k->circ_k = (float)(40.0 * p->g / (2.0 * 3.14159265358979323846));
   for (int w = 0; w < SPP_MAX_WALLS; ++w) {
     k->wall_x1[w] = k->wall_y1[w] = k->wall_x2[w] = k->wall_y2[w] = 0.0f;
     k->wall_ex[w] = k->wall_ey[w] = k->wall_len[w] = 0.0f;
@@ -207,7 +211,7 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
   k->wall_A = k->wall_sigma = k->wall_rc = k->wall_rf = k->wall_g_over_pi = 0.0f;
   k->wall_cut = 0.0f;
   k->wall_gcont_over_2pi = 0.0f;
-  if (k->closed) {
+  if (k->closed && !k->circle) {
     /* Box::Init_Topology (parallel/box.h:97-101), then the extra segments */
     double seg[SPP_MAX_WALLS][4] = {{-p->L, -p->L, -p->L, p->L},
                                     {-p->L, p->L, p->L, p->L},
@@ -368,8 +372,9 @@ SPP_HD int spp_pair_kind(const SppConsts* k) {
  *   R12       A ((sigma/d)^13 - (sigma/r_c)^13) dr / d  ->  t = A (q^13 - c^13) r, q = sigma r
  * The alignment term sin(theta_j - theta_i) = s_j c_i - c_j s_i factors:
  * the loop sums s_j and c_j and spp_align_sum combines them once. */
-SPP_HD void spp_pair_abp_lkw(const SppConsts* k, int law, int kind, int wrap, SppAccF* a, float xi,
-                             float yi, float ci, float si, float xj, float yj, float cj, float sj) {
+SPP_HD void spp_pair_abp_lkwv(const SppConsts* k, int law, int kind, int wrap, SppAccF* a, float xi,
+                              float yi, float ci, float si, float xj, float yj, float cj, float sj,
+                              int valid) {
   float dx, dy, d2;
   if (wrap) {
     d2 = spp_sep_cl(k, 0, xi, yi, xj, yj, &dx, &dy);
@@ -379,8 +384,8 @@ SPP_HD void spp_pair_abp_lkw(const SppConsts* k, int law, int kind, int wrap, Sp
     d2 = fmaf(dx, dx, dy * dy);
   }
   const int aligns = (kind != SPP_KIND_BEADS && kind != SPP_KIND_CHAIN);
-  const int in_rep = (law != SPP_FORCE_NONE) && (d2 < k->rrep2) && (d2 > 0.0f);
-  const int in_al = aligns && d2 < k->ral2;
+  const int in_rep = valid && (law != SPP_FORCE_NONE) && (d2 < k->rrep2) && (d2 > 0.0f);
+  const int in_al = valid && aligns && d2 < k->ral2;
   float r = 0.0f;
   if (law != SPP_FORCE_NONE || kind == SPP_KIND_CONT_ALPHA) r = spp_rsqrtf(d2);
   if (law != SPP_FORCE_NONE) {
@@ -407,6 +412,13 @@ SPP_HD void spp_pair_abp_lkw(const SppConsts* k, int law, int kind, int wrap, Sp
     if (kind == SPP_KIND_CONT_ALPHA && in_al && d2 > 0.0f)
       a->tq = a->tq - (k->alpha_over_pi * (dx * si - dy * ci)) * r;
   }
+}
+
+/* The pair term of a list entry that exists (valid = 0 masks a padding
+ * entry of a kernel's grouped loads: it then adds exactly nothing). */
+SPP_HD void spp_pair_abp_lkw(const SppConsts* k, int law, int kind, int wrap, SppAccF* a, float xi,
+                             float yi, float ci, float si, float xj, float yj, float cj, float sj) {
+  spp_pair_abp_lkwv(k, law, kind, wrap, a, xi, yi, ci, si, xj, yj, cj, sj, 1);
 }
 
 /* The alignment torque sum of the ABP and continuous kinds from the
@@ -558,6 +570,18 @@ SPP_HD void spp_wall_terms(const SppConsts* k, float x, float y, float c, float 
   *wtq = tq;
 }
 
+/* The circular box (Box::Interact, parallel/box.h:285-294, CIRCULAR_BOX
+ * without PERIODIC_BOUNDARY_CONDITION): a particle at distance r > L - 1
+ * from the centre turns away from the circle of radius L by
+ *   40 g (v_y x - v_x y) / (2 pi r (L - r)),
+ * added to its torque with the pair terms (the continuous model's Move
+ * multiplies that sum by g once more, particle.h:273). */
+SPP_HD float spp_circle_torque(const SppConsts* k, float x, float y, float c, float s) {
+  const float r = sqrtf(fmaf(x, x, y * y));
+  if (!(r > k->L - 1.0f)) return 0.0f;
+  return k->circ_k * (fmaf(s, x, -(c * y)) / (r * (k->L - r)));
+}
+
 /* Self-propulsion plus received force, and the torque (RepulsiveParticle::
  * Reset :559-564 and the alignment normalisations), plus, with walls
  * (k->n_walls > 0, a closed box; a compile-time constant in the specialised
@@ -568,7 +592,10 @@ SPP_HD void spp_wall_terms(const SppConsts* k, float x, float y, float c, float 
 SPP_HD void spp_abp_forces(const SppConsts* k, int walls, const SppAccF* a, float xi, float yi,
                            float ci, float si, float* fx, float* fy, float* tau) {
   float wfx = 0.0f, wfy = 0.0f, wtq = 0.0f;
-  if (walls) spp_wall_terms(k, xi, yi, ci, si, &wfx, &wfy, &wtq);
+  if (walls) {
+    spp_wall_terms(k, xi, yi, ci, si, &wfx, &wfy, &wtq);
+    if (k->circle) wtq = wtq + spp_circle_torque(k, xi, yi, ci, si);
+  }
   *fx = fmaf(k->v0, ci, a->fx);
   *fy = fmaf(k->v0, si, a->fy);
   float S = spp_align_sum(k, a, ci, si);

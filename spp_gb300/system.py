@@ -22,6 +22,7 @@ prints and exits (shared/cell.h:45-49, parallel/box.h:224-228).
 """
 import ctypes as C
 from dataclasses import dataclass
+from typing import Optional
 
 import numpy as np
 
@@ -89,6 +90,24 @@ class System:
         abi.check(abi.lib().spp_download_state(self._h, abi.fptr(x), abi.fptr(y), abi.fptr(th),
                                                abi.iptr(ix), abi.iptr(iy), n), "spp_download_state")
         return x, y, th, ix, iy
+
+    @property
+    def has_tumble(self):
+        """Run-and-tumble swimmers carry a per-particle tumble state."""
+        return int(self.params.rot_noise) == abi.NOISE_TUMBLE
+
+    def download_tumble(self):
+        """Run-and-tumble state per particle id (int32: 0 running, +-c in the
+        c-th step of a tumble), or None without run and tumble."""
+        if not self.has_tumble:
+            return None
+        st = np.empty(self.n, np.int32)
+        abi.check(abi.lib().spp_download_tumble(self._h, abi.iptr(st), self.n), "spp_download_tumble")
+        return st
+
+    def upload_tumble(self, state):
+        st = np.ascontiguousarray(state, np.int32)
+        abi.check(abi.lib().spp_upload_tumble(self._h, abi.iptr(st), self.n), "spp_upload_tumble")
 
     def step(self, nsteps):
         abi.check(abi.lib().spp_step(self._h, int(nsteps)), "spp_step")
@@ -214,6 +233,7 @@ class Snapshot:
     img_x: np.ndarray
     img_y: np.ndarray
     step: int
+    tumble: Optional[np.ndarray] = None   # run-and-tumble state (RTPChain), if any
 
 
 class Box:
@@ -259,11 +279,13 @@ class Box:
     def Save(self) -> Snapshot:
         x, y, th, ix, iy = self.system.download()
         o = self.system.observables()
-        return Snapshot(x, y, th, ix, iy, self._step0 + int(o.step))
+        return Snapshot(x, y, th, ix, iy, self._step0 + int(o.step), self.system.download_tumble())
 
     def Load(self, snap: Snapshot):
         self.system.upload(snap.x, snap.y, snap.theta, step0=snap.step, img_x=snap.img_x,
                            img_y=snap.img_y)
+        if snap.tumble is not None:
+            self.system.upload_tumble(snap.tumble)
         self._step0 = snap.step
         self.t = snap.step * self.params.dt
 

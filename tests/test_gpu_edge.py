@@ -178,6 +178,58 @@ def test_checkpoint_file_resume_is_bitexact(gpu_lib, tmp_path):
         assert np.array_equal(u, v)
 
 
+def test_run_and_tumble_checkpoint_resume_is_bitexact(gpu_lib, tmp_path):
+    """RTPChain swimmers inside ring membranes, checkpointed mid-run while
+    swimmers are tumbling: the tumble state (RTPChain::tumble_flag and
+    tumble_elapesed_time, shared/particle.h:1063-1064) is part of the
+    checkpoint, so the resumed run equals the uninterrupted one bit for bit,
+    through the file and through Box.Save / Box.Load.  Without the tumble
+    state the resumed run differs."""
+    from spp_gb300 import Box, checkpoint
+    p = configs.vesicle_config(n_rings=16, ring_size=64, swimmers_per_ring=16, L=48.0,
+                               integrator=abi.INT_RK2, seed=9)
+    x, y, th = configs.vesicle_state(p)
+    p.rot_noise = abi.NOISE_TUMBLE
+    p.tumble_rate, p.tumble_time, p.tumble_torque = 20.0, 0.03, 3.0
+    path = tmp_path / "rtp.npz"
+    with System(p) as a:
+        a.upload(x, y, th)
+        a.step(120)
+        mid = a.download_tumble()
+        checkpoint.save(path, a)
+        a.step(80)
+        end_a = a.download()
+    assert np.count_nonzero(mid) > 0    # swimmers were tumbling at the checkpoint
+    with checkpoint.resume(path) as b:
+        assert np.array_equal(b.download_tumble(), mid)
+        b.step(80)
+        end_b = b.download()
+    for u, v in zip(end_a, end_b):
+        assert np.array_equal(u, v)
+    box = Box(p)
+    box.Init(x, y, th)
+    box.Multi_Step(120)
+    snap = box.Save()
+    box.Multi_Step(80)
+    end_c = box.Save()
+    box.Load(snap)
+    box.Multi_Step(80)
+    end_d = box.Save()
+    for u, v in ((end_c.x, end_d.x), (end_c.theta, end_d.theta), (end_c.tumble, end_d.tumble)):
+        assert np.array_equal(u, v)
+    assert np.array_equal(end_c.x, end_a[0])
+    with System(p) as c:       # the same snapshot without its tumble state
+        c.upload(snap.x, snap.y, snap.theta, step0=snap.step, img_x=snap.img_x, img_y=snap.img_y)
+        c.step(80)
+        assert not np.array_equal(c.download()[2], end_a[2])
+    with System(p) as d:
+        d.upload(x, y, th)
+        bad = np.zeros(p.n, np.int32)
+        bad[0] = 1                        # particle 0 is a membrane bead: it never tumbles
+        with pytest.raises(SppError):
+            d.upload_tumble(bad)
+
+
 def test_densifying_flocks_keep_recovering(gpu_lib):
     """Continuous Vicsek without noise or repulsion: flocks densify, the
     neighbour list overflows again and again as the run goes on; recovery

@@ -494,6 +494,30 @@ def test_walls_bitexact_vs_mirror(gpu_lib, model, integ, n):
     assert not gpu[3].any() and not gpu[4].any()
 
 
+@pytest.mark.parametrize("model,integ", [(abi.MODEL_ABP, abi.INT_RK2), (abi.MODEL_ABP, abi.INT_RK4),
+                                         (abi.MODEL_CONTINUOUS, abi.INT_EULER),
+                                         (abi.MODEL_CONTINUOUS, abi.INT_RK2)])
+@pytest.mark.parametrize("n", [4096, 20000])
+def test_circular_box_bitexact_vs_mirror(gpu_lib, model, integ, n):
+    """Circular box (parallel/box.h:285-294): no wrap, no minimum image, the
+    circle's torque on particles beyond r = L - 1; four lanes per particle
+    at 4096, one at 20,000.  After 600 more steps every particle is still
+    inside the circle."""
+    L = 40.0 if n == 4096 else 86.0
+    p = configs.circle_config(n=n, L=L, model=model, integrator=integ)
+    x, y, th = configs.circle_state(p)
+    gpu, _ = run_gpu(p, x, y, th, 150)
+    ref = O.run32(p, O.State32(x, y, th), 150)
+    assert_bitexact(gpu, ref)
+    assert not gpu[3].any() and not gpu[4].any()
+    with System(p) as s:
+        s.upload(*gpu[:3])
+        s.step(600)
+        gx, gy, _, _, _ = s.download()
+    r = np.hypot(gx.astype(np.float64), gy.astype(np.float64))
+    assert r.max() < p.L
+
+
 def test_star_trap_bitexact_vs_mirror(gpu_lib):
     """ABP in a closed box holding a two-hand star trap (four segments)."""
     p = configs.walls_config(n=2500, L=30.0, extra_walls=configs.star_trap_walls(2))

@@ -124,3 +124,42 @@ def test_star_trap_segments():
     a = O.State64(x.astype(np.float64), y.astype(np.float64), th.astype(np.float64))
     O.run64(p, a, 100)
     assert np.abs(s32.x - a.x).max() < 1e-3
+
+
+@pytest.mark.parametrize("model,integ", [(abi.MODEL_ABP, abi.INT_RK2), (abi.MODEL_CONTINUOUS, abi.INT_EULER)])
+def test_circular_box_mirror_tracks_fp64(model, integ):
+    """The circular box (parallel/box.h:285-294): the kernels' FP32 arithmetic
+    (CPU mirror) against the FP64 restatement over 100 steps of particles
+    pressed against the circle (the lattice fills it almost to the edge),
+    and the circle holds them.  Quantile bounds: a pair the two precisions
+    put on different sides of the alignment cutoff parts a few particles by
+    more than rounding."""
+    p = configs.circle_config(n=1600, L=26.0, model=model, integrator=integ)
+    x, y, th = configs.circle_state(p)
+    a = O.run64(p, O.State64(x, y, th), 100)
+    b = O.run32(p, O.State32(x, y, th), 100)
+    r64 = np.hypot(a.x, a.y)
+    assert r64.max() < p.L and (r64 > p.L - 1).sum() > 0   # the circle torque acted
+    err = np.maximum(np.abs(b.x - a.x), np.abs(b.y - a.y))
+    assert np.quantile(err, 0.99) < 1e-4 and err.max() < 0.01
+    assert np.all(b.ix == 0) and np.all(b.iy == 0)
+
+
+def test_circle_torque_formula():
+    """The FP32 circle torque against the formula of parallel/box.h:292,
+    40 g (v_y x - v_x y) / (2 pi r (L - r)), evaluated in FP64."""
+    p = configs.circle_config(n=8, L=10.0)
+    rng = np.random.default_rng(3)
+    for _ in range(200):
+        r = rng.uniform(8.5, 9.99)
+        phi, th = rng.uniform(-np.pi, np.pi, 2)
+        x, y = np.float32(r * np.cos(phi)), np.float32(r * np.sin(phi))
+        th = np.float32(th)
+        got = O.circle_torque32(p, x, y, th)
+        xd, yd = float(x), float(y)
+        rd = np.hypot(xd, yd)
+        want = 40 * p.g * (np.sin(th) * xd - np.cos(th) * yd) / (2 * np.pi * rd * (p.L - rd))
+        if not rd > p.L - 1:
+            want = 0.0
+        assert abs(got - want) <= 1e-4 * (1 + abs(want)), (got, want)
+    assert O.circle_torque32(p, np.float32(3.0), np.float32(4.0), np.float32(0.3)) == 0.0
