@@ -296,14 +296,29 @@ extern "C" void ref_spring(double dx, double dy, double sigma, double A, double*
 
 /* The reference's walls (Wall::Init, Wall::Interact, shared/wall.h) on one
  * particle, for the segments p->walls[0 .. p->n_walls) alone.  out4 =
- * {f.x, f.y, torque} of a RepulsiveParticle, or {0, 0, 0, torque} of a
- * ContinuousParticle.  The harness is built with the reference's
+ * {f.x, f.y, torque} of a RepulsiveParticle, {0, 0, 0, torque} of a
+ * ContinuousParticle, or {neighbour count, angle sum} of a VicsekParticle.  The harness is built with the reference's
  * PERIODIC_BOUNDARY_CONDITION, so the box is set 1e9 wide here: then the
  * Periodic_Transform calls of Wall change nothing, as in the reference's
  * closed-box build. */
 extern "C" void ref_wall_terms(const SppParams* p, double x, double y, double th, double* out4) {
   set_box(1e9);
   out4[0] = out4[1] = out4[2] = out4[3] = 0.0;
+  if (p->model == SPP_MODEL_VICSEK_REF_ANGLE) {
+    /* {neighbor_size, average_theta} the walls add to a reset VicsekParticle */
+    VicsekParticle q;
+    q.r.x = x; q.r.y = y; q.theta = th;
+    q.v.x = std::cos(th); q.v.y = std::sin(th);
+    q.Reset();
+    for (int e = 0; e < p->n_walls; ++e) {
+      Wall w;
+      w.Init(p->walls[e][0], p->walls[e][1], p->walls[e][2], p->walls[e][3]);
+      w.Interact(&q);
+    }
+    out4[0] = q.neighbor_size;
+    out4[1] = q.average_theta;
+    return;
+  }
   if (p->model == SPP_MODEL_CONTINUOUS) {
     ContinuousParticle::gw = p->g_w_cont;
     ContinuousParticle q;

@@ -307,6 +307,7 @@ static int vicsek_run32(const SppParams* p, const SppConsts* k, int nsteps, int6
       FOR_CANDIDATES(&cl, k, x[i], y[i], n, j, {
         spp_pair_vicsek(k, &a, x[i], y[i], x[j], y[j], c[j], s[j], th[j], j == i);
       });
+      if (k->closed && k->model == SPP_MODEL_VICSEK_REF_ANGLE) spp_vicsek_walls(k, &a, x[i], y[i], th[i]);
       if (a.ovf) rc = SPP_ERR_OVERFLOW;
       spp_u32x4 d = spp_draw(k->seed, k->system, (uint32_t)i, step, SPP_RNG_VICSEK);
       int gx = ix[i], gy = iy[i];
@@ -689,6 +690,17 @@ void orc32_wall_terms(const SppParams* p, float x, float y, float th, float* out
     k.wall_len[e] = k.wall_len[e + 4];
   }
   k.n_walls = p->n_walls;
+  for (int e = 0; e < p->n_walls; ++e) k.wall_theta[e] = k.wall_theta[e + 4];
+  if (p->model == SPP_MODEL_VICSEK_REF_ANGLE) {
+    /* {count, angle sum, 0}: the neighbours and angle sum the walls add */
+    SppAcc a;
+    spp_acc_zero(&a);
+    spp_vicsek_walls(&k, &a, x, y, th);
+    out3[0] = (float)a.cnt;
+    out3[1] = spp_fx_value(a.at);
+    out3[2] = 0.0f;
+    return;
+  }
   float s, c;
   spp_sincosf(th, &s, &c);
   spp_wall_terms(&k, x, y, c, s, &out3[0], &out3[1], &out3[2]);

@@ -440,6 +440,31 @@ static void wall_terms64(const SppParams* p, const owall* w, int nw, double x, d
   }
 }
 
+/* Wall::Interact(VicsekParticle*), shared/wall.h:163-190, of the walls
+ * w[0..nw): where the particle's foot lies inside a segment and its distance
+ * is below 1, the wall counts as a neighbour and adds the particle's own
+ * heading relative to the wall's direction, folded to [-pi/2, pi/2], to the
+ * angle sum (as the reference writes it). */
+static void vicsek_walls64(const SppParams* p, const owall* w, int nw, double x, double y, double th,
+                           int* nb, double* ath) {
+  for (int e = 0; e < nw; ++e) {
+    double r1x = pt(x - w[e].x1, p->L), r1y = pt(y - w[e].y1, p->L);
+    double proj = r1x * w[e].dx + r1y * w[e].dy;
+    if (!(proj < w[e].len && proj > 0)) continue;
+    double drx = r1x - w[e].dx * proj, dry = r1y - w[e].dy * proj;
+    double dth = th - w[e].theta;
+    dth -= 2 * M_PI * (int)(dth / M_PI);
+    if (dth > M_PI / 2 || dth < -M_PI / 2) {
+      dth += M_PI;
+      dth -= 2 * M_PI * (int)(dth / M_PI);
+    }
+    if (drx * drx + dry * dry < 1) {
+      (*nb)++;
+      *ath += dth;
+    }
+  }
+}
+
 /* The walls of a closed box on every particle after the pair sums
  * (parallel/box.h:296-302). */
 static void walls_interact(ostate* s) {
@@ -484,7 +509,14 @@ void orc64_wall_terms(const SppParams* p, double x, double y, double th, double*
   for (int e = 0; e < nw; ++e) w[e] = w[e + 4];
   out4[0] = out4[1] = out4[2] = out4[3] = 0.0;
   g_closed = 1;
-  wall_terms64(p, w, nw, x, y, th, cos(th), sin(th), &out4[0], &out4[1], &out4[2], &out4[3]);
+  if (p->model == SPP_MODEL_VICSEK_REF_ANGLE) {
+    /* {count, angle sum, 0, 0} */
+    int nb = 0;
+    vicsek_walls64(p, w, nw, x, y, th, &nb, &out4[1]);
+    out4[0] = nb;
+  } else {
+    wall_terms64(p, w, nw, x, y, th, cos(th), sin(th), &out4[0], &out4[1], &out4[2], &out4[3]);
+  }
   g_closed = 0;
 }
 
@@ -844,6 +876,11 @@ static void vicsek_step(ostate* s, int64_t step) {
     }
   } else if (p->model == SPP_MODEL_VICSEK_REF_ANGLE) {
     interact_all(s, vicsek_angle_pair);
+    if (p->boundary == SPP_BOUNDARY_WALLS) {
+      owall w[SPP_MAX_WALLS];
+      const int nw = box_walls(p, w);
+      for (int i = 0; i < n; ++i) vicsek_walls64(p, w, nw, s->x[i], s->y[i], s->th[i], &s->nb[i], &s->ath[i]);
+    }
     for (int i = 0; i < n; ++i) { /* VicsekParticle::Move, particle.h:148-163 */
       double avg = s->nb[i] > 0 ? s->ath[i] / s->nb[i] : s->th[i];
       s->th[i] = avg + p->eta * orc_uniform_pm_pi(p, i, step);

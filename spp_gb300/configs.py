@@ -243,7 +243,25 @@ def walls_config(n=4096, L=40.0, model=abi.MODEL_ABP, integrator=abi.INT_RK2, se
     p.Dr, p.dt, p.skin = 0.1, 0.005, 0.3
     if model == abi.MODEL_CONTINUOUS:
         p.g, p.alpha, p.v0, p.dt = 1.0, 0.0, 0.5, 0.01
+    if model in (abi.MODEL_VICSEK_REF_ANGLE, abi.MODEL_VICSEK_REF_VECTOR):
+        p.v0, p.r_align, p.dt, p.eta = 0.5, 1.0, 1.0, 0.3
     return p
+
+
+def vicsek_walls_state(p, seed=None, half=None):
+    """Discrete Vicsek particles of a closed box: uniform in the central
+    square of half-width `half` (default L/2, so that they stay inside the
+    box for a few dozen steps: VicsekParticle feels walls only as alignment,
+    nothing keeps it in), headings uniform."""
+    seed = p.seed if seed is None else seed
+    half = p.L / 2 if half is None else half
+    ids = np.arange(p.n, dtype=np.uint32)
+    r = draw(seed, 0, ids, 0, RNG_INIT_POS)
+    x = ((2 * u01_f32(r[0]).astype(np.float64) - 1) * half).astype(np.float32)
+    y = ((2 * u01_f32(r[1]).astype(np.float64) - 1) * half).astype(np.float32)
+    t = draw(seed, 0, ids, 0, RNG_INIT_ANGLE)
+    th = ((2 * u01_f32(t[0]).astype(np.float64) - 1) * math.pi).astype(np.float32)
+    return x, y, th
 
 
 def star_trap_walls(n_hands=2, half_delta=0.3, r_big=15.0, r_small=6.0):

@@ -175,9 +175,11 @@ int validate(const SppParams* p) {
     if (p->n_walls != 0) return fail(SPP_ERR_INVALID, "the circular box has no wall segments (n_walls = 0)");
   }
   if (p->boundary == SPP_BOUNDARY_WALLS) {
-    if (p->model != SPP_MODEL_ABP && p->model != SPP_MODEL_CONTINUOUS)
-      return fail(SPP_ERR_UNSUPPORTED, "walls are built for SPP_MODEL_ABP and SPP_MODEL_CONTINUOUS "
-                                       "(Wall::Interact of RepulsiveParticle and ContinuousParticle)");
+    if (p->model != SPP_MODEL_ABP && p->model != SPP_MODEL_CONTINUOUS &&
+        p->model != SPP_MODEL_VICSEK_REF_ANGLE && p->model != SPP_MODEL_VICSEK_REF_VECTOR)
+      return fail(SPP_ERR_UNSUPPORTED, "walls are built for SPP_MODEL_ABP, SPP_MODEL_CONTINUOUS, "
+                                       "SPP_MODEL_VICSEK_REF_ANGLE and SPP_MODEL_VICSEK_REF_VECTOR "
+                                       "(the reference's Wall::Interact overloads)");
     if (p->n_walls < 0 || p->n_walls > SPP_MAX_WALLS - 4)
       return fail(SPP_ERR_INVALID, "n_walls must be 0 .. SPP_MAX_WALLS - 4 (the box has 4 walls)");
     for (int w = 0; w < p->n_walls; ++w) {

@@ -328,6 +328,7 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_vicsek_step(SppConsts k, DevState
         }
       }
     }
+    if (k.closed && k.model == SPP_MODEL_VICSEK_REF_ANGLE) spp_vicsek_walls(&k, &a, p.x, p.y, th0);
     if (a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
     const spp_u32x4 r = spp_draw(k.seed, k.system, id, step, SPP_RNG_VICSEK);
     float x, y, t, c, s;
@@ -511,6 +512,7 @@ __global__ void __launch_bounds__(SPP_SMALL_THREADS, 1) k_vicsek_small(SppConsts
           a.ovf |= __shfl_xor_sync(0xffffffffu, a.ovf, o);
         }
         if (valid && q == 0) {
+          if (k.closed && need_theta) spp_vicsek_walls(&k, &a, p.x, p.y, sth[me]);
           if (a.ovf) ovf = 1u;
           const spp_u32x4 r = spp_draw(k.seed, k.system, d.id[i], step, SPP_RNG_VICSEK);
           float x, y, th, c, sn;

@@ -83,6 +83,7 @@ typedef struct SppConsts {
   float circ_k;                /* 40 g / (2 pi): the circle's torque prefactor */
   float wall_x1[SPP_MAX_WALLS], wall_y1[SPP_MAX_WALLS], wall_x2[SPP_MAX_WALLS], wall_y2[SPP_MAX_WALLS];
   float wall_ex[SPP_MAX_WALLS], wall_ey[SPP_MAX_WALLS], wall_len[SPP_MAX_WALLS];
+  float wall_theta[SPP_MAX_WALLS];   /* Wall::theta, the direction angle (wall.h:38-41) */
   float wall_A, wall_sigma, wall_rc, wall_rf, wall_g_over_pi;
   float wall_cut;              /* e^(-r_c/sigma) (1/r_c^2 + 1/(sigma r_c)), the truncation shift */
   float wall_gcont_over_2pi;   /* ContinuousParticle::gw / (2 pi) */
@@ -206,7 +207,7 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
   k->circ_k = (float)(40.0 * p->g / (2.0 * 3.14159265358979323846));
   for (int w = 0; w < SPP_MAX_WALLS; ++w) {
     k->wall_x1[w] = k->wall_y1[w] = k->wall_x2[w] = k->wall_y2[w] = 0.0f;
-    k->wall_ex[w] = k->wall_ey[w] = k->wall_len[w] = 0.0f;
+    k->wall_ex[w] = k->wall_ey[w] = k->wall_len[w] = k->wall_theta[w] = 0.0f;
   }
   k->wall_A = k->wall_sigma = k->wall_rc = k->wall_rf = k->wall_g_over_pi = 0.0f;
   k->wall_cut = 0.0f;
@@ -229,6 +230,14 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
       k->wall_y1[w] = (float)seg[w][1];
       k->wall_x2[w] = (float)seg[w][2];
       k->wall_y2[w] = (float)seg[w][3];
+      {
+        /* Wall::Init: atan of the direction, +pi when it points to -x, then
+         * theta -= 2 pi (int)(theta / pi) */
+        double th = atan((dy / len) / (dx / len));
+        if (dx / len < 0.) th += 3.14159265358979323846;
+        th -= 2 * 3.14159265358979323846 * (int)(th / 3.14159265358979323846);
+        k->wall_theta[w] = (float)th;
+      }
       k->wall_ex[w] = (float)(dx / len);
       k->wall_ey[w] = (float)(dy / len);
       k->wall_len[w] = (float)len;
@@ -724,6 +733,33 @@ SPP_HD void spp_pair_vicsek(const SppConsts* k, SppAcc* a, float xi, float yi, f
 /* New heading and position of particle i (VicsekParticle::Move :148-163,
  * VicsekParticle2::Move :198-213, configured rule). xi_u is the Philox word
  * of the Vicsek noise stream. */
+/* Wall::Interact(VicsekParticle*) (shared/wall.h:163-190) of every wall of a
+ * closed box: a particle whose foot on the segment lies inside it and whose
+ * distance from it is below 1 counts the wall as a neighbour and adds, as
+ * the reference writes it, its own heading relative to the wall's direction
+ * folded to [-pi/2, pi/2] (dtheta = theta - theta_w, dtheta -= 2 pi
+ * (int)(dtheta / pi), and once more after adding pi when |dtheta| > pi/2)
+ * to the angle sum that VicsekParticle::Move averages.  Into the exact
+ * fixed-point angle sum. */
+SPP_HD void spp_vicsek_walls(const SppConsts* k, SppAcc* a, float x, float y, float th) {
+  for (int w = 0; w < k->n_walls; ++w) {
+    const float ex = k->wall_ex[w], ey = k->wall_ey[w];
+    const float r1x = x - k->wall_x1[w], r1y = y - k->wall_y1[w];
+    const float proj = fmaf(r1x, ex, r1y * ey);
+    if (!(proj < k->wall_len[w] && proj > 0.0f)) continue;
+    const float dx = r1x - ex * proj, dy = r1y - ey * proj;
+    if (!(fmaf(dx, dx, dy * dy) < 1.0f)) continue;
+    float dth = th - k->wall_theta[w];
+    dth = fmaf(-SPP_TWO_PI_F, truncf(dth / SPP_PI_F), dth);
+    if (dth > 0.5f * SPP_PI_F || dth < -0.5f * SPP_PI_F) {
+      dth = dth + SPP_PI_F;
+      dth = fmaf(-SPP_TWO_PI_F, truncf(dth / SPP_PI_F), dth);
+    }
+    a->cnt += 1;
+    spp_fx_add_guarded(&a->at, dth, &a->ovf);
+  }
+}
+
 SPP_HD void spp_vicsek_update(const SppConsts* k, const SppAcc* a, float x0, float y0, float th0,
                               float c0, float s0, uint32_t xi_bits, float* x, float* y, float* th,
                               float* c, float* s, int* imgx, int* imgy) {
@@ -747,8 +783,8 @@ SPP_HD void spp_vicsek_update(const SppConsts* k, const SppAcc* a, float x0, flo
   }
   spp_sincosf(t, s, c);
   *th = t;
-  *x = spp_wrap_coord_f(fmaf(k->v0dt, *c, x0), k->L, k->L2, imgx);
-  *y = spp_wrap_coord_f(fmaf(k->v0dt, *s, y0), k->L, k->L2, imgy);
+  *x = spp_move_coord(k, k->closed, fmaf(k->v0dt, *c, x0), imgx);
+  *y = spp_move_coord(k, k->closed, fmaf(k->v0dt, *s, y0), imgy);
 }
 
 /* ------------------------------------------------------------------ */

@@ -232,7 +232,8 @@ def main(parts=("runs", "gram_schmidt", "order_parameters", "records")):
         O.run64(p, s, steps, fn="ref")
         blob[f"{name}/out"] = np.stack([s.x, s.y, s.th, s.xu, s.yu])
         meta[name] = {"params": {k: v for k, v in p.as_dict().items()}, "steps": steps}
-    for model, name in ((abi.MODEL_ABP, "walls_abp"), (abi.MODEL_CONTINUOUS, "walls_continuous")):
+    for model, name in ((abi.MODEL_ABP, "walls_abp"), (abi.MODEL_CONTINUOUS, "walls_continuous"),
+                        (abi.MODEL_VICSEK_REF_ANGLE, "walls_vicsek")):
         p, pts = wall_case(model)
         blob[f"{name}/in"] = pts
         blob[f"{name}/out"] = np.array([O.wall_terms(p, *q, fn="ref") for q in pts])

@@ -518,6 +518,25 @@ def test_circular_box_bitexact_vs_mirror(gpu_lib, model, integ, n):
     assert r.max() < p.L
 
 
+@pytest.mark.parametrize("model", [abi.MODEL_VICSEK_REF_ANGLE, abi.MODEL_VICSEK_REF_VECTOR])
+@pytest.mark.parametrize("n,L", [(2000, 60.0), (30000, 240.0)])
+def test_vicsek_walls_bitexact_vs_mirror(gpu_lib, model, n, L):
+    """The discrete Vicsek models in a closed box with two oblique segments:
+    VicsekParticle counts a wall within distance 1 as a neighbour and adds
+    its folded relative heading (Wall::Interact(VicsekParticle*),
+    shared/wall.h:163-190); VicsekParticle2 has no wall overload (the empty
+    Wall::Interact(BasicDynamicParticle*), :159-161), so only the closed box
+    acts on it.  2000 particles run in the one-cluster kernel, 30,000 through
+    the multi-kernel step."""
+    p = configs.walls_config(n=n, L=L, model=model, seed=4,
+                             extra_walls=((-10.0, -4.0, 8.0, 12.0), (6.0, -14.0, -12.0, 2.0)))
+    x, y, th = configs.vicsek_walls_state(p, half=30.0 if n == 2000 else 110.0)
+    gpu, _ = run_gpu(p, x, y, th, 30)
+    ref = O.run32(p, O.State32(x, y, th), 30)
+    assert_bitexact(gpu, ref)
+    assert not gpu[3].any() and not gpu[4].any()
+
+
 def test_star_trap_bitexact_vs_mirror(gpu_lib):
     """ABP in a closed box holding a two-hand star trap (four segments)."""
     p = configs.walls_config(n=2500, L=30.0, extra_walls=configs.star_trap_walls(2))

@@ -20,7 +20,7 @@ from make_golden import WALL_SEGMENTS, wall_case  # noqa: E402
 from test_oracle_pin import load_golden, params_from  # noqa: E402
 
 
-@pytest.mark.parametrize("name", ["walls_abp", "walls_continuous"])
+@pytest.mark.parametrize("name", ["walls_abp", "walls_continuous", "walls_vicsek"])
 def test_wall_terms_match_golden(name):
     """RepulsiveParticle force and torque, ContinuousParticle torque, against
     the reference's outputs on 400 particles near four segments."""
@@ -32,7 +32,7 @@ def test_wall_terms_match_golden(name):
     assert np.count_nonzero(np.any(ref != 0, axis=1)) > 200
 
 
-@pytest.mark.parametrize("model", [abi.MODEL_ABP, abi.MODEL_CONTINUOUS])
+@pytest.mark.parametrize("model", [abi.MODEL_ABP, abi.MODEL_CONTINUOUS, abi.MODEL_VICSEK_REF_ANGLE])
 def test_wall_terms_match_reference(model):
     if O.ref() is None:
         pytest.skip("reference checkout absent; the golden fixtures pin the walls instead")
@@ -163,3 +163,39 @@ def test_circle_torque_formula():
             want = 0.0
         assert abs(got - want) <= 1e-4 * (1 + abs(want)), (got, want)
     assert O.circle_torque32(p, np.float32(3.0), np.float32(4.0), np.float32(0.3)) == 0.0
+
+
+def test_vicsek_wall_alignment_fp32_vs_fp64():
+    """VicsekParticle's wall term (shared/wall.h:163-190): the kernels' FP32
+    count and folded angle against the FP64 restatement at the same float
+    inputs.  The count may differ only where the distance or the foot lies
+    within rounding of its bound; the angle within FP32 rounding except next
+    to a fold (dtheta = +-pi/2), where the two may fold differently."""
+    p, pts = wall_case(abi.MODEL_VICSEK_REF_ANGLE)
+    bad_cnt = 0
+    hits = 0
+    for x, y, th in pts:
+        x, y, th = float(np.float32(x)), float(np.float32(y)), float(np.float32(th))
+        a = O.wall_terms(p, x, y, th)
+        b = O.wall_terms(p, x, y, th, fn="orc32")
+        if a[0] != b[0]:
+            bad_cnt += 1
+            continue
+        hits += a[0] > 0
+        if a[0] > 0:
+            d = abs(a[1] - b[1])
+            assert d < 1e-5 or abs(d - np.pi) < 1e-5 * a[0], (x, y, th, a, b)
+    assert bad_cnt <= 2 and hits > 100
+
+
+def test_vicsek_walls_mirror_tracks_fp64():
+    """VicsekParticle (angle average) in a closed box with two oblique
+    segments across the flock: the FP32 mirror against the FP64 restatement
+    over 10 steps (the angle average is well conditioned; walls add
+    neighbours and angles)."""
+    p = configs.walls_config(n=2000, L=60.0, model=abi.MODEL_VICSEK_REF_ANGLE, seed=4)
+    x, y, th = configs.vicsek_walls_state(p)
+    a = O.run64(p, O.State64(x, y, th), 10)
+    b = O.run32(p, O.State32(x, y, th), 10)
+    e = np.abs((b.th.astype(np.float64) - a.th + np.pi) % (2 * np.pi) - np.pi)
+    assert np.quantile(e, 0.99) < 1e-5 and np.max(np.abs(b.x - a.x)) < 1e-3
