@@ -113,6 +113,33 @@ __device__ __forceinline__ void stage_pair(const SppConsts& k, const DevState& d
 #ifndef SPP_STAGE_MIN_BLOCKS
 #define SPP_STAGE_MIN_BLOCKS 8   /* 8 x 256 threads per SM: 32 registers */
 #endif
+/* Where the stage kernel fetches the per-particle inputs that the
+ * neighbour walk does not need (heading, the step's noise and start-of-step
+ * position, the list-build position, the id for the noise): 0 after the
+ * walk; 1 into registers before it (their latency overlaps the walk, at the
+ * price of registers held through it); 2 after the walk, with L1 prefetches
+ * of their lines issued before it (the overlap without the registers). */
+#ifndef SPP_STAGE_PREFETCH
+#define SPP_STAGE_PREFETCH 2
+#endif
+
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
+/* The per-particle inputs of a stage besides the state the neighbours read. */
+template <bool BEADLIKE>
+__device__ __forceinline__ void stage_inputs(const DevState& d, const StageBufs& b, int i, int last,
+                                             uint32_t* pid, float* th0, float* dth_in, float2* p0,
+                                             float2* rf) {
+  if (!BEADLIKE && b.stage == 0) *pid = d.id[i];
+  *th0 = d.theta[i];
+  if (b.stage > 0) {
+    *dth_in = d.dth[i];
+    *p0 = reinterpret_cast<const float2*>(d.pos)[2 * (size_t)i];
+  }
+  if (last) *rf = d.ref[i];
+}
 /* the chain pair loop (bead offsets, lever-arm torques) needs more than
  * 32 registers: 4 x 256 threads per SM there.
  * LANES threads per particle (LANES = k.lanes: 1, or 4 for small ABP /
@@ -150,13 +177,18 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
       q_end = q_begin + (int)((lc >> (16 * lane_r)) & 0xffffull);
     }
     if (head) {
-      if (BEADLIKE || b.stage == 0) pid = d.id[i];
-      th0 = d.theta[i];
-      if (b.stage > 0) {
-        dth_in = d.dth[i];
-        p0 = reinterpret_cast<const float2*>(d.pos)[2 * (size_t)i];
+      if (BEADLIKE) pid = d.id[i];
+      if (SPP_STAGE_PREFETCH == 1) {
+        stage_inputs<BEADLIKE>(d, b, i, last, &pid, &th0, &dth_in, &p0, &rf);
+      } else if (SPP_STAGE_PREFETCH == 2) {
+        if (!BEADLIKE && b.stage == 0) prefetch_l1(d.id + i);
+        prefetch_l1(d.theta + i);
+        if (b.stage > 0) {
+          prefetch_l1(d.dth + i);
+          prefetch_l1(d.pos + i);
+        }
+        if (last) prefetch_l1(d.ref + i);
       }
-      if (last) rf = d.ref[i];
     }
   }
   const int frozen = d.ctl->frozen;
@@ -206,6 +238,7 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
       }
     }
   if (head) {
+    if (SPP_STAGE_PREFETCH != 1) stage_inputs<BEADLIKE>(d, b, i, last, &pid, &th0, &dth_in, &p0, &rf);
     if (LAW == SPP_FORCE_R12_TRUNC && a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
     float fx, fy, tau;
     int turns = 1;

@@ -277,6 +277,54 @@ SPP_HD float spp_normal_f(uint32_t x0, uint32_t x1) {
 }
 
 /* ------------------------------------------------------------------ */
+/* two-lane FP32 operations                                            */
+/* ------------------------------------------------------------------ */
+/* A pair of floats handled together.  On sm_103a one packed instruction
+ * (add / sub / fma .rn.f32x2) performs both lanes, each lane correctly
+ * rounded exactly as the scalar operation, so the CPU's two scalar
+ * operations return the same bits. */
+typedef struct { float x, y; } spp_f2;
+
+SPP_HD spp_f2 spp_f2_make(float x, float y) { spp_f2 r; r.x = x; r.y = y; return r; }
+#if defined(__CUDA_ARCH__)
+SPP_HD unsigned long long spp_f2_pack(spp_f2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+SPP_HD spp_f2 spp_f2_unpack(unsigned long long r) {
+  spp_f2 a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+/* a - b */
+SPP_HD spp_f2 spp_sub2(spp_f2 a, spp_f2 b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(spp_f2_pack(a)), "l"(spp_f2_pack(b)));
+  return spp_f2_unpack(r);
+}
+/* a + b */
+SPP_HD spp_f2 spp_add2(spp_f2 a, spp_f2 b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(spp_f2_pack(a)), "l"(spp_f2_pack(b)));
+  return spp_f2_unpack(r);
+}
+/* fmaf(t, b, c) in both lanes */
+SPP_HD spp_f2 spp_fma2s(float t, spp_f2 b, spp_f2 c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(spp_f2_pack(spp_f2_make(t, t))),
+      "l"(spp_f2_pack(b)), "l"(spp_f2_pack(c)));
+  return spp_f2_unpack(r);
+}
+#else
+SPP_HD spp_f2 spp_sub2(spp_f2 a, spp_f2 b) { return spp_f2_make(a.x - b.x, a.y - b.y); }
+SPP_HD spp_f2 spp_add2(spp_f2 a, spp_f2 b) { return spp_f2_make(a.x + b.x, a.y + b.y); }
+SPP_HD spp_f2 spp_fma2s(float t, spp_f2 b, spp_f2 c) {
+  return spp_f2_make(fmaf(t, b.x, c.x), fmaf(t, b.y, c.y));
+}
+#endif
+
+/* ------------------------------------------------------------------ */
 /* periodic wraps                                                      */
 /* ------------------------------------------------------------------ */
 /* theta -> theta - 2 pi floor(theta / 2 pi + 1/2), as shared/particle.h:599. */

@@ -342,7 +342,7 @@ SPP_HD float spp_move_coord(const SppConsts* k, int closed, float x, int* img) {
  * contributors in the same order). */
 typedef struct SppAccF {
   float fx, fy;     /* received force */
-  float ss, sc;     /* sums of sin theta_j and cos theta_j over the aligning neighbours:
+  float sc, ss;     /* sums of cos theta_j and sin theta_j over the aligning neighbours:
                        sum_j sin(theta_j - theta_i) = cos theta_i ss - sin theta_i sc */
   float tq;         /* torque terms that do not factor that way (the alpha term of the
                        continuous model, lever-arm torques of chains) */
@@ -388,8 +388,9 @@ SPP_HD void spp_pair_abp_lkwv(const SppConsts* k, int law, int kind, int wrap, S
   if (wrap) {
     d2 = spp_sep_cl(k, 0, xi, yi, xj, yj, &dx, &dy);
   } else { /* both particles far from the boundary, or a closed box: the plain difference */
-    dx = xi - xj;
-    dy = yi - yj;
+    const spp_f2 dr = spp_sub2(spp_f2_make(xi, yi), spp_f2_make(xj, yj));
+    dx = dr.x;
+    dy = dr.y;
     d2 = fmaf(dx, dx, dy * dy);
   }
   const int aligns = (kind != SPP_KIND_BEADS && kind != SPP_KIND_CHAIN);
@@ -409,14 +410,16 @@ SPP_HD void spp_pair_abp_lkwv(const SppConsts* k, int law, int kind, int wrap, S
       t = in_rep ? (k->k_rep * (q13 - k->c13)) * r : 0.0f;
       if (!(fabsf(t * dx) < SPP_FX_RANGE && fabsf(t * dy) < SPP_FX_RANGE)) { a->ovf = 1; t = 0.0f; }
     }
-    a->fx = fmaf(t, dx, a->fx);
-    a->fy = fmaf(t, dy, a->fy);
+    const spp_f2 f = spp_fma2s(t, spp_f2_make(dx, dy), spp_f2_make(a->fx, a->fy));
+    a->fx = f.x;
+    a->fy = f.y;
   }
   if (aligns) {
     a->cnt += in_al;
     if (in_al) {
-      a->ss = a->ss + sj;
-      a->sc = a->sc + cj;
+      const spp_f2 cs = spp_add2(spp_f2_make(a->sc, a->ss), spp_f2_make(cj, sj));
+      a->sc = cs.x;
+      a->ss = cs.y;
     }
     if (kind == SPP_KIND_CONT_ALPHA && in_al && d2 > 0.0f)
       a->tq = a->tq - (k->alpha_over_pi * (dx * si - dy * ci)) * r;
