@@ -122,6 +122,15 @@ __device__ __forceinline__ void stage_pair(const SppConsts& k, const DevState& d
 #ifndef SPP_STAGE_PREFETCH
 #define SPP_STAGE_PREFETCH 2
 #endif
+/* List entries of a thread kept in shared memory during the walk (0: read
+ * from global memory group by group) and how many of their loads are issued
+ * together when they are fetched. */
+#ifndef SPP_STAGE_SMEM_LIST
+#define SPP_STAGE_SMEM_LIST 0
+#endif
+#ifndef SPP_STAGE_FILL
+#define SPP_STAGE_FILL 8
+#endif
 
 __device__ __forceinline__ void prefetch_l1(const void* p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
@@ -202,6 +211,22 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
      * minimum-image corrections (they would not change any separation). */
     const int inner = fabsf(pi.x) < k.interior && fabsf(pi.y) < k.interior;
     const int all_inner = __all_sync(__activemask(), inner);
+#if SPP_STAGE_SMEM_LIST
+    /* the thread's list entries (up to SPP_STAGE_SMEM_LIST of them) are
+     * fetched first, SPP_STAGE_FILL at a time with their loads in flight
+     * together, into the thread's column of shared memory: the walk then
+     * waits on one global round trip per group (the neighbour states) */
+    __shared__ int32_t slist[SPP_STAGE_SMEM_LIST][SPP_BLOCK];
+    const int q_fill = min(q_end, q_begin + SPP_STAGE_SMEM_LIST);
+    for (int q = q_begin; q < q_fill; q += SPP_STAGE_FILL) {
+      int32_t v[SPP_STAGE_FILL];
+#pragma unroll
+      for (int u = 0; u < SPP_STAGE_FILL; ++u) v[u] = q + u < q_fill ? __ldg(nb + (size_t)(q + u) * stride) : 0;
+#pragma unroll
+      for (int u = 0; u < SPP_STAGE_FILL; ++u)
+        if (q + u < q_fill) slist[q + u - q_begin][threadIdx.x] = v[u];
+    }
+#endif
     /* list entries and neighbour states are loaded SPP_STAGE_GROUP at a time
      * (independent loads in flight), the pairs evaluated in list order */
     for (int q0 = q_begin; q0 < q_end; q0 += SPP_STAGE_GROUP) {
@@ -209,7 +234,12 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
       float4 pg[SPP_STAGE_GROUP];
 #pragma unroll
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
-        jg[u] = q0 + u < q_end ? __ldg(nb + (size_t)(q0 + u) * stride) : i;
+        const int q = q0 + u;
+#if SPP_STAGE_SMEM_LIST
+        jg[u] = q < q_end ? (q < q_fill ? slist[q - q_begin][threadIdx.x] : __ldg(nb + (size_t)q * stride)) : i;
+#else
+        jg[u] = q < q_end ? __ldg(nb + (size_t)q * stride) : i;
+#endif
         if (!spp_index_ok(d.ctl, jg[u], d.n)) jg[u] = i;
       }
 #pragma unroll

@@ -294,10 +294,13 @@ int spp_polarization_series(SppSystem* s, int nframes, int every, double* p, dou
   OCUDA(cudaMalloc((void**)&sums, sizeof(unsigned long long) * 2 * (size_t)nframes));
   std::vector<long long> host(2 * (size_t)nframes);
   cudaError_t e = cudaMemsetAsync(sums, 0, sizeof(unsigned long long) * 2 * (size_t)nframes, st);
+  /* the Verlet-list models may freeze on a full neighbour list; their frames
+   * wait for the steps (re-run by spp_sync) before P is read.  The Vicsek
+   * models have no list: their frames queue up without host round trips. */
+  const bool listed = k.model == SPP_MODEL_ABP || k.model == SPP_MODEL_CONTINUOUS || k.model == SPP_MODEL_BEADS;
   for (int f = 0; f < nframes && rc == SPP_OK && e == cudaSuccess; ++f) {
     rc = spp_step(s, every);
-    /* a step that froze on a full neighbour list is re-run here, before P is read */
-    if (rc == SPP_OK) rc = spp_sync(s);
+    if (rc == SPP_OK && listed) rc = spp_sync(s);
     if (rc == SPP_OK) {
       rc = spp_internal_view(s, &d, &k, &st);
       launch_polarization_into(d, sums + 2 * (size_t)f, st);
@@ -308,6 +311,7 @@ int spp_polarization_series(SppSystem* s, int nframes, int every, double* p, dou
   if (rc == SPP_OK && e == cudaSuccess)
     e = cudaMemcpyAsync(host.data(), sums, sizeof(long long) * host.size(), cudaMemcpyDeviceToHost, st);
   if (rc == SPP_OK && e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (rc == SPP_OK && e == cudaSuccess && !listed) rc = spp_sync(s);   /* device-side status */
   cudaFree(sums);
   if (rc != SPP_OK) return rc;
   if (e != cudaSuccess) return ofail(SPP_ERR_CUDA, cudaGetErrorString(e));
