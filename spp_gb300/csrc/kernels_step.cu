@@ -246,11 +246,16 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) pg[u] = __ldg(b.cur + jg[u]);
 #pragma unroll
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
-        /* the minimum image only off the interior of a periodic box */
-        if (all_inner || CLOSED)
-          stage_pair<LAW, KIND>(k, d, 0, &a, nbi, jg[u], pi, pg[u], q0 + u < q_end);
-        else
-          stage_pair<LAW, KIND>(k, d, 1, &a, nbi, jg[u], pi, pg[u], q0 + u < q_end);
+        /* entries past the list end are skipped (a warp whose lanes all
+         * reached their ends skips the whole term); the term itself has no
+         * branches.  The minimum image only off the interior of a periodic
+         * box. */
+        if (q0 + u < q_end) {
+          if (all_inner || CLOSED)
+            stage_pair<LAW, KIND>(k, d, 0, &a, nbi, jg[u], pi, pg[u], 1);
+          else
+            stage_pair<LAW, KIND>(k, d, 1, &a, nbi, jg[u], pi, pg[u], 1);
+        }
       }
     }
     if (LANES > 1) {
