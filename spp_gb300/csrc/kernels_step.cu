@@ -91,7 +91,7 @@ __device__ __forceinline__ void finish_step(const SppConsts& k, const DevState& 
 }
 
 #ifndef SPP_STAGE_GROUP
-#define SPP_STAGE_GROUP 3        /* neighbours whose loads are issued together (1: one-ahead prefetch) */
+#define SPP_STAGE_GROUP 2        /* neighbours whose loads are issued together (1: one-ahead prefetch) */
 #endif
 
 /* One neighbour's contribution; the chain kind also needs the neighbour's
@@ -120,7 +120,7 @@ __device__ __forceinline__ void stage_pair(const SppConsts& k, const DevState& d
  * price of registers held through it); 2 after the walk, with L1 prefetches
  * of their lines issued before it (the overlap without the registers). */
 #ifndef SPP_STAGE_PREFETCH
-#define SPP_STAGE_PREFETCH 2
+#define SPP_STAGE_PREFETCH 0
 #endif
 /* List entries of a thread kept in shared memory during the walk (0: read
  * from global memory group by group) and how many of their loads are issued
