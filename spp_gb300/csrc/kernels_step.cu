@@ -47,8 +47,8 @@ struct StageBufs {
 __device__ __forceinline__ void finish_step(const SppConsts& k, const DevState& d, float my_disp2,
                                             float my_step2, cudaGraphConditionalHandle cond,
                                             int use_cond) {
-  __shared__ float warp_disp[SPP_BLOCK / 32];
-  __shared__ float warp_step[SPP_BLOCK / 32];
+  __shared__ float warp_disp[32];   /* one per warp of the block (at most 32) */
+  __shared__ float warp_step[32];
   __shared__ int is_last;
   const float m1 = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(my_disp2)));
   const float m2 = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(my_step2)));
@@ -110,8 +110,11 @@ __device__ __forceinline__ void stage_pair(const SppConsts& k, const DevState& d
   }
 }
 
+#ifndef SPP_STAGE_BLOCK
+#define SPP_STAGE_BLOCK 256      /* threads per block of the stage kernel */
+#endif
 #ifndef SPP_STAGE_MIN_BLOCKS
-#define SPP_STAGE_MIN_BLOCKS 8   /* 8 x 256 threads per SM: 32 registers */
+#define SPP_STAGE_MIN_BLOCKS (2048 / SPP_STAGE_BLOCK)   /* a full SM: 32 registers */
 #endif
 /* Where the stage kernel fetches the per-particle inputs that the
  * neighbour walk does not need (heading, the step's noise and start-of-step
@@ -161,7 +164,7 @@ __device__ __forceinline__ void stage_inputs(const DevState& d, const StageBufs&
  * position) is loaded before the neighbour walk, so those loads overlap it,
  * and the frozen flag is read alongside rather than ahead of them. */
 template <int LAW, int KIND, int LANES, int CLOSED>
-__global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_STAGE_MIN_BLOCKS) k_abp_stage(SppConsts k, DevState d, StageBufs b,
+__global__ void __launch_bounds__(SPP_STAGE_BLOCK, KIND == SPP_KIND_CHAIN ? 1024 / SPP_STAGE_BLOCK : SPP_STAGE_MIN_BLOCKS) k_abp_stage(SppConsts k, DevState d, StageBufs b,
                                                          cudaGraphConditionalHandle cond,
                                                          int use_cond) {
   constexpr bool BEADLIKE = (KIND == SPP_KIND_BEADS || KIND == SPP_KIND_CHAIN);
@@ -216,7 +219,7 @@ __global__ void __launch_bounds__(SPP_BLOCK, KIND == SPP_KIND_CHAIN ? 4 : SPP_ST
      * fetched first, SPP_STAGE_FILL at a time with their loads in flight
      * together, into the thread's column of shared memory: the walk then
      * waits on one global round trip per group (the neighbour states) */
-    __shared__ int32_t slist[SPP_STAGE_SMEM_LIST][SPP_BLOCK];
+    __shared__ int32_t slist[SPP_STAGE_SMEM_LIST][SPP_STAGE_BLOCK];
     const int q_fill = min(q_end, q_begin + SPP_STAGE_SMEM_LIST);
     for (int q = q_begin; q < q_fill; q += SPP_STAGE_FILL) {
       int32_t v[SPP_STAGE_FILL];
@@ -672,26 +675,26 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
   }
   const int kind = spp_pair_kind(&k);
   const int lanes = (kind == SPP_KIND_BEADS || kind == SPP_KIND_CHAIN) ? 1 : k.lanes;
-  int nb = blocks_for(d.n * lanes);
+  int nb = (d.n * lanes + SPP_STAGE_BLOCK - 1) / SPP_STAGE_BLOCK;
   if (nb == 0) nb = 1;
   /* closed boxes (walls) exist for the ABP and continuous kinds only */
 #define SPP_STAGE_CASE(L, K)                                                                   \
   if (k.force_law == L && kind == K) {                                                        \
     if (lanes == SPP_GATHER_LANES)                                                            \
-      k_abp_stage<L, K, SPP_GATHER_LANES, 0><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond); \
+      k_abp_stage<L, K, SPP_GATHER_LANES, 0><<<nb, SPP_STAGE_BLOCK, 0, s>>>(k, d, b, cond, use_cond); \
     else                                                                                      \
-      k_abp_stage<L, K, 1, 0><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond);             \
+      k_abp_stage<L, K, 1, 0><<<nb, SPP_STAGE_BLOCK, 0, s>>>(k, d, b, cond, use_cond);             \
   } else
 #define SPP_STAGE_CASE_W(L, K)                                                                 \
   if (k.force_law == L && kind == K) {                                                        \
     if (lanes == SPP_GATHER_LANES && k.closed)                                                \
-      k_abp_stage<L, K, SPP_GATHER_LANES, 1><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond); \
+      k_abp_stage<L, K, SPP_GATHER_LANES, 1><<<nb, SPP_STAGE_BLOCK, 0, s>>>(k, d, b, cond, use_cond); \
     else if (lanes == SPP_GATHER_LANES)                                                       \
-      k_abp_stage<L, K, SPP_GATHER_LANES, 0><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond); \
+      k_abp_stage<L, K, SPP_GATHER_LANES, 0><<<nb, SPP_STAGE_BLOCK, 0, s>>>(k, d, b, cond, use_cond); \
     else if (k.closed)                                                                        \
-      k_abp_stage<L, K, 1, 1><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond);             \
+      k_abp_stage<L, K, 1, 1><<<nb, SPP_STAGE_BLOCK, 0, s>>>(k, d, b, cond, use_cond);             \
     else                                                                                      \
-      k_abp_stage<L, K, 1, 0><<<nb, SPP_BLOCK, 0, s>>>(k, d, b, cond, use_cond);             \
+      k_abp_stage<L, K, 1, 0><<<nb, SPP_STAGE_BLOCK, 0, s>>>(k, d, b, cond, use_cond);             \
   } else
   SPP_STAGE_CASE_W(SPP_FORCE_HARMONIC, SPP_KIND_ABP)
   SPP_STAGE_CASE_W(SPP_FORCE_R12_TRUNC, SPP_KIND_ABP)
@@ -708,7 +711,7 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
 #undef SPP_STAGE_CASE_W
   if (launches) *launches += 1;
   if (nstages == 1) {
-    k_commit<<<nb, SPP_BLOCK, 0, s>>>(d);
+    k_commit<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(d);
     if (launches) *launches += 1;
   }
 }

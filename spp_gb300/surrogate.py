@@ -221,9 +221,38 @@ class SweepResult:
     timings: dict
 
 
+def pilot_points(points, candidates, count, how, seed):
+    """The pilot subset: `count` of the `candidates` (indices).  how="random":
+    a seeded random draw.  how="cheap": the parameter plane (eta, rho) is cut
+    into a 6 x 6 grid of strata, and each stratum gives its smallest systems
+    in proportion to its share of the candidates, so the pilot still covers
+    the plane while its full runs, which every later decision waits for,
+    take a small share of the particle-steps."""
+    candidates = np.asarray(candidates)
+    if how == "random":
+        return np.random.default_rng(seed).permutation(candidates)[:count]
+    eta = np.array([points[i].eta for i in candidates])
+    rho = np.array([points[i].n / (4.0 * points[i].L * points[i].L) for i in candidates])
+    size = np.array([points[i].n for i in candidates])
+    def cut(v):
+        edges = np.quantile(v, np.linspace(0, 1, 7)[1:-1])
+        return np.searchsorted(edges, v, side="right")
+    stratum = cut(eta) * 6 + cut(rho)
+    picked = []
+    frac = count / len(candidates)
+    for s_ in np.unique(stratum):
+        members = np.flatnonzero(stratum == s_)
+        members = members[np.argsort(size[members], kind="stable")]
+        picked.extend(members[:max(1, int(round(frac * len(members))))].tolist())
+    picked = np.array(picked)
+    if len(picked) > count:   # rounding: drop the largest
+        picked = picked[np.argsort(size[picked], kind="stable")][:count]
+    return candidates[picked]
+
+
 def run_sweep(points, max_steps=20000, window=500, pilot_frac=0.2, holdout_frac=0.1, tol=0.02,
               max_rounds=2, run_frac=0.5, surrogate=None, seed=4, x0=None, use_surrogate=True,
-              chunk=2000, exchange=None):
+              chunk=2000, exchange=None, pilot_select="random"):
     """Runs the sweep and returns a SweepResult.  With use_surrogate=False
     every point runs to the end (the plain batched sweep).
 
@@ -253,7 +282,10 @@ def run_sweep(points, max_steps=20000, window=500, pilot_frac=0.2, holdout_frac=
     heldout[order[:n_hold]] = True
     pilot = np.zeros(n, bool)
     n_pilot = max(2, int(round(pilot_frac * n)))
-    pilot[order[n_hold:n_hold + n_pilot]] = True
+    if pilot_select == "random":
+        pilot[order[n_hold:n_hold + n_pilot]] = True
+    else:
+        pilot[pilot_points(points, order[n_hold:], n_pilot, pilot_select, seed)] = True
     stationary_from = max_steps // 2
     x, y, th = x0 if x0 is not None else configs.sweep_state(points, seed=seed)
     sizes = np.array([p.n for p in points], np.int64)
