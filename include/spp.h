@@ -296,6 +296,24 @@ typedef struct SppRingShape {
   double sw_cm_x, sw_cm_y, sw_xx, sw_yy, sw_xy, sw_lambda1, sw_lambda2, sw_Rg, sw_Delta;
 } SppRingShape;
 int spp_ring_shapes(SppSystem* s, SppRingShape* out, int n_rings);
+/* The motion terms of Box::Compute_All_Variables (parallel/beadbox.h:325-434)
+ * per ring vesicle, between the frame of the last mark and now.  The
+ * reference keeps r_original, theta and t of a saved frame
+ * (Save_Particles_Positions, :315-322); spp_ring_motion_mark saves the same
+ * on the device.  spp_ring_motion then gives, with v = (r - r_old) / (t -
+ * t_old) and the swimmers' spin = (theta - theta_old, folded to [-pi, pi))
+ * / (t - t_old): the centre-of-mass velocities, the angular momenta about
+ * the centres (the swimmers' in the membrane's frame, as the reference
+ * writes it), the rotation rates mb_l / (mb_xx + mb_yy) and sw_l / (sw_xx +
+ * sw_yy + |mb_cm - sw_cm|^2), and the mean swimmer spin; then it marks the
+ * current frame, as the reference does.  SPP_ERR_INVALID without a mark or
+ * if no step was taken since it. */
+typedef struct SppRingMotion {
+  double mb_v_cm_x, mb_v_cm_y, mb_l, mb_omega;
+  double sw_v_cm_x, sw_v_cm_y, sw_l, sw_omega, sw_spin;
+} SppRingMotion;
+int spp_ring_motion_mark(SppSystem* s);
+int spp_ring_motion(SppSystem* s, SppRingMotion* out, int n_rings);
 
 /* ---- batches of independent systems (parameter sweeps) ----
  * Replaces the task farm of serial/mpi-main.cpp:157-176 (one MPI rank per

@@ -122,3 +122,37 @@ def ring_shape(x, y):
     l2 = 0.5 * (xx + yy) - 0.5 * root
     return dict(cm_x=cx, cm_y=cy, xx=xx, yy=yy, xy=xy, lambda1=l1, lambda2=l2, Rg=math.sqrt(xx + yy),
                 Delta=((l1 - l2) / (l1 + l2)) ** 2)
+
+
+def ring_motion(mb_now, mb_old, sw_now, sw_old, th_now, th_old, elapsed):
+    """Box::Compute_All_Variables' motion terms (parallel/beadbox.h:325-434)
+    of one vesicle in FP64, from the unwrapped positions (x, y) of its
+    membrane beads and swimmers now and at the marked frame, the swimmers'
+    headings then and now, and the time between the frames: the centre-of-
+    mass velocities, the angular momenta, the rotation rates and the mean
+    swimmer spin (the heading change folded as the reference folds it)."""
+    mx, my = (np.asarray(a, np.float64) for a in mb_now)
+    ox, oy = (np.asarray(a, np.float64) for a in mb_old)
+    sx, sy = (np.asarray(a, np.float64) for a in sw_now)
+    px, py = (np.asarray(a, np.float64) for a in sw_old)
+    Nm, Ns = len(mx), len(sx)
+    mvx, mvy = (mx - ox) / elapsed, (my - oy) / elapsed
+    svx, svy = (sx - px) / elapsed, (sy - py) / elapsed
+    dth = np.asarray(th_now, np.float64) - np.asarray(th_old, np.float64)
+    dth -= 2 * math.pi * np.floor(dth / (2 * math.pi))
+    dth -= 2 * math.pi * np.floor(dth / math.pi)
+    mcx, mcy = mx.sum() / Nm, my.sum() / Nm
+    scx, scy = sx.sum() / Ns, sy.sum() / Ns
+    mb_v = (mvx.sum() / Nm, mvy.sum() / Nm)
+    sw_v = (svx.sum() / Ns, svy.sum() / Ns)
+    mxx = (mx * mx).sum() / Nm - mcx * mcx
+    myy = (my * my).sum() / Nm - mcy * mcy
+    sxx = (sx * sx).sum() / Ns - scx * scx
+    syy = (sy * sy).sum() / Ns - scy * scy
+    mb_l = (mx * mvy - my * mvx).sum() / Nm - mcx * mb_v[1] + mcy * mb_v[0]
+    sw_l = ((sx * svy - sy * svx).sum() / Ns - scx * mb_v[1] + scy * mb_v[0] - mcx * sw_v[1] + mcy * sw_v[0]
+            + mcx * mb_v[1] - mcy * mb_v[0])
+    return dict(mb_v_cm_x=mb_v[0], mb_v_cm_y=mb_v[1], mb_l=mb_l, mb_omega=mb_l / (mxx + myy),
+                sw_v_cm_x=sw_v[0], sw_v_cm_y=sw_v[1], sw_l=sw_l,
+                sw_omega=sw_l / (sxx + syy + (mcx - scx) ** 2 + (mcy - scy) ** 2),
+                sw_spin=(dth / elapsed).sum() / Ns)

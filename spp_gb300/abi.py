@@ -72,6 +72,11 @@ class SppObservables(C.Structure):
     ]
 
 
+class SppRingMotion(C.Structure):
+    _fields_ = [(f, C.c_double) for f in ("mb_v_cm_x", "mb_v_cm_y", "mb_l", "mb_omega", "sw_v_cm_x",
+                                          "sw_v_cm_y", "sw_l", "sw_omega", "sw_spin")]
+
+
 class SppProfile(C.Structure):
     _fields_ = [("steps", C.c_int64), ("stage_launches", C.c_int64), ("stage_ms", C.c_double),
                 ("rebuilds", C.c_int64), ("rebuild_ms", C.c_double), ("total_ms", C.c_double)]
@@ -180,6 +185,8 @@ PROTOTYPES = {
     "spp_radial_distribution": (C.c_int, [_P, C.c_double, C.c_int, _U64]),
     "spp_pair_distribution": (C.c_int, [_P, C.c_double, C.c_double, C.c_int, C.c_int, _U64]),
     "spp_ring_shapes": (C.c_int, [_P, C.POINTER(SppRingShape), C.c_int]),
+    "spp_ring_motion_mark": (C.c_int, [_P]),
+    "spp_ring_motion": (C.c_int, [_P, C.c_void_p, C.c_int]),
     "spp_mlp_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(_P)]),
     "spp_mlp_destroy": (C.c_int, [_P]),
     "spp_mlp_num_params": (C.c_int, [_P]),

@@ -63,6 +63,11 @@ struct SppSystem {
   int64_t graph_kernels = 0;
   int64_t direct_rebuilds = 0;
   int64_t regrowths = 0;         /* neighbour-list regrowths after an overflow */
+  /* frame marked for spp_ring_motion: unwrapped positions and headings by
+   * particle id, and the step counter at the mark (-1: none) */
+  double2* mark_xy = nullptr;
+  float* mark_th = nullptr;
+  int64_t mark_step = -1;
   int64_t target_step = 0;       /* step the caller has asked to reach */
   int64_t step0 = 0;
   bool uploaded = false;
@@ -118,6 +123,11 @@ void free_lyap(SppSystem* s) {
 }
 
 void free_dev(SppSystem* s) {
+  if (s->mark_xy) cudaFree(s->mark_xy);
+  if (s->mark_th) cudaFree(s->mark_th);
+  s->mark_xy = nullptr;
+  s->mark_th = nullptr;
+  s->mark_step = -1;
   DevState& d = s->d;
   void* ptrs[] = {d.pos, d.half, d.half2, d.theta, d.img, d.id, d.inv, d.kacc, d.dth, d.ref, d.pos_alt,
                   d.theta_alt, d.img_alt, d.id_alt, d.key, d.rank, d.cell_count, d.cell_start,
@@ -562,6 +572,24 @@ void spp_internal_count_launches(SppSystem* s, int n) {
   if (s) s->host_launches += n;
 }
 
+int spp_internal_mark(SppSystem* s, double2** xy, float** th, int64_t** step) {
+  if (!s->mark_xy) {
+    int rc = dalloc(&s->mark_xy, (size_t)s->p.n);
+    if (rc == SPP_OK) rc = dalloc(&s->mark_th, (size_t)s->p.n);
+    if (rc != SPP_OK) return rc;
+  }
+  *xy = s->mark_xy;
+  *th = s->mark_th;
+  *step = &s->mark_step;
+  return SPP_OK;
+}
+
+int64_t spp_internal_step(SppSystem* s) {
+  Ctl c;
+  if (read_ctl(s, &c) != SPP_OK) return -1;
+  return (int64_t)c.step;
+}
+
 extern "C" {
 
 int spp_abi_version(void) { return SPP_ABI_VERSION; }
@@ -817,6 +845,7 @@ int spp_upload_state(SppSystem* s, const float* x, const float* y, const float* 
   s->step0 = step0;
   s->target_step = step0;
   s->uploaded = true;
+  s->mark_step = -1;   /* a new state: no frame marked */
   return recover(s);
 }
 

@@ -171,6 +171,70 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_obs_ring_sums(DevState d, SppCons
   if (threadIdx.x < 5) sums[(size_t)blockIdx.x * 5 + threadIdx.x] = red[threadIdx.x][0];
 }
 
+/* Positions (unwrapped, FP64) and headings of every particle, by id: the
+ * frame spp_ring_motion measures from (Save_Particles_Positions,
+ * parallel/beadbox.h:315-322). */
+__global__ void __launch_bounds__(SPP_BLOCK) k_obs_mark(DevState d, SppConsts k, double2* xy, float* th) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n) return;
+  const uint32_t id = d.id[i];
+  const float4 p = d.pos[i];
+  const int2 g = d.img[i];
+  xy[id] = make_double2((double)p.x + (double)k.L2 * (double)g.x, (double)p.y + (double)k.L2 * (double)g.y);
+  th[id] = d.theta[i];
+}
+
+/* Per ring, sums over its beads (block 2r) and its swimmers (block 2r + 1)
+ * of x, y, x^2, y^2, xy, v_x, v_y, x v_y - y v_x and (swimmers) the spin,
+ * with v = (r - r_marked) / elapsed and the spin the heading change folded
+ * to [-pi, pi) as beadbox.h:354-356 folds it, over elapsed; FP64, fixed
+ * reduction tree. */
+constexpr int MOTION_SUMS = 9;
+__global__ void __launch_bounds__(SPP_BLOCK) k_obs_ring_motion(DevState d, SppConsts k, int n_rings, int ring_size,
+                                                               int sw_per_ring, const double2* mxy,
+                                                               const float* mth, double inv_elapsed,
+                                                               double* sums) {
+  __shared__ double red[MOTION_SUMS][SPP_BLOCK];
+  const int ring = blockIdx.x >> 1, part = blockIdx.x & 1;
+  const int first = part == 0 ? ring * ring_size : n_rings * ring_size + ring * sw_per_ring;
+  const int count = part == 0 ? ring_size : sw_per_ring;
+  double a[MOTION_SUMS];
+  for (int c = 0; c < MOTION_SUMS; ++c) a[c] = 0.0;
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int q = threadIdx.x; q < count; q += blockDim.x) {
+    const uint32_t id = (uint32_t)(first + q);
+    const uint32_t slot = d.inv[id];
+    const float4 p = d.pos[slot];
+    const int2 g = d.img[slot];
+    const double x = (double)p.x + (double)k.L2 * (double)g.x;
+    const double y = (double)p.y + (double)k.L2 * (double)g.y;
+    const double2 m = mxy[id];
+    const double vx = (x - m.x) * inv_elapsed, vy = (y - m.y) * inv_elapsed;
+    a[0] += x;
+    a[1] += y;
+    a[2] += x * x;
+    a[3] += y * y;
+    a[4] += x * y;
+    a[5] += vx;
+    a[6] += vy;
+    a[7] += x * vy - y * vx;
+    if (part == 1) {
+      double dth = (double)d.theta[slot] - (double)mth[id];
+      dth -= two_pi * floor(dth / two_pi);
+      dth -= two_pi * floor(dth / (0.5 * two_pi));
+      a[8] += dth * inv_elapsed;
+    }
+  }
+  for (int c = 0; c < MOTION_SUMS; ++c) red[c][threadIdx.x] = a[c];
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int c = 0; c < MOTION_SUMS; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < MOTION_SUMS) sums[(size_t)blockIdx.x * MOTION_SUMS + threadIdx.x] = red[threadIdx.x][0];
+}
+
 /* The reference's formulas (beadbox.h:402-428) from the five sums of n points. */
 void shape_from_sums(const double* m, int n, double* cm_x, double* cm_y, double* xx, double* yy, double* xy,
                      double* l1, double* l2, double* rg, double* delta) {
@@ -406,6 +470,98 @@ int spp_ring_shapes(SppSystem* s, SppRingShape* out, int n_rings) {
       shape_from_sums(&h[10 * (size_t)r + 5], sw, &o.sw_cm_x, &o.sw_cm_y, &o.sw_xx, &o.sw_yy, &o.sw_xy,
                       &o.sw_lambda1, &o.sw_lambda2, &o.sw_Rg, &o.sw_Delta);
   }
+  return SPP_OK;
+}
+
+int spp_ring_motion_mark(SppSystem* s) {
+  if (!s) return ofail(SPP_ERR_INVALID, "NULL argument");
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  DevState d;
+  SppConsts k;
+  cudaStream_t st;
+  rc = spp_internal_view(s, &d, &k, &st);
+  if (rc != SPP_OK) return rc;
+  double2* xy;
+  float* th;
+  int64_t* step;
+  rc = spp_internal_mark(s, &xy, &th, &step);
+  if (rc != SPP_OK) return rc;
+  k_obs_mark<<<nblk(d.n), SPP_BLOCK, 0, st>>>(d, k, xy, th);
+  spp_internal_count_launches(s, 1);
+  OCUDA(cudaGetLastError());
+  const int64_t now = spp_internal_step(s);   /* waits for the stream */
+  if (now < 0) return ofail(SPP_ERR_CUDA, "ring motion: reading the step counter failed");
+  *step = now;
+  return SPP_OK;
+}
+
+int spp_ring_motion(SppSystem* s, SppRingMotion* out, int n_rings) {
+  if (!s || !out) return ofail(SPP_ERR_INVALID, "NULL argument");
+  int rc = spp_sync(s);
+  if (rc != SPP_OK) return rc;
+  DevState d;
+  SppConsts k;
+  cudaStream_t st;
+  rc = spp_internal_view(s, &d, &k, &st);
+  if (rc != SPP_OK) return rc;
+  if (k.model != SPP_MODEL_BEADS || k.n_beads <= 0 || k.ring_size <= 0)
+    return ofail(SPP_ERR_INVALID, "ring motion needs a bead model with rings");
+  const int nr = k.n_beads / k.ring_size;
+  if (n_rings != nr) return ofail(SPP_ERR_INVALID, "n_rings differs from the system's ring count");
+  double2* xy;
+  float* th;
+  int64_t* mark;
+  rc = spp_internal_mark(s, &xy, &th, &mark);
+  if (rc != SPP_OK) return rc;
+  if (*mark < 0) return ofail(SPP_ERR_INVALID, "no frame marked: call spp_ring_motion_mark first");
+  const int64_t now = spp_internal_step(s);
+  if (now < 0) return ofail(SPP_ERR_CUDA, "ring motion: reading the step counter failed");
+  if (now <= *mark) return ofail(SPP_ERR_INVALID, "no step taken since the marked frame");
+  const double elapsed = (double)(now - *mark) * (double)k.dt;
+  const int sw = (d.n - k.n_beads) / nr;
+  double* sums = nullptr;
+  OCUDA(cudaMalloc((void**)&sums, sizeof(double) * 2 * MOTION_SUMS * (size_t)nr));
+  k_obs_ring_motion<<<2 * nr, SPP_BLOCK, 0, st>>>(d, k, nr, k.ring_size, sw, xy, th, 1.0 / elapsed, sums);
+  spp_internal_count_launches(s, 1);
+  std::vector<double> h(2 * MOTION_SUMS * (size_t)nr);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), sums, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(sums);
+  if (e != cudaSuccess) return ofail(SPP_ERR_CUDA, std::string("ring motion: ") + cudaGetErrorString(e));
+  for (int r = 0; r < nr; ++r) {
+    /* Compute_All_Variables, parallel/beadbox.h:385-428 */
+    const double* m = &h[2 * MOTION_SUMS * (size_t)r];
+    const double* w = m + MOTION_SUMS;
+    const double Nm = k.ring_size, Ns = sw;
+    SppRingMotion& o = out[r];
+    memset(&o, 0, sizeof(o));
+    const double mcx = m[0] / Nm, mcy = m[1] / Nm;
+    o.mb_v_cm_x = m[5] / Nm;
+    o.mb_v_cm_y = m[6] / Nm;
+    const double mxx = m[2] / Nm - mcx * mcx, myy = m[3] / Nm - mcy * mcy;
+    o.mb_l = m[7] / Nm - mcx * o.mb_v_cm_y + mcy * o.mb_v_cm_x;
+    o.mb_omega = o.mb_l / (mxx + myy);
+    if (sw > 0) {
+      const double scx = w[0] / Ns, scy = w[1] / Ns;
+      o.sw_v_cm_x = w[5] / Ns;
+      o.sw_v_cm_y = w[6] / Ns;
+      const double sxx = w[2] / Ns - scx * scx, syy = w[3] / Ns - scy * scy;
+      o.sw_l = w[7] / Ns - scx * o.mb_v_cm_y + scy * o.mb_v_cm_x - mcx * o.sw_v_cm_y + mcy * o.sw_v_cm_x +
+               mcx * o.mb_v_cm_y - mcy * o.mb_v_cm_x;
+      o.sw_spin = w[8] / Ns;
+      const double dcx = mcx - scx, dcy = mcy - scy;
+      o.sw_omega = o.sw_l / (sxx + syy + dcx * dcx + dcy * dcy);
+    }
+  }
+  /* the current frame becomes the marked one (Save_Particles_Positions at
+   * the end of Compute_All_Variables) */
+  k_obs_mark<<<nblk(d.n), SPP_BLOCK, 0, st>>>(d, k, xy, th);
+  spp_internal_count_launches(s, 1);
+  OCUDA(cudaGetLastError());
+  OCUDA(cudaStreamSynchronize(st));
+  *mark = now;
   return SPP_OK;
 }
 

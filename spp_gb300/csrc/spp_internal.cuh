@@ -96,6 +96,11 @@ struct DevState {
  * (observables.cu), and the host-launch counter */
 int spp_internal_view(SppSystem* s, DevState* d, SppConsts* k, cudaStream_t* st);
 void spp_internal_count_launches(SppSystem* s, int n);
+/* api.cu: the marked-frame buffers of spp_ring_motion (n entries each, by
+ * particle id; allocated on first use) and the mark's step (-1: none) */
+int spp_internal_mark(SppSystem* s, double2** xy, float** th, int64_t** step);
+/* api.cu: the absolute step counter (waits for the stream); -1 on error */
+int64_t spp_internal_step(SppSystem* s);
 
 /* api.cu: sets the message spp_last_error() returns on the calling thread */
 void spp_internal_set_error(const char* msg);

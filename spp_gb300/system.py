@@ -215,6 +215,21 @@ class System:
         abi.check(abi.lib().spp_ring_shapes(self._h, out, nr), "spp_ring_shapes")
         return {name: np.array([getattr(o, name) for o in out]) for name, _ in abi.SppRingShape._fields_}
 
+    def ring_motion_mark(self):
+        """Save the current frame (positions and headings) for ring_motion
+        (Save_Particles_Positions, parallel/beadbox.h:315-322)."""
+        abi.check(abi.lib().spp_ring_motion_mark(self._h), "spp_ring_motion_mark")
+
+    def ring_motion(self):
+        """Per ring vesicle, the motion since the marked frame: centre-of-mass
+        velocities, angular momenta, rotation rates and the swimmers' mean spin
+        (Box::Compute_All_Variables, parallel/beadbox.h:325-434); marks the
+        current frame.  Returns a dict of arrays."""
+        nr = int(self.params.n_rings)
+        out = (abi.SppRingMotion * nr)()
+        abi.check(abi.lib().spp_ring_motion(self._h, out, nr), "spp_ring_motion")
+        return {name: np.array([getattr(o, name) for o in out]) for name, _ in abi.SppRingMotion._fields_}
+
     def profile(self, nsteps):
         pr = abi.SppProfile()
         abi.check(abi.lib().spp_profile(self._h, int(nsteps), C.byref(pr)), "spp_profile")

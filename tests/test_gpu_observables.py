@@ -7,7 +7,7 @@ import pytest
 
 from oracle import analysis_oracle as A
 from oracle import oracle as O
-from spp_gb300 import Batch, System, configs, observables
+from spp_gb300 import SppError, Batch, System, configs, observables
 
 pytestmark = pytest.mark.gpu
 
@@ -154,6 +154,46 @@ def test_ring_shapes_match_fp64(gpu_lib):
             assert shapes["sw_" + key][r] == pytest.approx(v, rel=1e-7, abs=1e-7), key
         # a ring of 64 beads at rest length 1 stays near-circular: R ~ 10.2, Delta small
         assert 9.0 < shapes["mb_Rg"][r] < 11.5 and shapes["mb_Delta"][r] < 0.05
+
+
+def test_ring_motion_matches_fp64(gpu_lib):
+    """The motion terms of Compute_All_Variables (parallel/beadbox.h:325-434)
+    per ring vesicle -- centre-of-mass velocities, angular momenta, rotation
+    rates, mean swimmer spin -- between a marked frame and the frame 60 steps
+    later, against the FP64 restatement on the same two frames; a second call
+    measures from the frame the first one marked."""
+    p = configs.vesicle_config(n_rings=16, ring_size=64, swimmers_per_ring=8)
+    x, y, th = configs.vesicle_state(p)
+    M, nr = p.ring_size, p.n_rings
+    sw = (p.n - nr * M) // nr
+
+    def frame(s):
+        gx, gy, gth, gix, giy = s.download()
+        return (gx.astype(np.float64) + 2 * p.L * gix, gy.astype(np.float64) + 2 * p.L * giy, gth)
+
+    with System(p) as s:
+        s.upload(x, y, th)
+        with pytest.raises(SppError):
+            s.ring_motion()                 # nothing marked yet
+        s.step(100)
+        s.ring_motion_mark()
+        f0 = frame(s)
+        s.step(60)
+        m1 = s.ring_motion()
+        f1 = frame(s)
+        s.step(40)
+        m2 = s.ring_motion()
+        f2 = frame(s)
+    for m, (a, b), steps in ((m1, (f0, f1), 60), (m2, (f1, f2), 40)):
+        for r in range(nr):
+            q0 = nr * M + r * sw
+            mb, swm = slice(r * M, (r + 1) * M), slice(q0, q0 + sw)
+            ref = A.ring_motion((b[0][mb], b[1][mb]), (a[0][mb], a[1][mb]), (b[0][swm], b[1][swm]),
+                                (a[0][swm], a[1][swm]), b[2][swm], a[2][swm], steps * p.dt)
+            for key, v in ref.items():
+                assert m[key][r] == pytest.approx(v, rel=1e-9, abs=1e-9), (key, r)
+    # swimmers turn at k_perp torque0 and the membranes drift slowly
+    assert np.all(np.abs(m1["mb_v_cm_x"]) < 1.0) and np.all(np.isfinite(m1["sw_omega"]))
 
 
 def test_radial_distribution_in_a_closed_box(gpu_lib):
