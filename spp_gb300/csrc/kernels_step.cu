@@ -90,6 +90,62 @@ __device__ __forceinline__ void finish_step(const SppConsts& k, const DevState& 
   }
 }
 
+/* The same bookkeeping without block-wide barriers, for the stage kernel:
+ * each warp folds its maxima into the block's shared words (fin[0..1], the
+ * float bits of non-negative values, so unsigned max is float max) and
+ * counts itself done in fin[2]; the warp that arrives last does the block's
+ * global part.  Warps that finish early leave at once instead of waiting at
+ * a barrier for the block's slowest warp.  fin is zeroed by the caller
+ * before any warp can arrive. */
+__device__ __forceinline__ void finish_step_nb(const SppConsts& k, const DevState& d, float my_disp2,
+                                               float my_step2, cudaGraphConditionalHandle cond,
+                                               int use_cond, unsigned* fin) {
+  const unsigned m1 = __reduce_max_sync(0xffffffffu, __float_as_uint(my_disp2));
+  const unsigned m2 = __reduce_max_sync(0xffffffffu, __float_as_uint(my_step2));
+  if ((threadIdx.x & 31) != 0) return;
+  atomicMax(&fin[0], m1);
+  atomicMax(&fin[1], m2);
+  __threadfence_block();
+  const unsigned done = atomicAdd(&fin[2], 1u);
+  if (done != (blockDim.x >> 5) - 1u) return;
+  /* the block's last warp */
+  __threadfence_block();
+  const unsigned b1 = atomicAdd(&fin[0], 0u), b2 = atomicAdd(&fin[1], 0u);
+  if (b1 > 0u) atomicMax(&d.ctl->dmax2_bits, b1);
+  if (b2 > 0u) atomicMax(&d.ctl->smax2_bits, b2);
+  __threadfence();
+  const unsigned prev = atomicAdd(&d.ctl->blocks_done, 1u);
+  if (prev != gridDim.x - 1) return;
+  /* the grid's last block decides, as finish_step does */
+  __threadfence();
+  volatile Ctl* c = d.ctl;
+  const int frozen = c->frozen;
+  const float dm = sqrtf(__uint_as_float(c->dmax2_bits));
+  const float sm = sqrtf(__uint_as_float(c->smax2_bits));
+  unsigned rebuild = 0u;
+  if (!frozen && k.half_skin > 0.0f) {
+    rebuild = (dm + 2.0f * sm > k.half_skin) ? 1u : 0u;
+    if (dm > k.half_skin) c->late_rebuilds = c->late_rebuilds + 1u;
+  }
+  c->need_rebuild = rebuild;
+  c->dmax2_bits = 0u;
+  c->smax2_bits = 0u;
+  c->blocks_done = 0u;
+  if (!frozen) c->step = c->step + 1u;
+  if (use_cond) cudaGraphSetConditional(cond, rebuild);
+}
+
+/* Stage-kernel shape knobs: SPP_STAGE_UNIFORM 1 walks the neighbour lists
+ * in warp-uniform trips up to the warp's longest list, masking the terms of
+ * lanes past their own end (no divergent loop exits); SPP_STAGE_FINISH_NB 1
+ * uses finish_step_nb. */
+#ifndef SPP_STAGE_UNIFORM
+#define SPP_STAGE_UNIFORM 1
+#endif
+#ifndef SPP_STAGE_FINISH_NB
+#define SPP_STAGE_FINISH_NB 1
+#endif
+
 #ifndef SPP_STAGE_GROUP
 #define SPP_STAGE_GROUP 2        /* neighbours whose loads are issued together (1: one-ahead prefetch) */
 #endif
@@ -174,6 +230,13 @@ __global__ void __launch_bounds__(SPP_STAGE_BLOCK, KIND == SPP_KIND_CHAIN ? 1024
   const int last = (b.stage == b.nstages - 1);
   const bool inb = i < d.n;
   const bool head = LANES == 1 || lane_r == 0;   /* the lane that finishes the particle */
+#if SPP_STAGE_FINISH_NB
+  __shared__ unsigned fin[3];
+  if (last) {   /* the same for the whole block */
+    if (threadIdx.x < 3) fin[threadIdx.x] = 0u;
+    __syncthreads();
+  }
+#endif
   float disp2 = 0.0f, step2 = 0.0f;
   float4 pi = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   int q_begin = 0, q_end = 0;
@@ -232,6 +295,37 @@ __global__ void __launch_bounds__(SPP_STAGE_BLOCK, KIND == SPP_KIND_CHAIN ? 1024
 #endif
     /* list entries and neighbour states are loaded SPP_STAGE_GROUP at a time
      * (independent loads in flight), the pairs evaluated in list order */
+#if SPP_STAGE_UNIFORM
+    /* trips up to the warp's longest list, the same for every lane: lanes
+     * past their own end load their own state and mask the term */
+    const int my_len = q_end - q_begin;
+    const int wmax = (int)__reduce_max_sync(__activemask(), (unsigned)my_len);
+    for (int t0 = 0; t0 < wmax; t0 += SPP_STAGE_GROUP) {
+      int jg[SPP_STAGE_GROUP];
+      float4 pg[SPP_STAGE_GROUP];
+#pragma unroll
+      for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
+        const int q = q_begin + t0 + u;
+#if SPP_STAGE_SMEM_LIST
+        jg[u] = t0 + u < my_len ? (q < q_fill ? slist[q - q_begin][threadIdx.x] : __ldg(nb + (size_t)q * stride)) : i;
+#else
+        jg[u] = t0 + u < my_len ? __ldg(nb + (size_t)q * stride) : i;
+#endif
+        if (!spp_index_ok(d.ctl, jg[u], d.n)) jg[u] = i;
+      }
+#pragma unroll
+      for (int u = 0; u < SPP_STAGE_GROUP; ++u) pg[u] = __ldg(b.cur + jg[u]);
+#pragma unroll
+      for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
+        if (t0 + u < wmax) {   /* warp-uniform */
+          if (all_inner || CLOSED)
+            stage_pair<LAW, KIND>(k, d, 0, &a, nbi, jg[u], pi, pg[u], t0 + u < my_len);
+          else
+            stage_pair<LAW, KIND>(k, d, 1, &a, nbi, jg[u], pi, pg[u], t0 + u < my_len);
+        }
+      }
+    }
+#else
     for (int q0 = q_begin; q0 < q_end; q0 += SPP_STAGE_GROUP) {
       int jg[SPP_STAGE_GROUP];
       float4 pg[SPP_STAGE_GROUP];
@@ -261,6 +355,7 @@ __global__ void __launch_bounds__(SPP_STAGE_BLOCK, KIND == SPP_KIND_CHAIN ? 1024
         }
       }
     }
+#endif
     if (LANES > 1) {
       /* the lanes of one particle are consecutive and all present */
       const unsigned gmask = ((1u << LANES) - 1u) << ((threadIdx.x & 31) & ~(LANES - 1));
@@ -366,7 +461,11 @@ __global__ void __launch_bounds__(SPP_STAGE_BLOCK, KIND == SPP_KIND_CHAIN ? 1024
     }
   }
   }
+#if SPP_STAGE_FINISH_NB
+  if (last) finish_step_nb(k, d, disp2, step2, cond, use_cond, fin);
+#else
   if (last) finish_step(k, d, disp2, step2, cond, use_cond);
+#endif
 }
 
 __global__ void __launch_bounds__(SPP_BLOCK) k_vicsek_step(SppConsts k, DevState d) {
