@@ -584,6 +584,8 @@ int spp_internal_mark(SppSystem* s, double2** xy, float** th, int64_t** step) {
   return SPP_OK;
 }
 
+double spp_internal_dt(SppSystem* s) { return s->p.dt; }
+
 int64_t spp_internal_step(SppSystem* s) {
   Ctl c;
   if (read_ctl(s, &c) != SPP_OK) return -1;

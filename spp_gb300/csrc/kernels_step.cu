@@ -137,10 +137,12 @@ __device__ __forceinline__ void finish_step_nb(const SppConsts& k, const DevStat
 
 /* Stage-kernel shape knobs: SPP_STAGE_UNIFORM 1 walks the neighbour lists
  * in warp-uniform trips up to the warp's longest list, masking the terms of
- * lanes past their own end (no divergent loop exits); SPP_STAGE_FINISH_NB 1
- * uses finish_step_nb. */
+ * lanes past their own end (no divergent loop exits; measured slower at the
+ * 1M workload, 33.3 against 32.7 us per launch: the masked terms cost more
+ * than the divergence); SPP_STAGE_FINISH_NB 1 uses finish_step_nb (32.7
+ * against 33.0 us). */
 #ifndef SPP_STAGE_UNIFORM
-#define SPP_STAGE_UNIFORM 1
+#define SPP_STAGE_UNIFORM 0
 #endif
 #ifndef SPP_STAGE_FINISH_NB
 #define SPP_STAGE_FINISH_NB 1

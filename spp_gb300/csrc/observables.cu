@@ -518,7 +518,7 @@ int spp_ring_motion(SppSystem* s, SppRingMotion* out, int n_rings) {
   const int64_t now = spp_internal_step(s);
   if (now < 0) return ofail(SPP_ERR_CUDA, "ring motion: reading the step counter failed");
   if (now <= *mark) return ofail(SPP_ERR_INVALID, "no step taken since the marked frame");
-  const double elapsed = (double)(now - *mark) * (double)k.dt;
+  const double elapsed = (double)(now - *mark) * spp_internal_dt(s);
   const int sw = (d.n - k.n_beads) / nr;
   double* sums = nullptr;
   OCUDA(cudaMalloc((void**)&sums, sizeof(double) * 2 * MOTION_SUMS * (size_t)nr));

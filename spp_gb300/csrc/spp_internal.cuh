@@ -101,6 +101,8 @@ void spp_internal_count_launches(SppSystem* s, int n);
 int spp_internal_mark(SppSystem* s, double2** xy, float** th, int64_t** step);
 /* api.cu: the absolute step counter (waits for the stream); -1 on error */
 int64_t spp_internal_step(SppSystem* s);
+/* api.cu: the time step as given (double) */
+double spp_internal_dt(SppSystem* s);
 
 /* api.cu: sets the message spp_last_error() returns on the calling thread */
 void spp_internal_set_error(const char* msg);
