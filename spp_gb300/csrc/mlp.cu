@@ -19,6 +19,7 @@
  */
 #include <cuda_bf16.h>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -123,6 +124,294 @@ __global__ void __launch_bounds__(H) k_mlp_forward(MlpDev m) {
     for (int q2 = 0; q2 < H / 32; ++q2) yy += red[j][q2];
     m.y[(size_t)e * m.B + s0 + j] = yy;
   }
+}
+
+/* ------------------------------------------------------------------ */
+/* tensor-core path: the 128 x 128 layer on mma.sync (TF32, FP32 sums)  */
+/* ------------------------------------------------------------------ */
+/* m16n8k8 TF32 products with FP32 accumulation.  BF16 weights are exact in
+ * TF32; an FP32 operand x is split into x_hi = tf32(x) and x_lo = tf32(x -
+ * x_hi), and the products taken as hi*w + lo*w (weights) or hi*hi + hi*lo +
+ * lo*hi (two FP32 operands), which keeps the FP32 accuracy of the scalar
+ * kernels (relative error ~2^-21 per product).  Fragment layout of m16n8k8
+ * (groupID g = lane / 4, t = lane % 4): A a0 (g, t), a1 (g+8, t), a2 (g,
+ * t+4), a3 (g+8, t+4); B b0 (k t, n g), b1 (k t+4, n g); C c0 (g, 2t), c1
+ * (g, 2t+1), c2 (g+8, 2t), c3 (g+8, 2t+1). */
+__device__ __forceinline__ uint32_t tf32_bits(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ void tf32_split(float x, uint32_t* hi, uint32_t* lo) {
+  *hi = tf32_bits(x);
+  *lo = tf32_bits(x - __uint_as_float(*hi));
+}
+__device__ __forceinline__ void mma_tf32(float* c, const uint32_t* a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+constexpr int TS = 32;        /* samples per block of k_mlp_fused */
+constexpr int WP = H + 4;     /* padded row stride of W2 in shared memory (floats) */
+constexpr int HP = H + 4;     /* padded row stride of the activation tiles */
+constexpr size_t FUSED_SMEM = sizeof(float) * ((size_t)H * WP + 2 * (size_t)TS * HP + (size_t)TS * H + 2 * TS);
+
+/* Forward (and with BACKWARD the per-sample deltas) of one member on TS
+ * samples, 4 warps: layer 1 and the output layer as FP32 FMAs, the 128 x
+ * 128 layer and its transpose on the tensor cores.  Writes the same arrays
+ * as k_mlp_forward / k_mlp_backward. */
+template <bool BACKWARD>
+__global__ void __launch_bounds__(H) k_mlp_fused(MlpDev m) {
+  extern __shared__ float fsm[];
+  float* w2f = fsm;                 /* [H][WP]: W2[j][k] */
+  float* hs = w2f + H * WP;         /* [TS][HP]: h1 */
+  float* t2 = hs + TS * HP;         /* [TS][HP]: h2, then dz2 */
+  float* zs1 = t2 + TS * HP;        /* [TS][H]: z1 */
+  float* dys = zs1 + TS * H;        /* [TS]: dy */
+  float* yts = dys + TS;            /* [TS]: y */
+  const int e = blockIdx.y;
+  const int s0 = blockIdx.x * TS;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, t = lane & 3;
+  const int in = m.in, P = n_params(in);
+  const __nv_bfloat16* w = m.w + (size_t)e * P;
+  const int nq = m.B - s0 < TS ? m.B - s0 : TS;
+  for (int idx = tid; idx < H * H; idx += H) w2f[(idx / H) * WP + (idx % H)] = __bfloat162float(w[off_w2(in) + idx]);
+  /* layer 1: thread j, every sample of the tile (rows past the batch: 0) */
+  {
+    const int j = tid;
+    const float b1j = __bfloat162float(w[off_b1(in) + j]);
+    for (int q = 0; q < TS; ++q) {
+      float z = 0.0f, h = 0.0f;
+      if (q < nq) {
+        const int sidx = s0 + q;
+        z = b1j;
+        for (int k = 0; k < in; ++k) z = fmaf(__bfloat162float(w[j * in + k]), m.x[(size_t)sidx * in + k], z);
+        h = gelu(z, nullptr);
+        const size_t es = ((size_t)e * m.B + sidx) * H + j;
+        m.z1[es] = z;
+        m.h1[es] = h;
+      }
+      zs1[q * H + j] = z;
+      hs[q * HP + j] = h;
+    }
+  }
+  __syncthreads();
+  /* z2 = h1 W2^T + b2: warp w owns columns [32 w, 32 w + 32), both 16-row halves */
+  float acc[2][4][4];
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[mt][nt][c] = 0.0f;
+  for (int k0 = 0; k0 < H; k0 += 8) {
+    uint32_t ah[2][4], al[2][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+      const int r = mt * 16 + g;
+      tf32_split(hs[r * HP + k0 + t], &ah[mt][0], &al[mt][0]);
+      tf32_split(hs[(r + 8) * HP + k0 + t], &ah[mt][1], &al[mt][1]);
+      tf32_split(hs[r * HP + k0 + t + 4], &ah[mt][2], &al[mt][2]);
+      tf32_split(hs[(r + 8) * HP + k0 + t + 4], &ah[mt][3], &al[mt][3]);
+    }
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+      const int n = warp * 32 + nt * 8 + g;
+      const uint32_t b0 = __float_as_uint(w2f[n * WP + k0 + t]);
+      const uint32_t b1 = __float_as_uint(w2f[n * WP + k0 + t + 4]);
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt) {
+        mma_tf32(acc[mt][nt], ah[mt], b0, b1);
+        mma_tf32(acc[mt][nt], al[mt], b0, b1);
+      }
+    }
+  }
+  /* z2, h2 */
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int q = mt * 16 + g + (c >= 2 ? 8 : 0);
+        const int j = warp * 32 + nt * 8 + 2 * t + (c & 1);
+        const float z2 = acc[mt][nt][c] + __bfloat162float(w[off_b2(in) + j]);
+        acc[mt][nt][c] = z2;
+        const float h2 = gelu(z2, nullptr);
+        t2[q * HP + j] = q < nq ? h2 : 0.0f;
+        if (q < nq) {
+          const size_t es = ((size_t)e * m.B + s0 + q) * H + j;
+          m.z2[es] = z2;
+          m.h2[es] = h2;
+        }
+      }
+  __syncthreads();
+  /* y = b3 + sum_j W3[j] h2[j], j in order, one thread per sample */
+  if (tid < nq) {
+    float yy = __bfloat162float(w[off_b3(in)]);
+    for (int j = 0; j < H; ++j) yy = fmaf(__bfloat162float(w[off_w3(in) + j]), t2[tid * HP + j], yy);
+    yts[tid] = yy;
+    m.y[(size_t)e * m.B + s0 + tid] = yy;
+    if (BACKWARD) {
+      const size_t es = (size_t)e * m.B + s0 + tid;
+      const float dy = 2.0f * m.sw[es] * (yy - m.t[s0 + tid]);
+      m.dy[es] = dy;
+      dys[tid] = dy;
+    }
+  } else if (tid < TS) {
+    dys[tid] = 0.0f;
+  }
+  if (!BACKWARD) return;
+  __syncthreads();
+  /* dz2 = dy W3[j] gelu'(z2), into the tile and global memory */
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int q = mt * 16 + g + (c >= 2 ? 8 : 0);
+        const int j = warp * 32 + nt * 8 + 2 * t + (c & 1);
+        float g2;
+        gelu(acc[mt][nt][c], &g2);
+        const float dz2 = dys[q] * __bfloat162float(w[off_w3(in) + j]) * g2;
+        t2[q * HP + j] = dz2;
+        if (q < nq) m.dz2[((size_t)e * m.B + s0 + q) * H + j] = dz2;
+      }
+  __syncthreads();
+  /* dh1 = dz2 W2 (sum over j), dz1 = dh1 gelu'(z1) */
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[mt][nt][c] = 0.0f;
+  for (int k0 = 0; k0 < H; k0 += 8) {
+    uint32_t ah[2][4], al[2][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+      const int r = mt * 16 + g;
+      tf32_split(t2[r * HP + k0 + t], &ah[mt][0], &al[mt][0]);
+      tf32_split(t2[(r + 8) * HP + k0 + t], &ah[mt][1], &al[mt][1]);
+      tf32_split(t2[r * HP + k0 + t + 4], &ah[mt][2], &al[mt][2]);
+      tf32_split(t2[(r + 8) * HP + k0 + t + 4], &ah[mt][3], &al[mt][3]);
+    }
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+      const int n = warp * 32 + nt * 8 + g;
+      const uint32_t b0 = __float_as_uint(w2f[(k0 + t) * WP + n]);
+      const uint32_t b1 = __float_as_uint(w2f[(k0 + t + 4) * WP + n]);
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt) {
+        mma_tf32(acc[mt][nt], ah[mt], b0, b1);
+        mma_tf32(acc[mt][nt], al[mt], b0, b1);
+      }
+    }
+  }
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int q = mt * 16 + g + (c >= 2 ? 8 : 0);
+        const int k = warp * 32 + nt * 8 + 2 * t + (c & 1);
+        if (q < nq) {
+          float g1;
+          gelu(zs1[q * H + k], &g1);
+          m.dz1[((size_t)e * m.B + s0 + q) * H + k] = acc[mt][nt][c] * g1;
+        }
+      }
+}
+
+/* Gradient of W2 on the tensor cores: dW2[j][k] = sum_s dz2[s][j] h1[s][k]
+ * (both FP32: hi*hi + hi*lo + lo*hi), one block of 4 warps per (member, 32 x
+ * 32 tile), the samples streamed through shared memory 32 at a time.  Each
+ * warp owns a 16 x 16 quarter (two m16n8 tiles).  Blocks with blockIdx.x ==
+ * 16 do the other parameters instead: thread j sums over the samples in
+ * order (W1, b1, b2, W3; thread 0 also b3). */
+constexpr int GS = 32;            /* samples per chunk */
+constexpr int GP = 36;            /* padded row stride of the chunk tiles */
+__global__ void __launch_bounds__(H) k_mlp_grads_tc(MlpDev m, float* grad) {
+  const int e = blockIdx.y;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int in = m.in, P = n_params(in);
+  const size_t eb = (size_t)e * m.B;
+  float* ge = grad + (size_t)e * P;
+  if (blockIdx.x == 16) {
+    const int j = tid;
+    float gb1 = 0.0f, gb2 = 0.0f, gw3 = 0.0f, gb3 = 0.0f;
+    float gw1[MAX_IN];
+#pragma unroll
+    for (int k = 0; k < MAX_IN; ++k) gw1[k] = 0.0f;
+    for (int sidx = 0; sidx < m.B; ++sidx) {
+      const float d1 = m.dz1[(eb + sidx) * H + j];
+      const float d2 = m.dz2[(eb + sidx) * H + j];
+      const float dy = m.dy[eb + sidx];
+#pragma unroll
+      for (int k = 0; k < MAX_IN; ++k)
+        if (k < in) gw1[k] = fmaf(d1, m.x[(size_t)sidx * in + k], gw1[k]);
+      gb1 += d1;
+      gb2 += d2;
+      gw3 = fmaf(dy, m.h2[(eb + sidx) * H + j], gw3);
+      gb3 += dy;
+    }
+    for (int k = 0; k < in; ++k) ge[j * in + k] = gw1[k];
+    ge[off_b1(in) + j] = gb1;
+    ge[off_b2(in) + j] = gb2;
+    ge[off_w3(in) + j] = gw3;
+    if (j == 0) ge[off_b3(in)] = gb3;
+    return;
+  }
+  __shared__ float dzs[GS][GP];   /* dz2[s][j0 + c] */
+  __shared__ float hsm[GS][GP];   /* h1[s][k0 + c] */
+  const int j0 = (blockIdx.x >> 2) * 32, k0 = (blockIdx.x & 3) * 32;
+  const int g = lane >> 2, t = lane & 3;
+  const int wm = (warp >> 1) * 16, wn = (warp & 1) * 16;   /* the warp's quarter */
+  float acc[2][4];
+#pragma unroll
+  for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[nt][c] = 0.0f;
+  for (int c0 = 0; c0 < m.B; c0 += GS) {
+    const int nc = m.B - c0 < GS ? m.B - c0 : GS;
+    for (int idx = tid; idx < GS * 32; idx += H) {
+      const int r = idx >> 5, c = idx & 31;
+      dzs[r][c] = r < nc ? m.dz2[(eb + c0 + r) * H + j0 + c] : 0.0f;
+      hsm[r][c] = r < nc ? m.h1[(eb + c0 + r) * H + k0 + c] : 0.0f;
+    }
+    __syncthreads();
+    for (int s8 = 0; s8 < GS; s8 += 8) {
+      /* A[j][s] = dz2[s][j]; B[s][k] = h1[s][k] */
+      uint32_t ah[4], al[4];
+      tf32_split(dzs[s8 + t][wm + g], &ah[0], &al[0]);
+      tf32_split(dzs[s8 + t][wm + g + 8], &ah[1], &al[1]);
+      tf32_split(dzs[s8 + t + 4][wm + g], &ah[2], &al[2]);
+      tf32_split(dzs[s8 + t + 4][wm + g + 8], &ah[3], &al[3]);
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) {
+        uint32_t bh0, bl0, bh1, bl1;
+        tf32_split(hsm[s8 + t][wn + nt * 8 + g], &bh0, &bl0);
+        tf32_split(hsm[s8 + t + 4][wn + nt * 8 + g], &bh1, &bl1);
+        mma_tf32(acc[nt], ah, bh0, bh1);
+        mma_tf32(acc[nt], ah, bl0, bl1);
+        mma_tf32(acc[nt], al, bh0, bh1);
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int j = j0 + wm + g + (c >= 2 ? 8 : 0);
+      const int k = k0 + wn + nt * 8 + 2 * t + (c & 1);
+      ge[off_w2(in) + (size_t)j * H + k] = acc[nt][c];
+    }
 }
 
 /* Per-sample deltas of the weighted squared error L_e = sum_s sw[e][s] (y - t)^2
@@ -301,6 +590,9 @@ struct SppMlp {
   int* tix = nullptr;
   /* graphs of TRAIN_GRAPH_ITERS training iterations, keyed by (B, lr) */
   struct TrainGraph { int B; float lr; cudaGraph_t graph; cudaGraphExec_t exec; };
+  /* the 128 x 128 layer on the tensor cores (k_mlp_fused, k_mlp_grads_tc);
+   * SPP_MLP_SCALAR=1 at creation selects the scalar FP32 kernels */
+  bool tensor_cores = true;
   std::vector<TrainGraph> graphs;
 };
 
@@ -393,6 +685,16 @@ int mlp_upload(SppMlp* m, const float* x, const float* t, const float* weights, 
 
 void mlp_fwd_bwd(SppMlp* m, int B, bool backward) {
   MlpDev d = mlp_dev(m, B);
+  if (m->tensor_cores) {
+    dim3 grid((B + TS - 1) / TS, m->E);
+    if (!backward) {
+      k_mlp_fused<false><<<grid, H, FUSED_SMEM, m->stream>>>(d);
+      return;
+    }
+    k_mlp_fused<true><<<grid, H, FUSED_SMEM, m->stream>>>(d);
+    k_mlp_grads_tc<<<dim3(17, m->E), H, 0, m->stream>>>(d, m->grad);
+    return;
+  }
   dim3 grid((B + CHUNK - 1) / CHUNK, m->E);
   k_mlp_forward<<<grid, H, 0, m->stream>>>(d);
   if (!backward) return;
@@ -451,6 +753,14 @@ int spp_mlp_create(int ensemble, int in_dim, SppMlp** out) {
   if (e == cudaSuccess) e = cudaMalloc((void**)&m->vel, sizeof(float) * tot);
   if (e == cudaSuccess) e = cudaMalloc((void**)&m->grad, sizeof(float) * tot);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking);
+  {
+    const char* env = getenv("SPP_MLP_SCALAR");
+    m->tensor_cores = !(env && env[0] == '1');
+  }
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_mlp_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FUSED_SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_mlp_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FUSED_SMEM);
   if (e == cudaSuccess) e = cudaMemset(m->master, 0, sizeof(float) * tot);
   if (e == cudaSuccess) e = cudaMemset(m->w, 0, sizeof(__nv_bfloat16) * tot);
   if (e == cudaSuccess) e = cudaMemset(m->mom, 0, sizeof(float) * tot);

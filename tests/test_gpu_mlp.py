@@ -94,3 +94,23 @@ def test_invalid_weights_are_rejected(gpu_lib):
     with pytest.raises(abi.SppError):
         mlp.train(x, t, iters=1, weights=w)
     mlp.close()
+
+
+def test_tensor_core_and_scalar_kernels_agree(gpu_lib, monkeypatch):
+    """The 128 x 128 layer on the tensor cores (TF32 products of split FP32
+    operands, FP32 sums) against the scalar FP32 kernels (SPP_MLP_SCALAR=1):
+    outputs and gradients agree to FP32 rounding."""
+    x, t = data(B=150)
+    outs = []
+    for scalar in ("0", "1"):
+        monkeypatch.setenv("SPP_MLP_SCALAR", scalar)
+        mlp = surrogate.Mlp(ensemble=3, seed=5)
+        y = mlp.predict(x)
+        g, loss = mlp.grad(x, t)
+        outs.append((y, g, loss))
+        mlp.close()
+    (y0, g0, l0), (y1, g1, l1) = outs
+    assert np.max(np.abs(y0 - y1)) < 1e-5
+    for e in range(3):
+        assert np.linalg.norm(g0[e] - g1[e]) / np.linalg.norm(g1[e]) < 1e-5
+    assert np.allclose(l0, l1, rtol=1e-5)
