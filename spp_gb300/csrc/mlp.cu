@@ -154,7 +154,11 @@ __device__ __forceinline__ void mma_tf32(float* c, const uint32_t* a, uint32_t b
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-constexpr int TS = 32;        /* samples per block of k_mlp_fused */
+#ifndef SPP_MLP_TS
+#define SPP_MLP_TS 16
+#endif
+constexpr int TS = SPP_MLP_TS; /* samples per block of k_mlp_fused (a multiple of 16) */
+constexpr int MT = TS / 16;     /* m16 tiles per block */
 constexpr int WP = H + 4;     /* padded row stride of W2 in shared memory (floats) */
 constexpr int HP = H + 4;     /* padded row stride of the activation tiles */
 constexpr size_t FUSED_SMEM = sizeof(float) * ((size_t)H * WP + 2 * (size_t)TS * HP + (size_t)TS * H + 2 * TS);
@@ -200,18 +204,18 @@ __global__ void __launch_bounds__(H) k_mlp_fused(MlpDev m) {
     }
   }
   __syncthreads();
-  /* z2 = h1 W2^T + b2: warp w owns columns [32 w, 32 w + 32), both 16-row halves */
-  float acc[2][4][4];
+  /* z2 = h1 W2^T + b2: warp w owns columns [32 w, 32 w + 32), every 16-row tile */
+  float acc[MT][4][4];
 #pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
+  for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
       for (int c = 0; c < 4; ++c) acc[mt][nt][c] = 0.0f;
   for (int k0 = 0; k0 < H; k0 += 8) {
-    uint32_t ah[2][4], al[2][4];
+    uint32_t ah[MT][4], al[MT][4];
 #pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
+    for (int mt = 0; mt < MT; ++mt) {
       const int r = mt * 16 + g;
       tf32_split(hs[r * HP + k0 + t], &ah[mt][0], &al[mt][0]);
       tf32_split(hs[(r + 8) * HP + k0 + t], &ah[mt][1], &al[mt][1]);
@@ -224,7 +228,7 @@ __global__ void __launch_bounds__(H) k_mlp_fused(MlpDev m) {
       const uint32_t b0 = __float_as_uint(w2f[n * WP + k0 + t]);
       const uint32_t b1 = __float_as_uint(w2f[n * WP + k0 + t + 4]);
 #pragma unroll
-      for (int mt = 0; mt < 2; ++mt) {
+      for (int mt = 0; mt < MT; ++mt) {
         mma_tf32(acc[mt][nt], ah[mt], b0, b1);
         mma_tf32(acc[mt][nt], al[mt], b0, b1);
       }
@@ -232,7 +236,7 @@ __global__ void __launch_bounds__(H) k_mlp_fused(MlpDev m) {
   }
   /* z2, h2 */
 #pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
+  for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
@@ -269,7 +273,7 @@ __global__ void __launch_bounds__(H) k_mlp_fused(MlpDev m) {
   __syncthreads();
   /* dz2 = dy W3[j] gelu'(z2), into the tile and global memory */
 #pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
+  for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
@@ -285,15 +289,15 @@ __global__ void __launch_bounds__(H) k_mlp_fused(MlpDev m) {
   __syncthreads();
   /* dh1 = dz2 W2 (sum over j), dz1 = dh1 gelu'(z1) */
 #pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
+  for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
       for (int c = 0; c < 4; ++c) acc[mt][nt][c] = 0.0f;
   for (int k0 = 0; k0 < H; k0 += 8) {
-    uint32_t ah[2][4], al[2][4];
+    uint32_t ah[MT][4], al[MT][4];
 #pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
+    for (int mt = 0; mt < MT; ++mt) {
       const int r = mt * 16 + g;
       tf32_split(t2[r * HP + k0 + t], &ah[mt][0], &al[mt][0]);
       tf32_split(t2[(r + 8) * HP + k0 + t], &ah[mt][1], &al[mt][1]);
@@ -306,14 +310,14 @@ __global__ void __launch_bounds__(H) k_mlp_fused(MlpDev m) {
       const uint32_t b0 = __float_as_uint(w2f[(k0 + t) * WP + n]);
       const uint32_t b1 = __float_as_uint(w2f[(k0 + t + 4) * WP + n]);
 #pragma unroll
-      for (int mt = 0; mt < 2; ++mt) {
+      for (int mt = 0; mt < MT; ++mt) {
         mma_tf32(acc[mt][nt], ah[mt], b0, b1);
         mma_tf32(acc[mt][nt], al[mt], b0, b1);
       }
     }
   }
 #pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
+  for (int mt = 0; mt < MT; ++mt)
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
@@ -331,9 +335,8 @@ __global__ void __launch_bounds__(H) k_mlp_fused(MlpDev m) {
 /* Gradient of W2 on the tensor cores: dW2[j][k] = sum_s dz2[s][j] h1[s][k]
  * (both FP32: hi*hi + hi*lo + lo*hi), one block of 4 warps per (member, 32 x
  * 32 tile), the samples streamed through shared memory 32 at a time.  Each
- * warp owns a 16 x 16 quarter (two m16n8 tiles).  Blocks with blockIdx.x ==
- * 16 do the other parameters instead: thread j sums over the samples in
- * order (W1, b1, b2, W3; thread 0 also b3). */
+ * warp owns a 16 x 16 quarter (two m16n8 tiles).  The other parameters
+ * are k_mlp_grad's (one thread per parameter). */
 constexpr int GS = 32;            /* samples per chunk */
 constexpr int GP = 36;            /* padded row stride of the chunk tiles */
 __global__ void __launch_bounds__(H) k_mlp_grads_tc(MlpDev m, float* grad) {
@@ -342,31 +345,6 @@ __global__ void __launch_bounds__(H) k_mlp_grads_tc(MlpDev m, float* grad) {
   const int in = m.in, P = n_params(in);
   const size_t eb = (size_t)e * m.B;
   float* ge = grad + (size_t)e * P;
-  if (blockIdx.x == 16) {
-    const int j = tid;
-    float gb1 = 0.0f, gb2 = 0.0f, gw3 = 0.0f, gb3 = 0.0f;
-    float gw1[MAX_IN];
-#pragma unroll
-    for (int k = 0; k < MAX_IN; ++k) gw1[k] = 0.0f;
-    for (int sidx = 0; sidx < m.B; ++sidx) {
-      const float d1 = m.dz1[(eb + sidx) * H + j];
-      const float d2 = m.dz2[(eb + sidx) * H + j];
-      const float dy = m.dy[eb + sidx];
-#pragma unroll
-      for (int k = 0; k < MAX_IN; ++k)
-        if (k < in) gw1[k] = fmaf(d1, m.x[(size_t)sidx * in + k], gw1[k]);
-      gb1 += d1;
-      gb2 += d2;
-      gw3 = fmaf(dy, m.h2[(eb + sidx) * H + j], gw3);
-      gb3 += dy;
-    }
-    for (int k = 0; k < in; ++k) ge[j * in + k] = gw1[k];
-    ge[off_b1(in) + j] = gb1;
-    ge[off_b2(in) + j] = gb2;
-    ge[off_w3(in) + j] = gw3;
-    if (j == 0) ge[off_b3(in)] = gb3;
-    return;
-  }
   __shared__ float dzs[GS][GP];   /* dz2[s][j0 + c] */
   __shared__ float hsm[GS][GP];   /* h1[s][k0 + c] */
   const int j0 = (blockIdx.x >> 2) * 32, k0 = (blockIdx.x & 3) * 32;
@@ -692,7 +670,9 @@ void mlp_fwd_bwd(SppMlp* m, int B, bool backward) {
       return;
     }
     k_mlp_fused<true><<<grid, H, FUSED_SMEM, m->stream>>>(d);
-    k_mlp_grads_tc<<<dim3(17, m->E), H, 0, m->stream>>>(d, m->grad);
+    const long long tot = (long long)m->E * m->P;
+    k_mlp_grad<<<(unsigned)((tot + 255) / 256), 256, 0, m->stream>>>(d, m->grad);
+    k_mlp_grads_tc<<<dim3(16, m->E), H, 0, m->stream>>>(d, m->grad);
     return;
   }
   dim3 grid((B + CHUNK - 1) / CHUNK, m->E);

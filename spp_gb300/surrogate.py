@@ -252,7 +252,7 @@ def pilot_points(points, candidates, count, how, seed):
 
 def run_sweep(points, max_steps=20000, window=500, pilot_frac=0.2, holdout_frac=0.1, tol=0.02,
               max_rounds=2, run_frac=0.5, surrogate=None, seed=4, x0=None, use_surrogate=True,
-              chunk=2000, exchange=None, pilot_select="random"):
+              chunk=2000, exchange=None, pilot_select="random", speculate_frac=0.0):
     """Runs the sweep and returns a SweepResult.  With use_surrogate=False
     every point runs to the end (the plain batched sweep).
 
@@ -309,6 +309,14 @@ def run_sweep(points, max_steps=20000, window=500, pilot_frac=0.2, holdout_frac=
             b.step(window)
             timings["runs_s"] += time.perf_counter() - t0
             f = features(points, b.poll())
+            if speculate_frac > 0:
+                # points likely to stay unsure (the largest start-up-window
+                # variance of P: fluctuating, near the transition) run to the
+                # end with the pilot and join its training data
+                cand = np.flatnonzero(~(pilot | heldout))
+                k_spec = int(round(speculate_frac * n))
+                spec = cand[np.argsort(-f[cand, 5], kind="stable")][:k_spec]
+                pilot[spec] = True
             # only the pilot and held-out points continue for now
             b.retire(np.flatnonzero(~(pilot | heldout)))
         run()
