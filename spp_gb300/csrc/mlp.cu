@@ -332,11 +332,50 @@ __global__ void __launch_bounds__(H) k_mlp_fused(MlpDev m) {
       }
 }
 
+/* Gradients of the parameters outside W2 (W1, b1, b2, W3, b3: 128 in + 385
+ * per member), 8 threads per parameter: thread r sums the samples s = r (mod
+ * 8) in order, and the eight partial sums combine through a fixed butterfly
+ * of xor shuffles (reproducible, no atomics). */
+constexpr int GSPLIT = 8;
+__global__ void __launch_bounds__(256) k_mlp_grad_small(MlpDev m, float* grad) {
+  const int in = m.in, P = n_params(in);
+  const int nsmall = off_w2(in) + (P - off_b2(in));
+  const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long item = gid / GSPLIT;
+  const int r = (int)(gid % GSPLIT);
+  const bool live = item < (long long)m.E * nsmall;   /* whole groups of 8 share it */
+  const int e = live ? (int)(item / nsmall) : 0;
+  const int u = live ? (int)(item % nsmall) : 0;
+  const int q = u < off_w2(in) ? u : u - off_w2(in) + off_b2(in);
+  const size_t eb = (size_t)e * m.B;
+  float g = 0.0f;
+  if (live) {
+    if (q < off_b1(in)) {
+      const int j = q / in, k = q % in;
+      for (int sidx = r; sidx < m.B; sidx += GSPLIT) g = fmaf(m.dz1[(eb + sidx) * H + j], m.x[(size_t)sidx * in + k], g);
+    } else if (q < off_w2(in)) {
+      const int j = q - off_b1(in);
+      for (int sidx = r; sidx < m.B; sidx += GSPLIT) g += m.dz1[(eb + sidx) * H + j];
+    } else if (q < off_w3(in)) {
+      const int j = q - off_b2(in);
+      for (int sidx = r; sidx < m.B; sidx += GSPLIT) g += m.dz2[(eb + sidx) * H + j];
+    } else if (q < off_b3(in)) {
+      const int j = q - off_w3(in);
+      for (int sidx = r; sidx < m.B; sidx += GSPLIT) g = fmaf(m.dy[eb + sidx], m.h2[(eb + sidx) * H + j], g);
+    } else {
+      for (int sidx = r; sidx < m.B; sidx += GSPLIT) g += m.dy[eb + sidx];
+    }
+  }
+#pragma unroll
+  for (int o = 1; o < GSPLIT; o <<= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
+  if (live && r == 0) grad[(size_t)e * P + q] = g;
+}
+
 /* Gradient of W2 on the tensor cores: dW2[j][k] = sum_s dz2[s][j] h1[s][k]
  * (both FP32: hi*hi + hi*lo + lo*hi), one block of 4 warps per (member, 32 x
  * 32 tile), the samples streamed through shared memory 32 at a time.  Each
  * warp owns a 16 x 16 quarter (two m16n8 tiles).  The other parameters
- * are k_mlp_grad's (one thread per parameter). */
+ * are k_mlp_grad_small's. */
 constexpr int GS = 32;            /* samples per chunk */
 constexpr int GP = 36;            /* padded row stride of the chunk tiles */
 __global__ void __launch_bounds__(H) k_mlp_grads_tc(MlpDev m, float* grad) {
@@ -670,8 +709,8 @@ void mlp_fwd_bwd(SppMlp* m, int B, bool backward) {
       return;
     }
     k_mlp_fused<true><<<grid, H, FUSED_SMEM, m->stream>>>(d);
-    const long long tot = (long long)m->E * m->P;
-    k_mlp_grad<<<(unsigned)((tot + 255) / 256), 256, 0, m->stream>>>(d, m->grad);
+    const long long small = (long long)m->E * (off_w2(m->in) + (m->P - off_b2(m->in))) * GSPLIT;
+    k_mlp_grad_small<<<(unsigned)((small + 255) / 256), 256, 0, m->stream>>>(d, m->grad);
     k_mlp_grads_tc<<<dim3(16, m->E), H, 0, m->stream>>>(d, m->grad);
     return;
   }
