@@ -577,6 +577,60 @@ def other_workload(args):
                                                  "60 training iterations of the 5-member surrogate on 300 samples"},
                           "train_ms_per_iteration": train_ms / 60}), flush=True)
         return
+    if w == "stage262k":
+        # the small case of the headline model for full kernel captures: the
+        # same density at a quarter of the particles, 100 steps from the
+        # random start, 200 steps of direct launches timed kernel by kernel
+        # (spp_profile, which a profiler sees), then --steps x 200 graph steps
+        n, L = 262144, 256.0
+        p = configs.abp_config(n=n, L=L, seed=1)
+        x, y, th = configs.random_state(n, L, seed=1)
+        with System(p) as s:
+            s.upload(x, y, th)
+            s.step(100)
+            s.sync()
+            pr = s.profile(200)
+            ms = [s.time_steps(200) for _ in range(max(1, args.steps))]
+            o = s.observables()
+        stage_us = pr.stage_ms / max(1, pr.stage_launches) * 1e3
+        achieved = 40.0 * n / (stage_us * 1e-6) / 1e9
+        print(json.dumps({"metric": "particle-steps/s", "workload": "stage262k",
+                          "value": n * 200 / (min(ms) / 1e3), "unit": "particle-steps/s", "n_gpus": 1,
+                          "ms_per_sim_step": min(ms) / 200, "stage_us": stage_us,
+                          "rebuild_us": pr.rebuild_ms / max(1, pr.rebuilds) * 1e3, "rebuilds_per_200": pr.rebuilds,
+                          "max_neighbors": o.max_neighbors, "list_capacity": o.list_capacity,
+                          "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                       "frac": achieved / peak, "alg_bytes_per_unit": 40},
+                          "config": {"workload": "repulsive ABP with the headline parameters at N=262,144, L=256 "
+                                                 "(the same density), 100 steps in"}}), flush=True)
+        return
+    if w == "mlp":
+        # the surrogate's training iteration (5 members, 7 -> 128 -> 128 -> 1,
+        # 300 samples) with the tensor-core kernels and with the scalar ones
+        from spp_gb300 import surrogate
+        rng = np.random.default_rng(1)
+        f = rng.standard_normal((300, 7)).astype(np.float32)
+        t = (0.5 + 0.3 * np.tanh(f[:, 0])).astype(np.float32)
+        iters = 50 * max(1, args.steps)
+        out = {}
+        for scalar in ("0", "1"):
+            os.environ["SPP_MLP_SCALAR"] = scalar
+            mlp = surrogate.Mlp(ensemble=5, seed=4)
+            mlp.train(f, t, iters=100)
+            t0 = time.perf_counter()
+            loss = mlp.train(f, t, iters=iters)
+            out["scalar" if scalar == "1" else "tensor_cores"] = {
+                "us_per_iteration": (time.perf_counter() - t0) / iters * 1e6,
+                "final_loss": [float(v) for v in loss]}
+            mlp.close()
+        os.environ.pop("SPP_MLP_SCALAR", None)
+        print(json.dumps({"metric": "us per training iteration", "workload": "mlp",
+                          "value": out["tensor_cores"]["us_per_iteration"], "unit": "us",
+                          "higher_is_better": False, "iterations": iters, **out,
+                          "config": {"workload": "5-member ensemble, 7 -> 128 -> 128 -> 1, 300 samples, Adam; "
+                                                 "host wall clock around Mlp.train after 100 warm iterations"}}),
+              flush=True)
+        return
     if w == "sweep" and dist_env()[0] > 1:
         sweep_sharded(args)
         return
@@ -666,7 +720,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-sweep", action="store_true", help="skip the 512-point sweep leg")
     ap.add_argument("--workload", default="abp",
-                    choices=["abp", "vicsek", "vesicles", "lyapunov", "sweep", "batch64"],
+                    choices=["abp", "vicsek", "vesicles", "lyapunov", "sweep", "batch64", "stage262k", "mlp"],
                     help="abp: the headline line (default); the others print their own line")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
