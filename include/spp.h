@@ -179,6 +179,9 @@ typedef struct SppObservables {
                              time step is too large for the skin) */
   int64_t list_regrowths; /* neighbour-list overflows met so far: each one grew the list and re-ran
                              the frozen steps */
+  int64_t bulk_timeouts;  /* warps of the stage kernel whose bulk copy of list rows into shared
+                             memory did not complete within the wait limit; they read the list from
+                             global memory instead (same results; a diagnostic, expected 0) */
 } SppObservables;
 
 typedef struct SppSystem SppSystem;

@@ -39,6 +39,7 @@ def orc():
         L.orc32_pairs.restype = C.c_int64
         L.orc32_cells.argtypes = [_P, _F, _F, C.c_int, C.c_int, _I, _I]
         L.orc32_philox.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.orc32_philox_ks.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.orc32_math.argtypes = [C.c_int, C.c_int, _F, _F, _F]
         L.orc32_fx_sum.argtypes = [C.c_int, _F, _I, _I, _F]
         L.orc32_renormalize.argtypes = [C.c_int, C.c_int, _F, _D, C.c_int]
@@ -351,11 +352,13 @@ def polarization(th):
     return P, px.value, py.value
 
 
-def philox(ctr, key):
+def philox(ctr, key, round_keys=False):
+    """Philox4x32-10 of counter ctr and key (k0, k1); round_keys=True takes
+    the kernels' route through precomputed round keys."""
     c = (C.c_uint32 * 4)(*ctr)
     k = (C.c_uint32 * 2)(*key)
     o = (C.c_uint32 * 4)()
-    orc().orc32_philox(c, k, o)
+    (orc().orc32_philox_ks if round_keys else orc().orc32_philox)(c, k, o)
     return tuple(o)
 
 

@@ -394,6 +394,13 @@ void orc32_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
   spp_u32x4 o = spp_philox4x32_10(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1]);
   memcpy(out, o.v, sizeof(o.v));
 }
+/* The kernels' draw from precomputed round keys (key = the 64-bit seed). */
+void orc32_philox_ks(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t ks[20];
+  spp_philox_round_keys((uint64_t)key[0] | ((uint64_t)key[1] << 32), ks);
+  spp_u32x4 o = spp_philox4x32_10_ks(ctr[0], ctr[1], ctr[2], ctr[3], ks);
+  memcpy(out, o.v, sizeof(o.v));
+}
 void orc32_math(int fn, int n, const float* a, const float* b, float* out) {
   for (int i = 0; i < n; ++i) {
     switch (fn) {

@@ -68,7 +68,7 @@ class SppObservables(C.Structure):
         ("step", C.c_int64), ("t", C.c_double), ("px", C.c_double), ("py", C.c_double),
         ("polarization", C.c_double), ("n_rebuilds", C.c_int64), ("n", C.c_int32),
         ("list_capacity", C.c_int32), ("max_neighbors", C.c_int32), ("cells_per_side", C.c_int32),
-        ("late_rebuilds", C.c_int64), ("list_regrowths", C.c_int64),
+        ("late_rebuilds", C.c_int64), ("list_regrowths", C.c_int64), ("bulk_timeouts", C.c_int64),
     ]
 
 

@@ -690,6 +690,7 @@ int spp_create(const SppParams* p, SppSystem** out) {
   SppSystem* s = new SppSystem();
   s->p = *p;
   spp_consts_from_params(&s->k, p);
+  prepare_abp_stage();
   s->uses_list = (p->model == SPP_MODEL_ABP || p->model == SPP_MODEL_CONTINUOUS ||
                   p->model == SPP_MODEL_BEADS);
   s->nstages = p->integrator == SPP_INT_RK4 ? 4 : (p->integrator == SPP_INT_RK2 ? 2 : 1);
@@ -949,6 +950,7 @@ int spp_observables(SppSystem* s, SppObservables* o) {
   o->cells_per_side = s->d.D;
   o->late_rebuilds = c.late_rebuilds;
   o->list_regrowths = s->regrowths;
+  o->bulk_timeouts = c.bulk_timeouts;
   return SPP_OK;
 }
 

@@ -151,6 +151,15 @@ __device__ __forceinline__ void finish_step_nb(const SppConsts& k, const DevStat
 #ifndef SPP_STAGE_GROUP
 #define SPP_STAGE_GROUP 2        /* neighbours whose loads are issued together (1: one-ahead prefetch) */
 #endif
+/* 1: with load groups of two, the pair's two 1/d are computed together by
+ * two-lane instructions (spp_rsqrtf2).  Measured at the 1M workload 600
+ * steps in: 33.2 us per launch against 31.8 (the extra live values spill
+ * at the 32-register bound a full SM of threads needs); at 40 registers
+ * and 6 blocks per SM it gains 1% (34.6 against 35.0 us), less than the
+ * occupancy costs.  Off. */
+#ifndef SPP_STAGE_RSQRT2
+#define SPP_STAGE_RSQRT2 0
+#endif
 
 /* One neighbour's contribution; the chain kind also needs the neighbour's
  * bead count (1 for membrane beads).  valid = 0 marks a padding entry of a
@@ -192,6 +201,59 @@ __device__ __forceinline__ void stage_pair(const SppConsts& k, const DevState& d
 #ifndef SPP_STAGE_FILL
 #define SPP_STAGE_FILL 8
 #endif
+
+/* List rows copied into shared memory by the bulk-copy engine: with one
+ * lane per particle and n a multiple of 4 (so that every row segment starts
+ * on a 16-byte boundary), lane 0 of each warp copies rows 0 .. R - 1 of the
+ * warp's 32 list columns (the column-major list keeps a row's 32 entries
+ * contiguous: 128 bytes) with cp.async.bulk, R = min(the warp's longest
+ * list, SPP_STAGE_BULK_ROWS), all completing on one mbarrier of the warp.
+ * The walk then takes its list entries from shared memory (entries past R
+ * from global memory) and only the neighbour states from L1/L2, so each
+ * pair waits on one memory round trip instead of two, and the list loads
+ * leave the SM's load pipe.  0 disables.  Measured at the 1M workload 600
+ * steps in (stage us per launch, same trajectory bits, no copy timed out):
+ * 16 rows 38.4, 12 rows 38.6, 8 rows 37.8 against 31.4 without; with the
+ * shared-memory carveout at its maximum (SPP_STAGE_CARVEOUT=100) 16 rows
+ * 38.2, 8 rows 38.6, 4 rows 37.1.  The warp's walk cannot start before all
+ * its rows have landed, and the list loads it saves were not what bound
+ * the kernel.  Off. */
+#ifndef SPP_STAGE_BULK_ROWS
+#define SPP_STAGE_BULK_ROWS 0
+#endif
+/* try_wait polls before a warp gives up on its copies (each poll may
+ * suspend the warp for a while); it then reads the list from global memory
+ * and counts itself in Ctl.bulk_timeouts */
+#define SPP_BULK_WAIT_LIMIT (1 << 20)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void bulk_issue_rows(uint32_t bar, uint32_t dst, const int32_t* src, size_t stride,
+                                                uint32_t bytes, int rows) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes * (uint32_t)rows)
+               : "memory");
+  for (int q = 0; q < rows; ++q)
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     dst + (uint32_t)q * 128u),
+                 "l"(src + (size_t)q * stride), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+/* true once the copies tracked by bar (phase 0) have landed */
+__device__ __forceinline__ bool bulk_wait(uint32_t bar) {
+  for (int it = 0; it < SPP_BULK_WAIT_LIMIT; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
 
 __device__ __forceinline__ void prefetch_l1(const void* p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
@@ -268,6 +330,30 @@ __global__ void __launch_bounds__(SPP_STAGE_BLOCK, KIND == SPP_KIND_CHAIN ? 1024
       }
     }
   }
+#if SPP_STAGE_BULK_ROWS > 0
+  __shared__ __align__(128) int32_t blist[SPP_STAGE_BLOCK / 32][SPP_STAGE_BULK_ROWS][32];
+  __shared__ __align__(8) unsigned long long bbar[SPP_STAGE_BLOCK / 32];
+  const int wl = threadIdx.x & 31, ww = threadIdx.x >> 5;
+  int rows = 0;            /* list rows of this warp in shared memory */
+  bool bulk_late = false;  /* copies issued but not seen complete */
+  if (LANES == 1 && (d.n & 3) == 0) {
+    const int first = tg - wl;   /* the warp's first particle */
+    rows = min((int)__reduce_max_sync(0xffffffffu, (unsigned)q_end), SPP_STAGE_BULK_ROWS);
+    if (first >= d.n) rows = 0;
+    if (rows > 0) {
+      const uint32_t bar = smem_u32(&bbar[ww]);
+      if (wl == 0)
+        bulk_issue_rows(bar, smem_u32(&blist[ww][0][0]), d.nbr + first, (size_t)d.n,
+                        (uint32_t)min(32, d.n - first) * 4u, rows);
+      __syncwarp();
+      if (!__all_sync(0xffffffffu, bulk_wait(bar))) {
+        bulk_late = true;
+        rows = 0;
+        if (wl == 0) atomicAdd(&d.ctl->bulk_timeouts, 1u);
+      }
+    }
+  }
+#endif
   const int frozen = d.ctl->frozen;
   if (inb && !frozen) {
     SppAccF a;
@@ -336,6 +422,8 @@ __global__ void __launch_bounds__(SPP_STAGE_BLOCK, KIND == SPP_KIND_CHAIN ? 1024
         const int q = q0 + u;
 #if SPP_STAGE_SMEM_LIST
         jg[u] = q < q_end ? (q < q_fill ? slist[q - q_begin][threadIdx.x] : __ldg(nb + (size_t)q * stride)) : i;
+#elif SPP_STAGE_BULK_ROWS > 0
+        jg[u] = q < q_end ? (q < rows ? blist[ww][q][wl] : __ldg(nb + (size_t)q * stride)) : i;
 #else
         jg[u] = q < q_end ? __ldg(nb + (size_t)q * stride) : i;
 #endif
@@ -343,6 +431,27 @@ __global__ void __launch_bounds__(SPP_STAGE_BLOCK, KIND == SPP_KIND_CHAIN ? 1024
       }
 #pragma unroll
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) pg[u] = __ldg(b.cur + jg[u]);
+#if SPP_STAGE_RSQRT2
+      if (SPP_STAGE_GROUP == 2 && KIND != SPP_KIND_CHAIN) {
+        /* both separations, then both 1/d in one two-lane Newton sequence
+         * (each lane the bits of spp_rsqrtf); a padding entry past the list
+         * end (j = i, d2 = 0) gets a finite r and is not applied */
+        float dx[2], dy[2], d2[2];
+        if (all_inner || CLOSED) {
+#pragma unroll
+          for (int u = 0; u < 2; ++u) d2[u] = spp_pair_sep(&k, 0, pi.x, pi.y, pg[u].x, pg[u].y, &dx[u], &dy[u]);
+        } else {
+#pragma unroll
+          for (int u = 0; u < 2; ++u) d2[u] = spp_pair_sep(&k, 1, pi.x, pi.y, pg[u].x, pg[u].y, &dx[u], &dy[u]);
+        }
+        spp_f2 r = spp_f2_make(0.0f, 0.0f);
+        if (spp_pair_needs_r(LAW, KIND)) r = spp_rsqrtf2(spp_f2_make(d2[0], d2[1]));
+        spp_pair_abp_apply(&k, LAW, KIND, &a, dx[0], dy[0], d2[0], r.x, pi.z, pi.w, pg[0].z, pg[0].w, 1);
+        if (q0 + 1 < q_end)
+          spp_pair_abp_apply(&k, LAW, KIND, &a, dx[1], dy[1], d2[1], r.y, pi.z, pi.w, pg[1].z, pg[1].w, 1);
+        continue;
+      }
+#endif
 #pragma unroll
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
         /* entries past the list end are skipped (a warp whose lanes all
@@ -463,6 +572,11 @@ __global__ void __launch_bounds__(SPP_STAGE_BLOCK, KIND == SPP_KIND_CHAIN ? 1024
     }
   }
   }
+#if SPP_STAGE_BULK_ROWS > 0
+  /* copies that were late must land before the block's shared memory is
+   * released */
+  if (bulk_late) bulk_wait(smem_u32(&bbar[ww]));
+#endif
 #if SPP_STAGE_FINISH_NB
   if (last) finish_step_nb(k, d, disp2, step2, cond, use_cond, fin);
 #else
@@ -502,7 +616,7 @@ __global__ void __launch_bounds__(SPP_BLOCK) k_vicsek_step(SppConsts k, DevState
     }
     if (k.closed && k.model == SPP_MODEL_VICSEK_REF_ANGLE) spp_vicsek_walls(&k, &a, p.x, p.y, th0);
     if (a.ovf) atomicOr(&d.ctl->fx_overflow, 1u);
-    const spp_u32x4 r = spp_draw(k.seed, k.system, id, step, SPP_RNG_VICSEK);
+    const spp_u32x4 r = spp_draw_k(&k, id, step, SPP_RNG_VICSEK);
     float x, y, t, c, s;
     int gx = 0, gy = 0;
     spp_vicsek_update(&k, &a, p.x, p.y, th0, p.z, p.w, r.v[0], &x, &y, &t, &c, &s, &gx, &gy);
@@ -686,7 +800,7 @@ __global__ void __launch_bounds__(SPP_SMALL_THREADS, 1) k_vicsek_small(SppConsts
         if (valid && q == 0) {
           if (k.closed && need_theta) spp_vicsek_walls(&k, &a, p.x, p.y, sth[me]);
           if (a.ovf) ovf = 1u;
-          const spp_u32x4 r = spp_draw(k.seed, k.system, d.id[i], step, SPP_RNG_VICSEK);
+          const spp_u32x4 r = spp_draw_k(&k, d.id[i], step, SPP_RNG_VICSEK);
           float x, y, th, c, sn;
           int gx = 0, gy = 0;
           spp_vicsek_update(&k, &a, p.x, p.y, __ldcg(src_th + i), p.z, p.w, r.v[0], &x, &y, &th, &c, &sn,
@@ -815,6 +929,21 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
     k_commit<<<blocks_for(d.n), SPP_BLOCK, 0, s>>>(d);
     if (launches) *launches += 1;
   }
+}
+
+/* Once per process, before any launch (graph capture included): the
+ * shared-memory carveout of the stage kernel of the headline model when it
+ * stages list rows in shared memory (SPP_STAGE_CARVEOUT, percent of the
+ * maximum), so that a full SM of blocks fits. */
+void prepare_abp_stage() {
+#if SPP_STAGE_BULK_ROWS > 0 && defined(SPP_STAGE_CARVEOUT)
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(k_abp_stage<SPP_FORCE_HARMONIC, SPP_KIND_ABP, 1, 0>,
+                         cudaFuncAttributePreferredSharedMemoryCarveout, SPP_STAGE_CARVEOUT);
+    cudaGetLastError();
+  });
+#endif
 }
 
 void launch_vicsek_step(const SppConsts& k, const DevState& d, cudaStream_t s, int64_t* launches) {

@@ -106,6 +106,37 @@ SPP_HD spp_u32x4 spp_philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32
   return o;
 }
 
+/* The round keys of key (k0, k1) = (seed low, seed high): round r uses
+ * (k0 + r W0, k1 + r W1) mod 2^32, ks[2r] and ks[2r + 1].  Kernels that
+ * draw for many particles take them precomputed (spp_philox4x32_10_ks)
+ * instead of advancing the key in every draw; the words are the same. */
+SPP_HD void spp_philox_round_keys(uint64_t seed, uint32_t* ks) {
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    ks[2 * r] = k0;
+    ks[2 * r + 1] = k1;
+    k0 += SPP_PHILOX_W0;
+    k1 += SPP_PHILOX_W1;
+  }
+}
+
+SPP_HD spp_u32x4 spp_philox4x32_10_ks(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                      const uint32_t* ks) {
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0, lo0, hi1, lo1;
+    spp_mulhilo(SPP_PHILOX_M0, c0, &hi0, &lo0);
+    spp_mulhilo(SPP_PHILOX_M1, c2, &hi1, &lo1);
+    uint32_t n0 = hi1 ^ c1 ^ ks[2 * r];
+    uint32_t n2 = hi0 ^ c3 ^ ks[2 * r + 1];
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+  }
+  spp_u32x4 o; o.v[0] = c0; o.v[1] = c1; o.v[2] = c2; o.v[3] = c3;
+  return o;
+}
+
 /* Draw for (seed, system, particle id, step, stream). */
 SPP_HD spp_u32x4 spp_draw(uint64_t seed, uint32_t system, uint32_t pid, uint32_t step,
                           uint32_t stream) {
@@ -316,13 +347,45 @@ SPP_HD spp_f2 spp_fma2s(float t, spp_f2 b, spp_f2 c) {
       "l"(spp_f2_pack(b)), "l"(spp_f2_pack(c)));
   return spp_f2_unpack(r);
 }
+/* a * b */
+SPP_HD spp_f2 spp_mul2(spp_f2 a, spp_f2 b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(spp_f2_pack(a)), "l"(spp_f2_pack(b)));
+  return spp_f2_unpack(r);
+}
+/* fmaf(a, b, c) lane by lane */
+SPP_HD spp_f2 spp_fma2(spp_f2 a, spp_f2 b, spp_f2 c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(spp_f2_pack(a)), "l"(spp_f2_pack(b)),
+      "l"(spp_f2_pack(c)));
+  return spp_f2_unpack(r);
+}
 #else
 SPP_HD spp_f2 spp_sub2(spp_f2 a, spp_f2 b) { return spp_f2_make(a.x - b.x, a.y - b.y); }
 SPP_HD spp_f2 spp_add2(spp_f2 a, spp_f2 b) { return spp_f2_make(a.x + b.x, a.y + b.y); }
 SPP_HD spp_f2 spp_fma2s(float t, spp_f2 b, spp_f2 c) {
   return spp_f2_make(fmaf(t, b.x, c.x), fmaf(t, b.y, c.y));
 }
+SPP_HD spp_f2 spp_mul2(spp_f2 a, spp_f2 b) { return spp_f2_make(a.x * b.x, a.y * b.y); }
+SPP_HD spp_f2 spp_fma2(spp_f2 a, spp_f2 b, spp_f2 c) {
+  return spp_f2_make(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+}
 #endif
+
+/* spp_rsqrtf of two values at once: the same steps lane by lane, so each
+ * lane returns the bits of the scalar call.  (-0.5) x equals -(0.5 x)
+ * exactly (scaling by a power of two, rounding symmetric about zero), which
+ * is the scalar form's -h. */
+SPP_HD spp_f2 spp_rsqrtf2(spp_f2 x) {
+  spp_f2 y = spp_f2_make(spp_u2f(0x5f375a86u - (spp_f2u(x.x) >> 1)),
+                         spp_u2f(0x5f375a86u - (spp_f2u(x.y) >> 1)));
+  const spp_f2 nh = spp_mul2(spp_f2_make(-0.5f, -0.5f), x);
+  const spp_f2 c15 = spp_f2_make(1.5f, 1.5f);
+  y = spp_mul2(y, spp_fma2(spp_mul2(nh, y), y, c15));
+  y = spp_mul2(y, spp_fma2(spp_mul2(nh, y), y, c15));
+  y = spp_mul2(y, spp_fma2(spp_mul2(nh, y), y, c15));
+  return y;
+}
 
 /* ------------------------------------------------------------------ */
 /* periodic wraps                                                      */

@@ -41,7 +41,7 @@ struct Ctl {
   uint32_t bad_range;     /* smallest index of an uploaded position outside [-L, L) (or ~0) */
   uint32_t long_n;        /* lists longer than the in-block sort queued by the last build */
   uint32_t bad_index;     /* SPP_CHECKED builds: a kernel met an index out of range */
-  uint32_t pad[1];
+  uint32_t bulk_timeouts; /* warps whose bulk copy of list rows did not arrive in time (they read global memory) */
 };
 
 /* SPP_CHECKED builds check every list, cell and slot index a hot kernel
@@ -131,6 +131,7 @@ void launch_gather_state(const SppConsts& k, const DevState& d, float* x, float*
                          int32_t* img_xy, cudaStream_t s);
 
 /* kernels_step.cu */
+void prepare_abp_stage();
 void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nstages,
                       cudaGraphConditionalHandle cond, int use_cond, cudaStream_t s,
                       int64_t* launches);

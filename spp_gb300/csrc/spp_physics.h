@@ -4,9 +4,10 @@
  * Written once, compiled into the sm_103a kernels and into the CPU mirror
  * (oracle/spp_mirror32.c), so that the mirror reproduces the kernels' bits
  * and can prove that binning, neighbour lists, particle reordering and graph
- * replay neither lose nor add anything.  Neighbour sums are accumulated in
- * int64 fixed point (spp_fp32.h), so the result does not depend on the order
- * the neighbours are visited in.
+ * replay neither lose nor add anything.  The result does not depend on the
+ * order the neighbours are visited in: the Verlet-list models sum in FP32 in
+ * ascending neighbour id (their lists are sorted by id at every build), and
+ * the Vicsek models in exact split int32 fixed point (spp_fp32.h).
  *
  * All interactions are written in gather form (particle i sums the terms it
  * receives from each neighbour j).  The reference visits every pair once and
@@ -87,7 +88,14 @@ typedef struct SppConsts {
   float wall_A, wall_sigma, wall_rc, wall_rf, wall_g_over_pi;
   float wall_cut;              /* e^(-r_c/sigma) (1/r_c^2 + 1/(sigma r_c)), the truncation shift */
   float wall_gcont_over_2pi;   /* ContinuousParticle::gw / (2 pi) */
+  uint32_t philox_ks[20];      /* Philox round keys of seed (spp_philox_round_keys) */
 } SppConsts;
+
+/* spp_draw(k->seed, k->system, pid, step, stream) from the precomputed
+ * round keys: the same four words. */
+SPP_HD spp_u32x4 spp_draw_k(const SppConsts* k, uint32_t pid, uint32_t step, uint32_t stream) {
+  return spp_philox4x32_10_ks(pid, step, stream, k->system, k->philox_ks);
+}
 
 #define SPP_GATHER_LANES 4
 #ifndef SPP_LANES_MAX_N
@@ -129,6 +137,7 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
   k->model = p->model; k->integrator = p->integrator;
   k->force_law = p->force_law; k->align_mode = p->align_mode;
   k->seed = p->seed; k->system = p->system_id; k->n = p->n;
+  spp_philox_round_keys(p->seed, k->philox_ks);
   k->L = (float)p->L; k->L2 = (float)(2.0 * p->L);
   k->dt = (float)p->dt; k->half_dt = (float)(0.5 * p->dt); k->dt6 = (float)(p->dt / 6.0);
   k->v0 = (float)p->v0; k->v0dt = (float)(p->v0 * p->dt);
@@ -367,6 +376,23 @@ SPP_HD int spp_pair_kind(const SppConsts* k) {
   return k->alpha_over_pi != 0.0f ? SPP_KIND_CONT_ALPHA : SPP_KIND_CONT;
 }
 
+/* The separation of a pair (minimum image where wrap is set) and its
+ * square. */
+SPP_HD float spp_pair_sep(const SppConsts* k, int wrap, float xi, float yi, float xj, float yj,
+                          float* dx, float* dy) {
+  if (wrap) return spp_sep_cl(k, 0, xi, yi, xj, yj, dx, dy);
+  /* both particles far from the boundary, or a closed box: the plain difference */
+  const spp_f2 dr = spp_sub2(spp_f2_make(xi, yi), spp_f2_make(xj, yj));
+  *dx = dr.x;
+  *dy = dr.y;
+  return fmaf(dr.x, dr.x, dr.y * dr.y);
+}
+
+/* Whether the term of (law, kind) needs r = 1/d. */
+SPP_HD int spp_pair_needs_r(int law, int kind) {
+  return law != SPP_FORCE_NONE || kind == SPP_KIND_CONT_ALPHA;
+}
+
 /* RepulsiveParticle::Interact (shared/particle.h:728-757) / ContinuousParticle::
  * Interact (:296-338), as received by i from j.  (c, s) = (cos, sin) theta.
  * law and kind are compile-time constants in the kernels (template
@@ -381,23 +407,13 @@ SPP_HD int spp_pair_kind(const SppConsts* k) {
  *   R12       A ((sigma/d)^13 - (sigma/r_c)^13) dr / d  ->  t = A (q^13 - c^13) r, q = sigma r
  * The alignment term sin(theta_j - theta_i) = s_j c_i - c_j s_i factors:
  * the loop sums s_j and c_j and spp_align_sum combines them once. */
-SPP_HD void spp_pair_abp_lkwv(const SppConsts* k, int law, int kind, int wrap, SppAccF* a, float xi,
-                              float yi, float ci, float si, float xj, float yj, float cj, float sj,
-                              int valid) {
-  float dx, dy, d2;
-  if (wrap) {
-    d2 = spp_sep_cl(k, 0, xi, yi, xj, yj, &dx, &dy);
-  } else { /* both particles far from the boundary, or a closed box: the plain difference */
-    const spp_f2 dr = spp_sub2(spp_f2_make(xi, yi), spp_f2_make(xj, yj));
-    dx = dr.x;
-    dy = dr.y;
-    d2 = fmaf(dx, dx, dy * dy);
-  }
+/* The term of one pair from its separation (dx, dy), d2 and r =
+ * spp_rsqrtf(d2) (r is not read where spp_pair_needs_r is 0). */
+SPP_HD void spp_pair_abp_apply(const SppConsts* k, int law, int kind, SppAccF* a, float dx, float dy,
+                               float d2, float r, float ci, float si, float cj, float sj, int valid) {
   const int aligns = (kind != SPP_KIND_BEADS && kind != SPP_KIND_CHAIN);
   const int in_rep = valid && (law != SPP_FORCE_NONE) && (d2 < k->rrep2) && (d2 > 0.0f);
   const int in_al = valid && aligns && d2 < k->ral2;
-  float r = 0.0f;
-  if (law != SPP_FORCE_NONE || kind == SPP_KIND_CONT_ALPHA) r = spp_rsqrtf(d2);
   if (law != SPP_FORCE_NONE) {
     float t;
     if (law == SPP_FORCE_HARMONIC) {
@@ -424,6 +440,15 @@ SPP_HD void spp_pair_abp_lkwv(const SppConsts* k, int law, int kind, int wrap, S
     if (kind == SPP_KIND_CONT_ALPHA && in_al && d2 > 0.0f)
       a->tq = a->tq - (k->alpha_over_pi * (dx * si - dy * ci)) * r;
   }
+}
+
+SPP_HD void spp_pair_abp_lkwv(const SppConsts* k, int law, int kind, int wrap, SppAccF* a, float xi,
+                              float yi, float ci, float si, float xj, float yj, float cj, float sj,
+                              int valid) {
+  float dx, dy;
+  const float d2 = spp_pair_sep(k, wrap, xi, yi, xj, yj, &dx, &dy);
+  const float r = spp_pair_needs_r(law, kind) ? spp_rsqrtf(d2) : 0.0f;
+  spp_pair_abp_apply(k, law, kind, a, dx, dy, d2, r, ci, si, cj, sj, valid);
 }
 
 /* The pair term of a list entry that exists (valid = 0 masks a padding
@@ -632,10 +657,10 @@ SPP_HD void spp_abp_forces(const SppConsts* k, int walls, const SppAccF* a, floa
 SPP_HD float spp_tumble_noise(const SppConsts* k, uint32_t pid, uint32_t step, int32_t* state) {
   int32_t s = *state;
   if (s == 0) {
-    const uint32_t u = spp_draw(k->seed, k->system, pid, step, SPP_RNG_TUMBLE).v[0] >> 8;
+    const uint32_t u = spp_draw_k(k, pid, step, SPP_RNG_TUMBLE).v[0] >> 8;
     if (u < k->tumble_u24) {
       /* 2 * gsl_rng_uniform_int(r, 2) - 1: -1 when the uniform is < 1/2 */
-      const uint32_t v = spp_draw(k->seed, k->system, pid, step, SPP_RNG_TUMBLE_SIGN).v[0] >> 8;
+      const uint32_t v = spp_draw_k(k, pid, step, SPP_RNG_TUMBLE_SIGN).v[0] >> 8;
       s = v < (1u << 23) ? -1 : 1;
     }
   } else {
@@ -649,7 +674,7 @@ SPP_HD float spp_tumble_noise(const SppConsts* k, uint32_t pid, uint32_t step, i
 
 /* The rotational-noise increment of particle pid at a step. */
 SPP_HD float spp_rot_noise(const SppConsts* k, uint32_t pid, uint32_t step) {
-  spp_u32x4 d = spp_draw(k->seed, k->system, pid, step, SPP_RNG_ROT_NOISE);
+  spp_u32x4 d = spp_draw_k(k, pid, step, SPP_RNG_ROT_NOISE);
   return k->sigma * spp_normal_f(d.v[0], d.v[1]);
 }
 

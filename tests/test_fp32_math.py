@@ -39,6 +39,20 @@ def test_numpy_philox_matches_c_on_many_counters():
         assert tuple(int(o[0]) for o in out) == O.philox(ctr, key)
 
 
+@pytest.mark.parametrize("ctr,key,expect", KAT)
+def test_philox_round_keys_known_answers(ctr, key, expect):
+    """The kernels draw through precomputed round keys (spp_draw_k)."""
+    assert O.philox(ctr, key, round_keys=True) == expect
+
+
+def test_philox_round_keys_match_on_many_counters():
+    rng = np.random.default_rng(1)
+    for _ in range(200):
+        ctr = [int(v) for v in rng.integers(0, 2**32, 4)]
+        key = [int(v) for v in rng.integers(0, 2**32, 2)]
+        assert O.philox(ctr, key, round_keys=True) == O.philox(ctr, key)
+
+
 def ulp_err(approx, exact):
     approx = approx.astype(np.float64)
     u = np.spacing(np.abs(exact).astype(np.float32)).astype(np.float64)
