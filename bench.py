@@ -330,7 +330,7 @@ def sweep_leg(sample_points=64, seed=4):
                               "answered_within_tol": int(within.sum()),
                               "particle_steps": res.particle_steps, "retired": int(ret.sum()),
                               "rounds": res.rounds, "runs_s": res.timings["runs_s"],
-                              "train_s": res.timings["train_s"]},
+                              "train_s": res.timings["train_s"], "phases": res.timings["phases"]},
         "batched_plain": {"points_per_hour": pph(n, plain.wall_s), "wall_s": plain.wall_s,
                           "particle_steps": plain.particle_steps},
         "point_by_point": {"points_per_hour": 3600.0 / mean_pp, "mean_s_per_point": mean_pp,
