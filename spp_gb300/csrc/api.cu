@@ -173,8 +173,10 @@ int validate(const SppParams* p) {
   }
   if (p->gather_lanes != 0 && p->gather_lanes != 1 && p->gather_lanes != SPP_GATHER_LANES)
     return fail(SPP_ERR_INVALID, "gather_lanes must be 0 (automatic), 1 or 4");
-  if (p->gather_lanes == SPP_GATHER_LANES && p->model != SPP_MODEL_ABP && p->model != SPP_MODEL_CONTINUOUS)
-    return fail(SPP_ERR_UNSUPPORTED, "gather_lanes = 4 is built for SPP_MODEL_ABP and SPP_MODEL_CONTINUOUS");
+  if (p->gather_lanes == SPP_GATHER_LANES && p->model != SPP_MODEL_ABP && p->model != SPP_MODEL_CONTINUOUS &&
+      !(p->model == SPP_MODEL_BEADS && p->chain_beads <= 1))
+    return fail(SPP_ERR_UNSUPPORTED,
+                "gather_lanes = 4 is built for SPP_MODEL_ABP, SPP_MODEL_CONTINUOUS and single-bead SPP_MODEL_BEADS");
   if (p->boundary != SPP_BOUNDARY_PERIODIC && p->boundary != SPP_BOUNDARY_WALLS &&
       p->boundary != SPP_BOUNDARY_CIRCLE)
     return fail(SPP_ERR_INVALID, "boundary must be SPP_BOUNDARY_PERIODIC, _WALLS or _CIRCLE");

@@ -889,7 +889,7 @@ void launch_abp_stage(const SppConsts& k, const DevState& d, int stage, int nsta
     b.out = bufs[out_sel[stage]];
   }
   const int kind = spp_pair_kind(&k);
-  const int lanes = (kind == SPP_KIND_BEADS || kind == SPP_KIND_CHAIN) ? 1 : k.lanes;
+  const int lanes = kind == SPP_KIND_CHAIN ? 1 : k.lanes;
   int nb = (d.n * lanes + SPP_STAGE_BLOCK - 1) / SPP_STAGE_BLOCK;
   if (nb == 0) nb = 1;
   /* closed boxes (walls) exist for the ABP and continuous kinds only */

@@ -200,15 +200,18 @@ static inline void spp_consts_from_params(SppConsts* k, const SppParams* p) {
     k->tumble_steps = c;
   }
   {
-    /* gather_lanes: 0 = automatic, else 1 or SPP_GATHER_LANES (ABP and
-     * continuous only; spp_create rejects the rest) */
-    const int lane_model = p->model == SPP_MODEL_ABP || p->model == SPP_MODEL_CONTINUOUS;
+    /* gather_lanes: 0 = automatic, else 1 or SPP_GATHER_LANES (ABP,
+     * continuous and single-bead bead models; spp_create rejects the rest).
+     * Automatic: four lanes for ABP and continuous systems of up to
+     * SPP_LANES_MAX_N particles, else one. */
+    const int auto_model = p->model == SPP_MODEL_ABP || p->model == SPP_MODEL_CONTINUOUS;
+    const int lane_model = auto_model || (p->model == SPP_MODEL_BEADS && p->chain_beads <= 1);
     if (!lane_model || p->gather_lanes == 1)
       k->lanes = 1;
     else if (p->gather_lanes == SPP_GATHER_LANES)
       k->lanes = SPP_GATHER_LANES;
     else
-      k->lanes = p->n <= SPP_LANES_MAX_N ? SPP_GATHER_LANES : 1;
+      k->lanes = auto_model && p->n <= SPP_LANES_MAX_N ? SPP_GATHER_LANES : 1;
   }
   k->closed = p->boundary == SPP_BOUNDARY_WALLS || p->boundary == SPP_BOUNDARY_CIRCLE ? 1 : 0;
   k->n_walls = 0;

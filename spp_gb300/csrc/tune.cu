@@ -69,7 +69,8 @@ extern "C" int spp_autotune(SppParams* p, const float* x, const float* y, const 
   if (p->model != SPP_MODEL_ABP && p->model != SPP_MODEL_CONTINUOUS && p->model != SPP_MODEL_BEADS)
     return tune_fail(SPP_ERR_UNSUPPORTED,
                      "spp_autotune: the Verlet-list models (ABP, continuous, beads) have a launch shape to tune");
-  const bool lane_model = p->model == SPP_MODEL_ABP || p->model == SPP_MODEL_CONTINUOUS;
+  const bool lane_model = p->model == SPP_MODEL_ABP || p->model == SPP_MODEL_CONTINUOUS ||
+                          (p->model == SPP_MODEL_BEADS && p->chain_beads <= 1);
   int lanes[2] = {p->gather_lanes, 0};
   int n_lanes = 1;
   if ((what & SPP_TUNE_LANES) && lane_model) {

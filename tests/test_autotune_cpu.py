@@ -82,8 +82,9 @@ def test_gather_lanes_is_checked_before_device_work(lib):
     p = configs.abp_config(n=64, L=8.0)
     assert lib.spp_create(C.byref(p.replace(gather_lanes=2)), C.byref(h)) == 1
     assert b"gather_lanes" in lib.spp_last_error()
-    beads = configs.reference_defaults(abi.MODEL_BEADS).replace(n=64, L=8.0, gather_lanes=4)
-    assert lib.spp_create(C.byref(beads), C.byref(h)) == 6
+    # multi-bead swimmers keep one thread per body
+    chains = configs.chain_config(n=64).replace(gather_lanes=4)
+    assert lib.spp_create(C.byref(chains), C.byref(h)) == 6
     vic = configs.vicsek_config(n=64, L=8.0).replace(gather_lanes=4)
     assert lib.spp_create(C.byref(vic), C.byref(h)) == 6
 

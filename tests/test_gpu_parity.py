@@ -329,11 +329,14 @@ def test_full_size_abp_properties(gpu_lib):
     assert o.n_rebuilds > 3
 
 
+@pytest.mark.parametrize("lanes", [1, 4])
 @pytest.mark.parametrize("integ", [abi.INT_RK2, abi.INT_RK4])
-def test_vesicles_bitexact_vs_mirror(gpu_lib, integ):
-    """Ring membranes (bonds + bending) with swimmers, bit-exact against the mirror."""
+def test_vesicles_bitexact_vs_mirror(gpu_lib, integ, lanes):
+    """Ring membranes (bonds + bending) with swimmers, bit-exact against the
+    mirror, with one or four threads per body in the neighbour sums."""
     p = configs.vesicle_config(n_rings=16, ring_size=64, swimmers_per_ring=16, L=48.0,
                                integrator=integ)
+    p.gather_lanes = lanes
     x, y, th = configs.vesicle_state(p)
     gpu, obs = run_gpu(p, x, y, th, 150)
     ref = O.run32(p, O.State32(x, y, th), 150)
