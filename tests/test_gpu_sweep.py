@@ -33,3 +33,21 @@ def test_sweep_with_and_without_surrogate(gpu_lib):
     assert np.all(res.bound[res.retired] <= 0.02)
     assert np.mean(err[res.retired] <= 0.02) >= 0.8
     assert np.median(err[res.retired]) <= 0.01
+
+
+def test_surrogate_saves_wall_time_on_the_full_sweep(gpu_lib):
+    """What the network gains in wall-clock time: the 512-point sweep (N
+    log-uniform in [1024, 65536], 20,000 steps), batched with the surrogate
+    against batched without it, in points per hour counting only the answers
+    within |dP| <= 0.02 of the full runs (measured: about 1.15x)."""
+    pts = configs.sweep_points(seed=4)
+    plain = surrogate.run_sweep(pts, use_surrogate=False, seed=4)
+    res = surrogate.run_sweep(pts, tol=0.02, seed=4)
+    err = np.abs(res.p_answer - plain.p_full)
+    within = err <= 0.02
+    gain = (within.sum() / res.wall_s) / (len(pts) / plain.wall_s)
+    print(f"wall {res.wall_s:.2f} s against {plain.wall_s:.2f} s, {within.sum()} of {len(pts)} within "
+          f"tolerance, gain {gain:.3f}, retired {res.retired.sum()}")
+    assert np.mean(within) >= 0.97
+    assert np.mean(err[res.retired] <= 0.02) >= 0.9
+    assert gain >= 1.05
