@@ -54,6 +54,10 @@ struct SppSystem {
   DevState d;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;   /* used only while capturing conditional bodies */
+  /* the tangent stages of a Lyapunov run, forked off `stream` so that each
+   * runs beside the base stage of the same Runge-Kutta stage */
+  cudaStream_t tan_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool own_stream = false;
   bool uses_list = false;        /* Verlet list models (ABP, continuous) */
   int nstages = 1;
@@ -476,6 +480,13 @@ int enqueue_lyap_step(SppSystem* s, cudaStream_t st, bool capture, int64_t* laun
     CUDA_TRY(cudaGraphConditionalHandleCreate(&handle, g, 0, cudaGraphCondAssignDefault));
   }
   const DevState& d = s->d;
+  /* Base and tangent stage s both read the stage input that stage s - 1
+   * wrote and write buffers the other does not touch, so they run side by
+   * side (the tangent stage on tan_stream); both finish before stage s + 1,
+   * whose base stage overwrites a buffer that a tangent stage of this step
+   * has read (RK2: the start state; RK4: half), and before the rebuild that
+   * reorders the slots. */
+  const bool fork = s->tan_stream != nullptr;
   for (int stage = 0; stage < s->nstages; ++stage) {
     const float4* cur;
     if (s->nstages == 2) cur = stage == 0 ? d.pos : d.half;
@@ -484,8 +495,18 @@ int enqueue_lyap_step(SppSystem* s, cudaStream_t st, bool capture, int64_t* laun
       static const int cur_sel[4] = {0, 1, 2, 1};
       cur = bufs[cur_sel[stage]];
     }
+    cudaStream_t ts = st;
+    if (fork) {
+      CUDA_TRY(cudaEventRecord(s->ev_fork, st));
+      CUDA_TRY(cudaStreamWaitEvent(s->tan_stream, s->ev_fork, 0));
+      ts = s->tan_stream;
+    }
     launch_abp_stage(s->k, d, stage, s->nstages, handle, capture ? 1 : 0, st, launches);
-    launch_tangent_stage(s->k, d, s->lyap, stage, s->nstages, cur, st, launches);
+    launch_tangent_stage(s->k, d, s->lyap, stage, s->nstages, cur, ts, launches);
+    if (fork) {
+      CUDA_TRY(cudaEventRecord(s->ev_join, s->tan_stream));
+      CUDA_TRY(cudaStreamWaitEvent(st, s->ev_join, 0));
+    }
   }
   CUDA_TRY(cudaGetLastError());
   if (!capture) return SPP_OK;
@@ -788,6 +809,9 @@ int spp_destroy(SppSystem* s) {
   free_dev(s);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   if (s->side) cudaStreamDestroy(s->side);
+  if (s->tan_stream) cudaStreamDestroy(s->tan_stream);
+  if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+  if (s->ev_join) cudaEventDestroy(s->ev_join);
   delete s;
   return SPP_OK;
 }
@@ -1119,6 +1143,11 @@ int spp_lyap_init(SppSystem* s, int K, uint64_t seed) {
   uint32_t err = 0;
   CUDA_TRY(cudaMemcpy(&err, L.error, sizeof(err), cudaMemcpyDeviceToHost));
   if (err) { free_lyap(s); return fail(SPP_ERR_NUMERIC, "initial tangent vectors are dependent"); }
+  if (!s->tan_stream) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&s->tan_stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+  }
   s->lyap_on = true;
   s->lyap_steps = 0;
   return SPP_OK;
