@@ -1144,9 +1144,21 @@ int spp_lyap_init(SppSystem* s, int K, uint64_t seed) {
   CUDA_TRY(cudaMemcpy(&err, L.error, sizeof(err), cudaMemcpyDeviceToHost));
   if (err) { free_lyap(s); return fail(SPP_ERR_NUMERIC, "initial tangent vectors are dependent"); }
   if (!s->tan_stream) {
-    CUDA_TRY(cudaStreamCreateWithFlags(&s->tan_stream, cudaStreamNonBlocking));
-    CUDA_TRY(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
-    CUDA_TRY(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+    /* all three or none: without them the tangent stages run on the base stream */
+    cudaStream_t ts = nullptr;
+    cudaEvent_t ef = nullptr, ej = nullptr;
+    if (cudaStreamCreateWithFlags(&ts, cudaStreamNonBlocking) == cudaSuccess &&
+        cudaEventCreateWithFlags(&ef, cudaEventDisableTiming) == cudaSuccess &&
+        cudaEventCreateWithFlags(&ej, cudaEventDisableTiming) == cudaSuccess) {
+      s->tan_stream = ts;
+      s->ev_fork = ef;
+      s->ev_join = ej;
+    } else {
+      cudaGetLastError();
+      if (ts) cudaStreamDestroy(ts);
+      if (ef) cudaEventDestroy(ef);
+      if (ej) cudaEventDestroy(ej);
+    }
   }
   s->lyap_on = true;
   s->lyap_steps = 0;
