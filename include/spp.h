@@ -116,9 +116,11 @@ typedef struct SppParams {
   int32_t rot_noise;      /* enum SppRotNoise (swimmers of SPP_MODEL_BEADS) */
   int32_t gather_lanes;   /* threads per particle in the Verlet-list neighbour sums of the
                            * ABP and continuous models: 0 = automatic (4 up to 16,384
-                           * particles, else 1), or 1 or 4 (spp_autotune chooses); the
-                           * other models take 0 or 1.  The lane count fixes the order in
-                           * which neighbour terms are added, so it is part of the result */
+                           * particles, else 1), or 1 or 4 (spp_autotune chooses);
+                           * single-bead SPP_MODEL_BEADS systems take 0 (one lane), 1 or
+                           * 4; the other models take 0 or 1.  The lane count fixes the
+                           * order in which neighbour terms are added, so it is part of
+                           * the result */
   double tumble_rate;     /* RTPChain::lambda: a tumble starts with probability rate * dt per step */
   double tumble_time;     /* RTPChain::t_tumble: a tumble lasts while its elapsed time < t_tumble */
   double tumble_torque;   /* RTPChain::torque_tumble: dtheta = k_perp dt (+-1) torque_tumble per step */
@@ -439,7 +441,8 @@ int spp_time_steps(SppSystem* s, int nsteps, double* ms);
  * (shared/parameters.h:93-99).  spp_autotune() times the candidate shapes
  * of a Verlet-list system (SPP_MODEL_ABP, _CONTINUOUS, _BEADS) on the device
  * and writes the fastest into *p:
- *   SPP_TUNE_LANES  gather_lanes in {1, 4} (ABP and continuous only): threads
+ *   SPP_TUNE_LANES  gather_lanes in {1, 4} (ABP, continuous and single-bead
+ *                   bead models): threads
  *                   per particle in the neighbour sums.  Changes the order of
  *                   the neighbour additions, hence the low bits of the result.
  *   SPP_TUNE_SKIN   skin in {0.5, 1, 1.5, 2} x p->skin: list length against

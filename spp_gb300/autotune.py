@@ -2,7 +2,7 @@
 
 ``autotune`` runs ``spp_autotune`` (include/spp.h) on a given state: it times
 every candidate shape -- threads per particle in the neighbour sums
-(``gather_lanes`` 1 or 4, ABP and continuous models) and the Verlet skin
+(``gather_lanes`` 1 or 4; ABP, continuous and single-bead bead models) and the Verlet skin
 (0.5, 1, 1.5, 2 x the requested one) -- and returns the parameters with the
 fastest written in.  ``tuned_params`` looks the system up in a ``TuneTable``
 first and measures only on a miss, on a seeded uniform state of the same
