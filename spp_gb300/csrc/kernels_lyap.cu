@@ -33,6 +33,9 @@ namespace {
 constexpr int TAN_GROUP = 4;
 constexpr int TAN_BLOCK = 128;
 constexpr int TAN_LOADS = 3;
+#ifndef TAN_PIPE
+#define TAN_PIPE 1   /* list entries loaded one group ahead in the neighbour walk */
+#endif
 
 __host__ __device__ inline int tan_padded(int K) { return (K + TAN_GROUP - 1) / TAN_GROUP * TAN_GROUP; }
 
@@ -89,11 +92,21 @@ __global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevSta
   /* list entries, then the neighbours' states and components, are loaded
    * TAN_LOADS at a time (independent loads in flight); the terms are added
    * in list order */
+#if TAN_PIPE
+  /* list entries one group ahead, as in k_abp_stage */
+  int jn[TAN_LOADS];
+#pragma unroll
+  for (int w = 0; w < TAN_LOADS; ++w) jn[w] = q_begin + w < q_end ? __ldg(nb + (size_t)(q_begin + w) * n) : i;
+#endif
   for (int q0 = q_begin; q0 < q_end; q0 += TAN_LOADS) {
     int jg[TAN_LOADS];
 #pragma unroll
     for (int w = 0; w < TAN_LOADS; ++w) {
+#if TAN_PIPE
+      jg[w] = jn[w];
+#else
       jg[w] = q0 + w < q_end ? __ldg(nb + (size_t)(q0 + w) * n) : i;
+#endif
       if (!spp_index_ok(d.ctl, jg[w], n)) jg[w] = i;
     }
     float4 pg[TAN_LOADS], ug[TAN_LOADS];
@@ -102,6 +115,13 @@ __global__ void __launch_bounds__(TAN_BLOCK) k_tangent_stage(SppConsts k, DevSta
       pg[w] = __ldg(t.cur + jg[w]);
       ug[w] = __ldg(reinterpret_cast<const float4*>(t.us_in + (size_t)jg[w] * KP + v0));
     }
+#if TAN_PIPE
+#pragma unroll
+    for (int w = 0; w < TAN_LOADS; ++w) {
+      const int q = q0 + TAN_LOADS + w;
+      jn[w] = q < q_end ? __ldg(nb + (size_t)q * n) : i;
+    }
+#endif
 #pragma unroll
     for (int w = 0; w < TAN_LOADS; ++w) {
       if (q0 + w < q_end) {

@@ -151,6 +151,15 @@ __device__ __forceinline__ void finish_step_nb(const SppConsts& k, const DevStat
 #ifndef SPP_STAGE_GROUP
 #define SPP_STAGE_GROUP 2        /* neighbours whose loads are issued together (1: one-ahead prefetch) */
 #endif
+/* 1: the walk loads each group's list entries one group ahead (measured at
+ * the 1M workload 600 steps in: 31.3 / 32.0 us per stage launch against
+ * 32.0 / 32.8 without; with groups of one, 33.5 / 34.7) */
+#ifndef SPP_STAGE_PIPE
+#define SPP_STAGE_PIPE 1
+#endif
+#if SPP_STAGE_PIPE && (SPP_STAGE_SMEM_LIST || SPP_STAGE_BULK_ROWS > 0 || SPP_STAGE_UNIFORM)
+#error "SPP_STAGE_PIPE is written for list entries read from global memory in the per-lane walk"
+#endif
 /* 1: with load groups of two, the pair's two 1/d are computed together by
  * two-lane instructions (spp_rsqrtf2).  Measured at the 1M workload 600
  * steps in: 33.2 us per launch against 31.8 (the extra live values spill
@@ -414,9 +423,33 @@ __global__ void __launch_bounds__(SPP_STAGE_BLOCK, KIND == SPP_KIND_CHAIN ? 1024
       }
     }
 #else
+#if SPP_STAGE_PIPE
+    /* list entries one group ahead: the next group's indices are loaded
+     * while this group's neighbour states arrive and its terms are summed */
+    int jn[SPP_STAGE_GROUP];
+#pragma unroll
+    for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
+      const int q = q_begin + u;
+      jn[u] = q < q_end ? __ldg(nb + (size_t)q * stride) : i;
+    }
+#endif
     for (int q0 = q_begin; q0 < q_end; q0 += SPP_STAGE_GROUP) {
       int jg[SPP_STAGE_GROUP];
       float4 pg[SPP_STAGE_GROUP];
+#if SPP_STAGE_PIPE
+#pragma unroll
+      for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
+        jg[u] = jn[u];
+        if (!spp_index_ok(d.ctl, jg[u], d.n)) jg[u] = i;
+      }
+#pragma unroll
+      for (int u = 0; u < SPP_STAGE_GROUP; ++u) pg[u] = __ldg(b.cur + jg[u]);
+#pragma unroll
+      for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
+        const int q = q0 + SPP_STAGE_GROUP + u;
+        jn[u] = q < q_end ? __ldg(nb + (size_t)q * stride) : i;
+      }
+#else
 #pragma unroll
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) {
         const int q = q0 + u;
@@ -431,6 +464,7 @@ __global__ void __launch_bounds__(SPP_STAGE_BLOCK, KIND == SPP_KIND_CHAIN ? 1024
       }
 #pragma unroll
       for (int u = 0; u < SPP_STAGE_GROUP; ++u) pg[u] = __ldg(b.cur + jg[u]);
+#endif
 #if SPP_STAGE_RSQRT2
       if (SPP_STAGE_GROUP == 2 && KIND != SPP_KIND_CHAIN) {
         /* both separations, then both 1/d in one two-lane Newton sequence
