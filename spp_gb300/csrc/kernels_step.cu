@@ -235,6 +235,7 @@ __device__ __forceinline__ void stage_pair(const SppConsts& k, const DevState& d
  * and counts itself in Ctl.bulk_timeouts */
 #define SPP_BULK_WAIT_LIMIT (1 << 20)
 
+#if SPP_STAGE_BULK_ROWS > 0
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -263,6 +264,7 @@ __device__ __forceinline__ bool bulk_wait(uint32_t bar) {
   }
   return false;
 }
+#endif
 
 __device__ __forceinline__ void prefetch_l1(const void* p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
