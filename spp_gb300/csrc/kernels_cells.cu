@@ -192,6 +192,11 @@ __device__ __forceinline__ uint32_t list_order(uint32_t id) {
 #ifndef SPP_LIST_ROWS
 #define SPP_LIST_ROWS 1
 #endif
+/* 1: the row walk loads both candidates' ids with their positions
+ * (rebuild 139.6 -> 136.8 us at the 1M workload) */
+#ifndef SPP_LIST_IDS_EARLY
+#define SPP_LIST_IDS_EARLY 1
+#endif
 /* blocks per SM the list build is compiled for (0: the compiler's choice) */
 #ifndef SPP_LIST_MIN_BLOCKS
 #define SPP_LIST_MIN_BLOCKS 0
@@ -217,9 +222,8 @@ __global__ void SPP_LIST_BOUNDS k_build_list(SppConsts k, DevState d, int with_l
       const int D = d.D;
       const uint32_t cap = (uint32_t)d.cap;
       /* one candidate j (cell-ordered slot) */
-      auto visit = [&](uint32_t j, float dx, float dy, float d2) {
+      auto visit = [&](uint32_t j, uint32_t idj, float dx, float dy, float d2) {
         if (d2 < k.rlist2) {
-          const uint32_t idj = d.id_alt[j];
           const unsigned long long key =
               ((unsigned long long)list_order<LANES>(idj) << 32) | (unsigned long long)j;
           if (LANES > 1) lane_cnt += 1ull << (16 * (idj & 3u));
@@ -298,13 +302,23 @@ __global__ void SPP_LIST_BOUNDS k_build_list(SppConsts k, DevState d, int with_l
           const uint32_t jb = t + 1 < total ? slot_of(t + 1) : ja;
           const float2 qa = reinterpret_cast<const float2*>(d.pos_alt)[2 * (size_t)ja];
           const float2 qb = reinterpret_cast<const float2*>(d.pos_alt)[2 * (size_t)jb];
+#if SPP_LIST_IDS_EARLY
+          /* both ids with the positions: an accepted candidate's key does not
+           * wait on a second load */
+          const uint32_t ida = d.id_alt[ja], idb = d.id_alt[jb];
+#endif
           float dxa, dya, dxb, dyb;
           const float d2a = wrap ? spp_pair_sep(&k, 1, p.x, p.y, qa.x, qa.y, &dxa, &dya)
                                  : spp_pair_sep(&k, 0, p.x, p.y, qa.x, qa.y, &dxa, &dya);
           const float d2b = wrap ? spp_pair_sep(&k, 1, p.x, p.y, qb.x, qb.y, &dxb, &dyb)
                                  : spp_pair_sep(&k, 0, p.x, p.y, qb.x, qb.y, &dxb, &dyb);
-          if ((int)ja != i) visit(ja, dxa, dya, d2a);
-          if (t + 1 < total && (int)jb != i) visit(jb, dxb, dyb, d2b);
+#if SPP_LIST_IDS_EARLY
+          if ((int)ja != i) visit(ja, ida, dxa, dya, d2a);
+          if (t + 1 < total && (int)jb != i) visit(jb, idb, dxb, dyb, d2b);
+#else
+          if ((int)ja != i && d2a < k.rlist2) visit(ja, d.id_alt[ja], dxa, dya, d2a);
+          if (t + 1 < total && (int)jb != i && d2b < k.rlist2) visit(jb, d.id_alt[jb], dxb, dyb, d2b);
+#endif
         }
       }
 #else
@@ -323,7 +337,7 @@ __global__ void SPP_LIST_BOUNDS k_build_list(SppConsts k, DevState d, int with_l
             float4 q = d.pos_alt[j];
             float dx, dy;
             float d2 = spp_sep(&k, p.x, p.y, q.x, q.y, &dx, &dy);
-            visit(j, dx, dy, d2);
+            if (d2 < k.rlist2) visit(j, d.id_alt[j], dx, dy, d2);
           }
         }
       }
